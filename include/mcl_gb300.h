@@ -1,0 +1,215 @@
+/*
+ * mcl_gb300.h - C ABI of the GB300 kinetic 2D Delaunay engine (libmcl_gb300.so).
+ *
+ * Plain C: opaque handles, POD structs, pointers and sizes, int status codes.
+ * CUDA streams are passed as `void*` (a cudaStream_t; NULL = the legacy
+ * default stream) so this header needs no CUDA include.
+ *
+ * The reference (hporro/mcleap) has no FFI: its call surface is the header-only
+ * C++ structs HostTriangulation, DeviceTriangulation and GridCount2d.  Each entry
+ * point below names the reference member it replaces (file:line in the
+ * reference); the C++ drop-in headers in include/mcleap/ keep those class and
+ * method names and forward to these functions.
+ *
+ * Mesh interchange format (the reference's AoS layout,
+ * include/Common_Triangulation.h:42-57): positions float2[V]; vertices
+ * int2[V] = {pos_index, he}; half-edges int4[HE] = {next, v, t, op} with the
+ * twin of half-edge i at i^1; triangles int[T] = {he}.  Vertex ids 0..3 are the
+ * corners of the +-1e7 bounding square and never move.
+ *
+ * Device pointers: arguments named *_dev are device memory, *_host host memory.
+ */
+#ifndef MCL_GB300_H
+#define MCL_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+enum {
+  MCL_OK = 0,
+  MCL_ERR_INVALID_ARGUMENT = 1,
+  MCL_ERR_CUDA = 2,               /* a CUDA runtime call failed */
+  MCL_ERR_OUT_OF_MEMORY = 3,
+  MCL_ERR_NO_CONVERGENCE = 4,     /* an iteration cap was reached (flip rounds, walks) */
+  MCL_ERR_CAPACITY = 5,           /* an output or work buffer was too small */
+  MCL_ERR_DEGENERATE_INPUT = 6,   /* duplicate point, point outside or on the bounding square,
+                                     or a mesh that was not valid before the step */
+  MCL_ERR_PREDICATE = 7,          /* exact predicate expansion capacity exceeded */
+  MCL_ERR_NO_DEVICE = 8           /* no usable CUDA device */
+};
+
+/* Layouts of fixed-capacity neighbour tables (include/Device_Triangulation.h:196-218):
+ * COLUMN: out[i] = count, out[(k+1)*n + i] = k-th neighbour of i
+ * ROW:    out[i*M] = count, out[i*M + k + 1] = k-th neighbour of i              */
+enum { MCL_LAYOUT_COLUMN = 0, MCL_LAYOUT_ROW = 1 };
+
+typedef struct { float x, y; } mcl_float2;
+
+typedef struct {
+  const mcl_float2* pos; /* [V] */
+  const int32_t* v;      /* [2*V] {pos_index, he} */
+  const int32_t* he;     /* [4*HE] {next, v, t, op} */
+  const int32_t* t;      /* [T] {he} */
+  int64_t V, HE, T;
+} mcl_aos_view;
+
+/* Counters of one call (zeroed at the start of each call that fills them). */
+typedef struct {
+  int64_t inverted_faces;        /* faces with orientation <= 0 after the move */
+  int64_t reverted_vertices;     /* vertices moved back while untangling */
+  int64_t removed_vertices;      /* vertices removed and reinserted */
+  int64_t lawson_flips;          /* Delaunay edge flips */
+  int64_t lawson_rounds;         /* parallel flip rounds */
+  int64_t removal_flips;         /* flips made while removing vertices */
+  int64_t insert_rounds;         /* parallel insertion rounds */
+  int64_t incircle_tests;        /* incircle evaluations */
+  int64_t incircle_fp64;         /* ... that the FP32 filter could not decide */
+  int64_t incircle_exact;        /* ... that the FP64 filter could not decide */
+  int64_t orient_fp64;           /* orientation tests past the FP32 filter */
+  int64_t orient_exact;          /* ... past the FP64 filter */
+  int64_t sos_decisions;         /* exactly cocircular quads decided by perturbation */
+  int64_t status;                /* MCL_OK or an error code */
+} mcl_step_stats;
+
+/* ---- library ------------------------------------------------------------ */
+const char* mcl_status_string(int status);
+/* Message of the last failing call on this host thread ("" if none). */
+const char* mcl_last_error(void);
+int mcl_version(void);
+
+/* ---- meshes --------------------------------------------------------------- */
+typedef struct mcl_mesh mcl_mesh;
+
+/* DeviceTriangulation(HostTriangulation*) = allocateMemory + transferToDevice
+ * (include/Device_Triangulation.h:232-236, :255-285). */
+int mcl_mesh_create_from_aos(const mcl_aos_view* aos_host, mcl_mesh** out);
+
+/* HostTriangulation::addDelaunayPoints (include/Host_Triangulation.h:287-300):
+ * sorts pts_host IN PLACE into the reference's Morton order (vertex id =
+ * 4 + sorted index) and builds the Delaunay triangulation of the bounding
+ * square plus the points on the GPU. */
+int mcl_mesh_build(mcl_float2* pts_host, int64_t n, mcl_mesh** out);
+
+/* ~DeviceTriangulation / freeMemory (include/Device_Triangulation.h:238-241, :287-306). */
+int mcl_mesh_destroy(mcl_mesh* m);
+
+/* m_pos_size, m_v_size, m_he_size, m_t_size (include/Device_Triangulation.h:134-137). */
+int mcl_mesh_sizes(const mcl_mesh* m, int64_t* V, int64_t* HE, int64_t* T);
+
+/* transferToHost (include/Device_Triangulation.h:245-253): any pointer may be NULL.
+ * Triangle ids are assigned canonically (by the smallest half-edge of each face). */
+int mcl_mesh_download_aos(mcl_mesh* m, mcl_float2* pos_host, int32_t* v_host, int32_t* he_host,
+                          int32_t* t_host);
+
+/* transferToDevice (include/Device_Triangulation.h:255-263) with new host arrays of
+ * the same sizes. */
+int mcl_mesh_upload_aos(mcl_mesh* m, const mcl_aos_view* aos_host);
+
+/* m_pos: the device position array (float2[V]).  The pointer changes after every
+ * call that moves points (positions are double-buffered); fetch it again. */
+int mcl_mesh_positions(mcl_mesh* m, mcl_float2** pos_dev);
+
+/* Copy the current positions (float2[V]) to device (to_host = 0) or host memory
+ * (to_host = 1, synchronous); the experiments copy dt.m_pos this way
+ * (experiments/moving_device_mesh.cu:106, :125). */
+int mcl_mesh_copy_positions(mcl_mesh* m, mcl_float2* dst, int to_host, void* stream);
+
+/* movePoints (include/Device_Triangulation.h:395-402): pos[i] += d[i] for i >= 4. */
+int mcl_move(mcl_mesh* m, const mcl_float2* d_dev, void* stream);
+/* integrateMovePoints (include/Device_Triangulation.h:403-410): pos[i] += v[i]*dt[i], i >= 4. */
+int mcl_integrate(mcl_mesh* m, const float* dt_dev, const mcl_float2* v_dev, void* stream);
+
+/* untangle / untangle2 (include/Device_Triangulation.h:422-495).  Unlike the
+ * reference (which only handles its B and C cases), this always returns a valid
+ * triangulation: vertices of inverted faces are moved back, removed and
+ * reinserted at their new positions, and the result is Delaunay. */
+int mcl_untangle(mcl_mesh* m, void* stream, mcl_step_stats* stats_host);
+
+/* delonize / delonize2 (include/Device_Triangulation.h:324-390): Lawson flips to the
+ * Delaunay triangulation (untangling first if any face is inverted). */
+int mcl_delaunay_restore(mcl_mesh* m, void* stream, mcl_step_stats* stats_host);
+
+/* One kinetic step: movePoints(d) + untangle + delonize in one persistent launch.
+ * stats_host may be NULL (then the call does not synchronise the stream). */
+int mcl_step(mcl_mesh* m, const mcl_float2* d_dev, void* stream, mcl_step_stats* stats_host);
+
+/* Same step with the displacement in host memory (copied in on `stream`). */
+int mcl_step_host(mcl_mesh* m, const mcl_float2* d_host, void* stream, mcl_step_stats* stats_host);
+
+/* Status of the last asynchronous step on this mesh (synchronises the stream). */
+int mcl_mesh_last_status(mcl_mesh* m, void* stream, mcl_step_stats* stats_host);
+
+/* oneRing<M> / oneRing2<M> (include/Device_Triangulation.h:499-517): neighbour ids
+ * around every vertex, in the layout given; at most M-1 neighbours are stored
+ * (the reference's truncation, include/kernels.cuh:68).  Order: clockwise
+ * (the reference's PREV_OUTGOING walk), starting at the smallest neighbour id.
+ * *truncated_host (may be NULL) receives the number of truncated vertices. */
+int mcl_one_ring(mcl_mesh* m, int layout, int max_ring, int32_t* ring_dev, void* stream,
+                 int64_t* truncated_host);
+
+/* closestNeighbors<M> / closestNeighbors2<M> (include/Device_Triangulation.h:519-547):
+ * nearest ring neighbour of every vertex (ties: smallest id). */
+int mcl_closest_neighbors(mcl_mesh* m, int layout, int max_ring, const int32_t* ring_dev,
+                          int32_t* closest_dev, void* stream);
+
+/* getFRNN<M,F> / getFRNN2<M,F> (include/Device_Triangulation.h:529-557): all
+ * vertices j != i with fl(fl(dx*dx) + fl(dy*dy)) <= fl(r*r) (dx = p_i - p_j in
+ * float), found by a walk over the mesh; at most F-1 per vertex, sorted
+ * ascending.  *overflow_host (may be NULL) receives the number of vertices
+ * whose list was truncated. */
+int mcl_mesh_frnn(mcl_mesh* m, float r, int layout, int max_frnn, int32_t* out_dev, void* stream,
+                  int64_t* overflow_host);
+
+/* ---- uniform-grid fixed-radius neighbours (include/gridCount2d.h) ---------- */
+typedef struct mcl_grid mcl_grid;
+
+enum { MCL_GRID_PERIODIC = 1 };
+
+/* GridCount2d(numP, min, cell_size, num_cells) (include/gridCount2d.h:50-71).
+ * flags: MCL_GRID_PERIODIC wraps the cells and uses minimum-image distances on
+ * a torus of size cell_size*num_cells. */
+int mcl_grid_create(int64_t num_points, float min_x, float min_y, float cell_x, float cell_y,
+                    int32_t cells_x, int32_t cells_y, int flags, mcl_grid** out);
+int mcl_grid_destroy(mcl_grid* g);
+
+/* GridCount2d::update(pos[, vel]) (include/gridCount2d.h:119-135, :174-260): sorts
+ * the points by cell (cells in Morton order, points inside a cell by their
+ * previous index) and permutes pos_dev (and vel_dev when not NULL) in place. */
+int mcl_grid_update(mcl_grid* g, mcl_float2* pos_dev, mcl_float2* vel_dev, void* stream);
+
+/* d_ind: perm_dev[i] = sorted position of the point that was at index i before
+ * the last update; cell tables for header-side functors (apply_f_frnn). */
+int mcl_grid_tables(mcl_grid* g, const int32_t** perm_dev, const int32_t** cell_start_dev,
+                    const int32_t** cell_count_dev, int32_t* cells_x, int32_t* cells_y);
+
+/* apply_f_frnn with the reference tests' SaveNeighborsFunctor
+ * (tests/grid2d_frnn.cu:26-60): for every sorted point i, the sorted indices j != i
+ * with fl(fl(dx*dx)+fl(dy*dy)) <= fl(r*r), ascending; ROW layout without the
+ * count slot: counts_dev[i], ids_dev[i*max_nb + k].  *overflow_host may be NULL. */
+int mcl_grid_frnn(mcl_grid* g, const mcl_float2* pos_dev, float r, int max_nb, int32_t* counts_dev,
+                  int32_t* ids_dev, void* stream, int64_t* overflow_host);
+
+/* mean_num_particle_in_cell (include/gridCount2d.h:314-334). */
+int mcl_grid_mean_occupancy(mcl_grid* g, float* mean_host);
+
+/* ---- diagnostics ------------------------------------------------------------ */
+/* The device predicate ladder evaluated on the host CPU (same source as the
+ * device code), for testing without a GPU.  kind 0 = orient2d on n records of
+ * 6 floats, 1 = incircle on n records of 8 floats, 2 = incircle with symbolic
+ * perturbation (ids: n records of 4 ints).  stage_out (may be NULL) receives
+ * the stage that decided each record (0 fp32, 1 fp64, 2 exact, 3 perturbation). */
+int mcl_debug_predicates_host(int kind, const float* pts, const int32_t* ids, int64_t n,
+                              int32_t* sign_out, int32_t* stage_out);
+/* The same on the GPU (device pointers). */
+int mcl_debug_predicates_device(int kind, const float* pts_dev, const int32_t* ids_dev, int64_t n,
+                                int32_t* sign_dev, int32_t* stage_dev, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MCL_GB300_H */

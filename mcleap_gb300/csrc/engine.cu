@@ -1,0 +1,1309 @@
+// GB300 kinetic Delaunay engine: the persistent step kernel and its phases.
+//
+// One cooperative launch runs a whole kinetic step on the device:
+//
+//   move      new = old + d (or + v*dt), corners fixed   [DeviceTriangulation::movePoints,
+//                                                          include/Device_Triangulation.h:395-410]
+//   classify  every edge: orientation of both faces, incircle of the quad;
+//             non-Delaunay edges go to a work-list       [delonize / untangle checks,
+//                                                          include/Device_Triangulation.h:31-116]
+//   repair    only when a face is inverted (the reference's untangle,
+//             include/Device_Triangulation.h:422-495, handles only its B/C cases):
+//             (1) revert vertices of non-positive faces to their old positions
+//                 until every face is positive;
+//             (2) remove the reverted vertices (flip each to degree 3, merge);
+//             (3) Lawson to Delaunay;
+//             (4) reinsert them at their new positions in parallel rounds
+//                 (locate by walking, 1-to-3 / 2-to-4 split, Lawson).
+//   lawson    parallel flip rounds over the work-list until it is empty
+//             [delonize2, include/Device_Triangulation.h:324-351]: a candidate
+//             flips when its hashed priority beats every candidate sharing a
+//             face with it, so each round flips an independent set and the
+//             highest-priority candidate always flips (no livelock).
+//
+// Rounds are separated by grid-wide barriers; nothing returns to the host
+// between rounds.  The same insertion rounds build the initial triangulation.
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "engine.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace mcl {
+
+constexpr int kThreads = 256;
+constexpr int kStage = 2048;
+constexpr unsigned kFull = 0xffffffffu;
+
+// ---------------------------------------------------------------------------
+// Block-aggregated append to a global work-list: items are staged in shared
+// memory and flushed with one atomicAdd per block when the stage fills up.
+struct Stage {
+  int n;
+  int base;
+  int warp_sum[kThreads / 32];
+  int items[kStage];
+};
+
+__device__ void stage_flush(Stage& S, int* gl, int* gcount, int gcap, DevState* st) {
+  __syncthreads();
+  if (threadIdx.x == 0) S.base = S.n ? atomicAdd(gcount, S.n) : 0;
+  __syncthreads();
+  const int n = S.n, base = S.base;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    if (base + i < gcap) gl[base + i] = S.items[i];
+    else atomicCAS(&st->status, MCL_OK, MCL_ERR_CAPACITY);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) S.n = 0;
+  __syncthreads();
+}
+
+// Block-collective: every thread of the block calls it with its k items.
+template <int K>
+__device__ void stage_push(Stage& S, const int (&mine)[K], int k, int* gl, int* gcount, int gcap,
+                           DevState* st) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  int x = k;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(kFull, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) S.warp_sum[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    int s = lane < nw ? S.warp_sum[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(kFull, s, o);
+      if (lane >= o) s += y;
+    }
+    if (lane < nw) S.warp_sum[lane] = s;
+  }
+  __syncthreads();
+  const int total = S.warp_sum[nw - 1];
+  const int off = (wid ? S.warp_sum[wid - 1] : 0) + x - k;
+  if (total == 0) {
+    __syncthreads();
+    return;
+  }
+  if (S.n + total > kStage) stage_flush(S, gl, gcount, gcap, st);
+  const int n0 = S.n;
+#pragma unroll
+  for (int j = 0; j < K; ++j)
+    if (j < k) S.items[n0 + off + j] = mine[j];
+  __syncthreads();
+  if (threadIdx.x == 0) S.n = n0 + total;
+  __syncthreads();
+}
+
+__device__ __forceinline__ void set_error(const KParams& P, int code) {
+  atomicCAS(&P.st->status, MCL_OK, code);
+}
+
+__device__ __forceinline__ bool enqueue_once(const KParams& P, int e, unsigned stamp) {
+  return atomicMax(P.qmark + e, stamp) < stamp;
+}
+
+__device__ void flush_counters(const KParams& P, LocalCounters& lc) {
+  // warp-reduce the common counter, atomics for the rare ones
+  unsigned long long inc = lc.incircle;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) inc += __shfl_down_sync(kFull, inc, o);
+  if ((threadIdx.x & 31) == 0 && inc) atomicAdd(&P.st->c[C_INCIRCLE], inc);
+  if (lc.incircle_fp64) atomicAdd(&P.st->c[C_INCIRCLE_FP64], lc.incircle_fp64);
+  if (lc.incircle_exact) atomicAdd(&P.st->c[C_INCIRCLE_EXACT], lc.incircle_exact);
+  if (lc.orient_fp64) atomicAdd(&P.st->c[C_ORIENT_FP64], lc.orient_fp64);
+  if (lc.orient_exact) atomicAdd(&P.st->c[C_ORIENT_EXACT], lc.orient_exact);
+  if (lc.sos) atomicAdd(&P.st->c[C_SOS], lc.sos);
+  if (lc.overflow) {
+    atomicAdd(&P.st->c[C_OVERFLOW], 1ull);
+    set_error(P, MCL_ERR_PREDICATE);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Phase: move.  pos (new) = pos_old + displacement; fixed vertices copy.
+__device__ void phase_move(const KParams& P) {
+  const int stride = gridDim.x * blockDim.x;
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < P.V; v += stride) {
+    float2 p = P.pos_old[v];
+    if (!P.vfix[v]) {
+      if (P.move_mode == MOVE_DISPLACE) {
+        const float2 d = P.disp[v];
+        p.x = fadd(p.x, d.x);
+        p.y = fadd(p.y, d.y);
+      } else if (P.move_mode == MOVE_INTEGRATE) {
+        const float2 u = P.vel[v];
+        const float t = P.dt[v];
+        p.x = fadd(p.x, fmul(u.x, t));
+        p.y = fadd(p.y, fmul(u.y, t));
+      }
+    }
+    P.pos[v] = p;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Phase: classify every edge.  Counts non-positive faces; when `push` is set,
+// appends the locally non-Delaunay edges of a valid mesh to work-list 0.
+__device__ void phase_classify(const KParams& P, Stage& S, unsigned qstamp, LocalCounters& lc) {
+  const int stride = gridDim.x * blockDim.x;
+  int bad = 0;
+  for (int base = blockIdx.x * blockDim.x; base < P.E; base += stride) {
+    const int e = base + threadIdx.x;
+    int mine[1];
+    int k = 0;
+    if (e < P.E) {
+      const int4 q = ld_ev(P, e);
+      if (q.x >= 0 && (bad_v(P, q.x) || bad_v(P, q.y) || q.z >= P.V || q.w >= P.V)) {
+        flag_error(P, MCL_ERR_DEGENERATE_INPUT);
+      } else if (q.x >= 0) {
+        const float2 a = ldpos(P, q.x), b = ldpos(P, q.y);
+        bool ok = true;
+        if (q.z >= 0) {
+          const float2 c = ldpos(P, q.z);
+          if (orient_v(P, a, b, c, lc) <= 0) { ok = false; ++bad; }
+        }
+        if (q.w >= 0) {
+          const float2 d = ldpos(P, q.w);
+          if (orient_v(P, b, a, d, lc) <= 0) { ok = false; ++bad; }
+        }
+        if (ok && edge_illegal(P, q, lc) && enqueue_once(P, e, qstamp)) mine[k++] = e;
+      }
+    }
+    stage_push<1>(S, mine, k, P.wl0, &P.st->wl_count[0], P.E, P.st);
+  }
+  stage_flush(S, P.wl0, &P.st->wl_count[0], P.E, P.st);
+  if (bad) atomicAdd(&P.st->inverted, bad);
+}
+
+// ---------------------------------------------------------------------------
+// Lawson flip rounds starting from work-list `src`.
+__device__ void phase_lawson(cg::grid_group& g, const KParams& P, Stage& S, int src, unsigned& stamp,
+                             LocalCounters& lc) {
+  const int stride = gridDim.x * blockDim.x;
+  const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+  for (int round = 0;; ++round) {
+    const int n = ld_i(&P.st->wl_count[src]);
+    if (n == 0) return;
+    if (round >= P.max_rounds) {
+      if (gtid == 0) set_error(P, MCL_ERR_NO_CONVERGENCE);
+      return;
+    }
+    const int dst = src ^ 1;
+    const int* in = src ? P.wl1 : P.wl0;
+    int* out = dst ? P.wl1 : P.wl0;
+    const unsigned sc = stamp++;
+    const unsigned sq = stamp++;
+    if (gtid == 0) {
+      P.st->wl_count[dst] = 0;
+      P.st->c[C_LAWSON_ROUNDS] += 1;
+    }
+    // A: which queued edges are still non-Delaunay
+    for (int i = gtid; i < n; i += stride) {
+      const int e = ld_i(in + i);
+      if (edge_illegal(P, ld_ev(P, e), lc)) __stcg(P.cand + e, sc);
+    }
+    g.sync();
+    // D: a candidate wins if no candidate sharing one of its two faces has a
+    // higher priority this round
+    for (int i = gtid; i < n; i += stride) {
+      const int e = ld_i(in + i);
+      if (ld_i(reinterpret_cast<const int*>(P.cand) + e) != (int)sc) continue;
+      const int4 w = ld_en(P, e);
+      const unsigned pe = mix32((unsigned)e ^ sc);
+      bool win = true;
+      if (bad_h(P, w.x) || bad_h(P, w.y) || bad_h(P, w.z) || bad_h(P, w.w)) {
+        flag_error(P, MCL_ERR_DEGENERATE_INPUT);
+        continue;
+      }
+      const int wing[4] = {w.x >> 1, w.y >> 1, w.z >> 1, w.w >> 1};
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const int f = wing[k];
+        if ((unsigned)ld_i(reinterpret_cast<const int*>(P.cand) + f) == sc &&
+            mix32((unsigned)f ^ sc) > pe)
+          win = false;
+      }
+      if (win) __stcg(P.win + e, sc);
+    }
+    g.sync();
+    // B: winners flip and queue their four wing edges, losers queue themselves
+    int flips = 0;
+    for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
+      const int i = base + threadIdx.x;
+      int mine[4];
+      int k = 0;
+      if (i < n) {
+        const int e = ld_i(in + i);
+        if ((unsigned)ld_i(reinterpret_cast<const int*>(P.cand) + e) == sc) {
+          if ((unsigned)ld_i(reinterpret_cast<const int*>(P.win) + e) == sc) {
+            const int4 w = ld_en(P, e);
+            if (flip_edge(P, e)) ++flips;
+            const int wing[4] = {w.x >> 1, w.y >> 1, w.z >> 1, w.w >> 1};
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+              if (enqueue_once(P, wing[j], sq)) mine[k++] = wing[j];
+          } else if (enqueue_once(P, e, sq)) {
+            mine[k++] = e;
+          }
+        }
+      }
+      stage_push<4>(S, mine, k, out, &P.st->wl_count[dst], P.E, P.st);
+    }
+    stage_flush(S, out, &P.st->wl_count[dst], P.E, P.st);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) flips += __shfl_down_sync(kFull, flips, o);
+    if ((threadIdx.x & 31) == 0 && flips) atomicAdd(&P.st->c[C_LAWSON_FLIPS], (unsigned long long)flips);
+    g.sync();
+    src = dst;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Repair (1): revert vertices of non-positive faces until all faces are positive.
+__device__ __forceinline__ float2 qpos(const KParams& P, int v) {
+  return ld_i(P.vmark + v) ? P.pos_old[v] : ldpos(P, v);
+}
+
+__device__ void mark_vertex(const KParams& P, int v, int& fresh) {
+  if (ld_i(P.vmark + v) == 0 && atomicExch(P.vmark + v, 1) == 0) ++fresh;
+}
+
+__device__ bool phase_fixpoint(cg::grid_group& g, const KParams& P, LocalCounters& lc) {
+  const int stride = gridDim.x * blockDim.x;
+  const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+  for (int pass = 0; pass < 256; ++pass) {
+    // counters are triple-buffered: slot (pass+1)%3 was last read two barriers ago
+    const int slot = pass % 3;
+    if (gtid == 0) {
+      P.st->fix_new[(pass + 1) % 3] = 0;
+      P.st->fix_bad[(pass + 1) % 3] = 0;
+      P.st->c[C_FIX_PASSES] += 1;
+    }
+    int fresh = 0, bad = 0;
+    for (int e = gtid; e < P.E; e += stride) {
+      const int4 q = ld_ev(P, e);
+      if (q.x < 0) continue;
+      if (bad_v(P, q.x) || bad_v(P, q.y) || q.z >= P.V || q.w >= P.V) {
+        flag_error(P, MCL_ERR_DEGENERATE_INPUT);
+        continue;
+      }
+      const float2 a = qpos(P, q.x), b = qpos(P, q.y);
+      if (q.z >= 0 && orient_v(P, a, b, qpos(P, q.z), lc) <= 0) {
+        ++bad;
+        mark_vertex(P, q.x, fresh); mark_vertex(P, q.y, fresh); mark_vertex(P, q.z, fresh);
+      }
+      if (q.w >= 0 && orient_v(P, b, a, qpos(P, q.w), lc) <= 0) {
+        ++bad;
+        mark_vertex(P, q.x, fresh); mark_vertex(P, q.y, fresh); mark_vertex(P, q.w, fresh);
+      }
+    }
+    if (fresh) atomicAdd(&P.st->fix_new[slot], fresh);
+    if (bad) atomicAdd(&P.st->fix_bad[slot], bad);
+    g.sync();
+    const int nfresh = ld_i(&P.st->fix_new[slot]);
+    const int nbad = ld_i(&P.st->fix_bad[slot]);
+    if (nfresh == 0) {
+      if (nbad) {
+        if (gtid == 0) set_error(P, MCL_ERR_DEGENERATE_INPUT);
+        return false;
+      }
+      return true;
+    }
+  }
+  if (gtid == 0) set_error(P, MCL_ERR_NO_CONVERGENCE);
+  return false;
+}
+
+// ---------------------------------------------------------------------------
+// Repair (2): removal of a vertex from a valid triangulation by flipping its
+// spokes until it has degree 3, then merging its three faces.  Runs in one
+// thread; the caller owns every face of the vertex's star.
+__device__ int remove_vertex(const KParams& P, int v, LocalCounters& lc, int& flips) {
+  const float2 pv = ldpos(P, v);
+  for (int guard = 0; guard < 4096; ++guard) {
+    const int s0 = ld_i(P.vhe + v);
+    if (s0 < 0 || s0 >= 2 * P.E) return MCL_ERR_DEGENERATE_INPUT;
+    int deg = 0;
+    int h = s0;
+    int flipped = -1;
+    do {
+      ++deg;
+      if (flipped < 0) {
+        // flipping spoke h = v->w replaces faces (v,w,*) and (w,v,*) by (d,c,a), (c,d,b)
+        const int e = h >> 1;
+        const int4 q = ld_ev(P, e);
+        if (bad_v(P, q.x) || bad_v(P, q.y) || q.z >= P.V || q.w >= P.V) return MCL_ERR_DEGENERATE_INPUT;
+        if (q.z >= 0 && q.w >= 0) {
+          const float2 a = ldpos(P, q.x), b = ldpos(P, q.y), c = ldpos(P, q.z), d = ldpos(P, q.w);
+          if (orient_v(P, d, c, a, lc) > 0 && orient_v(P, c, d, b, lc) > 0) flipped = e;
+        }
+      }
+      h = he_prev(P, h) ^ 1;
+      if (h < 0 || h >= 2 * P.E) return MCL_ERR_DEGENERATE_INPUT;
+    } while (h != s0 && deg < 1024);
+    if (deg >= 1024) return MCL_ERR_CAPACITY;
+    if (deg == 3) break;
+    if (deg < 3 || flipped < 0) return MCL_ERR_NO_CONVERGENCE;
+    if (!flip_edge(P, flipped)) return MCL_ERR_DEGENERATE_INPUT;
+    ++flips;
+  }
+  // merge the three faces (v,x,y), (v,y,z), (v,z,x) into (x,y,z)
+  const int s0 = ld_i(P.vhe + v);
+  const int s1 = he_prev(P, s0) ^ 1;
+  const int s2 = he_prev(P, s1) ^ 1;
+  if ((he_prev(P, s2) ^ 1) != s0) return MCL_ERR_NO_CONVERGENCE;
+  const int lxy = he_next(P, s0), lyz = he_next(P, s1), lzx = he_next(P, s2);
+  if (bad_h(P, s1) || bad_h(P, s2) || bad_h(P, lxy) || bad_h(P, lyz) || bad_h(P, lzx)) return MCL_ERR_DEGENERATE_INPUT;
+  const int x = he_origin(P, lxy), y = he_origin(P, lyz), z = he_origin(P, lzx);
+  if (bad_v(P, x) || bad_v(P, y) || bad_v(P, z)) return MCL_ERR_DEGENERATE_INPUT;
+  he_set_face(P, lxy, z, lyz, lzx);
+  he_set_face(P, lyz, x, lzx, lxy);
+  he_set_face(P, lzx, y, lxy, lyz);
+  if (ld_i(P.vhe + x) == (s0 ^ 1)) __stcg(P.vhe + x, lxy);
+  if (ld_i(P.vhe + y) == (s1 ^ 1)) __stcg(P.vhe + y, lyz);
+  if (ld_i(P.vhe + z) == (s2 ^ 1)) __stcg(P.vhe + z, lzx);
+  const int es[3] = {s0 >> 1, s1 >> 1, s2 >> 1};
+  for (int k = 0; k < 3; ++k) {
+    P.vfree[3 * v + k] = es[k];
+    __stcg(P.ev + es[k], make_int4(-1, -1, -1, -1));
+    __stcg(P.en + es[k], make_int4(-1, -1, -1, -1));
+  }
+  P.vhint[v] = lxy;
+  P.vaux[v] = x;
+  __stcg(P.vhe + v, -1);
+  return MCL_OK;
+}
+
+// Iterate the outgoing half-edges of v counter-clockwise.
+template <typename F>
+__device__ bool for_spokes(const KParams& P, int v, F f) {
+  const int s0 = ld_i(P.vhe + v);
+  if (s0 < 0 || s0 >= 2 * P.E) return false;
+  int h = s0;
+  for (int k = 0; k < 1024; ++k) {
+    f(h);
+    h = he_prev(P, h) ^ 1;
+    if (h < 0 || h >= 2 * P.E) return false;
+    if (h == s0) return true;
+  }
+  return false;
+}
+
+__device__ bool phase_remove(cg::grid_group& g, const KParams& P, Stage& S, unsigned& stamp, LocalCounters& lc) {
+  const int stride = gridDim.x * blockDim.x;
+  const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+  int src = 0;
+  for (int round = 0;; ++round) {
+    const int n = ld_i(&P.st->vl_count[src]);
+    if (n == 0) return true;
+    if (round >= P.max_rounds) {
+      if (gtid == 0) set_error(P, MCL_ERR_NO_CONVERGENCE);
+      return false;
+    }
+    const int dst = src ^ 1;
+    const int* in = src ? P.vl1 : P.vl0;
+    int* out = dst ? P.vl1 : P.vl0;
+    const unsigned sk = stamp++;
+    if (gtid == 0) {
+      P.st->vl_count[dst] = 0;
+      P.st->c[C_REMOVE_ROUNDS] += 1;
+    }
+    // claim every face of the star
+    for (int i = gtid; i < n; i += stride) {
+      const int v = ld_i(in + i);
+      const unsigned long long key = ((unsigned long long)sk << 32) | (unsigned)(~mix32((unsigned)v ^ sk));
+      for_spokes(P, v, [&](int h) { atomicMax(P.claim + face_min(P, h), key); });
+    }
+    g.sync();
+    for (int i = gtid; i < n; i += stride) {
+      const int v = ld_i(in + i);
+      const unsigned long long key = ((unsigned long long)sk << 32) | (unsigned)(~mix32((unsigned)v ^ sk));
+      bool win = true;
+      const bool ok = for_spokes(P, v, [&](int h) {
+        if (__ldcg(P.claim + face_min(P, h)) != key) win = false;
+      });
+      P.vlocf[v] = (ok && win) ? 1 : 0;
+      if (!ok) set_error(P, MCL_ERR_DEGENERATE_INPUT);
+    }
+    g.sync();
+    int removed = 0, flips = 0;
+    for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
+      const int i = base + threadIdx.x;
+      int mine[1];
+      int k = 0;
+      if (i < n) {
+        const int v = ld_i(in + i);
+        if (__ldcg(P.vlocf + v) == 1) {
+          const int rc = remove_vertex(P, v, lc, flips);
+          if (rc != MCL_OK) set_error(P, rc);
+          else ++removed;
+        } else if (ld_i(&P.st->status) == MCL_OK) {
+          mine[k++] = v;
+        }
+      }
+      stage_push<1>(S, mine, k, out, &P.st->vl_count[dst], P.V, P.st);
+    }
+    stage_flush(S, out, &P.st->vl_count[dst], P.V, P.st);
+    if (removed) atomicAdd(&P.st->c[C_REMOVED], (unsigned long long)removed);
+    if (flips) atomicAdd(&P.st->c[C_REMOVAL_FLIPS], (unsigned long long)flips);
+    g.sync();
+    src = dst;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Point location: visibility walk with exact orientation tests from half-edge h.
+// Returns a half-edge of the face containing p; *on is the half-edge p lies on
+// (or -1).  Errors are returned as negative MCL codes.
+__device__ int locate(const KParams& P, float2 p, int h, int* on, LocalCounters& lc) {
+  *on = -1;
+  for (int it = 0; it < P.walk_cap; ++it) {
+    if (h < 0 || h >= 2 * P.E) return -MCL_ERR_DEGENERATE_INPUT;
+    const int hs[3] = {h, he_next(P, h), he_prev(P, h)};
+    int o[3];
+    for (int k = 0; k < 3; ++k) {
+      if (hs[k] < 0 || hs[k] >= 2 * P.E) return -MCL_ERR_DEGENERATE_INPUT;
+      o[k] = he_origin(P, hs[k]);
+      if (o[k] < 0 || o[k] >= P.V) return -MCL_ERR_DEGENERATE_INPUT;
+    }
+    const float2 q[3] = {ldpos(P, o[0]), ldpos(P, o[1]), ldpos(P, o[2])};
+    int s[3] = {1, 1, 1};
+    int cross = -1;
+    const int start = it % 3;
+    for (int k = 0; k < 3 && cross < 0; ++k) {
+      const int i = (start + k) % 3;
+      s[i] = orient_v(P, q[i], q[(i + 1) % 3], p, lc);
+      if (s[i] < 0) cross = i;
+    }
+    if (cross >= 0) {
+      const int t = hs[cross] ^ 1;
+      if (he_apex(P, t) < 0) return -MCL_ERR_DEGENERATE_INPUT;  // outside the bounding square
+      h = t;
+      continue;
+    }
+    int zeros = 0, zi = -1;
+    for (int i = 0; i < 3; ++i)
+      if (s[i] == 0) { ++zeros; zi = i; }
+    if (zeros >= 2) return -MCL_ERR_DEGENERATE_INPUT;  // coincides with a vertex
+    if (zeros == 1) {
+      if (he_apex(P, hs[zi] ^ 1) < 0) return -MCL_ERR_DEGENERATE_INPUT;  // on the bounding square
+      *on = hs[zi];
+    }
+    return h;
+  }
+  return -MCL_ERR_NO_CONVERGENCE;
+}
+
+// 1-to-3 split of the face of half-edge h0 by v with free edges f0, f1, f2.
+__device__ void split13(const KParams& P, int v, int h0, const int* f) {
+  const int h1 = he_next(P, h0), h2 = he_prev(P, h0);
+  const int x0 = he_origin(P, h0), x1 = he_origin(P, h1), x2 = he_origin(P, h2);
+  const int f0 = f[0], f1 = f[1], f2 = f[2];
+  __stcg(P.ev + f0, make_int4(v, x0, x1, x2));
+  __stcg(P.ev + f1, make_int4(v, x1, x2, x0));
+  __stcg(P.ev + f2, make_int4(v, x2, x0, x1));
+  __stcg(P.en + f0, make_int4(h0, 2 * f1 + 1, 2 * f2, h2));
+  __stcg(P.en + f1, make_int4(h1, 2 * f2 + 1, 2 * f0, h0));
+  __stcg(P.en + f2, make_int4(h2, 2 * f0 + 1, 2 * f1, h1));
+  he_set_face(P, h0, v, 2 * f1 + 1, 2 * f0);
+  he_set_face(P, h1, v, 2 * f2 + 1, 2 * f1);
+  he_set_face(P, h2, v, 2 * f0 + 1, 2 * f2);
+  __stcg(P.vhe + v, 2 * f0);
+}
+
+// 2-to-4 split of the edge of half-edge g (v lies on it) with free edges f0..f2.
+__device__ void split24(const KParams& P, int v, int g, const int* f) {
+  const int h0 = g, h1 = g ^ 1;
+  const int n0 = he_next(P, h0), p0 = he_prev(P, h0);
+  const int n1 = he_next(P, h1), p1 = he_prev(P, h1);
+  const int a = he_origin(P, h0), b = he_origin(P, h1);
+  const int c = he_apex(P, h0), d = he_apex(P, h1);
+  const int f0 = f[0], f1 = f[1], f2 = f[2];
+  // faces: (a,v,c) (v,b,c) (b,v,d) (v,a,d)
+  he_set_origin(P, h1, v);
+  he_set_face(P, h0, c, 2 * f1, p0);
+  he_set_face(P, h1, d, n1, 2 * f2 + 1);
+  he_set_face(P, p0, v, h0, 2 * f1);
+  he_set_face(P, n0, v, 2 * f1 + 1, 2 * f0);
+  he_set_face(P, p1, v, 2 * f0 + 1, 2 * f2);
+  he_set_face(P, n1, v, 2 * f2 + 1, h1);
+  __stcg(P.ev + f0, make_int4(v, b, c, d));
+  __stcg(P.en + f0, make_int4(n0, 2 * f1 + 1, 2 * f2, p1));
+  __stcg(P.ev + f1, make_int4(v, c, a, b));
+  __stcg(P.en + f1, make_int4(p0, h0, 2 * f0, n0));
+  __stcg(P.ev + f2, make_int4(v, d, b, a));
+  __stcg(P.en + f2, make_int4(p1, 2 * f0 + 1, h1, n1));
+  __stcg(P.vhe + v, 2 * f0);
+  if (ld_i(P.vhe + b) == h1) __stcg(P.vhe + b, n0);
+}
+
+__device__ int insert_start(const KParams& P, int v) {
+  int h = __ldcg(P.vhint + v);
+  if (h >= 0 && h < 2 * P.E && he_origin(P, h) >= 0 && he_apex(P, h) >= 0) return h;
+  const int x = __ldcg(P.vaux + v);
+  if (x >= 0 && x < P.V) {
+    h = ld_i(P.vhe + x);
+    if (h >= 0 && h < 2 * P.E) return h;
+  }
+  return 0;  // half-edge 0 is never freed: edge 0 is a side of the bounding square
+}
+
+__device__ bool phase_insert(cg::grid_group& g, const KParams& P, Stage& S, Stage& S2, unsigned& stamp,
+                             LocalCounters& lc) {
+  const int stride = gridDim.x * blockDim.x;
+  const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+  int src = 0;
+  for (int round = 0;; ++round) {
+    const int n = ld_i(&P.st->vl_count[src]);
+    if (n == 0) return true;
+    if (round >= P.max_rounds) {
+      if (gtid == 0) set_error(P, MCL_ERR_NO_CONVERGENCE);
+      return false;
+    }
+    const int dst = src ^ 1;
+    const int* in = src ? P.vl1 : P.vl0;
+    int* out = dst ? P.vl1 : P.vl0;
+    const unsigned sk = stamp++;
+    const unsigned sq = stamp++;
+    if (gtid == 0) {
+      P.st->vl_count[dst] = 0;
+      P.st->wl_count[0] = 0;
+      P.st->c[C_INSERT_ROUNDS] += 1;
+    }
+    // locate and claim
+    for (int i = gtid; i < n; i += stride) {
+      const int v = ld_i(in + i);
+      int on = -1;
+      const int h = locate(P, ldpos(P, v), insert_start(P, v), &on, lc);
+      if (h < 0) {
+        set_error(P, -h);
+        P.vlocf[v] = -1;
+        continue;
+      }
+      P.vloc[v] = on >= 0 ? on : h;
+      P.vlocf[v] = on >= 0 ? 2 : 0;  // bit 1: on the edge of vloc, bit 0: winner
+      const unsigned long long key = ((unsigned long long)sk << 32) | (unsigned)(~mix32((unsigned)v ^ sk));
+      if (on >= 0) {
+        atomicMax(P.claim + face_min(P, on), key);
+        atomicMax(P.claim + face_min(P, on ^ 1), key);
+      } else {
+        atomicMax(P.claim + face_min(P, h), key);
+      }
+    }
+    g.sync();
+    for (int i = gtid; i < n; i += stride) {
+      const int v = ld_i(in + i);
+      const int fl = __ldcg(P.vlocf + v);
+      if (fl < 0) continue;
+      const unsigned long long key = ((unsigned long long)sk << 32) | (unsigned)(~mix32((unsigned)v ^ sk));
+      const int h = __ldcg(P.vloc + v);
+      bool win = __ldcg(P.claim + face_min(P, h)) == key;
+      if (fl & 2) win = win && __ldcg(P.claim + face_min(P, h ^ 1)) == key;
+      if (win) P.vlocf[v] = fl | 1;
+    }
+    g.sync();
+    int inserted = 0;
+    for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
+      const int i = base + threadIdx.x;
+      int mine[8];
+      int k = 0;
+      int again[1];
+      int ka = 0;
+      if (i < n) {
+        const int v = ld_i(in + i);
+        const int fl = __ldcg(P.vlocf + v);
+        if (fl >= 0 && (fl & 1)) {
+          const int f[3] = {__ldcg(P.vfree + 3 * v), __ldcg(P.vfree + 3 * v + 1), __ldcg(P.vfree + 3 * v + 2)};
+          int link[4];
+          int nl = 0;
+          if ((unsigned)f[0] >= (unsigned)P.E || (unsigned)f[1] >= (unsigned)P.E || (unsigned)f[2] >= (unsigned)P.E ||
+              bad_h(P, __ldcg(P.vloc + v))) {
+            flag_error(P, MCL_ERR_DEGENERATE_INPUT);
+          } else if (fl & 2) {
+            const int gg = __ldcg(P.vloc + v);
+            link[nl++] = he_prev(P, gg);
+            link[nl++] = he_next(P, gg);
+            link[nl++] = he_prev(P, gg ^ 1);
+            link[nl++] = he_next(P, gg ^ 1);
+            split24(P, v, gg, f);
+          } else {
+            const int h = __ldcg(P.vloc + v);
+            link[nl++] = h;
+            link[nl++] = he_next(P, h);
+            link[nl++] = he_prev(P, h);
+            split13(P, v, h, f);
+          }
+          ++inserted;
+          for (int j = 0; j < nl; ++j)
+            if (bad_h(P, link[j])) { link[j] = 0; flag_error(P, MCL_ERR_DEGENERATE_INPUT); }
+          for (int j = 0; j < nl; ++j)
+            if (enqueue_once(P, link[j] >> 1, sq)) mine[k++] = link[j] >> 1;
+          for (int j = 0; j < 3; ++j)
+            if (enqueue_once(P, f[j], sq)) mine[k++] = f[j];
+        } else if (fl >= 0) {
+          __stcg(P.vhint + v, __ldcg(P.vloc + v));
+          again[ka++] = v;
+        }
+      }
+      stage_push<8>(S, mine, k, P.wl0, &P.st->wl_count[0], P.E, P.st);
+      stage_push<1>(S2, again, ka, out, &P.st->vl_count[dst], P.V, P.st);
+    }
+    stage_flush(S, P.wl0, &P.st->wl_count[0], P.E, P.st);
+    stage_flush(S2, out, &P.st->vl_count[dst], P.V, P.st);
+    (void)inserted;
+    g.sync();
+    phase_lawson(g, P, S, 0, stamp, lc);
+    g.sync();
+    src = dst;
+  }
+}
+
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kThreads) k_engine(KParams P) {
+  cg::grid_group g = cg::this_grid();
+  __shared__ Stage S, S2;
+  if (threadIdx.x == 0) { S.n = 0; S2.n = 0; }
+  __syncthreads();
+  LocalCounters lc = {0, 0, 0, 0, 0, 0, 0};
+  unsigned stamp = ld_i(reinterpret_cast<const int*>(&P.st->epoch));
+  const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+
+  if (P.mode == ENGINE_BUILD) {
+    phase_insert(g, P, S, S2, stamp, lc);
+  } else {
+    if (P.move_mode != MOVE_NONE) {
+      phase_move(P);
+      g.sync();
+    }
+    const unsigned q0 = stamp++;
+    phase_classify(P, S, q0, lc);
+    g.sync();
+    const int inverted = ld_i(&P.st->inverted);
+    if (inverted == 0) {
+      phase_lawson(g, P, S, 0, stamp, lc);
+    } else {
+      if (gtid == 0) P.st->c[C_INVERTED] += (unsigned long long)inverted;
+      // (1) revert until valid
+      bool ok = phase_fixpoint(g, P, lc);
+      g.sync();
+      if (ok) {
+        // removal list: reverted vertices that actually moved
+        const int stride = gridDim.x * blockDim.x;
+        if (gtid == 0) { P.st->vl_count[0] = 0; P.st->vl_count[1] = 0; }
+        g.sync();
+        for (int base = blockIdx.x * blockDim.x; base < P.V; base += stride) {
+          const int v = base + threadIdx.x;
+          int mine[1];
+          int k = 0;
+          if (v < P.V && ld_i(P.vmark + v) && !P.vfix[v]) {
+            const float2 pn = ldpos(P, v), po = P.pos_old[v];
+            if (__float_as_uint(pn.x) != __float_as_uint(po.x) || __float_as_uint(pn.y) != __float_as_uint(po.y)) {
+              P.target[v] = pn;
+              __stcg(P.pos + v, po);
+              mine[k++] = v;
+            }
+          }
+          stage_push<1>(S, mine, k, P.vl0, &P.st->vl_count[0], P.V, P.st);
+        }
+        stage_flush(S, P.vl0, &P.st->vl_count[0], P.V, P.st);
+        g.sync();
+        const int nrem = ld_i(&P.st->vl_count[0]);
+        if (gtid == 0) P.st->c[C_REVERTED] += (unsigned long long)nrem;
+        // (2) remove them (list ends in vl[0] or vl[1]; reinsertion needs the
+        // full list, so it is rebuilt from vmark afterwards)
+        ok = phase_remove(g, P, S, stamp, lc);
+        g.sync();
+        // (3) Lawson over every edge of the reduced mesh
+        if (gtid == 0) { P.st->wl_count[0] = 0; P.st->inverted = 0; }
+        g.sync();
+        const unsigned q1 = stamp++;
+        phase_classify(P, S, q1, lc);
+        g.sync();
+        phase_lawson(g, P, S, 0, stamp, lc);
+        g.sync();
+        // (4) reinsert at the new positions
+        if (gtid == 0) { P.st->vl_count[0] = 0; P.st->vl_count[1] = 0; }
+        g.sync();
+        for (int base = blockIdx.x * blockDim.x; base < P.V; base += stride) {
+          const int v = base + threadIdx.x;
+          int mine[1];
+          int k = 0;
+          if (v < P.V && ld_i(P.vhe + v) < 0 && ld_i(P.vmark + v)) {
+            __stcg(P.pos + v, __ldcg(P.target + v));
+            mine[k++] = v;
+          }
+          stage_push<1>(S, mine, k, P.vl0, &P.st->vl_count[0], P.V, P.st);
+        }
+        stage_flush(S, P.vl0, &P.st->vl_count[0], P.V, P.st);
+        g.sync();
+        if (ok) phase_insert(g, P, S, S2, stamp, lc);
+      }
+    }
+  }
+  flush_counters(P, lc);
+  g.sync();
+  if (gtid == 0) P.st->epoch = stamp;
+}
+
+// ---------------------------------------------------------------------------
+// Host side.
+static thread_local std::string g_last_error;
+
+static int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+static int cuda_fail(cudaError_t e, const char* what) {
+  return fail(e == cudaErrorMemoryAllocation ? MCL_ERR_OUT_OF_MEMORY : MCL_ERR_CUDA,
+              std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call)                                   \
+  do {                                             \
+    cudaError_t _e = (call);                       \
+    if (_e != cudaSuccess) return cuda_fail(_e, #call); \
+  } while (0)
+
+static void free_mesh(mcl_mesh* m) {
+  if (!m) return;
+  void* ptrs[] = {m->pos[0], m->pos[1], m->ev, m->en, m->vhe, m->vfix, m->cand, m->win, m->qmark,
+                  m->wl[0], m->wl[1], m->vl[0], m->vl[1], m->vmark, m->claim, m->vfree, m->vhint,
+                  m->vaux, m->vloc, m->vlocf, m->target, m->dstage, m->scratch, m->st};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (m->st_host) cudaFreeHost(m->st_host);
+  delete m;
+}
+
+static int alloc_mesh(int64_t V, int64_t E, mcl_mesh** out) {
+  if (V < 4 || E < 5 || V > (1ll << 30) || E > (1ll << 29))
+    return fail(MCL_ERR_INVALID_ARGUMENT, "mesh size out of range");
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  mcl_mesh* m = new mcl_mesh();
+  std::memset(m, 0, sizeof(*m));
+  m->device = dev;
+  m->V = V;
+  m->E = E;
+  m->T = 2 * (V - 4) + 2;
+  m->cur = 0;
+  m->valid_cur = true;
+  cudaError_t e = cudaSuccess;
+  auto A = [&](void** p, size_t bytes) {
+    if (e == cudaSuccess) e = cudaMalloc(p, bytes);
+  };
+  A((void**)&m->pos[0], 8 * V);
+  A((void**)&m->pos[1], 8 * V);
+  A((void**)&m->ev, 16 * E);
+  A((void**)&m->en, 16 * E);
+  A((void**)&m->vhe, 4 * V);
+  A((void**)&m->vfix, V);
+  A((void**)&m->cand, 4 * E);
+  A((void**)&m->win, 4 * E);
+  A((void**)&m->qmark, 4 * E);
+  A((void**)&m->wl[0], 4 * E);
+  A((void**)&m->wl[1], 4 * E);
+  A((void**)&m->vl[0], 4 * V);
+  A((void**)&m->vl[1], 4 * V);
+  A((void**)&m->vmark, 4 * V);
+  A((void**)&m->claim, 8 * 2 * E);
+  A((void**)&m->vfree, 12 * V);
+  A((void**)&m->vhint, 4 * V);
+  A((void**)&m->vaux, 4 * V);
+  A((void**)&m->vloc, 4 * V);
+  A((void**)&m->vlocf, 4 * V);
+  A((void**)&m->target, 8 * V);
+  A((void**)&m->dstage, 8 * V);
+  A((void**)&m->scratch, 64);
+  A((void**)&m->st, sizeof(DevState));
+  if (e == cudaSuccess) e = cudaMallocHost((void**)&m->st_host, sizeof(DevState));
+  if (e != cudaSuccess) {
+    free_mesh(m);
+    return cuda_fail(e, "cudaMalloc(mesh)");
+  }
+  e = cudaMemset(m->cand, 0, 4 * E);
+  if (e == cudaSuccess) e = cudaMemset(m->win, 0, 4 * E);
+  if (e == cudaSuccess) e = cudaMemset(m->qmark, 0, 4 * E);
+  if (e == cudaSuccess) e = cudaMemset(m->claim, 0, 16 * E);
+  if (e == cudaSuccess) e = cudaMemset(m->vaux, 0xff, 4 * V);
+  if (e == cudaSuccess) e = cudaMemset(m->vhint, 0xff, 4 * V);
+  DevState s;
+  std::memset(&s, 0, sizeof(s));
+  s.epoch = 1;
+  if (e == cudaSuccess) e = cudaMemcpy(m->st, &s, sizeof(s), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    free_mesh(m);
+    return cuda_fail(e, "mesh init");
+  }
+  int nsm = 0, per_sm = 0;
+  e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_engine, kThreads, 0);
+  if (e != cudaSuccess || per_sm < 1) {
+    free_mesh(m);
+    return cuda_fail(e == cudaSuccess ? cudaErrorInvalidConfiguration : e, "occupancy(k_engine)");
+  }
+  m->coop_threads = kThreads;
+  m->coop_blocks = nsm * per_sm;
+  *out = m;
+  return MCL_OK;
+}
+
+// Convert and validate the reference AoS arrays; returns false on malformed input.
+static bool aos_to_soa(const mcl_aos_view* a, std::vector<int4>& ev, std::vector<int4>& en, std::vector<int>& vhe,
+                       std::string& why) {
+  const int64_t V = a->V, HE = a->HE, E = HE / 2;
+  if (HE % 2 || V < 4 || E < 5) { why = "bad sizes"; return false; }
+  const int32_t* he = a->he;
+  ev.assign(E, make_int4(0, 0, 0, 0));
+  en.assign(E, make_int4(0, 0, 0, 0));
+  std::vector<int> prev(HE, -1);
+  for (int64_t h = 0; h < HE; ++h) {
+    const int nx = he[4 * h], v = he[4 * h + 1], t = he[4 * h + 2], op = he[4 * h + 3];
+    if (nx < 0 || nx >= HE || v < 0 || v >= V) { why = "half-edge index out of range"; return false; }
+    if (t >= 0 && (op < 0 || op >= V)) { why = "opposite vertex out of range"; return false; }
+    if (prev[nx] != -1) { why = "two half-edges share a next"; return false; }
+    prev[nx] = (int)h;
+  }
+  for (int64_t h = 0; h < HE; ++h) {
+    const int nx = he[4 * h];
+    // the twin's origin must be this half-edge's destination
+    if (he[4 * (h ^ 1) + 1] != he[4 * nx + 1]) { why = "twin/next inconsistent"; return false; }
+    if (he[4 * h + 2] >= 0) {
+      const int n2 = he[4 * nx], n3 = he[4 * n2];
+      if (n3 != h) { why = "inner face is not a triangle"; return false; }
+      if (he[4 * h + 3] != he[4 * n2 + 1]) { why = "opposite vertex inconsistent"; return false; }
+    }
+  }
+  for (int64_t e = 0; e < E; ++e) {
+    const int32_t* h0 = he + 8 * e;
+    const int32_t* h1 = h0 + 4;
+    ev[e] = make_int4(h0[1], h1[1], h0[2] >= 0 ? h0[3] : -1, h1[2] >= 0 ? h1[3] : -1);
+    en[e] = make_int4(h0[0], prev[2 * e], h1[0], prev[2 * e + 1]);
+  }
+  vhe.assign(V, -1);
+  for (int64_t v = 0; v < V; ++v) {
+    const int h = a->v[2 * v + 1];
+    if (h < 0 || h >= HE || he[4 * h + 1] != v) { why = "vertex he is not outgoing"; return false; }
+    vhe[v] = h;
+  }
+  return true;
+}
+
+static int upload_soa(mcl_mesh* m, const mcl_float2* pos, const std::vector<int4>& ev, const std::vector<int4>& en,
+                      const std::vector<int>& vhe) {
+  std::vector<unsigned char> fix(m->V, 0);
+  for (int i = 0; i < 4 && i < m->V; ++i) fix[i] = 1;
+  m->cur = 0;
+  m->valid_cur = true;
+  CK(cudaMemcpy(m->pos[0], pos, 8 * m->V, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(m->pos[1], pos, 8 * m->V, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(m->ev, ev.data(), 16 * m->E, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(m->en, en.data(), 16 * m->E, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(m->vhe, vhe.data(), 4 * m->V, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(m->vfix, fix.data(), m->V, cudaMemcpyHostToDevice));
+  return MCL_OK;
+}
+
+static KParams make_params(mcl_mesh* m, int mode) {
+  KParams P;
+  std::memset(&P, 0, sizeof(P));
+  P.V = (int)m->V;
+  P.E = (int)m->E;
+  P.ev = m->ev;
+  P.en = m->en;
+  P.vhe = m->vhe;
+  P.vfix = m->vfix;
+  P.cand = m->cand;
+  P.win = m->win;
+  P.qmark = m->qmark;
+  P.wl0 = m->wl[0];
+  P.wl1 = m->wl[1];
+  P.vl0 = m->vl[0];
+  P.vl1 = m->vl[1];
+  P.vmark = m->vmark;
+  P.claim = m->claim;
+  P.vfree = m->vfree;
+  P.vhint = m->vhint;
+  P.vaux = m->vaux;
+  P.vloc = m->vloc;
+  P.vlocf = m->vlocf;
+  P.target = m->target;
+  P.st = m->st;
+  P.mode = mode;
+  P.max_rounds = 1 << 16;
+  P.walk_cap = 1 << 18;
+  return P;
+}
+
+// Reset the per-call part of the device state (counters, lists, status).
+__global__ void k_reset_state(DevState* st) {
+  const unsigned ep = st->epoch;
+  DevState z;
+  memset(&z, 0, sizeof(z));
+  z.epoch = ep;
+  *st = z;
+}
+
+static int launch_engine(mcl_mesh* m, KParams& P, cudaStream_t s) {
+  k_reset_state<<<1, 1, 0, s>>>(m->st);
+  CK(cudaGetLastError());
+  CK(cudaMemsetAsync(m->vmark, 0, 4 * m->V, s));
+  void* args[] = {&P};
+  CK(cudaLaunchCooperativeKernel((void*)k_engine, dim3(m->coop_blocks), dim3(m->coop_threads), args, 0, s));
+  return MCL_OK;
+}
+
+static void fill_stats(const DevState& s, mcl_step_stats* o) {
+  o->inverted_faces = (int64_t)s.c[C_INVERTED];
+  o->reverted_vertices = (int64_t)s.c[C_REVERTED];
+  o->removed_vertices = (int64_t)s.c[C_REMOVED];
+  o->lawson_flips = (int64_t)s.c[C_LAWSON_FLIPS];
+  o->lawson_rounds = (int64_t)s.c[C_LAWSON_ROUNDS];
+  o->removal_flips = (int64_t)s.c[C_REMOVAL_FLIPS];
+  o->insert_rounds = (int64_t)s.c[C_INSERT_ROUNDS];
+  o->incircle_tests = (int64_t)s.c[C_INCIRCLE];
+  o->incircle_fp64 = (int64_t)s.c[C_INCIRCLE_FP64];
+  o->incircle_exact = (int64_t)s.c[C_INCIRCLE_EXACT];
+  o->orient_fp64 = (int64_t)s.c[C_ORIENT_FP64];
+  o->orient_exact = (int64_t)s.c[C_ORIENT_EXACT];
+  o->sos_decisions = (int64_t)s.c[C_SOS];
+  o->status = s.status;
+}
+
+static int finish(mcl_mesh* m, cudaStream_t s, mcl_step_stats* stats) {
+  if (!stats) return MCL_OK;
+  CK(cudaMemcpyAsync(m->st_host, m->st, sizeof(DevState), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  fill_stats(*m->st_host, stats);
+  m->last_status = m->st_host->status;
+  if (m->st_host->status != MCL_OK)
+    return fail(m->st_host->status, std::string("device status: ") + mcl_status_string(m->st_host->status));
+  return MCL_OK;
+}
+
+// Run the engine.  Position buffers: pos[cur] holds the positions the mesh
+// must be repaired to; when valid_cur is false (points were moved since the
+// last validated state) pos[cur^1] holds the validated positions.  A fused move
+// (valid_cur true) reads pos[cur] and writes pos[cur^1].
+static int run_step(mcl_mesh* m, int move_mode, const float2* d, cudaStream_t s, mcl_step_stats* stats) {
+  KParams P = make_params(m, ENGINE_STEP);
+  if (move_mode != MOVE_NONE) {
+    P.pos_old = m->pos[m->cur];
+    P.pos = m->pos[m->cur ^ 1];
+    P.move_mode = move_mode;
+    P.disp = d;
+    m->cur ^= 1;
+  } else {
+    P.pos = m->pos[m->cur];
+    P.pos_old = m->valid_cur ? m->pos[m->cur] : m->pos[m->cur ^ 1];
+  }
+  int rc = launch_engine(m, P, s);
+  if (rc != MCL_OK) return rc;
+  m->valid_cur = true;
+  return finish(m, s, stats);
+}
+
+}  // namespace mcl
+
+using namespace mcl;
+
+// ---------------------------------------------------------------------------
+// Plain move kernels for the API calls that only move (movePoints without a step).
+__global__ void k_move_only(int V, const unsigned char* fix, const float2* src, float2* dst, const float2* d,
+                            const float* dt, const float2* vel, int mode) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= V) return;
+  float2 p = src[v];
+  if (!fix[v]) {
+    if (mode == MOVE_DISPLACE) {
+      p.x = fadd(p.x, d[v].x);
+      p.y = fadd(p.y, d[v].y);
+    } else {
+      p.x = fadd(p.x, fmul(vel[v].x, dt[v]));
+      p.y = fadd(p.y, fmul(vel[v].y, dt[v]));
+    }
+  }
+  dst[v] = p;
+}
+
+extern "C" {
+
+const char* mcl_status_string(int status) {
+  switch (status) {
+    case MCL_OK: return "ok";
+    case MCL_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case MCL_ERR_CUDA: return "CUDA error";
+    case MCL_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case MCL_ERR_NO_CONVERGENCE: return "iteration cap reached";
+    case MCL_ERR_CAPACITY: return "buffer capacity exceeded";
+    case MCL_ERR_DEGENERATE_INPUT: return "degenerate input (duplicate point, point outside the bounding square, or invalid mesh)";
+    case MCL_ERR_PREDICATE: return "exact predicate capacity exceeded";
+    case MCL_ERR_NO_DEVICE: return "no CUDA device";
+    default: return "unknown status";
+  }
+}
+
+const char* mcl_last_error(void) { return g_last_error.c_str(); }
+int mcl_version(void) { return 1; }
+
+int mcl_mesh_create_from_aos(const mcl_aos_view* a, mcl_mesh** out) {
+  if (!a || !out || !a->pos || !a->v || !a->he) return fail(MCL_ERR_INVALID_ARGUMENT, "null argument");
+  std::vector<int4> ev, en;
+  std::vector<int> vhe;
+  std::string why;
+  if (!aos_to_soa(a, ev, en, vhe, why)) return fail(MCL_ERR_INVALID_ARGUMENT, "malformed mesh: " + why);
+  mcl_mesh* m = nullptr;
+  int rc = alloc_mesh(a->V, a->HE / 2, &m);
+  if (rc != MCL_OK) return rc;
+  rc = upload_soa(m, a->pos, ev, en, vhe);
+  if (rc != MCL_OK) { free_mesh(m); return rc; }
+  *out = m;
+  return MCL_OK;
+}
+
+int mcl_mesh_upload_aos(mcl_mesh* m, const mcl_aos_view* a) {
+  if (!m || !a) return fail(MCL_ERR_INVALID_ARGUMENT, "null argument");
+  if (a->V != m->V || a->HE != 2 * m->E) return fail(MCL_ERR_INVALID_ARGUMENT, "size mismatch");
+  std::vector<int4> ev, en;
+  std::vector<int> vhe;
+  std::string why;
+  if (!aos_to_soa(a, ev, en, vhe, why)) return fail(MCL_ERR_INVALID_ARGUMENT, "malformed mesh: " + why);
+  return upload_soa(m, a->pos, ev, en, vhe);
+}
+
+int mcl_mesh_destroy(mcl_mesh* m) {
+  if (!m) return MCL_OK;
+  cudaDeviceSynchronize();
+  free_mesh(m);
+  return MCL_OK;
+}
+
+int mcl_mesh_sizes(const mcl_mesh* m, int64_t* V, int64_t* HE, int64_t* T) {
+  if (!m) return fail(MCL_ERR_INVALID_ARGUMENT, "null mesh");
+  if (V) *V = m->V;
+  if (HE) *HE = 2 * m->E;
+  if (T) *T = m->T;
+  return MCL_OK;
+}
+
+int mcl_mesh_positions(mcl_mesh* m, mcl_float2** pos_dev) {
+  if (!m || !pos_dev) return fail(MCL_ERR_INVALID_ARGUMENT, "null argument");
+  *pos_dev = reinterpret_cast<mcl_float2*>(m->pos[m->cur]);
+  return MCL_OK;
+}
+
+int mcl_mesh_copy_positions(mcl_mesh* m, mcl_float2* dst, int to_host, void* stream) {
+  if (!m || !dst) return fail(MCL_ERR_INVALID_ARGUMENT, "null argument");
+  CK(cudaMemcpyAsync(dst, m->pos[m->cur], 8 * m->V, to_host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice,
+                     (cudaStream_t)stream));
+  if (to_host) CK(cudaStreamSynchronize((cudaStream_t)stream));
+  return MCL_OK;
+}
+
+int mcl_mesh_download_aos(mcl_mesh* m, mcl_float2* pos, int32_t* v, int32_t* he, int32_t* t) {
+  if (!m) return fail(MCL_ERR_INVALID_ARGUMENT, "null mesh");
+  CK(cudaDeviceSynchronize());
+  const int64_t V = m->V, E = m->E, HE = 2 * E;
+  if (pos) CK(cudaMemcpy(pos, m->pos[m->cur], 8 * V, cudaMemcpyDeviceToHost));
+  if (!v && !he && !t) return MCL_OK;
+  std::vector<int4> ev(E), en(E);
+  std::vector<int> vhe(V);
+  CK(cudaMemcpy(ev.data(), m->ev, 16 * E, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(en.data(), m->en, 16 * E, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(vhe.data(), m->vhe, 4 * V, cudaMemcpyDeviceToHost));
+  auto org = [&](int64_t h) { const int4& q = ev[h >> 1]; return (h & 1) ? q.y : q.x; };
+  auto apex = [&](int64_t h) { const int4& q = ev[h >> 1]; return (h & 1) ? q.w : q.z; };
+  auto nxt = [&](int64_t h) { const int4& q = en[h >> 1]; return (h & 1) ? q.z : q.x; };
+  auto prv = [&](int64_t h) { const int4& q = en[h >> 1]; return (h & 1) ? q.w : q.y; };
+  std::vector<int> face(HE, -1);
+  int64_t nf = 0;
+  std::vector<int> owner;
+  owner.reserve(m->T);
+  for (int64_t h = 0; h < HE; ++h) {
+    if (apex(h) < 0 || org(h) < 0) continue;
+    const int64_t n = nxt(h), p = prv(h);
+    if (h < n && h < p) {
+      face[h] = (int)nf++;
+      owner.push_back((int)h);
+    }
+  }
+  for (int64_t h = 0; h < HE; ++h) {
+    if (apex(h) < 0 || org(h) < 0) continue;
+    const int64_t n = nxt(h), p = prv(h);
+    face[h] = face[std::min(h, std::min(n, p))];
+  }
+  if (he) {
+    for (int64_t h = 0; h < HE; ++h) {
+      he[4 * h] = nxt(h);
+      he[4 * h + 1] = org(h);
+      he[4 * h + 2] = face[h];
+      he[4 * h + 3] = apex(h) >= 0 ? apex(h) : -1;
+    }
+  }
+  if (v) {
+    for (int64_t i = 0; i < V; ++i) {
+      v[2 * i] = (int)i;
+      v[2 * i + 1] = vhe[i];
+    }
+  }
+  if (t) {
+    for (int64_t i = 0; i < (int64_t)owner.size() && i < m->T; ++i) t[i] = owner[i];
+  }
+  if (nf != m->T) return fail(MCL_ERR_DEGENERATE_INPUT, "face count mismatch on download");
+  return MCL_OK;
+}
+
+int mcl_move(mcl_mesh* m, const mcl_float2* d_dev, void* stream) {
+  if (!m || !d_dev) return fail(MCL_ERR_INVALID_ARGUMENT, "null argument");
+  cudaStream_t s = (cudaStream_t)stream;
+  const int src = m->cur, dst = m->valid_cur ? m->cur ^ 1 : m->cur;
+  k_move_only<<<(unsigned)((m->V + 255) / 256), 256, 0, s>>>((int)m->V, m->vfix, m->pos[src], m->pos[dst],
+                                                              (const float2*)d_dev, nullptr, nullptr, MOVE_DISPLACE);
+  CK(cudaGetLastError());
+  m->cur = dst;
+  m->valid_cur = false;
+  return MCL_OK;
+}
+
+int mcl_integrate(mcl_mesh* m, const float* dt_dev, const mcl_float2* v_dev, void* stream) {
+  if (!m || !dt_dev || !v_dev) return fail(MCL_ERR_INVALID_ARGUMENT, "null argument");
+  cudaStream_t s = (cudaStream_t)stream;
+  const int src = m->cur, dst = m->valid_cur ? m->cur ^ 1 : m->cur;
+  k_move_only<<<(unsigned)((m->V + 255) / 256), 256, 0, s>>>((int)m->V, m->vfix, m->pos[src], m->pos[dst], nullptr,
+                                                              dt_dev, (const float2*)v_dev, MOVE_INTEGRATE);
+  CK(cudaGetLastError());
+  m->cur = dst;
+  m->valid_cur = false;
+  return MCL_OK;
+}
+
+int mcl_untangle(mcl_mesh* m, void* stream, mcl_step_stats* stats) {
+  if (!m) return fail(MCL_ERR_INVALID_ARGUMENT, "null mesh");
+  return run_step(m, MOVE_NONE, nullptr, (cudaStream_t)stream, stats);
+}
+
+int mcl_delaunay_restore(mcl_mesh* m, void* stream, mcl_step_stats* stats) {
+  if (!m) return fail(MCL_ERR_INVALID_ARGUMENT, "null mesh");
+  return run_step(m, MOVE_NONE, nullptr, (cudaStream_t)stream, stats);
+}
+
+int mcl_step(mcl_mesh* m, const mcl_float2* d_dev, void* stream, mcl_step_stats* stats) {
+  if (!m || !d_dev) return fail(MCL_ERR_INVALID_ARGUMENT, "null argument");
+  if (!m->valid_cur) {
+    int rc = mcl_move(m, d_dev, stream);
+    if (rc != MCL_OK) return rc;
+    return run_step(m, MOVE_NONE, nullptr, (cudaStream_t)stream, stats);
+  }
+  return run_step(m, MOVE_DISPLACE, (const float2*)d_dev, (cudaStream_t)stream, stats);
+}
+
+int mcl_step_host(mcl_mesh* m, const mcl_float2* d_host, void* stream, mcl_step_stats* stats) {
+  if (!m || !d_host) return fail(MCL_ERR_INVALID_ARGUMENT, "null argument");
+  cudaStream_t s = (cudaStream_t)stream;
+  CK(cudaMemcpyAsync(m->dstage, d_host, 8 * m->V, cudaMemcpyHostToDevice, s));
+  return mcl_step(m, reinterpret_cast<const mcl_float2*>(m->dstage), stream, stats);
+}
+
+int mcl_mesh_last_status(mcl_mesh* m, void* stream, mcl_step_stats* stats) {
+  if (!m) return fail(MCL_ERR_INVALID_ARGUMENT, "null mesh");
+  mcl_step_stats tmp;
+  return finish(m, (cudaStream_t)stream, stats ? stats : &tmp);
+}
+
+// HostTriangulation::addDelaunayPoints on the GPU: Morton sort on the host with
+// the reference's comparator (include/Host_Triangulation.h:287-300, std::sort so
+// that ties resolve as in the reference), then parallel insertion rounds.
+// libmorton's m2D_e_LUT<uint_fast32_t,uint_fast32_t>(x, y) as the reference
+// calls it: each float truncated to an integer (two's complement for negative
+// values), the low 32 bits of x in the even bit positions, y in the odd ones.
+static uint64_t mcl_morton_key(float x, float y) {
+  auto spread = [](uint64_t w) {
+    w &= 0xFFFFFFFFull;
+    w = (w | (w << 16)) & 0x0000FFFF0000FFFFull;
+    w = (w | (w << 8)) & 0x00FF00FF00FF00FFull;
+    w = (w | (w << 4)) & 0x0F0F0F0F0F0F0F0Full;
+    w = (w | (w << 2)) & 0x3333333333333333ull;
+    w = (w | (w << 1)) & 0x5555555555555555ull;
+    return w;
+  };
+  return spread((uint64_t)(int64_t)x) | (spread((uint64_t)(int64_t)y) << 1);
+}
+
+int mcl_mesh_build(mcl_float2* pts, int64_t n, mcl_mesh** out) {
+  if (!pts || !out || n < 0) return fail(MCL_ERR_INVALID_ARGUMENT, "null argument");
+  const float lo = -10000000.0f, hi = 10000000.0f;
+  for (int64_t i = 0; i < n; ++i) {
+    if (!(pts[i].x > lo && pts[i].x < hi && pts[i].y > lo && pts[i].y < hi))
+      return fail(MCL_ERR_DEGENERATE_INPUT, "point outside the bounding square");
+  }
+  std::sort(pts, pts + n, [](const mcl_float2& a, const mcl_float2& b) {
+    return mcl_morton_key(a.x, a.y) < mcl_morton_key(b.x, b.y);
+  });
+  const int64_t V = n + 4, E = 5 + 3 * n;
+  mcl_mesh* m = nullptr;
+  int rc = alloc_mesh(V, E, &m);
+  if (rc != MCL_OK) return rc;
+  // bounding square: the reference's seed (include/Host_Triangulation.h:107-137)
+  std::vector<mcl_float2> pos(V);
+  pos[0] = {lo, lo}; pos[1] = {hi, lo}; pos[2] = {hi, hi}; pos[3] = {lo, hi};
+  for (int64_t i = 0; i < n; ++i) pos[4 + i] = pts[i];
+  const int seed_he[10][4] = {{2, 0, 0, 2},  {9, 1, -1, -1}, {4, 1, 0, 0},  {1, 2, -1, -1}, {0, 2, 0, 1},
+                              {6, 0, 1, 3},  {8, 2, 1, 0},   {3, 3, -1, -1}, {5, 3, 1, 2},  {7, 0, -1, -1}};
+  std::vector<int4> ev(E, make_int4(-1, -1, -1, -1)), en(E, make_int4(-1, -1, -1, -1));
+  int prev[10];
+  for (int h = 0; h < 10; ++h) prev[seed_he[h][0]] = h;
+  for (int e = 0; e < 5; ++e) {
+    const int* a = seed_he[2 * e];
+    const int* b = seed_he[2 * e + 1];
+    ev[e] = make_int4(a[1], b[1], a[2] >= 0 ? a[3] : -1, b[2] >= 0 ? b[3] : -1);
+    en[e] = make_int4(a[0], prev[2 * e], b[0], prev[2 * e + 1]);
+  }
+  std::vector<int> vhe(V, -1);
+  vhe[0] = 0; vhe[1] = 2; vhe[2] = 6; vhe[3] = 8;
+  rc = upload_soa(m, pos.data(), ev, en, vhe);
+  if (rc != MCL_OK) { free_mesh(m); return rc; }
+  // pending list and free edge slots: vertex 4+i owns edges 5+3i .. 7+3i
+  std::vector<int> vfree(3 * V, -1), list(n), hint(V, 0);
+  for (int64_t i = 0; i < n; ++i) {
+    list[i] = (int)(4 + i);
+    for (int k = 0; k < 3; ++k) vfree[3 * (4 + i) + k] = (int)(5 + 3 * i + k);
+  }
+  cudaError_t e = cudaMemcpy(m->vfree, vfree.data(), 12 * V, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && n) e = cudaMemcpy(m->vl[0], list.data(), 4 * n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(m->vhint, hint.data(), 4 * V, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) { free_mesh(m); return cuda_fail(e, "build upload"); }
+  KParams P = make_params(m, ENGINE_BUILD);
+  P.pos = m->pos[0];
+  P.pos_old = m->pos[0];
+  k_reset_state<<<1, 1>>>(m->st);
+  const int n32 = (int)n;
+  e = cudaMemcpy(&m->st->vl_count[0], &n32, sizeof(int), cudaMemcpyHostToDevice);
+  void* args[] = {&P};
+  if (e == cudaSuccess)
+    e = cudaLaunchCooperativeKernel((void*)k_engine, dim3(m->coop_blocks), dim3(m->coop_threads), args, 0, 0);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(m->st_host, m->st, sizeof(DevState), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(m->pos[1], m->pos[0], 8 * V, cudaMemcpyDeviceToDevice);
+  if (e != cudaSuccess) { free_mesh(m); return cuda_fail(e, "build"); }
+  if (m->st_host->status != MCL_OK) {
+    const int st = m->st_host->status;
+    free_mesh(m);
+    return fail(st, std::string("build failed: ") + mcl_status_string(st));
+  }
+  *out = m;
+  return MCL_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,230 @@
+// Internal declarations of the GB300 kinetic Delaunay engine.
+//
+// Device mesh layout (structure of arrays, one record per undirected edge e;
+// half-edge ids are 2e and 2e+1 and the twin of half-edge h is h^1, the same
+// numbering as the reference's AoS half-edges, include/Common_Triangulation.h:47-53):
+//
+//   ev[e] : int4 {origin(2e), origin(2e+1), apex(2e), apex(2e+1)}
+//           apex(h) = vertex opposite h in the face left of h, -1 = outside
+//   en[e] : int4 {next(2e), prev(2e), next(2e+1), prev(2e+1)}
+//   vhe[v]: one outgoing half-edge of v (-1 while v is detached)
+//   pos   : float2[V], double-buffered (old / new positions of a step)
+//
+// One edge's quad (a, b, c, d) sits in a single 16-byte load, which is all the
+// Delaunay and orientation classification reads besides four positions.  Flips,
+// splits and vertex removal rewrite whole records of their own edges and only
+// the one-side fields {apex, next, prev} of neighbouring edges, so concurrent
+// operations on faces they own never write the same word.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "predicates.cuh"
+#include "../../include/mcl_gb300.h"
+
+namespace mcl {
+
+// Device-side counters (indices into DevState::c).
+enum Counter {
+  C_LAWSON_FLIPS = 0,
+  C_LAWSON_ROUNDS,
+  C_INVERTED,
+  C_REVERTED,
+  C_REMOVED,
+  C_REMOVAL_FLIPS,
+  C_INSERT_ROUNDS,
+  C_INCIRCLE,
+  C_INCIRCLE_FP64,
+  C_INCIRCLE_EXACT,
+  C_ORIENT_FP64,
+  C_ORIENT_EXACT,
+  C_SOS,
+  C_OVERFLOW,
+  C_FIX_PASSES,
+  C_REMOVE_ROUNDS,
+  C_COUNT
+};
+
+struct DevState {
+  int wl_count[2];         // edge work-list sizes
+  int vl_count[2];         // vertex work-list sizes
+  int status;              // MCL_OK or the first error
+  int inverted;            // faces with orientation <= 0 found by the last classification
+  int fix_new[3];          // vertices newly reverted per fixpoint pass (triple-buffered)
+  int fix_bad[3];          // non-positive faces seen per fixpoint pass
+  unsigned int epoch;      // next unused stamp
+  unsigned int pad;
+  unsigned long long c[C_COUNT];
+};
+
+enum MoveMode { MOVE_NONE = 0, MOVE_DISPLACE = 1, MOVE_INTEGRATE = 2 };
+enum EngineMode { ENGINE_STEP = 0, ENGINE_BUILD = 1 };
+
+struct KParams {
+  int V, E;
+  float2* pos;             // positions the mesh is repaired to (new)
+  const float2* pos_old;   // positions at which the mesh was last valid
+  int4* ev;
+  int4* en;
+  int* vhe;
+  const unsigned char* vfix;  // 1 = fixed vertex (bounding corners)
+  unsigned int* cand;      // per edge: stamp of the round in which it is a flip candidate
+  unsigned int* win;       // per edge: stamp of the round in which it won
+  unsigned int* qmark;     // per edge: stamp of the last work-list it was queued on
+  int* wl0;
+  int* wl1;
+  int* vl0;
+  int* vl1;
+  int* vmark;              // per vertex: reverted flag
+  unsigned long long* claim;  // per half-edge: face claims {stamp, ~priority}
+  int* vfree;              // 3 per vertex: free edge slots for (re)insertion
+  int* vhint;              // per vertex: half-edge to start point location from
+  int* vaux;               // per vertex: a neighbour at removal time
+  int* vloc;               // per vertex: located half-edge (+ on-edge flag in vlocf)
+  int* vlocf;
+  float2* target;          // per vertex: position to reinsert at
+  DevState* st;
+  // move inputs
+  const float2* disp;
+  const float* dt;
+  const float2* vel;
+  int move_mode;
+  int mode;
+  int max_rounds;
+  int walk_cap;
+};
+
+// ---------------------------------------------------------------------------
+// Accessors.  Mesh records are mutated by other blocks inside the persistent
+// kernels, so they are read with L2-coherent loads (ld.global.cg).
+__device__ __forceinline__ int4 ld_ev(const KParams& P, int e) { return __ldcg(P.ev + e); }
+__device__ __forceinline__ int4 ld_en(const KParams& P, int e) { return __ldcg(P.en + e); }
+__device__ __forceinline__ int ld_i(const int* p) { return __ldcg(p); }
+
+__device__ __forceinline__ int he_origin(const KParams& P, int h) {
+  return ld_i(reinterpret_cast<const int*>(P.ev) + 4 * (h >> 1) + (h & 1));
+}
+__device__ __forceinline__ int he_apex(const KParams& P, int h) {
+  return ld_i(reinterpret_cast<const int*>(P.ev) + 4 * (h >> 1) + 2 + (h & 1));
+}
+__device__ __forceinline__ int he_next(const KParams& P, int h) {
+  return ld_i(reinterpret_cast<const int*>(P.en) + 4 * (h >> 1) + 2 * (h & 1));
+}
+__device__ __forceinline__ int he_prev(const KParams& P, int h) {
+  return ld_i(reinterpret_cast<const int*>(P.en) + 4 * (h >> 1) + 2 * (h & 1) + 1);
+}
+// Rewrite the face-side fields of half-edge h (its origin is unchanged).
+__device__ __forceinline__ void he_set_face(const KParams& P, int h, int apex, int next, int prev) {
+  int* ev = reinterpret_cast<int*>(P.ev) + 4 * (h >> 1);
+  int* en = reinterpret_cast<int*>(P.en) + 4 * (h >> 1);
+  __stcg(ev + 2 + (h & 1), apex);
+  __stcg(en + 2 * (h & 1), next);
+  __stcg(en + 2 * (h & 1) + 1, prev);
+}
+__device__ __forceinline__ void he_set_origin(const KParams& P, int h, int v) {
+  __stcg(reinterpret_cast<int*>(P.ev) + 4 * (h >> 1) + (h & 1), v);
+}
+
+__device__ __forceinline__ int face_min(const KParams& P, int h) {
+  const int n = he_next(P, h), p = he_prev(P, h);
+  return min(h, min(n, p));
+}
+
+// 32-bit bijective mixer (murmur3 finaliser); distinct inputs give distinct
+// priorities, so flip / claim conflicts never tie.
+__device__ __forceinline__ unsigned int mix32(unsigned int x) {
+  x ^= x >> 16;
+  x *= 0x85ebca6bu;
+  x ^= x >> 13;
+  x *= 0xc2b2ae35u;
+  x ^= x >> 16;
+  return x;
+}
+
+struct LocalCounters {
+  unsigned long long orient_fp64, orient_exact, incircle_fp64, incircle_exact, sos;
+  unsigned long long incircle;
+  int overflow;
+};
+
+__device__ __forceinline__ float2 ldpos(const KParams& P, int v) { return __ldcg(P.pos + v); }
+
+__device__ __forceinline__ int orient_v(const KParams& P, float2 a, float2 b, float2 c, LocalCounters& lc) {
+  return orient2d(a.x, a.y, b.x, b.y, c.x, c.y, &lc, &lc.overflow);
+}
+
+__device__ __forceinline__ bool bad_v(const KParams& P, int v) { return (unsigned)v >= (unsigned)P.V; }
+__device__ __forceinline__ bool bad_h(const KParams& P, int h) { return (unsigned)h >= (unsigned)(2 * P.E); }
+__device__ __forceinline__ void flag_error(const KParams& P, int code) { atomicCAS(&P.st->status, 0, code); }
+
+// Is edge e locally non-Delaunay (d inside the circle of the left face a,b,c)?
+__device__ __forceinline__ bool edge_illegal(const KParams& P, const int4 q, LocalCounters& lc) {
+  if (q.x < 0 || q.z < 0 || q.w < 0) return false;
+  if (bad_v(P, q.x) || bad_v(P, q.y) || bad_v(P, q.z) || bad_v(P, q.w)) {
+    flag_error(P, MCL_ERR_DEGENERATE_INPUT);
+    return false;
+  }
+  const float2 a = ldpos(P, q.x), b = ldpos(P, q.y), c = ldpos(P, q.z), d = ldpos(P, q.w);
+  lc.incircle++;
+  return incircle_sos(a.x, a.y, b.x, b.y, c.x, c.y, d.x, d.y, q.x, q.y, q.z, q.w, &lc, &lc.overflow) > 0;
+}
+
+// Edge flip of e = (a,b,c,d): the diagonal a-b becomes d-c.  Faces after the
+// flip: (d,c,a) left of 2e and (c,d,b) left of 2e+1.  Only e's own records and
+// the facing-side fields of its four wing half-edges are written.
+__device__ __forceinline__ bool flip_edge(const KParams& P, int e) {
+  const int4 q = ld_ev(P, e);
+  const int4 w = ld_en(P, e);
+  const int a = q.x, b = q.y, c = q.z, d = q.w;
+  const int n0 = w.x, p0 = w.y, n1 = w.z, p1 = w.w;
+  if (bad_v(P, a) || bad_v(P, b) || bad_v(P, c) || bad_v(P, d) || bad_h(P, n0) || bad_h(P, p0) ||
+      bad_h(P, n1) || bad_h(P, p1)) {
+    flag_error(P, MCL_ERR_DEGENERATE_INPUT);
+    return false;
+  }
+  const int h0 = 2 * e, h1 = 2 * e + 1;
+  __stcg(P.ev + e, make_int4(d, c, a, b));
+  __stcg(P.en + e, make_int4(p0, n1, p1, n0));
+  he_set_face(P, p0, d, n1, h0);
+  he_set_face(P, n1, c, h0, p0);
+  he_set_face(P, p1, c, n0, h1);
+  he_set_face(P, n0, d, h1, p1);
+  if (ld_i(P.vhe + a) == h0) __stcg(P.vhe + a, n1);
+  if (ld_i(P.vhe + b) == h1) __stcg(P.vhe + b, n0);
+  return true;
+}
+
+}  // namespace mcl
+
+struct mcl_mesh {
+  int device;
+  int64_t V, E, T;
+  int cur;                 // index of the current position buffer
+  bool valid_cur;          // pos[cur] is the last validated state
+  float2* pos[2];
+  int4* ev;
+  int4* en;
+  int* vhe;
+  unsigned char* vfix;
+  unsigned int* cand;
+  unsigned int* win;
+  unsigned int* qmark;
+  int* wl[2];
+  int* vl[2];
+  int* vmark;
+  unsigned long long* claim;
+  int* vfree;
+  int* vhint;
+  int* vaux;
+  int* vloc;
+  int* vlocf;
+  float2* target;
+  float2* dstage;          // device staging buffer for host displacements
+  unsigned long long* scratch;  // small device scratch for query counters
+  mcl::DevState* st;
+  mcl::DevState* st_host;  // pinned mirror
+  int coop_blocks;
+  int coop_threads;
+  int last_status;
+};

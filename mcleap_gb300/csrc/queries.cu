@@ -1,0 +1,595 @@
+// Neighbourhood queries on the device mesh and the uniform grid, plus the
+// predicate diagnostics entry points.
+//
+//   one-ring      DeviceTriangulation::oneRing / oneRing2   (include/kernels.cuh:54-121)
+//   closest       DeviceTriangulation::closestNeighbors[2]  (include/kernels.cuh:129-165)
+//   mesh FRNN     DeviceTriangulation::getFRNN / getFRNN2   (include/kernels.cuh:169-272)
+//   grid          GridCount2d (include/gridCount2d.h): counting sort of points
+//                 into cells ordered along a Morton curve, stable inside a cell,
+//                 then fixed-radius queries over the (2w+1)^2 cell stencil.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "engine.cuh"
+
+using namespace mcl;
+
+namespace {
+
+thread_local std::string g_err;
+
+int qfail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+#define QCK(call)                                                                       \
+  do {                                                                                  \
+    cudaError_t _e = (call);                                                            \
+    if (_e != cudaSuccess) return qfail(MCL_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(_e)); \
+  } while (0)
+
+// Reference squared distance, include/kernels.cuh:125-127: no FMA contraction.
+__device__ __forceinline__ float sqdist(float2 a, float2 b) {
+  const float dx = __fsub_rn(a.x, b.x), dy = __fsub_rn(a.y, b.y);
+  return __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
+}
+
+struct MeshView {
+  const int4* ev;
+  const int4* en;
+  const int* vhe;
+  const float2* pos;
+  int V, E;
+};
+
+__device__ __forceinline__ int mv_origin(const MeshView& M, int h) {
+  return __ldg(reinterpret_cast<const int*>(M.ev) + 4 * (h >> 1) + (h & 1));
+}
+__device__ __forceinline__ int mv_next(const MeshView& M, int h) {
+  return __ldg(reinterpret_cast<const int*>(M.en) + 4 * (h >> 1) + 2 * (h & 1));
+}
+// The reference's PREV_OUTGOING(h) = next(twin(h)): the next outgoing half-edge
+// clockwise around the origin (include/kernels.cuh:52).
+__device__ __forceinline__ int mv_rot(const MeshView& M, int h) { return mv_next(M, h ^ 1); }
+
+constexpr int kMaxDeg = 4096;
+
+// ---------------------------------------------------------------------------
+__global__ void k_one_ring(MeshView M, int layout, int max_ring, int* ring, unsigned long long* truncated) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= M.V) return;
+  const int h0 = __ldg(M.vhe + i);
+  if (h0 < 0) return;
+  // first pass: start at the spoke to the smallest neighbour id
+  int start = h0, best = 0x7fffffff, deg = 0;
+  int h = h0;
+  do {
+    const int w = mv_origin(M, h ^ 1);
+    if (w < best) { best = w; start = h; }
+    h = mv_rot(M, h);
+    ++deg;
+  } while (h != h0 && deg < kMaxDeg);
+  const int cap = max_ring - 1;
+  int cnt = 0;
+  h = start;
+  for (int k = 0; k < deg; ++k) {
+    if (cnt >= cap) break;
+    const int w = mv_origin(M, h ^ 1);
+    if (layout == MCL_LAYOUT_COLUMN) ring[(size_t)(cnt + 1) * M.V + i] = w;
+    else ring[(size_t)i * max_ring + cnt + 1] = w;
+    ++cnt;
+    h = mv_rot(M, h);
+  }
+  if (layout == MCL_LAYOUT_COLUMN) ring[i] = cnt;
+  else ring[(size_t)i * max_ring] = cnt;
+  if (deg > cap) atomicAdd(truncated, 1ull);
+}
+
+__global__ void k_closest(const float2* pos, int V, int layout, int max_ring, const int* ring, int* out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= V) return;
+  const int cnt = layout == MCL_LAYOUT_COLUMN ? ring[i] : ring[(size_t)i * max_ring];
+  const float2 p = pos[i];
+  int best = -1;
+  float bd = 0.f;
+  for (int k = 0; k < cnt; ++k) {
+    const int j = layout == MCL_LAYOUT_COLUMN ? ring[(size_t)(k + 1) * V + i] : ring[(size_t)i * max_ring + k + 1];
+    const float d = sqdist(p, pos[j]);
+    if (best < 0 || d < bd || (d == bd && j < best)) { best = j; bd = d; }
+  }
+  out[i] = best;
+}
+
+// Mesh FRNN: depth-first search over the mesh from i through vertices within r
+// (the reference's getFRNN, include/Host_Triangulation.h:525-560 and
+// include/kernels.cuh:169-219).  The found set is kept in a thread-local list,
+// then written sorted ascending.
+constexpr int kFrnnLocal = 256;
+
+__global__ void k_mesh_frnn(MeshView M, float r2, int layout, int max_frnn, int* out, unsigned long long* overflow) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= M.V) return;
+  int found[kFrnnLocal];
+  int nf = 0;
+  int top = 0;  // stack = found[top..nf): vertices whose rings are still to scan
+  bool over = false;
+  const float2 pi = M.pos[i];
+  int cur = i;
+  for (int guard = 0; guard < (1 << 20); ++guard) {
+    const int h0 = __ldg(M.vhe + cur);
+    if (h0 >= 0) {
+      int h = h0, deg = 0;
+      do {
+        const int w = mv_origin(M, h ^ 1);
+        if (w != i) {
+          bool seen = false;
+          for (int k = 0; k < nf; ++k)
+            if (found[k] == w) { seen = true; break; }
+          if (!seen && sqdist(pi, M.pos[w]) <= r2) {
+            if (nf < kFrnnLocal) found[nf++] = w;
+            else over = true;
+          }
+        }
+        h = mv_rot(M, h);
+        ++deg;
+      } while (h != h0 && deg < kMaxDeg);
+    }
+    if (top >= nf) break;
+    cur = found[top++];
+  }
+  // insertion sort
+  for (int a = 1; a < nf; ++a) {
+    const int x = found[a];
+    int b = a - 1;
+    while (b >= 0 && found[b] > x) { found[b + 1] = found[b]; --b; }
+    found[b + 1] = x;
+  }
+  const int cap = max_frnn - 1;
+  const int cnt = nf < cap ? nf : cap;
+  for (int k = 0; k < cnt; ++k) {
+    if (layout == MCL_LAYOUT_COLUMN) out[(size_t)(k + 1) * M.V + i] = found[k];
+    else out[(size_t)i * max_frnn + k + 1] = found[k];
+  }
+  if (layout == MCL_LAYOUT_COLUMN) out[i] = cnt;
+  else out[(size_t)i * max_frnn] = cnt;
+  if (over || nf > cap) atomicAdd(overflow, 1ull);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Grid.
+struct mcl_grid {
+  int64_t n;
+  float minx, miny, cx, cy;
+  int nx, ny;
+  int flags;
+  int morton;           // cells numbered along a Morton curve (else row-major)
+  int mbits;            // Morton side = 1 << mbits
+  int64_t ncells;       // size of the cell tables
+  int* cell;            // per point: cell id (input order)
+  int* count;           // per cell
+  int* start;           // per cell
+  int* cursor;          // per cell scatter cursor
+  int* perm;            // d_ind: sorted slot of input point i
+  int* src;             // per sorted slot: input index
+  float2* tmp;          // sorted positions / velocities scratch
+  float2* tmp2;
+  void* scan_tmp;
+  size_t scan_tmp_bytes;
+};
+
+namespace {
+
+__device__ __forceinline__ unsigned spread16(unsigned w) {
+  w &= 0xffff;
+  w = (w | (w << 8)) & 0x00FF00FFu;
+  w = (w | (w << 4)) & 0x0F0F0F0Fu;
+  w = (w | (w << 2)) & 0x33333333u;
+  w = (w | (w << 1)) & 0x55555555u;
+  return w;
+}
+
+struct GridView {
+  float minx, miny, cx, cy;
+  int nx, ny, morton, periodic;
+};
+
+__device__ __forceinline__ int cell_coord(float p, float mn, float c, int n, int periodic) {
+  float kf = floorf(__fdiv_rn(__fsub_rn(p, mn), c));
+  kf = fminf(fmaxf(kf, -1.0e9f), 1.0e9f);  // also maps NaN to a border cell
+  int k = (int)kf;
+  if (periodic) {
+    k %= n;
+    if (k < 0) k += n;
+  } else {
+    k = k < 0 ? 0 : (k >= n ? n - 1 : k);
+  }
+  return k;
+}
+
+__device__ __forceinline__ int cell_id(const GridView& G, int x, int y) {
+  return G.morton ? (int)(spread16((unsigned)x) | (spread16((unsigned)y) << 1)) : y * G.nx + x;
+}
+
+__global__ void k_grid_hash(GridView G, int n, const float2* pos, int* cell, int* count) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float2 p = pos[i];
+  const int c = cell_id(G, cell_coord(p.x, G.minx, G.cx, G.nx, G.periodic),
+                        cell_coord(p.y, G.miny, G.cy, G.ny, G.periodic));
+  cell[i] = c;
+  atomicAdd(count + c, 1);
+}
+
+// Exclusive scan of the cell counts, single-pass per block + block offsets.
+__global__ void k_scan_blocks(const int* in, int* out, int* block_sums, int64_t n) {
+  __shared__ int s[1024];
+  const int64_t i = (int64_t)blockIdx.x * 1024 + threadIdx.x;
+  const int x = i < n ? in[i] : 0;
+  s[threadIdx.x] = x;
+  __syncthreads();
+  for (int o = 1; o < 1024; o <<= 1) {
+    const int y = threadIdx.x >= o ? s[threadIdx.x - o] : 0;
+    __syncthreads();
+    s[threadIdx.x] += y;
+    __syncthreads();
+  }
+  if (i < n) out[i] = s[threadIdx.x] - x;
+  if (threadIdx.x == 1023) block_sums[blockIdx.x] = s[1023];
+}
+
+__global__ void k_scan_add(int* out, const int* block_prefix, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * 1024 + threadIdx.x;
+  if (i < n) out[i] += block_prefix[blockIdx.x];
+}
+
+__global__ void k_grid_scatter(int n, const int* cell, int* cursor, int* perm, int* src) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int slot = atomicAdd(cursor + cell[i], 1);
+  perm[i] = slot;
+  src[slot] = i;
+}
+
+// Make the order inside each cell stable (ascending input index).
+__global__ void k_grid_sort_cells(int64_t ncells, const int* start, const int* count, int* src, int* perm) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncells) return;
+  const int b = start[c], k = count[c];
+  for (int a = b + 1; a < b + k; ++a) {
+    const int x = src[a];
+    int j = a - 1;
+    while (j >= b && src[j] > x) { src[j + 1] = src[j]; --j; }
+    src[j + 1] = x;
+  }
+  for (int a = b; a < b + k; ++a) perm[src[a]] = a;
+}
+
+__global__ void k_gather(int n, const int* src, const float2* in, float2* out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = in[src[i]];
+}
+
+constexpr int kGridLocal = 256;
+
+__global__ void k_grid_frnn(GridView G, int n, const float2* pos, const int* start, const int* count, float r2,
+                            int wx, int wy, float Lx, float Ly, int max_nb, int* counts, int* ids,
+                            unsigned long long* overflow) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float2 p = pos[i];
+  const int x0 = cell_coord(p.x, G.minx, G.cx, G.nx, G.periodic);
+  const int y0 = cell_coord(p.y, G.miny, G.cy, G.ny, G.periodic);
+  int found[kGridLocal];
+  int nf = 0;
+  bool over = false;
+  const float hx = 0.5f * Lx, hy = 0.5f * Ly;
+  // distinct stencil rows / columns (a periodic stencil wider than the grid
+  // visits every row or column once)
+  const bool allx = G.periodic && 2 * wx + 1 >= G.nx, ally = G.periodic && 2 * wy + 1 >= G.ny;
+  const int ylo = ally ? 0 : y0 - wy, yhi = ally ? G.ny - 1 : y0 + wy;
+  const int xlo = allx ? 0 : x0 - wx, xhi = allx ? G.nx - 1 : x0 + wx;
+  for (int yy = ylo; yy <= yhi; ++yy) {
+    int y = yy;
+    if (G.periodic) { y %= G.ny; if (y < 0) y += G.ny; }
+    else if (y < 0 || y >= G.ny) continue;
+    for (int xx = xlo; xx <= xhi; ++xx) {
+      int x = xx;
+      if (G.periodic) { x %= G.nx; if (x < 0) x += G.nx; }
+      else if (x < 0 || x >= G.nx) continue;
+      const int c = cell_id(G, x, y);
+      const int b = start[c], k = count[c];
+      for (int j = b; j < b + k; ++j) {
+        if (j == i) continue;
+        const float2 q = pos[j];
+        float dx = __fsub_rn(p.x, q.x), dy = __fsub_rn(p.y, q.y);
+        if (G.periodic) {
+          if (dx > hx) dx = __fsub_rn(dx, Lx); else if (dx < -hx) dx = __fadd_rn(dx, Lx);
+          if (dy > hy) dy = __fsub_rn(dy, Ly); else if (dy < -hy) dy = __fadd_rn(dy, Ly);
+        }
+        const float d = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
+        if (d <= r2) {
+          if (nf < kGridLocal) found[nf++] = j;
+          else over = true;
+        }
+      }
+    }
+  }
+  for (int a = 1; a < nf; ++a) {
+    const int x = found[a];
+    int b = a - 1;
+    while (b >= 0 && found[b] > x) { found[b + 1] = found[b]; --b; }
+    found[b + 1] = x;
+  }
+  const int cnt = nf < max_nb ? nf : max_nb;
+  for (int k = 0; k < cnt; ++k) ids[(size_t)i * max_nb + k] = found[k];
+  counts[i] = cnt;
+  if (over || nf > max_nb) atomicAdd(overflow, 1ull);
+}
+
+__global__ void k_mean_occupancy(int64_t ncells, const int* count, unsigned long long* acc) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncells) return;
+  const int k = count[c];
+  if (k > 0) {
+    atomicAdd(acc, 1ull);
+    atomicAdd(acc + 1, (unsigned long long)k);
+  }
+}
+
+// Exclusive scan of n ints (device), with a temporary of per-block sums.
+int scan_exclusive(const int* in, int* out, int64_t n, int* tmp, int* tmp2, cudaStream_t s) {
+  const int64_t nb = (n + 1023) / 1024;
+  k_scan_blocks<<<(unsigned)nb, 1024, 0, s>>>(in, out, tmp, n);
+  if (nb > 1) {
+    std::vector<int> sums(nb);
+    QCK(cudaMemcpyAsync(sums.data(), tmp, 4 * nb, cudaMemcpyDeviceToHost, s));
+    QCK(cudaStreamSynchronize(s));
+    int64_t run = 0;
+    for (int64_t b = 0; b < nb; ++b) {
+      const int64_t x = sums[b];
+      sums[b] = (int)run;
+      run += x;
+    }
+    QCK(cudaMemcpyAsync(tmp2, sums.data(), 4 * nb, cudaMemcpyHostToDevice, s));
+    QCK(cudaStreamSynchronize(s));
+    k_scan_add<<<(unsigned)nb, 1024, 0, s>>>(out, tmp2, n);
+  }
+  QCK(cudaGetLastError());
+  return MCL_OK;
+}
+
+GridView view_of(const mcl_grid* g) {
+  GridView G;
+  G.minx = g->minx; G.miny = g->miny; G.cx = g->cx; G.cy = g->cy;
+  G.nx = g->nx; G.ny = g->ny; G.morton = g->morton; G.periodic = (g->flags & MCL_GRID_PERIODIC) ? 1 : 0;
+  return G;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Predicate diagnostics.
+namespace {
+
+struct StageCounters {
+  unsigned long long orient_fp64, orient_exact, incircle_fp64, incircle_exact, sos;
+};
+
+__host__ __device__ inline int eval_pred(int kind, const float* q, const int* ids, int* stage) {
+  StageCounters c = {0, 0, 0, 0, 0};
+  int ovf = 0, s;
+  if (kind == 0) {
+    s = orient2d(q[0], q[1], q[2], q[3], q[4], q[5], &c, &ovf);
+    *stage = c.orient_exact ? 2 : (c.orient_fp64 ? 1 : 0);
+  } else if (kind == 1) {
+    s = incircle(q[0], q[1], q[2], q[3], q[4], q[5], q[6], q[7], &c, &ovf);
+    *stage = c.incircle_exact ? 2 : (c.incircle_fp64 ? 1 : 0);
+  } else {
+    s = incircle_sos(q[0], q[1], q[2], q[3], q[4], q[5], q[6], q[7], ids[0], ids[1], ids[2], ids[3], &c, &ovf);
+    *stage = c.sos ? 3 : (c.incircle_exact ? 2 : (c.incircle_fp64 ? 1 : 0));
+  }
+  if (ovf) *stage = -1;
+  return s;
+}
+
+__global__ void k_debug_pred(int kind, const float* pts, const int* ids, int64_t n, int* sign, int* stage) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int w = kind == 0 ? 6 : 8;
+  int st = 0;
+  const int s = eval_pred(kind, pts + w * i, ids ? ids + 4 * i : nullptr, &st);
+  sign[i] = s;
+  if (stage) stage[i] = st;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mcl_debug_predicates_host(int kind, const float* pts, const int32_t* ids, int64_t n, int32_t* sign,
+                              int32_t* stage) {
+  if (!pts || !sign || kind < 0 || kind > 2 || (kind == 2 && !ids)) return qfail(MCL_ERR_INVALID_ARGUMENT, "bad args");
+  const int w = kind == 0 ? 6 : 8;
+  for (int64_t i = 0; i < n; ++i) {
+    int st = 0;
+    sign[i] = eval_pred(kind, pts + w * i, ids ? ids + 4 * i : nullptr, &st);
+    if (stage) stage[i] = st;
+  }
+  return MCL_OK;
+}
+
+int mcl_debug_predicates_device(int kind, const float* pts, const int32_t* ids, int64_t n, int32_t* sign,
+                                int32_t* stage, void* stream) {
+  if (!pts || !sign || kind < 0 || kind > 2 || (kind == 2 && !ids)) return qfail(MCL_ERR_INVALID_ARGUMENT, "bad args");
+  if (n == 0) return MCL_OK;
+  k_debug_pred<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(kind, pts, ids, n, sign, stage);
+  QCK(cudaGetLastError());
+  return MCL_OK;
+}
+
+int mcl_one_ring(mcl_mesh* m, int layout, int max_ring, int32_t* ring, void* stream, int64_t* truncated) {
+  if (!m || !ring || max_ring < 2 || (layout != MCL_LAYOUT_COLUMN && layout != MCL_LAYOUT_ROW))
+    return qfail(MCL_ERR_INVALID_ARGUMENT, "bad args");
+  cudaStream_t s = (cudaStream_t)stream;
+  unsigned long long* cnt = m->scratch;
+  MeshView M{m->ev, m->en, m->vhe, m->pos[m->cur], (int)m->V, (int)m->E};
+  QCK(cudaMemsetAsync(cnt, 0, 8, s));
+  k_one_ring<<<(unsigned)((m->V + 255) / 256), 256, 0, s>>>(M, layout, max_ring, ring, cnt);
+  QCK(cudaGetLastError());
+  if (truncated) {
+    unsigned long long t = 0;
+    QCK(cudaMemcpyAsync(&t, cnt, 8, cudaMemcpyDeviceToHost, s));
+    QCK(cudaStreamSynchronize(s));
+    *truncated = (int64_t)t;
+  }
+  return MCL_OK;
+}
+
+int mcl_closest_neighbors(mcl_mesh* m, int layout, int max_ring, const int32_t* ring, int32_t* out, void* stream) {
+  if (!m || !ring || !out || max_ring < 2) return qfail(MCL_ERR_INVALID_ARGUMENT, "bad args");
+  k_closest<<<(unsigned)((m->V + 255) / 256), 256, 0, (cudaStream_t)stream>>>(m->pos[m->cur], (int)m->V, layout,
+                                                                              max_ring, ring, out);
+  QCK(cudaGetLastError());
+  return MCL_OK;
+}
+
+int mcl_mesh_frnn(mcl_mesh* m, float r, int layout, int max_frnn, int32_t* out, void* stream, int64_t* overflow) {
+  if (!m || !out || max_frnn < 2 || !(r >= 0.f)) return qfail(MCL_ERR_INVALID_ARGUMENT, "bad args");
+  cudaStream_t s = (cudaStream_t)stream;
+  unsigned long long* cnt = m->scratch;
+  MeshView M{m->ev, m->en, m->vhe, m->pos[m->cur], (int)m->V, (int)m->E};
+  QCK(cudaMemsetAsync(cnt, 0, 8, s));
+  k_mesh_frnn<<<(unsigned)((m->V + 127) / 128), 128, 0, s>>>(M, r * r, layout, max_frnn, out, cnt);
+  QCK(cudaGetLastError());
+  if (overflow) {
+    unsigned long long t = 0;
+    QCK(cudaMemcpyAsync(&t, cnt, 8, cudaMemcpyDeviceToHost, s));
+    QCK(cudaStreamSynchronize(s));
+    *overflow = (int64_t)t;
+  }
+  return MCL_OK;
+}
+
+int mcl_grid_create(int64_t n, float minx, float miny, float cx, float cy, int32_t nx, int32_t ny, int flags,
+                    mcl_grid** out) {
+  if (!out || n < 0 || nx < 1 || ny < 1 || !(cx > 0.f) || !(cy > 0.f) || (int64_t)nx * ny > (1ll << 30))
+    return qfail(MCL_ERR_INVALID_ARGUMENT, "bad grid");
+  mcl_grid* g = new mcl_grid();
+  std::memset(g, 0, sizeof(*g));
+  g->n = n; g->minx = minx; g->miny = miny; g->cx = cx; g->cy = cy; g->nx = nx; g->ny = ny; g->flags = flags;
+  int side = 1, bits = 0;
+  while (side < std::max(nx, ny)) { side <<= 1; ++bits; }
+  const int64_t mcells = (int64_t)side * side;
+  g->morton = (side <= 65536 && mcells <= 4 * (int64_t)nx * ny + 1024) ? 1 : 0;
+  g->mbits = bits;
+  g->ncells = g->morton ? mcells : (int64_t)nx * ny;
+  const int64_t nn = std::max<int64_t>(n, 1);
+  const int64_t nb = (g->ncells + 1023) / 1024 + 1;
+  cudaError_t e = cudaSuccess;
+  auto A = [&](void** p, size_t b) { if (e == cudaSuccess) e = cudaMalloc(p, b); };
+  A((void**)&g->cell, 4 * nn);
+  A((void**)&g->count, 4 * g->ncells);
+  A((void**)&g->start, 4 * g->ncells);
+  A((void**)&g->cursor, 4 * g->ncells);
+  A((void**)&g->perm, 4 * nn);
+  A((void**)&g->src, 4 * nn);
+  A((void**)&g->tmp, 8 * nn);
+  A((void**)&g->tmp2, 8 * nn);
+  A(&g->scan_tmp, 8 * nb);
+  if (e == cudaSuccess) e = cudaMemset(g->count, 0, 4 * g->ncells);
+  if (e == cudaSuccess) e = cudaMemset(g->start, 0, 4 * g->ncells);
+  if (e != cudaSuccess) {
+    mcl_grid_destroy(g);
+    return qfail(MCL_ERR_OUT_OF_MEMORY, "grid allocation");
+  }
+  *out = g;
+  return MCL_OK;
+}
+
+int mcl_grid_destroy(mcl_grid* g) {
+  if (!g) return MCL_OK;
+  void* ptrs[] = {g->cell, g->count, g->start, g->cursor, g->perm, g->src, g->tmp, g->tmp2, g->scan_tmp};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  delete g;
+  return MCL_OK;
+}
+
+int mcl_grid_update(mcl_grid* g, mcl_float2* pos, mcl_float2* vel, void* stream) {
+  if (!g || !pos) return qfail(MCL_ERR_INVALID_ARGUMENT, "bad args");
+  cudaStream_t s = (cudaStream_t)stream;
+  const int n = (int)g->n;
+  if (n == 0) return MCL_OK;
+  const GridView G = view_of(g);
+  QCK(cudaMemsetAsync(g->count, 0, 4 * g->ncells, s));
+  k_grid_hash<<<(n + 255) / 256, 256, 0, s>>>(G, n, (const float2*)pos, g->cell, g->count);
+  int* tmp = (int*)g->scan_tmp;
+  const int64_t nb = (g->ncells + 1023) / 1024;
+  int rc = scan_exclusive(g->count, g->start, g->ncells, tmp, tmp + nb + 1, s);
+  if (rc != MCL_OK) return rc;
+  QCK(cudaMemcpyAsync(g->cursor, g->start, 4 * g->ncells, cudaMemcpyDeviceToDevice, s));
+  k_grid_scatter<<<(n + 255) / 256, 256, 0, s>>>(n, g->cell, g->cursor, g->perm, g->src);
+  k_grid_sort_cells<<<(unsigned)((g->ncells + 255) / 256), 256, 0, s>>>(g->ncells, g->start, g->count, g->src,
+                                                                         g->perm);
+  k_gather<<<(n + 255) / 256, 256, 0, s>>>(n, g->src, (const float2*)pos, g->tmp);
+  QCK(cudaMemcpyAsync(pos, g->tmp, 8 * (size_t)n, cudaMemcpyDeviceToDevice, s));
+  if (vel) {
+    k_gather<<<(n + 255) / 256, 256, 0, s>>>(n, g->src, (const float2*)vel, g->tmp2);
+    QCK(cudaMemcpyAsync(vel, g->tmp2, 8 * (size_t)n, cudaMemcpyDeviceToDevice, s));
+  }
+  QCK(cudaGetLastError());
+  return MCL_OK;
+}
+
+int mcl_grid_tables(mcl_grid* g, const int32_t** perm, const int32_t** start, const int32_t** count, int32_t* cx,
+                    int32_t* cy) {
+  if (!g) return qfail(MCL_ERR_INVALID_ARGUMENT, "null grid");
+  if (perm) *perm = g->perm;
+  if (start) *start = g->start;
+  if (count) *count = g->count;
+  if (cx) *cx = g->nx;
+  if (cy) *cy = g->ny;
+  return MCL_OK;
+}
+
+int mcl_grid_frnn(mcl_grid* g, const mcl_float2* pos, float r, int max_nb, int32_t* counts, int32_t* ids, void* stream,
+                  int64_t* overflow) {
+  if (!g || !pos || !counts || !ids || max_nb < 1 || !(r >= 0.f)) return qfail(MCL_ERR_INVALID_ARGUMENT, "bad args");
+  cudaStream_t s = (cudaStream_t)stream;
+  const int n = (int)g->n;
+  if (n == 0) return MCL_OK;
+  const GridView G = view_of(g);
+  const int wx = std::max(1, (int)std::ceil(r / g->cx)), wy = std::max(1, (int)std::ceil(r / g->cy));
+  unsigned long long* ovf = (unsigned long long*)g->scan_tmp;
+  QCK(cudaMemsetAsync(ovf, 0, 8, s));
+  k_grid_frnn<<<(n + 127) / 128, 128, 0, s>>>(G, n, (const float2*)pos, g->start, g->count, r * r, wx, wy,
+                                              g->cx * g->nx, g->cy * g->ny, max_nb, counts, ids, ovf);
+  QCK(cudaGetLastError());
+  if (overflow) {
+    unsigned long long t = 0;
+    QCK(cudaMemcpyAsync(&t, ovf, 8, cudaMemcpyDeviceToHost, s));
+    QCK(cudaStreamSynchronize(s));
+    *overflow = (int64_t)t;
+  }
+  return MCL_OK;
+}
+
+int mcl_grid_mean_occupancy(mcl_grid* g, float* mean) {
+  if (!g || !mean) return qfail(MCL_ERR_INVALID_ARGUMENT, "bad args");
+  unsigned long long* acc = (unsigned long long*)g->scan_tmp;
+  QCK(cudaMemset(acc, 0, 16));
+  k_mean_occupancy<<<(unsigned)((g->ncells + 255) / 256), 256>>>(g->ncells, g->count, acc);
+  unsigned long long h[2];
+  QCK(cudaMemcpy(h, acc, 16, cudaMemcpyDeviceToHost));
+  *mean = h[0] ? (float)h[1] / (float)h[0] : 0.f;
+  return MCL_OK;
+}
+
+}  // extern "C"

@@ -13,8 +13,18 @@
 
 #include "Host_Triangulation.h"
 #include "predicates.h"
+#include <random>
 
 extern "C" {
+
+// The reference tests' input generator (tests/test_frnn.cu:21-28,
+// tests/test_closest_neighbors.cu:21-28): std::mt19937 seeded with `seed`,
+// uniform_real_distribution<float>(-bounds, bounds), x then y per point.
+void ref_gen_points(unsigned seed, long n, float bounds, float* out) {
+  std::mt19937 rng{seed};
+  std::uniform_real_distribution<float> pos_r(-bounds, bounds);
+  for (long i = 0; i < n; ++i) { out[2 * i] = pos_r(rng); out[2 * i + 1] = pos_r(rng); }
+}
 
 void* ref_build(float* xy, long n) {
   std::vector<glm::vec2> pts;

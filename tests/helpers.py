@@ -1,0 +1,95 @@
+"""Shared helpers for the tests: seeded synthetic inputs in the scaled unit
+square (coordinates x 2^13, exact in float32), displacement generators and
+comparison utilities."""
+import numpy as np
+
+SCALE = np.float32(8192.0)
+
+
+def uniform_points(n, seed):
+    rng = np.random.default_rng(seed)
+    return (rng.random((n, 2), dtype=np.float32) * SCALE).astype(np.float32)
+
+
+def spacing(n):
+    return float(SCALE) / np.sqrt(n)
+
+
+def gaussian_disp(V, sigma, seed, clamp_pos=None):
+    """N(0, sigma^2) per coordinate for vertices 4.., zero for the corners; when
+    clamp_pos is given, the displacement is shrunk so pos+d stays in [0, 8192)."""
+    rng = np.random.default_rng(seed)
+    d = (rng.standard_normal((V, 2)) * sigma).astype(np.float32)
+    d[:4] = 0
+    if clamp_pos is not None:
+        hi = np.nextafter(SCALE, np.float32(0))
+        target = np.clip(clamp_pos + d, np.float32(0), hi).astype(np.float32)
+        d = (target - clamp_pos).astype(np.float32)
+        d[:4] = 0
+    return d
+
+
+def taylor_green_disp(pos, n, frac=0.5):
+    """Taylor-Green vortex u = (sin 2pi x cos 2pi y, -cos 2pi x sin 2pi y) on the
+    unit torus, evaluated in float64 at the scaled positions; dt so that the
+    largest displacement is `frac` x mean spacing.  Returned as float32 with
+    zero for the corners; positions stay inside [0, 8192) by wrapping."""
+    p = pos.astype(np.float64) / float(SCALE)
+    u = np.sin(2 * np.pi * p[:, 0]) * np.cos(2 * np.pi * p[:, 1])
+    v = -np.cos(2 * np.pi * p[:, 0]) * np.sin(2 * np.pi * p[:, 1])
+    dt = frac * spacing(n)
+    d = np.stack([u, v], 1) * dt
+    new = (pos.astype(np.float64) + d) % float(SCALE)
+    d32 = (new.astype(np.float32) - pos).astype(np.float32)
+    d32[:4] = 0
+    return d32
+
+
+def csr_from_table(table, layout, V, M):
+    """(counts, ids) from a reference-layout neighbour table."""
+    t = np.asarray(table)
+    if layout == 0:
+        t = t.reshape(M, V)
+        counts = t[0].astype(np.int32)
+        rows = [t[1:1 + counts[i], i] for i in range(V)]
+    else:
+        t = t.reshape(V, M)
+        counts = t[:, 0].astype(np.int32)
+        rows = [t[i, 1:1 + counts[i]] for i in range(V)]
+    return counts, rows
+
+
+_CUDART = None
+
+
+def cudart():
+    """The CUDA runtime library already loaded by torch (for raw device copies)."""
+    global _CUDART
+    if _CUDART is None:
+        import ctypes
+        import glob
+        import os
+
+        import torch
+
+        cands = []
+        base = os.path.dirname(torch.__file__)
+        cands += glob.glob(os.path.join(base, "lib", "libcudart.so*"))
+        for sp in __import__("site").getsitepackages():
+            cands += glob.glob(os.path.join(sp, "nvidia", "cuda_runtime", "lib", "libcudart.so*"))
+        cands += glob.glob("/usr/local/cuda/lib64/libcudart.so*")
+        for c in cands:
+            try:
+                _CUDART = ctypes.CDLL(c)
+                break
+            except OSError:
+                continue
+        _CUDART.cudaMemcpy.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int]
+    return _CUDART
+
+
+def d2h(ptr, count, dtype=np.int32):
+    out = np.zeros(count, dtype)
+    rc = cudart().cudaMemcpy(out.ctypes.data, ptr, out.nbytes, 2)
+    assert rc == 0, rc
+    return out

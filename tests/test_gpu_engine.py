@@ -1,0 +1,310 @@
+"""GPU parity tests: the CUDA engine through the C ABI against the oracle.
+
+Bar: bit-identical sorted edge sets (the unique Delaunay triangulation with
+symbolic perturbation), identical neighbour sets, identical predicate signs.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from helpers import csr_from_table, gaussian_disp, spacing, taylor_green_disp, uniform_points
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+G = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+@pytest.fixture(scope="module")
+def M():
+    import torch
+
+    import mcleap_gb300 as M
+    from mcleap_gb300 import build as B
+
+    assert torch.cuda.is_available()
+    B.build()
+    M.lib()
+    return M
+
+
+def cuda(a):
+    import torch
+
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def build_pair(M, pts):
+    """GPU-built mesh and the oracle's exact triangulation of the same points."""
+    p = pts.copy()
+    ht = M.HostTriangulation()
+    ht.addDelaunayPoints(p)
+    return ht, p
+
+
+def test_build_matches_oracle_and_reference_order(M):
+    g = np.load(os.path.join(G, "test_frnn_1000.npz"))
+    ht, srt = build_pair(M, g["points"])
+    assert np.array_equal(srt, g["sorted_points"])
+    assert np.array_equal(ht.edges(), g["edges"])
+    for n, seed in ((10, 1), (1000, 2), (20000, 3)):
+        pts = uniform_points(n, seed)
+        ht, srt = build_pair(M, pts)
+        assert np.array_equal(srt, O.morton_sort(pts))
+        ref = O.Mesh.build(srt, exact=True)
+        assert np.array_equal(ht.edges(), ref.edges())
+        assert ht.m_he.shape[0] == 6 * n + 10 and ht.m_t.shape[0] == 2 * n + 2
+        # the downloaded AoS is a valid reference-layout mesh
+        chk = O.Mesh.from_aos(ht.m_pos, ht.m_v, ht.m_he, ht.m_t, exact=True)
+        assert chk.check(exact=True) == dict(non_delaunay=0, creased=0, inverted_faces=0, zero_faces=0)
+
+
+def test_build_lattice_degenerate(M):
+    # cocircular and collinear lattice points: the perturbed triangulation is unique
+    xs, ys = np.meshgrid(np.arange(40), np.arange(30))
+    pts = (np.stack([xs.ravel(), ys.ravel()], 1) * 8 + 1).astype(np.float32)
+    ht, srt = build_pair(M, pts)
+    ref = O.Mesh.build(srt, exact=True)
+    assert np.array_equal(ht.edges(), ref.edges())
+
+
+def test_kinetic_golden_steps(M):
+    g = np.load(os.path.join(G, "kinetic_2000.npz"))
+    ht, srt = build_pair(M, g["sorted_points"])
+    assert np.array_equal(srt, g["sorted_points"])
+    assert np.array_equal(ht.edges(), g["edges_step0"])
+    dt = M.DeviceTriangulation(ht)
+    for step in (1, 2, 3):
+        st = dt.step(cuda(g[f"disp_step{step}"]))
+        assert st["status"] == 0
+        dt.transferToHost()
+        assert np.array_equal(ht.edges(), g[f"dt_edges_step{step}"]), step
+
+
+@pytest.mark.parametrize("n,sigma,steps", [(10000, 0.1, 5), (10000, 0.3, 3), (3000, 1.0, 3)])
+def test_random_walk_matches_exact_dt(M, n, sigma, steps):
+    pts = uniform_points(n, 100 + n)
+    ht, srt = build_pair(M, pts)
+    dt = M.DeviceTriangulation(ht)
+    ref = O.Mesh.build(srt, exact=True)
+    total_inverted = 0
+    for k in range(steps):
+        pos = ref.positions()
+        d = gaussian_disp(n + 4, sigma * spacing(n), 1000 * k + n, clamp_pos=pos)
+        st = dt.step(cuda(d))
+        assert st["status"] == 0, st
+        total_inverted += st["inverted_faces"]
+        ref.move(d)
+        dt.transferToHost()
+        assert np.array_equal(ht.m_pos, ref.positions())
+        exact = O.Mesh.build(ref.positions()[4:], exact=True)
+        assert np.array_equal(ht.edges(), exact.edges()), (k, st)
+    assert total_inverted > 0  # the untangling path was exercised
+
+
+def test_taylor_green_matches_exact_dt(M):
+    n = 20000
+    pts = uniform_points(n, 77)
+    ht, srt = build_pair(M, pts)
+    dt = M.DeviceTriangulation(ht)
+    pos = ht.m_pos.copy()
+    for k in range(4):
+        d = taylor_green_disp(pos, n)
+        st = dt.step(cuda(d))
+        assert st["status"] == 0, st
+        pos = (pos + d).astype(np.float32)
+        pos[:4] = ht.m_pos[:4]
+        dt.transferToHost()
+        assert np.array_equal(ht.m_pos, pos)
+        exact = O.Mesh.build(pos[4:], exact=True)
+        assert np.array_equal(ht.edges(), exact.edges()), (k, st)
+
+
+def test_separate_calls_equal_fused_step(M):
+    n = 5000
+    pts = uniform_points(n, 9)
+    ht1, srt = build_pair(M, pts)
+    ht2 = M.HostTriangulation()
+    ht2.m_pos, ht2.m_v, ht2.m_he, ht2.m_t = [a.copy() for a in (ht1.m_pos, ht1.m_v, ht1.m_he, ht1.m_t)]
+    a, b = M.DeviceTriangulation(ht1), M.DeviceTriangulation(ht2)
+    d = gaussian_disp(n + 4, 0.2 * spacing(n), 5, clamp_pos=ht1.m_pos)
+    a.step(cuda(d))
+    b.movePoints(cuda(d))
+    b.untangle2()
+    b.delonize2()
+    a.transferToHost()
+    b.transferToHost()
+    assert np.array_equal(ht1.edges(), ht2.edges())
+    assert np.array_equal(ht1.m_pos, ht2.m_pos)
+
+
+def test_one_ring_and_closest(M):
+    import torch
+
+    g = np.load(os.path.join(G, "test_frnn_1000.npz"))
+    ht, _ = build_pair(M, g["points"])
+    dt = M.DeviceTriangulation(ht)
+    V = dt.m_pos_size
+    counts, ids = O.ring_sets_from_edges(g["edges"], V)
+    offs = np.concatenate([[0], np.cumsum(counts)])
+    for layout in (0, 1):
+        Mr = 64
+        ring = torch.zeros(V * Mr, dtype=torch.int32, device="cuda")
+        trunc = dt.oneRing(Mr, ring, layout=layout)
+        assert trunc == 0
+        c, rows = csr_from_table(ring.cpu().numpy(), layout, V, Mr)
+        assert np.array_equal(c, counts)
+        for i in range(V):
+            r = rows[i]
+            assert r[0] == r.min()  # starts at the smallest id
+            assert np.array_equal(np.sort(r), ids[offs[i]:offs[i + 1]])
+    # truncation to M-1 like the reference
+    ring = torch.zeros(V * 4, dtype=torch.int32, device="cuda")
+    assert dt.oneRing(4, ring) > 0
+    # closest neighbours (tests/test_closest_neighbors.cu): brute-force argmin
+    cl = np.load(os.path.join(G, "closest.npz"))
+    for n in (10, 100, 1000):
+        from oracle import oracle as O2  # noqa: F401
+
+        pts = cl[f"pos_{n}"][4:].copy()
+        ht2, _ = build_pair(M, pts)
+        assert np.array_equal(ht2.m_pos, cl[f"pos_{n}"])
+        dt2 = M.DeviceTriangulation(ht2)
+        Vn = dt2.m_pos_size
+        ring = torch.zeros(Vn * 100, dtype=torch.int32, device="cuda")
+        out = torch.zeros(Vn, dtype=torch.int32, device="cuda")
+        dt2.oneRing2(100, ring)
+        dt2.closestNeighbors2(100, ring, out)
+        assert np.array_equal(out.cpu().numpy(), cl[f"closest_{n}"])
+
+
+@pytest.mark.parametrize("r", [5, 10, 20, 30, 40, 50])
+def test_mesh_frnn_reference_test(M, r):
+    # tests/test_frnn.cu: counts must equal brute force; here the sets must
+    import torch
+
+    g = np.load(os.path.join(G, "test_frnn_1000.npz"))
+    ht, _ = build_pair(M, g["points"])
+    dt = M.DeviceTriangulation(ht)
+    V = dt.m_pos_size
+    F = 100
+    for layout in (0, 1):
+        out = torch.zeros(V * F, dtype=torch.int32, device="cuda")
+        assert dt.getFRNN(F, float(r), out, layout=layout) == 0
+        c, rows = csr_from_table(out.cpu().numpy(), layout, V, F)
+        assert np.array_equal(c, g[f"frnn_counts_r{r}"])
+        assert np.array_equal(np.concatenate(rows), g[f"frnn_ids_r{r}"])
+
+
+def test_mesh_frnn_random(M):
+    import torch
+
+    n = 20000
+    pts = uniform_points(n, 4)
+    ht, _ = build_pair(M, pts)
+    dt = M.DeviceTriangulation(ht)
+    V = dt.m_pos_size
+    r = 3 * spacing(n)
+    F = 64
+    out = torch.zeros(V * F, dtype=torch.int32, device="cuda")
+    assert dt.getFRNN2(F, r, out) == 0
+    c, rows = csr_from_table(out.cpu().numpy(), 1, V, F)
+    bc, bids = O.frnn_brute(ht.m_pos, r)
+    assert np.array_equal(c, bc)
+    assert np.array_equal(np.concatenate(rows), bids)
+
+
+def grid_check(M, pos, cell, ncell, mn, rad, max_nb, periodic=False, L=0.0):
+    import torch
+
+    n = len(pos)
+    g = M.GridCount2d(n, mn, (cell, cell), (ncell, ncell), periodic=periodic)
+    d = cuda(pos)
+    g.update(d)
+    sp = d.cpu().numpy()
+    perm = None
+    counts = torch.zeros(n, dtype=torch.int32, device="cuda")
+    ids = torch.zeros(n * max_nb, dtype=torch.int32, device="cuda")
+    ov = g.frnn(d, rad, max_nb, counts, ids)
+    c = counts.cpu().numpy()
+    rows = ids.cpu().numpy().reshape(n, max_nb)
+    bc, bids = O.frnn_brute(sp, rad, periodic=periodic, L=L)
+    assert np.array_equal(np.sort(sp, axis=0), np.sort(pos, axis=0))
+    return g, sp, c, rows, bc, bids, ov, perm
+
+
+def test_grid_reference_lattices(M):
+    # tests/grid2d_frnn.cu lattice tests: on-boundary distances counted exactly
+    for side, step, rad, ncell in ((10, 1.0, 1.0, 10), (20, 0.5, 1.0, 10), (40, 0.25, 0.25, 10)):
+        xs, ys = np.meshgrid(np.arange(side), np.arange(side))
+        pos = (np.stack([xs.ravel(), ys.ravel()], 1) * step).astype(np.float32)
+        g, sp, c, rows, bc, bids, ov, _ = grid_check(M, pos, 1.0, ncell, (0.0, 0.0), rad, 40)
+        assert ov == 0
+        assert np.array_equal(c, bc)
+        assert np.array_equal(np.concatenate([rows[i, :c[i]] for i in range(len(pos))]), bids)
+
+
+def test_grid_random_and_permutation(M):
+    rng = np.random.default_rng(10)
+    pos = rng.uniform(-50, 50, (10000, 2)).astype(np.float32)
+    g, sp, c, rows, bc, bids, ov, _ = grid_check(M, pos, 1.0, 100, (-50.0, -50.0), 1.0, 40)
+    assert ov == 0 and np.array_equal(c, bc)
+    assert np.array_equal(np.concatenate([rows[i, :c[i]] for i in range(len(pos))]), bids)
+    from helpers import d2h
+
+    t = g.tables()
+    perm = d2h(t["perm"], len(pos))
+    # d_ind: input point i now sits at sorted slot perm[i]
+    assert np.array_equal(sp[perm], pos)
+    assert np.array_equal(np.sort(perm), np.arange(len(pos)))
+    assert g.mean_num_particle_in_cell() > 0
+
+
+def test_grid_periodic_torus(M):
+    n = 20000
+    pos = uniform_points(n, 12)
+    h = spacing(n)
+    ncell = int(8192 // (3 * h))
+    cell = 8192.0 / ncell
+    g, sp, c, rows, bc, bids, ov, _ = grid_check(M, pos, cell, ncell, (0.0, 0.0), 3 * h, 64, periodic=True, L=8192.0)
+    assert ov == 0 and np.array_equal(c, bc)
+    assert np.array_equal(np.concatenate([rows[i, :c[i]] for i in range(n)]), bids)
+
+
+def test_device_predicates_match_host_and_golden(M):
+    import torch
+
+    from mcleap_gb300 import _lib as L
+
+    g = np.load(os.path.join(G, "predicates.npz"))
+    for kind, key, gold in ((0, "orient_pts", "orient_exact"), (1, "incircle_pts", "incircle_exact")):
+        pts = cuda(g[key])
+        n = len(g[key])
+        sign = torch.zeros(n, dtype=torch.int32, device="cuda")
+        stage = torch.zeros(n, dtype=torch.int32, device="cuda")
+        L.check(L.lib().mcl_debug_predicates_device(kind, pts.data_ptr(), None, n, sign.data_ptr(), stage.data_ptr(),
+                                                    None))
+        torch.cuda.synchronize()
+        assert np.array_equal(sign.cpu().numpy(), g[gold])
+        hs, hst = L.predicates_host(kind, g[key])
+        assert np.array_equal(stage.cpu().numpy(), hst)
+
+
+def test_errors_are_reported(M):
+    from mcleap_gb300 import McleapError
+
+    pts = uniform_points(100, 1)
+    dup = np.concatenate([pts, pts[:1]]).astype(np.float32)
+    with pytest.raises(McleapError) as ei:
+        M.HostTriangulation().addDelaunayPoints(dup)
+    assert ei.value.code == 6
+    bad = pts.copy()
+    bad[3] = (2e7, 0)
+    with pytest.raises(McleapError):
+        M.HostTriangulation().addDelaunayPoints(bad)
+    # a malformed mesh is rejected before it reaches the device
+    ht = M.HostTriangulation()
+    ht.addDelaunayPoints(pts.copy())
+    ht.m_he[5, 0] = 10 ** 6
+    with pytest.raises(McleapError):
+        M.DeviceTriangulation(ht)
