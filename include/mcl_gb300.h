@@ -73,6 +73,7 @@ typedef struct {
   int64_t orient_exact;          /* ... past the FP64 filter */
   int64_t sos_decisions;         /* exactly cocircular quads decided by perturbation */
   int64_t status;                /* MCL_OK or an error code */
+  int64_t error_site;            /* engine source location that reported `status` */
 } mcl_step_stats;
 
 /* ---- library ------------------------------------------------------------ */
@@ -197,6 +198,17 @@ int mcl_grid_frnn(mcl_grid* g, const mcl_float2* pos_dev, float r, int max_nb, i
 int mcl_grid_mean_occupancy(mcl_grid* g, float* mean_host);
 
 /* ---- diagnostics ------------------------------------------------------------ */
+/* Structural invariants of the device mesh; counts8[k] = violations of kind k:
+ * 0 next/prev not inverse, 1 inner face not a 3-cycle, 2 apex != origin(prev),
+ * 3 origin(next) != origin(twin), 4 vertex half-edge not outgoing,
+ * 5 face orientation <= 0 (exact), 6 dead edge, 7 index out of range.
+ * All zero for a valid triangulation. */
+int mcl_mesh_validate(mcl_mesh* m, int64_t* counts8);
+/* Device diagnostics record of the last call: out68[0] = 1 + id of the first
+ * vertex whose removal failed (0 if none), out68[1] = its degree, then its
+ * neighbour ids in counter-clockwise order. */
+int mcl_debug_state(mcl_mesh* m, int32_t* out68);
+
 /* The device predicate ladder evaluated on the host CPU (same source as the
  * device code), for testing without a GPU.  kind 0 = orient2d on n records of
  * 6 floats, 1 = incircle on n records of 8 floats, 2 = incircle with symbolic

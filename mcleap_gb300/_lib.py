@@ -33,7 +33,7 @@ EXPORTS = [
     "mcl_untangle", "mcl_delaunay_restore", "mcl_step", "mcl_step_host", "mcl_mesh_last_status",
     "mcl_one_ring", "mcl_closest_neighbors", "mcl_mesh_frnn",
     "mcl_grid_create", "mcl_grid_destroy", "mcl_grid_update", "mcl_grid_tables", "mcl_grid_frnn",
-    "mcl_grid_mean_occupancy", "mcl_debug_predicates_host", "mcl_debug_predicates_device",
+    "mcl_grid_mean_occupancy", "mcl_debug_predicates_host", "mcl_debug_predicates_device", "mcl_mesh_validate", "mcl_debug_state",
 ]
 
 
@@ -50,7 +50,7 @@ class AosView(C.Structure):
 
 STAT_FIELDS = ["inverted_faces", "reverted_vertices", "removed_vertices", "lawson_flips", "lawson_rounds",
                "removal_flips", "insert_rounds", "incircle_tests", "incircle_fp64", "incircle_exact",
-               "orient_fp64", "orient_exact", "sos_decisions", "status"]
+               "orient_fp64", "orient_exact", "sos_decisions", "status", "error_site"]
 
 
 class StepStats(C.Structure):
@@ -99,6 +99,8 @@ def lib():
             "mcl_grid_frnn": ([vp, vp, f32, i32, vp, vp, vp, C.POINTER(i64)], i32),
             "mcl_grid_mean_occupancy": ([vp, C.POINTER(f32)], i32),
             "mcl_debug_predicates_host": ([i32, vp, vp, i64, vp, vp], i32),
+            "mcl_mesh_validate": ([vp, vp], i32),
+            "mcl_debug_state": ([vp, vp], i32),
             "mcl_debug_predicates_device": ([i32, vp, vp, i64, vp, vp, vp], i32),
         }
         for name, (args, res) in sig.items():

@@ -59,7 +59,7 @@ __device__ void stage_flush(Stage& S, int* gl, int* gcount, int gcap, DevState* 
   const int n = S.n, base = S.base;
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     if (base + i < gcap) gl[base + i] = S.items[i];
-    else atomicCAS(&st->status, MCL_OK, MCL_ERR_CAPACITY);
+    else if (atomicCAS(&st->status, MCL_OK, MCL_ERR_CAPACITY) == MCL_OK) st->site = __LINE__;
   }
   __syncthreads();
   if (threadIdx.x == 0) S.n = 0;
@@ -105,9 +105,7 @@ __device__ void stage_push(Stage& S, const int (&mine)[K], int k, int* gl, int* 
   __syncthreads();
 }
 
-__device__ __forceinline__ void set_error(const KParams& P, int code) {
-  atomicCAS(&P.st->status, MCL_OK, code);
-}
+#define set_error(P, code) flag_error_at(P, code, __LINE__)
 
 __device__ __forceinline__ bool enqueue_once(const KParams& P, int e, unsigned stamp) {
   return atomicMax(P.qmark + e, stamp) < stamp;
@@ -326,6 +324,89 @@ __device__ bool phase_fixpoint(cg::grid_group& g, const KParams& P, LocalCounter
 }
 
 // ---------------------------------------------------------------------------
+// Removal by ear clipping: retriangulate the star polygon of v (its link cycle,
+// v left out) with exact orientation tests.  Used when no spoke flip is valid,
+// which happens with exactly collinear neighbours (points clamped onto the
+// same line of the box, lattices).  A simple polygon always has an ear whose
+// closed triangle holds no other polygon vertex, so this always completes.
+// The k spoke edges become k-3 diagonals plus the 3 free edges of v.
+constexpr int kEarMax = 128;
+
+__device__ int remove_vertex_ears(const KParams& P, int v, LocalCounters& lc) {
+  int sp[kEarMax], lk[kEarMax], w[kEarMax], nx[kEarMax], pv[kEarMax], bnd[kEarMax];
+  float2 q[kEarMax];
+  const int s0 = ld_i(P.vhe + v);
+  if (bad_h(P, s0)) return MCL_ERR_DEGENERATE_INPUT | (__LINE__ << 8);
+  int k = 0, h = s0;
+  do {
+    if (k >= kEarMax) return MCL_ERR_CAPACITY | (__LINE__ << 8);
+    sp[k] = h;
+    lk[k] = he_next(P, h);
+    if (bad_h(P, lk[k])) return MCL_ERR_DEGENERATE_INPUT | (__LINE__ << 8);
+    w[k] = he_origin(P, lk[k]);
+    if (bad_v(P, w[k])) return MCL_ERR_DEGENERATE_INPUT | (__LINE__ << 8);
+    q[k] = ldpos(P, w[k]);
+    ++k;
+    h = he_prev(P, h) ^ 1;
+    if (bad_h(P, h)) return MCL_ERR_DEGENERATE_INPUT | (__LINE__ << 8);
+  } while (h != s0);
+  if (k < 3) return MCL_ERR_DEGENERATE_INPUT | (__LINE__ << 8);
+  for (int j = 0; j < k; ++j) {
+    nx[j] = j + 1 == k ? 0 : j + 1;
+    pv[j] = j == 0 ? k - 1 : j - 1;
+    bnd[j] = lk[j];
+  }
+  int remaining = k, j = 0, used = 3;
+  while (remaining > 3) {
+    bool found = false;
+    for (int t = 0; t < remaining && !found; ++t) {
+      const int a = pv[j], b = j, c = nx[j];
+      if (orient_v(P, q[a], q[b], q[c], lc) > 0) {
+        bool empty = true;
+        for (int m = nx[c]; m != a && empty; m = nx[m]) {
+          if (orient_v(P, q[a], q[b], q[m], lc) >= 0 && orient_v(P, q[b], q[c], q[m], lc) >= 0 &&
+              orient_v(P, q[c], q[a], q[m], lc) >= 0)
+            empty = false;
+        }
+        found = empty;
+      }
+      if (!found) j = nx[j];
+    }
+    if (!found) return MCL_ERR_NO_CONVERGENCE | (__LINE__ << 8);
+    const int a = pv[j], b = j, c = nx[j];
+    const int g = sp[used++] >> 1;
+    const int d0 = 2 * g, d1 = 2 * g + 1;  // d0: w_c -> w_a inside the ear, d1: w_a -> w_c outside
+    __stcg(P.ev + g, make_int4(w[c], w[a], w[b], -1));
+    __stcg(P.en + g, make_int4(bnd[a], bnd[b], -1, -1));
+    he_set_face(P, bnd[a], w[c], bnd[b], d0);
+    he_set_face(P, bnd[b], w[a], d0, bnd[a]);
+    bnd[a] = d1;
+    nx[a] = c;
+    pv[c] = a;
+    --remaining;
+    j = c;
+  }
+  {
+    const int a = j, b = nx[a], c = nx[b];
+    he_set_face(P, bnd[a], w[c], bnd[b], bnd[c]);
+    he_set_face(P, bnd[b], w[a], bnd[c], bnd[a]);
+    he_set_face(P, bnd[c], w[b], bnd[a], bnd[b]);
+    __stcg(P.vhint + v, bnd[a]);
+  }
+  for (int i = 0; i < k; ++i)
+    if (ld_i(P.vhe + w[i]) == (sp[i] ^ 1)) __stcg(P.vhe + w[i], lk[i]);
+  for (int r = 0; r < 3; ++r) {
+    const int e = sp[r] >> 1;
+    __stcg(P.vfree + 3 * v + r, e);
+    __stcg(P.ev + e, make_int4(-1, -1, -1, -1));
+    __stcg(P.en + e, make_int4(-1, -1, -1, -1));
+  }
+  __stcg(P.vaux + v, w[0]);
+  __stcg(P.vhe + v, -1);
+  return MCL_OK;
+}
+
+// ---------------------------------------------------------------------------
 // Repair (2): removal of a vertex from a valid triangulation by flipping its
 // spokes until it has degree 3, then merging its three faces.  Runs in one
 // thread; the caller owns every face of the vertex's star.
@@ -333,7 +414,7 @@ __device__ int remove_vertex(const KParams& P, int v, LocalCounters& lc, int& fl
   const float2 pv = ldpos(P, v);
   for (int guard = 0; guard < 4096; ++guard) {
     const int s0 = ld_i(P.vhe + v);
-    if (s0 < 0 || s0 >= 2 * P.E) return MCL_ERR_DEGENERATE_INPUT;
+    if (s0 < 0 || s0 >= 2 * P.E) return MCL_ERR_DEGENERATE_INPUT | (__LINE__ << 8);
     int deg = 0;
     int h = s0;
     int flipped = -1;
@@ -343,30 +424,44 @@ __device__ int remove_vertex(const KParams& P, int v, LocalCounters& lc, int& fl
         // flipping spoke h = v->w replaces faces (v,w,*) and (w,v,*) by (d,c,a), (c,d,b)
         const int e = h >> 1;
         const int4 q = ld_ev(P, e);
-        if (bad_v(P, q.x) || bad_v(P, q.y) || q.z >= P.V || q.w >= P.V) return MCL_ERR_DEGENERATE_INPUT;
+        if (bad_v(P, q.x) || bad_v(P, q.y) || q.z >= P.V || q.w >= P.V) return MCL_ERR_DEGENERATE_INPUT | (__LINE__ << 8);
         if (q.z >= 0 && q.w >= 0) {
           const float2 a = ldpos(P, q.x), b = ldpos(P, q.y), c = ldpos(P, q.z), d = ldpos(P, q.w);
           if (orient_v(P, d, c, a, lc) > 0 && orient_v(P, c, d, b, lc) > 0) flipped = e;
         }
       }
       h = he_prev(P, h) ^ 1;
-      if (h < 0 || h >= 2 * P.E) return MCL_ERR_DEGENERATE_INPUT;
+      if (h < 0 || h >= 2 * P.E) return MCL_ERR_DEGENERATE_INPUT | (__LINE__ << 8);
     } while (h != s0 && deg < 1024);
-    if (deg >= 1024) return MCL_ERR_CAPACITY;
+    if (deg >= 1024) return MCL_ERR_CAPACITY | (__LINE__ << 8);
     if (deg == 3) break;
-    if (deg < 3 || flipped < 0) return MCL_ERR_NO_CONVERGENCE;
-    if (!flip_edge(P, flipped)) return MCL_ERR_DEGENERATE_INPUT;
+    if (deg < 3) return MCL_ERR_DEGENERATE_INPUT | (__LINE__ << 8);
+    if (flipped < 0) {
+      // no spoke flip is valid (exactly collinear neighbours): clip ears
+      const int rc = remove_vertex_ears(P, v, lc);
+      if (rc != MCL_OK && atomicCAS(&P.st->dbg[0], 0, v + 1) == 0) {
+        P.st->dbg[1] = deg;
+        int hh = s0;
+        for (int k = 0; k < deg && k < 64; ++k) {
+          P.st->dbg[2 + k] = he_origin(P, hh ^ 1);
+          hh = he_prev(P, hh) ^ 1;
+        }
+      }
+      ++flips;  // counted as one repair operation
+      return rc;
+    }
+    if (!flip_edge(P, flipped)) return MCL_ERR_DEGENERATE_INPUT | (__LINE__ << 8);
     ++flips;
   }
   // merge the three faces (v,x,y), (v,y,z), (v,z,x) into (x,y,z)
   const int s0 = ld_i(P.vhe + v);
   const int s1 = he_prev(P, s0) ^ 1;
   const int s2 = he_prev(P, s1) ^ 1;
-  if ((he_prev(P, s2) ^ 1) != s0) return MCL_ERR_NO_CONVERGENCE;
+  if ((he_prev(P, s2) ^ 1) != s0) return MCL_ERR_NO_CONVERGENCE | (__LINE__ << 8);
   const int lxy = he_next(P, s0), lyz = he_next(P, s1), lzx = he_next(P, s2);
-  if (bad_h(P, s1) || bad_h(P, s2) || bad_h(P, lxy) || bad_h(P, lyz) || bad_h(P, lzx)) return MCL_ERR_DEGENERATE_INPUT;
+  if (bad_h(P, s1) || bad_h(P, s2) || bad_h(P, lxy) || bad_h(P, lyz) || bad_h(P, lzx)) return MCL_ERR_DEGENERATE_INPUT | (__LINE__ << 8);
   const int x = he_origin(P, lxy), y = he_origin(P, lyz), z = he_origin(P, lzx);
-  if (bad_v(P, x) || bad_v(P, y) || bad_v(P, z)) return MCL_ERR_DEGENERATE_INPUT;
+  if (bad_v(P, x) || bad_v(P, y) || bad_v(P, z)) return MCL_ERR_DEGENERATE_INPUT | (__LINE__ << 8);
   he_set_face(P, lxy, z, lyz, lzx);
   he_set_face(P, lyz, x, lzx, lxy);
   he_set_face(P, lzx, y, lxy, lyz);
@@ -446,7 +541,7 @@ __device__ bool phase_remove(cg::grid_group& g, const KParams& P, Stage& S, unsi
         const int v = ld_i(in + i);
         if (__ldcg(P.vlocf + v) == 1) {
           const int rc = remove_vertex(P, v, lc, flips);
-          if (rc != MCL_OK) set_error(P, rc);
+          if (rc != MCL_OK) flag_error_at(P, rc & 0xff, 100000 + (rc >> 8));
           else ++removed;
         } else if (ld_i(&P.st->status) == MCL_OK) {
           mine[k++] = v;
@@ -502,7 +597,7 @@ __device__ int locate(const KParams& P, float2 p, int h, int* on, LocalCounters&
     }
     return h;
   }
-  return -MCL_ERR_NO_CONVERGENCE;
+  return -(MCL_ERR_NO_CONVERGENCE | (__LINE__ << 8));
 }
 
 // 1-to-3 split of the face of half-edge h0 by v with free edges f0, f1, f2.
@@ -587,7 +682,7 @@ __device__ bool phase_insert(cg::grid_group& g, const KParams& P, Stage& S, Stag
       int on = -1;
       const int h = locate(P, ldpos(P, v), insert_start(P, v), &on, lc);
       if (h < 0) {
-        set_error(P, -h);
+        flag_error_at(P, (-h) & 0xff, 200000 + ((-h) >> 8));
         P.vlocf[v] = -1;
         continue;
       }
@@ -980,6 +1075,7 @@ static void fill_stats(const DevState& s, mcl_step_stats* o) {
   o->orient_exact = (int64_t)s.c[C_ORIENT_EXACT];
   o->sos_decisions = (int64_t)s.c[C_SOS];
   o->status = s.status;
+  o->error_site = s.site;
 }
 
 static int finish(mcl_mesh* m, cudaStream_t s, mcl_step_stats* stats) {
@@ -1013,6 +1109,40 @@ static int run_step(mcl_mesh* m, int move_mode, const float2* d, cudaStream_t s,
   if (rc != MCL_OK) return rc;
   m->valid_cur = true;
   return finish(m, s, stats);
+}
+
+// Structural invariants of the device mesh (counted per kind):
+//  0 next/prev not inverse   1 inner face not a 3-cycle   2 apex != origin(prev)
+//  3 origin(next) != origin(twin)   4 vhe not outgoing   5 face not positive
+//  6 dead edge   7 index out of range
+__global__ void k_validate(KParams P, unsigned long long* bad) {
+  LocalCounters lc = {0, 0, 0, 0, 0, 0, 0};
+  const int HE = 2 * P.E;
+  for (int h = blockIdx.x * blockDim.x + threadIdx.x; h < HE + P.V; h += gridDim.x * blockDim.x) {
+    if (h >= HE) {
+      const int v = h - HE;
+      const int o = ld_i(P.vhe + v);
+      if (o < 0) continue;
+      if (bad_h(P, o)) { atomicAdd(bad + 7, 1ull); continue; }
+      if (he_origin(P, o) != v) atomicAdd(bad + 4, 1ull);
+      continue;
+    }
+    if (he_origin(P, h) < 0) { atomicAdd(bad + 6, 1ull); continue; }
+    const int n = he_next(P, h), p = he_prev(P, h);
+    if (bad_h(P, n) || bad_h(P, p)) { atomicAdd(bad + 7, 1ull); continue; }
+    if (he_prev(P, n) != h || he_next(P, p) != h) atomicAdd(bad + 0, 1ull);
+    if (he_origin(P, n) != he_origin(P, h ^ 1)) atomicAdd(bad + 3, 1ull);
+    const int ap = he_apex(P, h);
+    if (ap >= 0) {
+      if (he_next(P, n) != p) atomicAdd(bad + 1, 1ull);
+      if (ap != he_origin(P, p)) atomicAdd(bad + 2, 1ull);
+      if (h < n && h < p) {
+        const int a = he_origin(P, h), b = he_origin(P, n), c = he_origin(P, p);
+        if (bad_v(P, a) || bad_v(P, b) || bad_v(P, c)) { atomicAdd(bad + 7, 1ull); continue; }
+        if (orient_v(P, ldpos(P, a), ldpos(P, b), ldpos(P, c), lc) <= 0) atomicAdd(bad + 5, 1ull);
+      }
+    }
+  }
 }
 
 }  // namespace mcl
@@ -1057,6 +1187,27 @@ const char* mcl_status_string(int status) {
 
 const char* mcl_last_error(void) { return g_last_error.c_str(); }
 int mcl_version(void) { return 1; }
+
+int mcl_debug_state(mcl_mesh* m, int32_t* out68) {
+  if (!m || !out68) return fail(MCL_ERR_INVALID_ARGUMENT, "null argument");
+  CK(cudaMemcpy(m->st_host, m->st, sizeof(DevState), cudaMemcpyDeviceToHost));
+  for (int i = 0; i < 68; ++i) out68[i] = m->st_host->dbg[i];
+  return MCL_OK;
+}
+
+int mcl_mesh_validate(mcl_mesh* m, int64_t* counts8) {
+  if (!m || !counts8) return fail(MCL_ERR_INVALID_ARGUMENT, "null argument");
+  KParams P = make_params(m, ENGINE_STEP);
+  P.pos = m->pos[m->cur];
+  P.pos_old = P.pos;
+  CK(cudaMemset(m->scratch, 0, 64));
+  k_validate<<<1024, 256>>>(P, m->scratch);
+  CK(cudaGetLastError());
+  unsigned long long h[8];
+  CK(cudaMemcpy(h, m->scratch, 64, cudaMemcpyDeviceToHost));
+  for (int i = 0; i < 8; ++i) counts8[i] = (int64_t)h[i];
+  return MCL_OK;
+}
 
 int mcl_mesh_create_from_aos(const mcl_aos_view* a, mcl_mesh** out) {
   if (!a || !out || !a->pos || !a->v || !a->he) return fail(MCL_ERR_INVALID_ARGUMENT, "null argument");

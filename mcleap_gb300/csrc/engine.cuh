@@ -54,7 +54,8 @@ struct DevState {
   int fix_new[3];          // vertices newly reverted per fixpoint pass (triple-buffered)
   int fix_bad[3];          // non-positive faces seen per fixpoint pass
   unsigned int epoch;      // next unused stamp
-  unsigned int pad;
+  int site;                // source line that set `status` (diagnostics)
+  int dbg[68];             // first failing vertex star: v, deg, then neighbour ids
   unsigned long long c[C_COUNT];
 };
 
@@ -156,7 +157,10 @@ __device__ __forceinline__ int orient_v(const KParams& P, float2 a, float2 b, fl
 
 __device__ __forceinline__ bool bad_v(const KParams& P, int v) { return (unsigned)v >= (unsigned)P.V; }
 __device__ __forceinline__ bool bad_h(const KParams& P, int h) { return (unsigned)h >= (unsigned)(2 * P.E); }
-__device__ __forceinline__ void flag_error(const KParams& P, int code) { atomicCAS(&P.st->status, 0, code); }
+__device__ __forceinline__ void flag_error_at(const KParams& P, int code, int line) {
+  if (atomicCAS(&P.st->status, 0, code) == 0) P.st->site = line;
+}
+#define flag_error(P, code) flag_error_at(P, code, __LINE__)
 
 // Is edge e locally non-Delaunay (d inside the circle of the left face a,b,c)?
 __device__ __forceinline__ bool edge_illegal(const KParams& P, const int4 q, LocalCounters& lc) {

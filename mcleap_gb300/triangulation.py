@@ -183,6 +183,13 @@ class DeviceTriangulation:
             return self.last_stats
         return None
 
+    def validate(self):
+        """Counts of structural invariant violations (all zero for a valid mesh)."""
+        out = np.zeros(8, np.int64)
+        L.check(L.lib().mcl_mesh_validate(self.handle, L.ptr(out)))
+        keys = ["next_prev", "not_triangle", "apex", "twin", "vertex_he", "orientation", "dead_edge", "range"]
+        return dict(zip(keys, out.tolist()))
+
     def status(self, stream=None):
         st = L.StepStats()
         L.check(L.lib().mcl_mesh_last_status(self.handle, _stream_ptr(stream), C.byref(st)))

@@ -26,6 +26,17 @@ def gaussian_disp(V, sigma, seed, clamp_pos=None):
         target = np.clip(clamp_pos + d, np.float32(0), hi).astype(np.float32)
         d = (target - clamp_pos).astype(np.float32)
         d[:4] = 0
+        # clamping can stack points on the same spot (a box corner); exact
+        # duplicates are rejected by the engine, so such points stay put
+        for _ in range(8):
+            new = (clamp_pos + d).astype(np.float32)
+            _, first, counts = np.unique(new, axis=0, return_index=True, return_counts=True)
+            if (counts == 1).all():
+                break
+            keep = np.zeros(len(new), bool)
+            keep[first] = True
+            dup = ~keep
+            d[dup] = 0
     return d
 
 

@@ -81,7 +81,7 @@ def test_kinetic_golden_steps(M):
         assert np.array_equal(ht.edges(), g[f"dt_edges_step{step}"]), step
 
 
-@pytest.mark.parametrize("n,sigma,steps", [(10000, 0.1, 5), (10000, 0.3, 3), (3000, 1.0, 3)])
+@pytest.mark.parametrize("n,sigma,steps", [(10000, 0.1, 5), (10000, 0.3, 3), (3000, 1.0, 4), (1000, 3.0, 4)])
 def test_random_walk_matches_exact_dt(M, n, sigma, steps):
     pts = uniform_points(n, 100 + n)
     ht, srt = build_pair(M, pts)
@@ -93,6 +93,7 @@ def test_random_walk_matches_exact_dt(M, n, sigma, steps):
         d = gaussian_disp(n + 4, sigma * spacing(n), 1000 * k + n, clamp_pos=pos)
         st = dt.step(cuda(d))
         assert st["status"] == 0, st
+        assert all(v == 0 for v in dt.validate().values())
         total_inverted += st["inverted_faces"]
         ref.move(d)
         dt.transferToHost()
