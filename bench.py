@@ -1,0 +1,332 @@
+"""Kinetic-step benchmark of the GB300 engine (Taylor-Green vortex, 1M points).
+
+One "step" = one kinetic step of the hot path on one mesh: move every point by
+its Taylor-Green displacement, untangle inverted faces, restore the Delaunay
+property with parallel Lawson flips (a single persistent launch).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--n POINTS] [--impl ours|reference]
+
+value: points x steps / device time of the K steps, displacements resident in
+HBM, L2 flushed (256 MB write) before every step and excluded from the timing.
+e2e:   the same steps through the C ABI with host displacement buffers
+(mcl_step_host: pinned host -> device copy inside the timed region) and a
+device -> host read of each step's counters.
+--impl reference: the reference's CPU kinetic path (restated in oracle/, the
+checker) on all host cores, each worker stepping an independent bounded
+sample of the same workload.
+
+Multi-GPU: meshes are independent, so N GPUs run N replicas (weak scaling).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "kinetic pts*steps/s (move + untangle + Delaunay restore), 1M pts Taylor-Green, plain single-mesh form"
+UNIT = "pts*steps/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--n", type=int, default=1_000_000)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--cpu-sample", type=int, default=20000)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+def clocks_start():
+    try:
+        f = open(os.path.join(ROOT, "gpurun_out", "clocks.csv") if os.path.isdir(os.path.join(ROOT, "gpurun_out"))
+                 else os.devnull, "w")
+        p = subprocess.Popen(
+            ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+             "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
+            text=True)
+        return p, f
+    except Exception:
+        return None, None
+
+
+def clocks_stop(p, f, gpu_index=0):
+    if p is None:
+        return None
+    time.sleep(0.25)
+    p.terminate()
+    try:
+        out, _ = p.communicate(timeout=5)
+    except Exception:
+        p.kill()
+        out = ""
+    if f is not None:
+        f.write(out)
+        f.close()
+    sm, mx, reasons = [], 0.0, set()
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    for line in out.strip().splitlines():
+        c = [x.strip() for x in line.split(",")]
+        if len(c) < 9 or c[0] != str(gpu_index):
+            continue
+        try:
+            sm.append(float(c[1]))
+            mx = max(mx, float(c[2]))
+        except ValueError:
+            continue
+        for nm, val in zip(names, c[5:9]):
+            if val.lower() == "active":
+                reasons.add(nm)
+    if not sm:
+        return None
+    return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"], "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------
+def cpu_reference(n, frac_n, seconds, seed, workers):
+    """The reference CPU kinetic path (oracle port: movePoint, untangle until
+    false, delonize restart-scan, FP64 predicates) on `workers` processes, each an
+    independent Taylor-Green mesh of `n` points with the displacement scale of
+    the `frac_n`-point workload; returns aggregate pts*steps/s."""
+    import multiprocessing as mp
+
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(workers) as pool:
+        res = pool.starmap(_cpu_worker, [(n, frac_n, seconds, seed + i) for i in range(workers)])
+    pts_steps = sum(r[0] for r in res)
+    wall = max(r[1] for r in res)
+    flips = sum(r[2] for r in res)
+    steps = sum(r[3] for r in res)
+    return pts_steps / wall, wall, flips, steps
+
+
+def _cpu_worker(n, frac_n, seconds, seed):
+    sys.path.insert(0, ROOT)
+    from mcleap_gb300 import workloads as W
+    from oracle import oracle as O
+
+    pts = O.morton_sort(W.uniform_points(n, seed))
+    m = O.Mesh.build(pts, exact=False)  # the reference's own build (FP64)
+    pos = m.positions()
+    # the same displacement per step relative to the local spacing as the GPU workload
+    frac = 0.5
+    t0 = time.perf_counter()
+    steps = flips = 0
+    while time.perf_counter() - t0 < seconds or steps == 0:
+        d = W.taylor_green_displacements(pos, n, 1, frac=frac)[0]
+        r = m.kinetic_step_ref(d)
+        flips += r["untangle_flips"] + r["delonize_flips"]
+        pos = m.positions()
+        steps += 1
+    wall = time.perf_counter() - t0
+    return n * steps, wall, flips, steps
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    import oracle.oracle as O
+
+    O.build()
+    workers = max(1, os.cpu_count() or 1)
+    sample = min(args.cpu_sample, args.n)
+    secs = max(3.0, args.cpu_seconds)
+    t_all = time.perf_counter()
+    value, wall, flips, steps = cpu_reference(sample, args.n, secs, 1234, workers)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"taylor-green {args.n} pts", "parallelism": "cpu processes"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": workers, "kind": "port",
+                         "sample": f"{workers} independent Taylor-Green meshes of {sample} points, "
+                                   f"{secs:.0f} s each; reference kinetic step = movePoint + untangle "
+                                   f"until false + delonize (restart scan), FP64 predicates"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "wall_s": time.perf_counter() - t_all,
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+def run_ours(args, rank, world, dist):
+    import ctypes as C
+
+    import torch
+
+    import mcleap_gb300 as M
+    from mcleap_gb300 import _lib as L
+    from mcleap_gb300 import build as B
+    from mcleap_gb300 import workloads as W
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    B.build()
+    n, K, Wm = args.n, args.steps, args.warmup
+    pts = W.uniform_points(n, 2026 + rank)
+    t0 = time.perf_counter()
+    ht = M.HostTriangulation()
+    ht.addDelaunayPoints(pts)
+    dt = M.DeviceTriangulation(ht)
+    t_build = time.perf_counter() - t0
+    V = dt.m_pos_size
+    E = dt.m_he_size // 2
+    # displacements for warm-up + timed + e2e steps (host float64 Taylor-Green)
+    total = Wm + K + (0 if args.no_e2e else K)
+    disp = W.taylor_green_displacements(ht.m_pos, n, total)
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+    dev_disp = [torch.from_numpy(d).to(f"cuda:{local}") for d in disp[:Wm + K]]
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+    lib = L.lib()
+    torch.cuda.synchronize()
+
+    # warm-up (untimed), with stats to check the status
+    for k in range(Wm):
+        st = L.StepStats()
+        L.check(lib.mcl_step(dt.handle, dev_disp[k].data_ptr(), sp, C.byref(st)))
+    torch.cuda.synchronize()
+    tot0 = dt.totals()
+
+    # timed region: K steps, device-resident inputs
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    cp, cf = clocks_start()
+    wall0 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        for k in range(K):
+            flush.fill_(k & 0xFF)  # L2 flush, outside the timed window
+            starts[k].record(stream)
+            L.check(lib.mcl_step(dt.handle, dev_disp[Wm + k].data_ptr(), sp, None))
+            ends[k].record(stream)
+    stream.synchronize()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    clocks = clocks_stop(cp, cf, local)
+    step_ms = np.array([s.elapsed_time(e) for s, e in zip(starts, ends)])
+    st = dt.status(stream)
+    if st["status"] != 0:
+        raise RuntimeError(f"engine status {st}")
+    tot1 = dt.totals()
+    dev_s = float(step_ms.sum()) / 1e3
+    if dist:
+        t = torch.tensor([dev_s], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dev_s = float(t.item())
+    value = world * n * K / dev_s
+    flips = tot1["lawson_flips"] - tot0["lawson_flips"] + tot1["removal_flips"] - tot0["removal_flips"]
+    wl_items = (tot1["incircle_tests"] - tot0["incircle_tests"]) - K * (E - 4)
+    inverted = tot1["inverted_faces"] - tot0["inverted_faces"]
+    removed = tot1["removed_vertices"] - tot0["removed_vertices"]
+
+    # roofline of the step kernel: algorithmic bytes per step (move 24 B/vertex,
+    # classification 16 B/edge + 8 B/vertex, 20 B per later work-list item,
+    # 96 B per flip), per launch, over the measured launch duration
+    alg_bytes = 24 * V + 16 * E + 8 * V + 20 * max(wl_items, 0) / K + 96 * flips / K
+    achieved = alg_bytes / (dev_s / K) / 1e9
+    peak, peak_kind = peaks()
+
+    # e2e: host displacements through the C ABI, per-step counters read back
+    e2e = None
+    if not args.no_e2e:
+        host_disp = [torch.from_numpy(d).pin_memory() for d in disp[Wm + K:Wm + 2 * K]]
+        stats = L.StepStats()
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        e0 = time.perf_counter()
+        for k in range(K):
+            L.check(lib.mcl_step_host(dt.handle, host_disp[k].data_ptr(), sp, C.byref(stats)))
+        torch.cuda.synchronize()
+        e_s = time.perf_counter() - e0
+        if dist:
+            t = torch.tensor([e_s], device=f"cuda:{local}")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e_s = float(t.item())
+        e2e = {"value": world * n * K / e_s, "unit": UNIT, "h2d_bytes_per_step": 8 * V,
+               "d2h_bytes_per_step": C.sizeof(L.StepStats), "ms_per_step": 1e3 * e_s / K}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        from oracle import oracle as O
+
+        O.build()
+        sample = min(args.cpu_sample, n)
+        v, w_s, fl, steps = cpu_reference(sample, n, args.cpu_seconds, 99, 1)
+        cpu = {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"1 core, Taylor-Green mesh of {sample} points for {w_s:.1f} s ({steps} steps); "
+                         f"reference kinetic step = movePoint + untangle until false + delonize (restart scan)"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": Wm,
+            "ms_per_step": 1e3 * dev_s / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"taylor-green {n} pts, dt = 0.5 x mean spacing, periodic wrap",
+                       "points": n, "vertices": V, "edges": E, "parallelism": f"replicas x{world}",
+                       "l2": "flushed (256 MB write) before every timed step"},
+            "flips_per_s": world * flips / dev_s,
+            "step_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99)),
+                        "max": float(step_ms.max())},
+            "per_step": {"flips": flips / K, "worklist_items": wl_items / K, "inverted_faces": inverted / K,
+                         "removed_vertices": removed / K},
+            "predicates": {k: tot1[k] - tot0[k] for k in ("incircle_tests", "incircle_fp64", "incircle_exact",
+                                                          "orient_fp64", "orient_exact", "sos_decisions")},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
+                         "kernel": "k_engine", "alg_bytes_per_launch": alg_bytes},
+            "e2e": e2e, "cpu_baseline": cpu, "clocks": clocks,
+            "gpu_launches": 2 * K,
+            "wall_s": wall, "build_s": t_build,
+        }
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist_mod
+
+        if args.impl == "ours":
+            torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist_mod.init_process_group("nccl" if args.impl == "ours" else "gloo")
+        dist = dist_mod
+    try:
+        if args.impl == "reference":
+            run_reference(args, rank, world)
+        else:
+            run_ours(args, rank, world, dist)
+    finally:
+        if dist is not None:
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

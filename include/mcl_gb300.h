@@ -141,6 +141,10 @@ int mcl_step(mcl_mesh* m, const mcl_float2* d_dev, void* stream, mcl_step_stats*
 /* Same step with the displacement in host memory (copied in on `stream`). */
 int mcl_step_host(mcl_mesh* m, const mcl_float2* d_host, void* stream, mcl_step_stats* stats_host);
 
+/* Counters summed over every call on this mesh since creation (synchronises
+ * the device); *calls_host (may be NULL) = number of engine launches. */
+int mcl_mesh_totals(mcl_mesh* m, mcl_step_stats* totals_host, int64_t* calls_host);
+
 /* Status of the last asynchronous step on this mesh (synchronises the stream). */
 int mcl_mesh_last_status(mcl_mesh* m, void* stream, mcl_step_stats* stats_host);
 

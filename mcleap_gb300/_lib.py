@@ -30,7 +30,7 @@ EXPORTS = [
     "mcl_status_string", "mcl_last_error", "mcl_version",
     "mcl_mesh_create_from_aos", "mcl_mesh_build", "mcl_mesh_destroy", "mcl_mesh_sizes",
     "mcl_mesh_download_aos", "mcl_mesh_upload_aos", "mcl_mesh_positions", "mcl_mesh_copy_positions", "mcl_move", "mcl_integrate",
-    "mcl_untangle", "mcl_delaunay_restore", "mcl_step", "mcl_step_host", "mcl_mesh_last_status",
+    "mcl_untangle", "mcl_delaunay_restore", "mcl_step", "mcl_step_host", "mcl_mesh_last_status", "mcl_mesh_totals",
     "mcl_one_ring", "mcl_closest_neighbors", "mcl_mesh_frnn",
     "mcl_grid_create", "mcl_grid_destroy", "mcl_grid_update", "mcl_grid_tables", "mcl_grid_frnn",
     "mcl_grid_mean_occupancy", "mcl_debug_predicates_host", "mcl_debug_predicates_device", "mcl_mesh_validate", "mcl_debug_state",
@@ -89,6 +89,7 @@ def lib():
             "mcl_step": ([vp, vp, vp, C.POINTER(StepStats)], i32),
             "mcl_step_host": ([vp, vp, vp, C.POINTER(StepStats)], i32),
             "mcl_mesh_last_status": ([vp, vp, C.POINTER(StepStats)], i32),
+            "mcl_mesh_totals": ([vp, C.POINTER(StepStats), C.POINTER(i64)], i32),
             "mcl_one_ring": ([vp, i32, i32, vp, vp, C.POINTER(i64)], i32),
             "mcl_closest_neighbors": ([vp, i32, i32, vp, vp, vp], i32),
             "mcl_mesh_frnn": ([vp, f32, i32, i32, vp, vp, C.POINTER(i64)], i32),

@@ -1044,10 +1044,15 @@ static KParams make_params(mcl_mesh* m, int mode) {
 
 // Reset the per-call part of the device state (counters, lists, status).
 __global__ void k_reset_state(DevState* st) {
+  // fold the last call's counters into the running totals, then clear them
+  for (int i = 0; i < C_COUNT; ++i) st->tot[i] += st->c[i];
+  st->calls += 1;
   const unsigned ep = st->epoch;
   DevState z;
   memset(&z, 0, sizeof(z));
   z.epoch = ep;
+  for (int i = 0; i < C_COUNT; ++i) z.tot[i] = st->tot[i];
+  z.calls = st->calls;
   *st = z;
 }
 
@@ -1187,6 +1192,18 @@ const char* mcl_status_string(int status) {
 
 const char* mcl_last_error(void) { return g_last_error.c_str(); }
 int mcl_version(void) { return 1; }
+
+int mcl_mesh_totals(mcl_mesh* m, mcl_step_stats* totals, int64_t* calls) {
+  if (!m || !totals) return fail(MCL_ERR_INVALID_ARGUMENT, "null argument");
+  CK(cudaDeviceSynchronize());
+  CK(cudaMemcpy(m->st_host, m->st, sizeof(DevState), cudaMemcpyDeviceToHost));
+  DevState t = *m->st_host;
+  for (int i = 0; i < C_COUNT; ++i) t.c[i] = t.tot[i] + t.c[i];
+  fill_stats(t, totals);
+  totals->status = m->st_host->status;
+  if (calls) *calls = (int64_t)t.calls;
+  return MCL_OK;
+}
 
 int mcl_debug_state(mcl_mesh* m, int32_t* out68) {
   if (!m || !out68) return fail(MCL_ERR_INVALID_ARGUMENT, "null argument");

@@ -56,6 +56,8 @@ struct DevState {
   unsigned int epoch;      // next unused stamp
   int site;                // source line that set `status` (diagnostics)
   int dbg[68];             // first failing vertex star: v, deg, then neighbour ids
+  unsigned long long tot[C_COUNT];  // running totals over all calls (never reset)
+  unsigned long long calls;
   unsigned long long c[C_COUNT];
 };
 

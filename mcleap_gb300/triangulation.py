@@ -183,6 +183,15 @@ class DeviceTriangulation:
             return self.last_stats
         return None
 
+    def totals(self):
+        """Counters summed over every call since creation, and the call count."""
+        st = L.StepStats()
+        calls = C.c_int64()
+        L.check(L.lib().mcl_mesh_totals(self.handle, C.byref(st), C.byref(calls)))
+        d = st.as_dict()
+        d["calls"] = calls.value
+        return d
+
     def validate(self):
         """Counts of structural invariant violations (all zero for a valid mesh)."""
         out = np.zeros(8, np.int64)

@@ -1,0 +1,71 @@
+"""Seeded synthetic workloads with the shapes of the reference's benchmark
+configurations (no dataset is involved).  Coordinates live in the unit square
+scaled by 2^13 (exact in float32): the reference's CPU point location needs
+inputs of magnitude >~ 1e3 next to its +-1e7 bounding square, and every exact
+orientation / incircle sign and every float distance comparison is unchanged
+by a power-of-two scale."""
+import numpy as np
+
+SCALE = np.float32(8192.0)
+
+
+def uniform_points(n, seed):
+    rng = np.random.default_rng(seed)
+    return (rng.random((n, 2), dtype=np.float32) * SCALE).astype(np.float32)
+
+
+def mean_spacing(n):
+    return float(SCALE) / np.sqrt(n)
+
+
+def taylor_green_displacements(pos, n, steps, frac=0.5):
+    """Displacements of `steps` forward-Euler steps of the Taylor-Green vortex
+    u = (sin 2pi x cos 2pi y, -cos 2pi x sin 2pi y) on the unit torus, dt such
+    that the largest displacement is `frac` x mean spacing.  The velocity is
+    evaluated in float64 at the current float32 positions; the new position is
+    wrapped into [0, 8192) and the float32 displacement is what the engine adds
+    (pos += d in float32), so host and device follow identical trajectories.
+    pos: (V, 2) float32 with the 4 bounding corners first.  Returns a list of
+    (V, 2) float32 arrays."""
+    p = pos.astype(np.float32).copy()
+    dt = frac * mean_spacing(n)
+    out = []
+    L = float(SCALE)
+    for _ in range(steps):
+        q = p[4:].astype(np.float64) / L
+        u = np.sin(2 * np.pi * q[:, 0]) * np.cos(2 * np.pi * q[:, 1])
+        v = -np.cos(2 * np.pi * q[:, 0]) * np.sin(2 * np.pi * q[:, 1])
+        new = (p[4:].astype(np.float64) + np.stack([u, v], 1) * dt) % L
+        new32 = new.astype(np.float32)
+        new32[new32 >= SCALE] = 0.0
+        d = np.zeros_like(p)
+        d[4:] = (new32 - p[4:]).astype(np.float32)
+        p[4:] = (p[4:] + d[4:]).astype(np.float32)
+        out.append(d)
+    return out
+
+
+def gaussian_displacements(pos, sigma, seed, steps):
+    """Gaussian random walk N(0, sigma^2) per coordinate, clamped to the box,
+    points that would land on an occupied spot stay put (exact duplicates are
+    not a triangulation input)."""
+    rng = np.random.default_rng(seed)
+    p = pos.astype(np.float32).copy()
+    hi = np.nextafter(SCALE, np.float32(0))
+    out = []
+    for _ in range(steps):
+        d = (rng.standard_normal(p.shape) * sigma).astype(np.float32)
+        d[:4] = 0
+        tgt = np.clip(p + d, np.float32(0), hi).astype(np.float32)
+        d = (tgt - p).astype(np.float32)
+        d[:4] = 0
+        for _ in range(64):
+            new = (p + d).astype(np.float32)
+            _, inv, cnt = np.unique(new, axis=0, return_inverse=True, return_counts=True)
+            dup = cnt[inv.ravel()] > 1
+            if not dup.any():
+                break
+            d[dup] = 0
+        p = (p + d).astype(np.float32)
+        out.append(d)
+    return out

@@ -134,6 +134,7 @@ def closest_test(R):
         pos = ref_aos(R, h)[0]
         d = ((pos[:, None, :] - pos[None, :, :]).astype(np.float32) ** 2).sum(-1, dtype=np.float32)
         np.fill_diagonal(d, np.inf)
+        out[f"points_{n}"] = pts
         out[f"pos_{n}"] = pos
         out[f"closest_{n}"] = d.argmin(1).astype(np.int32)
         R.ref_free(h)

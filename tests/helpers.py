@@ -28,14 +28,12 @@ def gaussian_disp(V, sigma, seed, clamp_pos=None):
         d[:4] = 0
         # clamping can stack points on the same spot (a box corner); exact
         # duplicates are rejected by the engine, so such points stay put
-        for _ in range(8):
+        for _ in range(64):
             new = (clamp_pos + d).astype(np.float32)
-            _, first, counts = np.unique(new, axis=0, return_index=True, return_counts=True)
-            if (counts == 1).all():
+            _, inv, counts = np.unique(new, axis=0, return_inverse=True, return_counts=True)
+            dup = counts[inv.ravel()] > 1
+            if not dup.any():
                 break
-            keep = np.zeros(len(new), bool)
-            keep[first] = True
-            dup = ~keep
             d[dup] = 0
     return d
 

@@ -165,9 +165,7 @@ def test_one_ring_and_closest(M):
     # closest neighbours (tests/test_closest_neighbors.cu): brute-force argmin
     cl = np.load(os.path.join(G, "closest.npz"))
     for n in (10, 100, 1000):
-        from oracle import oracle as O2  # noqa: F401
-
-        pts = cl[f"pos_{n}"][4:].copy()
+        pts = cl[f"points_{n}"].copy()
         ht2, _ = build_pair(M, pts)
         assert np.array_equal(ht2.m_pos, cl[f"pos_{n}"])
         dt2 = M.DeviceTriangulation(ht2)
