@@ -201,6 +201,24 @@ int mcl_grid_frnn(mcl_grid* g, const mcl_float2* pos_dev, float r, int max_nb, i
 /* mean_num_particle_in_cell (include/gridCount2d.h:314-334). */
 int mcl_grid_mean_occupancy(mcl_grid* g, float* mean_host);
 
+/* Grid fixed-radius neighbours for callers that cannot allocate device memory
+ * (frameworks that own all GPU memory, loops that must not block in an
+ * allocator).  No counterpart in the reference: it does what mcl_grid_create +
+ * mcl_grid_update + mcl_grid_frnn do, but allocates nothing and leaves pos_dev
+ * untouched.  Its scratch is one fixed array in the library's device image
+ * (5.3 MB held on every GPU that loads the library until exit); limits: n <=
+ * 262144 points and at most 262144 cell-table entries, else MCL_ERR_CAPACITY.
+ * Outputs (caller-owned device buffers): sorted_pos_dev[n] = positions in cell
+ * order, perm_dev[n] = sorted slot of input point i, counts_dev[n] and
+ * ids_dev[n*max_nb] = neighbours in sorted index space, as mcl_grid_frnn.
+ * The first call on a device looks up the array's device address (do it before
+ * any stream capture).  All calls share the array, so calls that overlap on the
+ * GPU race; serialise them (one stream, or events). */
+int mcl_grid_frnn_noalloc(const mcl_float2* pos_dev, int64_t n, float min_x, float min_y, float cell_x,
+                          float cell_y, int32_t cells_x, int32_t cells_y, int flags, float r, int max_nb,
+                          mcl_float2* sorted_pos_dev, int32_t* perm_dev, int32_t* counts_dev, int32_t* ids_dev,
+                          void* stream, int64_t* overflow_host);
+
 /* ---- diagnostics ------------------------------------------------------------ */
 /* Structural invariants of the device mesh; counts8[k] = violations of kind k:
  * 0 next/prev not inverse, 1 inner face not a 3-cycle, 2 apex != origin(prev),

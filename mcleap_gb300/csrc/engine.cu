@@ -860,6 +860,12 @@ static int fail(int code, const std::string& msg) {
   return code;
 }
 
+}  // namespace mcl
+
+void mcl_set_last_error(const std::string& msg) { mcl::g_last_error = msg; }
+
+namespace mcl {
+
 static int cuda_fail(cudaError_t e, const char* what) {
   return fail(e == cudaErrorMemoryAllocation ? MCL_ERR_OUT_OF_MEMORY : MCL_ERR_CUDA,
               std::string(what) + ": " + cudaGetErrorString(e));
@@ -1190,7 +1196,7 @@ const char* mcl_status_string(int status) {
   }
 }
 
-const char* mcl_last_error(void) { return g_last_error.c_str(); }
+const char* mcl_last_error(void) { return mcl::g_last_error.c_str(); }
 int mcl_version(void) { return 1; }
 
 int mcl_mesh_totals(mcl_mesh* m, mcl_step_stats* totals, int64_t* calls) {

@@ -19,9 +19,13 @@
 
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <string>
 
 #include "predicates.cuh"
 #include "../../include/mcl_gb300.h"
+
+// Message returned by mcl_last_error() on this host thread.
+void mcl_set_last_error(const std::string& msg);
 
 namespace mcl {
 

@@ -10,7 +10,9 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -20,10 +22,8 @@ using namespace mcl;
 
 namespace {
 
-thread_local std::string g_err;
-
 int qfail(int code, const std::string& msg) {
-  g_err = msg;
+  mcl_set_last_error(msg);
   return code;
 }
 
@@ -343,6 +343,30 @@ __global__ void k_mean_occupancy(int64_t ncells, const int* count, unsigned long
   }
 }
 
+// Exclusive scan of up to a few hundred thousand ints in one block, entirely on
+// the device (each thread scans a contiguous chunk, then the chunk totals).
+__global__ void k_scan_one_block(const int* in, int* out, int64_t n) {
+  __shared__ int tot[1024];
+  const int64_t per = (n + blockDim.x - 1) / blockDim.x;
+  const int64_t lo = threadIdx.x * per, hi = min(n, lo + per);
+  int run = 0;
+  for (int64_t i = lo; i < hi; ++i) run += in[i];
+  tot[threadIdx.x] = run;
+  __syncthreads();
+  for (int o = 1; o < (int)blockDim.x; o <<= 1) {
+    const int y = threadIdx.x >= (unsigned)o ? tot[threadIdx.x - o] : 0;
+    __syncthreads();
+    tot[threadIdx.x] += y;
+    __syncthreads();
+  }
+  int acc = threadIdx.x ? tot[threadIdx.x - 1] : 0;
+  for (int64_t i = lo; i < hi; ++i) {
+    const int x = in[i];
+    out[i] = acc;
+    acc += x;
+  }
+}
+
 // Exclusive scan of n ints (device), with a temporary of per-block sums.
 int scan_exclusive(const int* in, int* out, int64_t n, int* tmp, int* tmp2, cudaStream_t s) {
   const int64_t nb = (n + 1023) / 1024;
@@ -593,3 +617,93 @@ int mcl_grid_mean_occupancy(mcl_grid* g, float* mean) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Grid neighbours without allocation.
+//
+// Some callers cannot allocate device memory at all: host frameworks that
+// reserve the whole GPU up front and hand memory out only through their own
+// pool, and real-time loops that must never block in an allocator.  For them
+// this variant of GridCount2d::update + apply_f_frnn keeps its scratch (cell
+// tables and per-point work arrays) in one fixed array that lives in the
+// library's device image, so the call itself allocates nothing.  Limits:
+// at most kNoAllocMaxPoints points and kNoAllocMaxCells cell-table entries
+// (the Morton-padded cell count; see mcl_grid_create).  Every GPU that loads the
+// library holds these 5.3 MB until the process exits.
+constexpr int64_t kNoAllocMaxPoints = 262144;
+constexpr int64_t kNoAllocMaxCells = 262144;
+constexpr int64_t kNoAllocWords = 2 * kNoAllocMaxPoints + 3 * kNoAllocMaxCells + 64;
+static __device__ __align__(256) int g_noalloc_scratch[kNoAllocWords];
+
+namespace {
+int* g_noalloc_ptr[64];  // device address of the scratch array, per device id
+std::mutex g_noalloc_mutex;
+
+int noalloc_scratch(int** out) {
+  int dev = 0;
+  QCK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return qfail(MCL_ERR_NO_DEVICE, "device id out of range");
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return qfail(MCL_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    g_noalloc_ptr[dev] = static_cast<int*>(p);
+  }
+  *out = g_noalloc_ptr[dev];
+  return MCL_OK;
+}
+}  // namespace
+
+extern "C" int mcl_grid_frnn_noalloc(const mcl_float2* pos, int64_t n, float min_x, float min_y, float cell_x,
+                                     float cell_y, int32_t cells_x, int32_t cells_y, int flags, float r, int max_nb,
+                                     mcl_float2* sorted_pos, int32_t* perm, int32_t* counts, int32_t* ids,
+                                     void* stream, int64_t* overflow) {
+  if (!pos || !sorted_pos || !perm || !counts || !ids || n < 0 || cells_x < 1 || cells_y < 1 || max_nb < 1 ||
+      !(cell_x > 0.f) || !(cell_y > 0.f) || !(r >= 0.f))
+    return qfail(MCL_ERR_INVALID_ARGUMENT, "bad args");
+  int side = 1;
+  while (side < std::max(cells_x, cells_y)) side <<= 1;
+  const int64_t mcells = (int64_t)side * side;
+  const int morton = (side <= 65536 && mcells <= 4 * (int64_t)cells_x * cells_y + 1024) ? 1 : 0;
+  const int64_t ncells = morton ? mcells : (int64_t)cells_x * cells_y;
+  if (n > kNoAllocMaxPoints)
+    return qfail(MCL_ERR_CAPACITY, "mcl_grid_frnn_noalloc: more than 262144 points");
+  if (ncells > kNoAllocMaxCells)
+    return qfail(MCL_ERR_CAPACITY, "mcl_grid_frnn_noalloc: cell table larger than 262144 entries");
+  if (n == 0) return MCL_OK;
+  int* base = nullptr;
+  const int rc = noalloc_scratch(&base);
+  if (rc != MCL_OK) return rc;
+  int* cell = base;
+  int* src = cell + kNoAllocMaxPoints;
+  int* count = src + kNoAllocMaxPoints;
+  int* start = count + kNoAllocMaxCells;
+  int* cursor = start + kNoAllocMaxCells;
+  unsigned long long* ovf = reinterpret_cast<unsigned long long*>(cursor + kNoAllocMaxCells);
+  cudaStream_t s = (cudaStream_t)stream;
+  GridView G;
+  G.minx = min_x; G.miny = min_y; G.cx = cell_x; G.cy = cell_y;
+  G.nx = cells_x; G.ny = cells_y; G.morton = morton; G.periodic = (flags & MCL_GRID_PERIODIC) ? 1 : 0;
+  const int nn = (int)n;
+  // the array keeps the previous call's contents: clear what must start at zero
+  QCK(cudaMemsetAsync(count, 0, 4 * ncells, s));
+  QCK(cudaMemsetAsync(ovf, 0, 8, s));
+  k_grid_hash<<<(nn + 255) / 256, 256, 0, s>>>(G, nn, (const float2*)pos, cell, count);
+  k_scan_one_block<<<1, 1024, 0, s>>>(count, start, ncells);
+  QCK(cudaMemcpyAsync(cursor, start, 4 * ncells, cudaMemcpyDeviceToDevice, s));
+  k_grid_scatter<<<(nn + 255) / 256, 256, 0, s>>>(nn, cell, cursor, perm, src);
+  k_grid_sort_cells<<<(unsigned)((ncells + 255) / 256), 256, 0, s>>>(ncells, start, count, src, perm);
+  k_gather<<<(nn + 255) / 256, 256, 0, s>>>(nn, src, (const float2*)pos, (float2*)sorted_pos);
+  const int wx = std::max(1, (int)std::ceil(r / cell_x)), wy = std::max(1, (int)std::ceil(r / cell_y));
+  k_grid_frnn<<<(nn + 127) / 128, 128, 0, s>>>(G, nn, (const float2*)sorted_pos, start, count, r * r, wx, wy,
+                                               cell_x * cells_x, cell_y * cells_y, max_nb, counts, ids, ovf);
+  QCK(cudaGetLastError());
+  if (overflow) {
+    unsigned long long t = 0;
+    QCK(cudaMemcpyAsync(&t, ovf, 8, cudaMemcpyDeviceToHost, s));
+    QCK(cudaStreamSynchronize(s));
+    *overflow = (int64_t)t;
+  }
+  return MCL_OK;
+}
