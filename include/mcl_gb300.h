@@ -230,6 +230,10 @@ int mcl_mesh_validate(mcl_mesh* m, int64_t* counts8);
  * vertex whose removal failed (0 if none), out68[1] = its degree, then its
  * neighbour ids in counter-clockwise order. */
 int mcl_debug_state(mcl_mesh* m, int32_t* out68);
+/* Device timestamps (ns, %globaltimer) of the last engine launch: [0] start,
+ * [1] after the classification barrier, [2 + r] end of flip round r (r < 40),
+ * [47] end; unused slots keep older values. */
+int mcl_debug_timeline(mcl_mesh* m, int64_t* out48);
 
 /* The device predicate ladder evaluated on the host CPU (same source as the
  * device code), for testing without a GPU.  kind 0 = orient2d on n records of

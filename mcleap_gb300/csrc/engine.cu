@@ -39,70 +39,36 @@ namespace cg = cooperative_groups;
 namespace mcl {
 
 constexpr int kThreads = 256;
-constexpr int kStage = 2048;
 constexpr unsigned kFull = 0xffffffffu;
 
 // ---------------------------------------------------------------------------
-// Block-aggregated append to a global work-list: items are staged in shared
-// memory and flushed with one atomicAdd per block when the stage fills up.
-struct Stage {
-  int n;
-  int base;
-  int warp_sum[kThreads / 32];
-  int items[kStage];
-};
-
-__device__ void stage_flush(Stage& S, int* gl, int* gcount, int gcap, DevState* st) {
-  __syncthreads();
-  if (threadIdx.x == 0) S.base = S.n ? atomicAdd(gcount, S.n) : 0;
-  __syncthreads();
-  const int n = S.n, base = S.base;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    if (base + i < gcap) gl[base + i] = S.items[i];
-    else if (atomicCAS(&st->status, MCL_OK, MCL_ERR_CAPACITY) == MCL_OK) st->site = __LINE__;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) S.n = 0;
-  __syncthreads();
-}
-
-// Block-collective: every thread of the block calls it with its k items.
+// Warp-aggregated append to a global work-list: one atomicAdd per warp that
+// has items, no block barrier (so warps never wait for each other between
+// loop iterations and memory latency overlaps freely).  All 32 lanes of the
+// warp must call it together; lanes without items pass k = 0.
 template <int K>
-__device__ void stage_push(Stage& S, const int (&mine)[K], int k, int* gl, int* gcount, int gcap,
-                           DevState* st) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+__device__ __forceinline__ void warp_push(const int (&mine)[K], int k, int* gl, int* gcount, int gcap,
+                                          DevState* st) {
+  const int lane = threadIdx.x & 31;
   int x = k;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
     const int y = __shfl_up_sync(kFull, x, o);
     if (lane >= o) x += y;
   }
-  if (lane == 31) S.warp_sum[wid] = x;
-  __syncthreads();
-  if (wid == 0) {
-    int s = lane < nw ? S.warp_sum[lane] : 0;
+  const int total = __shfl_sync(kFull, x, 31);
+  if (total == 0) return;
+  int base = 0;
+  if (lane == 31) base = atomicAdd(gcount, total);
+  base = __shfl_sync(kFull, base, 31);
+  const int off = base + x - k;
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(kFull, s, o);
-      if (lane >= o) s += y;
+  for (int j = 0; j < K; ++j) {
+    if (j < k) {
+      if (off + j < gcap) __stcg(gl + off + j, mine[j]);
+      else if (atomicCAS(&st->status, MCL_OK, MCL_ERR_CAPACITY) == MCL_OK) st->site = __LINE__;
     }
-    if (lane < nw) S.warp_sum[lane] = s;
   }
-  __syncthreads();
-  const int total = S.warp_sum[nw - 1];
-  const int off = (wid ? S.warp_sum[wid - 1] : 0) + x - k;
-  if (total == 0) {
-    __syncthreads();
-    return;
-  }
-  if (S.n + total > kStage) stage_flush(S, gl, gcount, gcap, st);
-  const int n0 = S.n;
-#pragma unroll
-  for (int j = 0; j < K; ++j)
-    if (j < k) S.items[n0 + off + j] = mine[j];
-  __syncthreads();
-  if (threadIdx.x == 0) S.n = n0 + total;
-  __syncthreads();
 }
 
 #define set_error(P, code) flag_error_at(P, code, __LINE__)
@@ -117,11 +83,11 @@ __device__ void flush_counters(const KParams& P, LocalCounters& lc) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) inc += __shfl_down_sync(kFull, inc, o);
   if ((threadIdx.x & 31) == 0 && inc) atomicAdd(&P.st->c[C_INCIRCLE], inc);
-  if (lc.incircle_fp64) atomicAdd(&P.st->c[C_INCIRCLE_FP64], lc.incircle_fp64);
-  if (lc.incircle_exact) atomicAdd(&P.st->c[C_INCIRCLE_EXACT], lc.incircle_exact);
-  if (lc.orient_fp64) atomicAdd(&P.st->c[C_ORIENT_FP64], lc.orient_fp64);
-  if (lc.orient_exact) atomicAdd(&P.st->c[C_ORIENT_EXACT], lc.orient_exact);
-  if (lc.sos) atomicAdd(&P.st->c[C_SOS], lc.sos);
+  if (lc.incircle_fp64) atomicAdd(&P.st->c[C_INCIRCLE_FP64], (unsigned long long)lc.incircle_fp64);
+  if (lc.incircle_exact) atomicAdd(&P.st->c[C_INCIRCLE_EXACT], (unsigned long long)lc.incircle_exact);
+  if (lc.orient_fp64) atomicAdd(&P.st->c[C_ORIENT_FP64], (unsigned long long)lc.orient_fp64);
+  if (lc.orient_exact) atomicAdd(&P.st->c[C_ORIENT_EXACT], (unsigned long long)lc.orient_exact);
+  if (lc.sos) atomicAdd(&P.st->c[C_SOS], (unsigned long long)lc.sos);
   if (lc.overflow) {
     atomicAdd(&P.st->c[C_OVERFLOW], 1ull);
     set_error(P, MCL_ERR_PREDICATE);
@@ -129,155 +95,318 @@ __device__ void flush_counters(const KParams& P, LocalCounters& lc) {
 }
 
 // ---------------------------------------------------------------------------
-// Phase: move.  pos (new) = pos_old + displacement; fixed vertices copy.
-__device__ void phase_move(const KParams& P) {
-  const int stride = gridDim.x * blockDim.x;
-  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < P.V; v += stride) {
-    float2 p = P.pos_old[v];
-    if (!P.vfix[v]) {
-      if (P.move_mode == MOVE_DISPLACE) {
-        const float2 d = P.disp[v];
-        p.x = fadd(p.x, d.x);
-        p.y = fadd(p.y, d.y);
-      } else if (P.move_mode == MOVE_INTEGRATE) {
-        const float2 u = P.vel[v];
-        const float t = P.dt[v];
-        p.x = fadd(p.x, fmul(u.x, t));
-        p.y = fadd(p.y, fmul(u.y, t));
-      }
-    }
-    P.pos[v] = p;
+// New position of v for a fused move: pos_old + displacement (or + v*dt);
+// fixed vertices (bounding corners) stay.  pos_old, disp, vel and dt are
+// read-only for the whole launch, so they go through the read-only cache.
+__device__ __forceinline__ float2 moved_pos(const KParams& P, int v) {
+  float2 p = __ldg(P.pos_old + v);
+  if (__ldg(P.vfix + v)) return p;
+  if (P.move_mode == MOVE_DISPLACE) {
+    const float2 d = __ldg(P.disp + v);
+    p.x = fadd(p.x, d.x);
+    p.y = fadd(p.y, d.y);
+  } else if (P.move_mode == MOVE_INTEGRATE) {
+    const float2 u = __ldg(P.vel + v);
+    const float t = __ldg(P.dt + v);
+    p.x = fadd(p.x, fmul(u.x, t));
+    p.y = fadd(p.y, fmul(u.y, t));
   }
+  return p;
+}
+
+// Phase A of a flip round for edge e (already known to be non-Delaunay): claim
+// both faces with a priority key, remember the face ids for phase B.
+__device__ __forceinline__ void claim_edge(const KParams& P, int e, unsigned sc) {
+  const int4 w = ld_en(P, e);
+  const int fa = min(2 * e, min(w.x, w.y)), fb = min(2 * e + 1, min(w.z, w.w));
+  const unsigned long long key = ((unsigned long long)sc << 32) | (unsigned)(~mix32((unsigned)e ^ sc));
+  atomicMax(P.claim + fa, key);
+  atomicMax(P.claim + fb, key);
+  __stcg(P.efa + e, make_int2(fa, fb));
+  __stcg(P.cand + e, sc);
+}
+
+// Full predicate ladder for one edge: counts its non-positive faces into `bad`
+// and returns true when both faces are positive and the edge is non-Delaunay.
+template <bool kFixedPos>
+__device__ __forceinline__ bool resolve_edge(const KParams& P, int e, LocalCounters& lc, int& bad) {
+  const int4 q = ld_ev(P, e);
+  const float2 a = ldpos_t<kFixedPos>(P, q.x), b = ldpos_t<kFixedPos>(P, q.y);
+  const float2 c = q.z >= 0 ? ldpos_t<kFixedPos>(P, q.z) : a;
+  const float2 d = q.w >= 0 ? ldpos_t<kFixedPos>(P, q.w) : a;
+  const int sa = q.z >= 0 ? orient_v(P, a, b, c, lc) : 1;
+  const int sb = q.w >= 0 ? orient_v(P, b, a, d, lc) : 1;
+  if (sa <= 0 || sb <= 0) {
+    bad += (sa <= 0) + (sb <= 0);
+    return false;
+  }
+  if (q.z < 0 || q.w < 0) return false;
+  lc.incircle++;
+  return incircle_sos(a.x, a.y, b.x, b.y, c.x, c.y, d.x, d.y, q.x, q.y, q.z, q.w, &lc, &lc.overflow) > 0;
 }
 
 // ---------------------------------------------------------------------------
-// Phase: classify every edge.  Counts non-positive faces; when `push` is set,
-// appends the locally non-Delaunay edges of a valid mesh to work-list 0.
-__device__ void phase_classify(const KParams& P, Stage& S, unsigned qstamp, LocalCounters& lc) {
+// Phase: (move +) classify every edge.  With a move, a vertex pass writes the
+// new positions first (one grid barrier).  Counts non-positive faces;
+// non-Delaunay edges of positive faces are queued on work-list 0 and claim
+// their faces for the first flip round (stamp sc).
+//
+// The edge loop evaluates only the FP32 filters: an out-of-line call to the
+// FP64 / exact / perturbation stages inside the loop would cost more than the
+// whole filter.  Edges the filters cannot decide (a few per million) go to the
+// hard list, which is resolved with the full ladder after the barrier; the
+// caller must call phase_classify_hard before reading `inverted`.
+template <bool kFixedPos>
+__device__ void phase_classify(cg::grid_group& g, const KParams& P, unsigned qstamp, unsigned sc,
+                               LocalCounters& lc) {
   const int stride = gridDim.x * blockDim.x;
+  if (P.move_mode != MOVE_NONE) {
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < P.V; v += stride) __stcg(P.pos + v, moved_pos(P, v));
+    g.sync();
+  }
   int bad = 0;
+  unsigned ninc = 0;
+  int def0 = -1, def1 = -1;  // edges deferred to the full ladder after the loop
   for (int base = blockIdx.x * blockDim.x; base < P.E; base += stride) {
     const int e = base + threadIdx.x;
     int mine[1];
     int k = 0;
+    int hard[1];
+    int kh = 0;
     if (e < P.E) {
       const int4 q = ld_ev(P, e);
       if (q.x >= 0 && (bad_v(P, q.x) || bad_v(P, q.y) || q.z >= P.V || q.w >= P.V)) {
         flag_error(P, MCL_ERR_DEGENERATE_INPUT);
       } else if (q.x >= 0) {
-        const float2 a = ldpos(P, q.x), b = ldpos(P, q.y);
-        bool ok = true;
-        if (q.z >= 0) {
-          const float2 c = ldpos(P, q.z);
-          if (orient_v(P, a, b, c, lc) <= 0) { ok = false; ++bad; }
+        const float2 a = ldpos_t<kFixedPos>(P, q.x), b = ldpos_t<kFixedPos>(P, q.y);
+        const float2 c = q.z >= 0 ? ldpos_t<kFixedPos>(P, q.z) : a;
+        const float2 d = q.w >= 0 ? ldpos_t<kFixedPos>(P, q.w) : a;
+        const int sa = q.z >= 0 ? orient2d_fp32(a.x, a.y, b.x, b.y, c.x, c.y) : 1;
+        const int sb = q.w >= 0 ? orient2d_fp32(b.x, b.y, a.x, a.y, d.x, d.y) : 1;
+        bool defer = false;
+        if (sa == 2 || sb == 2) {
+          defer = true;
+        } else if (sa <= 0 || sb <= 0) {
+          bad += (sa <= 0) + (sb <= 0);
+        } else if (q.z >= 0 && q.w >= 0) {
+          ++ninc;
+          const int si = incircle_fp32(a.x, a.y, b.x, b.y, c.x, c.y, d.x, d.y);
+          if (si == 2) {
+            defer = true;
+          } else if (si > 0 && enqueue_once(P, e, qstamp)) {
+            claim_edge(P, e, sc);
+            mine[k++] = e;
+          }
         }
-        if (q.w >= 0) {
-          const float2 d = ldpos(P, q.w);
-          if (orient_v(P, b, a, d, lc) <= 0) { ok = false; ++bad; }
+        if (defer) {
+          if (def0 < 0) def0 = e;
+          else if (def1 < 0) def1 = e;
+          else hard[kh++] = e;
         }
-        if (ok && edge_illegal(P, q, lc) && enqueue_once(P, e, qstamp)) mine[k++] = e;
       }
     }
-    stage_push<1>(S, mine, k, P.wl0, &P.st->wl_count[0], P.E, P.st);
+    if (__any_sync(kFull, k > 0)) warp_push(mine, k, P.wl0, &P.st->wl_count[0], P.E, P.st);
+    if (__any_sync(kFull, kh > 0)) warp_push(hard, kh, P.hard, &P.st->hard_count, P.E, P.st);
   }
-  stage_flush(S, P.wl0, &P.st->wl_count[0], P.E, P.st);
+  // the deferred edges, with the full predicate ladder (out of the loop, so
+  // the out-of-line calls do not weigh on the loop above)
+  {
+    int mine[2];
+    int k = 0;
+    const int defs[2] = {def0, def1};
+    for (int j = 0; j < 2; ++j) {
+      const int e = defs[j];
+      if (e >= 0 && resolve_edge<kFixedPos>(P, e, lc, bad) && enqueue_once(P, e, qstamp)) {
+        claim_edge(P, e, sc);
+        mine[k++] = e;
+      }
+    }
+    if (__any_sync(kFull, k > 0)) warp_push(mine, k, P.wl0, &P.st->wl_count[0], P.E, P.st);
+  }
+  lc.incircle += ninc;
   if (bad) atomicAdd(&P.st->inverted, bad);
 }
 
+// Resolve the hard list of phase_classify (after its barrier) with the full
+// predicate ladder.  Returns after a barrier when there was anything to do.
+template <bool kFixedPos>
+__device__ void phase_classify_hard(cg::grid_group& g, const KParams& P, unsigned qstamp, unsigned sc,
+                                    LocalCounters& lc) {
+  const int n = ld_i(&P.st->hard_count);
+  if (n == 0) return;  // uniform: read after the classification barrier
+  const int stride = gridDim.x * blockDim.x;
+  int bad = 0;
+  for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
+    const int i = base + threadIdx.x;
+    int mine[1];
+    int k = 0;
+    if (i < n) {
+      const int e = ld_i(P.hard + i);
+      if (resolve_edge<kFixedPos>(P, e, lc, bad) && enqueue_once(P, e, qstamp)) {
+        claim_edge(P, e, sc);
+        mine[k++] = e;
+      }
+    }
+    if (__any_sync(kFull, k > 0)) warp_push(mine, k, P.wl0, &P.st->wl_count[0], P.E, P.st);
+  }
+  if (bad) atomicAdd(&P.st->inverted, bad);
+  g.sync();
+}
+
+__device__ __forceinline__ void timeline(const KParams& P, int slot) {
+  if (blockIdx.x == 0 && threadIdx.x == 0 && slot < kTimeline) {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    P.st->ts[slot] = t;
+  }
+}
+
 // ---------------------------------------------------------------------------
-// Lawson flip rounds starting from work-list `src`.
-__device__ void phase_lawson(cg::grid_group& g, const KParams& P, Stage& S, int src, unsigned& stamp,
-                             LocalCounters& lc) {
+// Lawson flip rounds starting from work-list `src`.  A round is two phases:
+//   A  every queued edge that is still non-Delaunay claims its two faces with
+//      a hashed priority (atomicMax on the face's smallest half-edge);
+//   B  an edge that holds both claims flips and queues its four wing edges;
+//      other candidates queue themselves again.
+// Winners share no face, so their writes never overlap; the candidate with the
+// highest priority always wins both faces, so every round flips at least once.
+// If pre_sc != 0 the first round's phase A was done by the classification.
+// One flip round over `in[0..n)` by the threads [t0, t0+nt) (a whole grid or a
+// single block); `sync` is the matching barrier.
+template <bool kFixedPos, typename Sync>
+__device__ __forceinline__ int lawson_round(const KParams& P, const int* in, int n, int* out, int* out_count,
+                                            unsigned sc, unsigned sq, bool do_phase_a, int t0, int nt,
+                                            LocalCounters& lc, Sync sync) {
+  if (do_phase_a) {
+    for (int i = t0; i < n; i += nt) {
+      const int e = ld_i(in + i);
+      if (edge_illegal<kFixedPos>(P, ld_ev(P, e), lc)) claim_edge(P, e, sc);
+    }
+    sync();
+  }
+  int flips = 0;
+  const int lane = threadIdx.x & 31;
+  for (int base = t0 - lane; base < n; base += nt) {
+    const int i = base + lane;
+    int mine[4];
+    int k = 0;
+    if (i < n) {
+      const int e = ld_i(in + i);
+      if ((unsigned)ld_i(reinterpret_cast<const int*>(P.cand) + e) == sc) {
+        const int2 f = __ldcg(P.efa + e);
+        const unsigned long long key = ((unsigned long long)sc << 32) | (unsigned)(~mix32((unsigned)e ^ sc));
+        if (__ldcg(P.claim + f.x) == key && __ldcg(P.claim + f.y) == key) {
+          const int4 w = ld_en(P, e);
+          if (flip_edge(P, e)) ++flips;
+          const int wing[4] = {w.x >> 1, w.y >> 1, w.z >> 1, w.w >> 1};
+#pragma unroll
+          for (int j = 0; j < 4; ++j)
+            if (enqueue_once(P, wing[j], sq)) mine[k++] = wing[j];
+        } else if (enqueue_once(P, e, sq)) {
+          mine[k++] = e;
+        }
+      }
+    }
+    if (__any_sync(kFull, k > 0)) warp_push(mine, k, out, out_count, P.E, P.st);
+  }
+  return flips;
+}
+
+// Rounds with at most this many queued edges run inside one block (block
+// barriers instead of grid barriers); the rest of the grid waits.
+constexpr int kTailItems = 2048;
+
+// ---------------------------------------------------------------------------
+// Lawson flip rounds starting from work-list `src`.  A round is two phases:
+//   A  every queued edge that is still non-Delaunay claims its two faces with
+//      a hashed priority (atomicMax on the face's smallest half-edge);
+//   B  an edge that holds both claims flips and queues its four wing edges;
+//      other candidates queue themselves again.
+// Winners share no face, so their writes never overlap; the candidate with the
+// highest priority always wins both faces, so every round flips at least once.
+// If pre_sc != 0 the first round's phase A was done by the classification.
+template <bool kFixedPos>
+__device__ void phase_lawson(cg::grid_group& g, const KParams& P, int src, unsigned& stamp,
+                             LocalCounters& lc, unsigned pre_sc) {
   const int stride = gridDim.x * blockDim.x;
   const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+  int flips = 0;
   for (int round = 0;; ++round) {
     const int n = ld_i(&P.st->wl_count[src]);
-    if (n == 0) return;
+    if (n == 0) break;
     if (round >= P.max_rounds) {
       if (gtid == 0) set_error(P, MCL_ERR_NO_CONVERGENCE);
-      return;
+      break;
+    }
+    if (n <= kTailItems && !(round == 0 && pre_sc)) {
+      // tail: block 0 finishes every remaining round on its own
+      if (blockIdx.x == 0) {
+        int s2 = src;
+        unsigned st2 = stamp;
+        for (int r2 = round; r2 < P.max_rounds; ++r2) {
+          const int m = ld_i(&P.st->wl_count[s2]);
+          if (m == 0) break;
+          const int d2 = s2 ^ 1;
+          const unsigned sc = st2++, sq = st2++;
+          if (threadIdx.x == 0) {
+            P.st->wl_count[d2] = 0;
+            P.st->c[C_LAWSON_ROUNDS] += 1;
+          }
+          __syncthreads();
+          flips += lawson_round<kFixedPos>(P, s2 ? P.wl1 : P.wl0, m, d2 ? P.wl1 : P.wl0, &P.st->wl_count[d2], sc, sq,
+                                           true, threadIdx.x, blockDim.x, lc, [] { __syncthreads(); });
+          __syncthreads();
+          timeline(P, 2 + (r2 < 40 ? r2 : 40));
+          s2 = d2;
+        }
+        if (threadIdx.x == 0) P.st->tail_stamp = st2;
+      }
+      g.sync();
+      stamp = (unsigned)ld_i(reinterpret_cast<const int*>(&P.st->tail_stamp));
+      break;
     }
     const int dst = src ^ 1;
     const int* in = src ? P.wl1 : P.wl0;
     int* out = dst ? P.wl1 : P.wl0;
-    const unsigned sc = stamp++;
+    unsigned sc;
+    bool phase_a = true;
+    if (round == 0 && pre_sc) {
+      sc = pre_sc;  // wl_count[dst] is still zero from the end of the last launch or phase
+      phase_a = false;
+      if (gtid == 0) P.st->c[C_LAWSON_ROUNDS] += 1;
+    } else {
+      sc = stamp++;
+      if (gtid == 0) {
+        P.st->wl_count[dst] = 0;
+        P.st->c[C_LAWSON_ROUNDS] += 1;
+      }
+    }
     const unsigned sq = stamp++;
-    if (gtid == 0) {
-      P.st->wl_count[dst] = 0;
-      P.st->c[C_LAWSON_ROUNDS] += 1;
-    }
-    // A: which queued edges are still non-Delaunay
-    for (int i = gtid; i < n; i += stride) {
-      const int e = ld_i(in + i);
-      if (edge_illegal(P, ld_ev(P, e), lc)) __stcg(P.cand + e, sc);
-    }
+    flips += lawson_round<kFixedPos>(P, in, n, out, &P.st->wl_count[dst], sc, sq, phase_a, gtid, stride, lc,
+                                     [&] { g.sync(); });
     g.sync();
-    // D: a candidate wins if no candidate sharing one of its two faces has a
-    // higher priority this round
-    for (int i = gtid; i < n; i += stride) {
-      const int e = ld_i(in + i);
-      if (ld_i(reinterpret_cast<const int*>(P.cand) + e) != (int)sc) continue;
-      const int4 w = ld_en(P, e);
-      const unsigned pe = mix32((unsigned)e ^ sc);
-      bool win = true;
-      if (bad_h(P, w.x) || bad_h(P, w.y) || bad_h(P, w.z) || bad_h(P, w.w)) {
-        flag_error(P, MCL_ERR_DEGENERATE_INPUT);
-        continue;
-      }
-      const int wing[4] = {w.x >> 1, w.y >> 1, w.z >> 1, w.w >> 1};
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        const int f = wing[k];
-        if ((unsigned)ld_i(reinterpret_cast<const int*>(P.cand) + f) == sc &&
-            mix32((unsigned)f ^ sc) > pe)
-          win = false;
-      }
-      if (win) __stcg(P.win + e, sc);
-    }
-    g.sync();
-    // B: winners flip and queue their four wing edges, losers queue themselves
-    int flips = 0;
-    for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
-      const int i = base + threadIdx.x;
-      int mine[4];
-      int k = 0;
-      if (i < n) {
-        const int e = ld_i(in + i);
-        if ((unsigned)ld_i(reinterpret_cast<const int*>(P.cand) + e) == sc) {
-          if ((unsigned)ld_i(reinterpret_cast<const int*>(P.win) + e) == sc) {
-            const int4 w = ld_en(P, e);
-            if (flip_edge(P, e)) ++flips;
-            const int wing[4] = {w.x >> 1, w.y >> 1, w.z >> 1, w.w >> 1};
-#pragma unroll
-            for (int j = 0; j < 4; ++j)
-              if (enqueue_once(P, wing[j], sq)) mine[k++] = wing[j];
-          } else if (enqueue_once(P, e, sq)) {
-            mine[k++] = e;
-          }
-        }
-      }
-      stage_push<4>(S, mine, k, out, &P.st->wl_count[dst], P.E, P.st);
-    }
-    stage_flush(S, out, &P.st->wl_count[dst], P.E, P.st);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) flips += __shfl_down_sync(kFull, flips, o);
-    if ((threadIdx.x & 31) == 0 && flips) atomicAdd(&P.st->c[C_LAWSON_FLIPS], (unsigned long long)flips);
-    g.sync();
+    timeline(P, 2 + (round < 40 ? round : 40));
     src = dst;
   }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) flips += __shfl_down_sync(kFull, flips, o);
+  if ((threadIdx.x & 31) == 0 && flips) atomicAdd(&P.st->c[C_LAWSON_FLIPS], (unsigned long long)flips);
 }
 
 // ---------------------------------------------------------------------------
 // Repair (1): revert vertices of non-positive faces until all faces are positive.
-__device__ __forceinline__ float2 qpos(const KParams& P, int v) {
-  return ld_i(P.vmark + v) ? P.pos_old[v] : ldpos(P, v);
+__device__ __forceinline__ bool marked(const KParams& P, int v, unsigned fs) {
+  return (unsigned)ld_i(P.vmark + v) == fs;
 }
 
-__device__ void mark_vertex(const KParams& P, int v, int& fresh) {
-  if (ld_i(P.vmark + v) == 0 && atomicExch(P.vmark + v, 1) == 0) ++fresh;
+__device__ __forceinline__ float2 qpos(const KParams& P, int v, unsigned fs) {
+  return marked(P, v, fs) ? P.pos_old[v] : ldpos(P, v);
 }
 
-__device__ bool phase_fixpoint(cg::grid_group& g, const KParams& P, LocalCounters& lc) {
+__device__ void mark_vertex(const KParams& P, int v, int& fresh, unsigned fs) {
+  if (!marked(P, v, fs) && (unsigned)atomicExch(P.vmark + v, (int)fs) != fs) ++fresh;
+}
+
+__device__ bool phase_fixpoint(cg::grid_group& g, const KParams& P, LocalCounters& lc, unsigned fs) {
   const int stride = gridDim.x * blockDim.x;
   const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
   for (int pass = 0; pass < 256; ++pass) {
@@ -296,14 +425,14 @@ __device__ bool phase_fixpoint(cg::grid_group& g, const KParams& P, LocalCounter
         flag_error(P, MCL_ERR_DEGENERATE_INPUT);
         continue;
       }
-      const float2 a = qpos(P, q.x), b = qpos(P, q.y);
-      if (q.z >= 0 && orient_v(P, a, b, qpos(P, q.z), lc) <= 0) {
+      const float2 a = qpos(P, q.x, fs), b = qpos(P, q.y, fs);
+      if (q.z >= 0 && orient_v(P, a, b, qpos(P, q.z, fs), lc) <= 0) {
         ++bad;
-        mark_vertex(P, q.x, fresh); mark_vertex(P, q.y, fresh); mark_vertex(P, q.z, fresh);
+        mark_vertex(P, q.x, fresh, fs); mark_vertex(P, q.y, fresh, fs); mark_vertex(P, q.z, fresh, fs);
       }
-      if (q.w >= 0 && orient_v(P, b, a, qpos(P, q.w), lc) <= 0) {
+      if (q.w >= 0 && orient_v(P, b, a, qpos(P, q.w, fs), lc) <= 0) {
         ++bad;
-        mark_vertex(P, q.x, fresh); mark_vertex(P, q.y, fresh); mark_vertex(P, q.w, fresh);
+        mark_vertex(P, q.x, fresh, fs); mark_vertex(P, q.y, fresh, fs); mark_vertex(P, q.w, fresh, fs);
       }
     }
     if (fresh) atomicAdd(&P.st->fix_new[slot], fresh);
@@ -495,7 +624,7 @@ __device__ bool for_spokes(const KParams& P, int v, F f) {
   return false;
 }
 
-__device__ bool phase_remove(cg::grid_group& g, const KParams& P, Stage& S, unsigned& stamp, LocalCounters& lc) {
+__device__ bool phase_remove(cg::grid_group& g, const KParams& P, unsigned& stamp, LocalCounters& lc) {
   const int stride = gridDim.x * blockDim.x;
   const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
   int src = 0;
@@ -547,9 +676,8 @@ __device__ bool phase_remove(cg::grid_group& g, const KParams& P, Stage& S, unsi
           mine[k++] = v;
         }
       }
-      stage_push<1>(S, mine, k, out, &P.st->vl_count[dst], P.V, P.st);
+      warp_push(mine, k, out, &P.st->vl_count[dst], P.V, P.st);
     }
-    stage_flush(S, out, &P.st->vl_count[dst], P.V, P.st);
     if (removed) atomicAdd(&P.st->c[C_REMOVED], (unsigned long long)removed);
     if (flips) atomicAdd(&P.st->c[C_REMOVAL_FLIPS], (unsigned long long)flips);
     g.sync();
@@ -654,7 +782,7 @@ __device__ int insert_start(const KParams& P, int v) {
   return 0;  // half-edge 0 is never freed: edge 0 is a side of the bounding square
 }
 
-__device__ bool phase_insert(cg::grid_group& g, const KParams& P, Stage& S, Stage& S2, unsigned& stamp,
+__device__ bool phase_insert(cg::grid_group& g, const KParams& P, unsigned& stamp,
                              LocalCounters& lc) {
   const int stride = gridDim.x * blockDim.x;
   const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -751,104 +879,143 @@ __device__ bool phase_insert(cg::grid_group& g, const KParams& P, Stage& S, Stag
           again[ka++] = v;
         }
       }
-      stage_push<8>(S, mine, k, P.wl0, &P.st->wl_count[0], P.E, P.st);
-      stage_push<1>(S2, again, ka, out, &P.st->vl_count[dst], P.V, P.st);
+      warp_push(mine, k, P.wl0, &P.st->wl_count[0], P.E, P.st);
+      warp_push(again, ka, out, &P.st->vl_count[dst], P.V, P.st);
     }
-    stage_flush(S, P.wl0, &P.st->wl_count[0], P.E, P.st);
-    stage_flush(S2, out, &P.st->vl_count[dst], P.V, P.st);
     (void)inserted;
     g.sync();
-    phase_lawson(g, P, S, 0, stamp, lc);
+    phase_lawson<false>(g, P, 0, stamp, lc, 0);
     g.sync();
     src = dst;
   }
 }
 
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kThreads) k_engine(KParams P) {
+// End of a launch: publish this launch's counters and status for the host,
+// add them to the running totals, and leave the working state clean for the
+// next launch (so no reset launch or memset precedes the next step).
+__device__ void finish_launch(const KParams& P, unsigned stamp) {
+  DevState* st = P.st;
+  for (int i = 0; i < C_COUNT; ++i) {
+    st->last[i] = st->c[i];
+    st->tot[i] += st->c[i];
+    st->c[i] = 0;
+  }
+  st->calls += 1;
+  st->last_status = st->status;
+  st->last_site = st->site;
+  st->status = 0;
+  st->site = 0;
+  st->wl_count[0] = st->wl_count[1] = 0;
+  st->vl_count[0] = st->vl_count[1] = 0;
+  st->inverted = 0;
+  st->hard_count = 0;
+  for (int i = 0; i < 3; ++i) st->fix_new[i] = st->fix_bad[i] = 0;
+  st->epoch = stamp;
+}
+
+// Repair of a step whose classification found inverted faces: revert, remove,
+// Lawson, reinsert.  Out of line, so k_step's hot loops keep their registers;
+// keeps its own counters and returns the next free stamp.
+__device__ __noinline__ unsigned repair_step(cg::grid_group g, const KParams P, unsigned stamp) {
+  LocalCounters lc = {0, 0, 0, 0, 0, 0, 0};
+  const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+  KParams Q = P;
+  Q.move_mode = MOVE_NONE;  // positions were moved by the classification
+  const int inverted = ld_i(&P.st->inverted);
+  if (gtid == 0) P.st->c[C_INVERTED] += (unsigned long long)inverted;
+  const unsigned fs = stamp++;  // revert marks of this launch
+  // (1) revert until valid
+  bool ok = phase_fixpoint(g, Q, lc, fs);
+  g.sync();
+  if (ok) {
+    // removal list: reverted vertices that actually moved
+    const int stride = gridDim.x * blockDim.x;
+    if (gtid == 0) { P.st->vl_count[0] = 0; P.st->vl_count[1] = 0; }
+    g.sync();
+    for (int base = blockIdx.x * blockDim.x; base < P.V; base += stride) {
+      const int v = base + threadIdx.x;
+      int mine[1];
+      int k = 0;
+      if (v < P.V && marked(Q, v, fs) && !P.vfix[v]) {
+        const float2 pn = ldpos(Q, v), po = P.pos_old[v];
+        if (__float_as_uint(pn.x) != __float_as_uint(po.x) || __float_as_uint(pn.y) != __float_as_uint(po.y)) {
+          __stcg(P.target + v, pn);
+          __stcg(P.pos + v, po);
+          mine[k++] = v;
+        }
+      }
+      warp_push(mine, k, P.vl0, &P.st->vl_count[0], P.V, P.st);
+    }
+    g.sync();
+    const int nrem = ld_i(&P.st->vl_count[0]);
+    if (gtid == 0) P.st->c[C_REVERTED] += (unsigned long long)nrem;
+    // (2) remove them
+    ok = phase_remove(g, Q, stamp, lc);
+    g.sync();
+    // (3) Lawson over every edge of the reduced mesh
+    if (gtid == 0) { P.st->wl_count[0] = 0; P.st->wl_count[1] = 0; P.st->inverted = 0; P.st->hard_count = 0; }
+    g.sync();
+    const unsigned q1 = stamp++;
+    const unsigned sc1 = stamp++;
+    phase_classify<false>(g, Q, q1, sc1, lc);
+    g.sync();
+    phase_classify_hard<false>(g, Q, q1, sc1, lc);
+    phase_lawson<false>(g, Q, 0, stamp, lc, sc1);
+    g.sync();
+    // (4) reinsert at the new positions
+    if (gtid == 0) { P.st->vl_count[0] = 0; P.st->vl_count[1] = 0; }
+    g.sync();
+    for (int base = blockIdx.x * blockDim.x; base < P.V; base += stride) {
+      const int v = base + threadIdx.x;
+      int mine[1];
+      int k = 0;
+      if (v < P.V && ld_i(P.vhe + v) < 0 && marked(Q, v, fs)) {
+        __stcg(P.pos + v, __ldcg(P.target + v));
+        mine[k++] = v;
+      }
+      warp_push(mine, k, P.vl0, &P.st->vl_count[0], P.V, P.st);
+    }
+    g.sync();
+    if (ok) phase_insert(g, Q, stamp, lc);
+  }
+  flush_counters(P, lc);
+  return stamp;
+}
+
+// One kinetic step in one persistent launch: (move +) classify; if a face is
+// inverted, repair; then Lawson rounds to the Delaunay triangulation.
+__global__ void __launch_bounds__(kThreads, 3) k_step(KParams P) {
   cg::grid_group g = cg::this_grid();
-  __shared__ Stage S, S2;
-  if (threadIdx.x == 0) { S.n = 0; S2.n = 0; }
-  __syncthreads();
   LocalCounters lc = {0, 0, 0, 0, 0, 0, 0};
   unsigned stamp = ld_i(reinterpret_cast<const int*>(&P.st->epoch));
   const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
-
-  if (P.mode == ENGINE_BUILD) {
-    phase_insert(g, P, S, S2, stamp, lc);
-  } else {
-    if (P.move_mode != MOVE_NONE) {
-      phase_move(P);
-      g.sync();
-    }
-    const unsigned q0 = stamp++;
-    phase_classify(P, S, q0, lc);
-    g.sync();
-    const int inverted = ld_i(&P.st->inverted);
-    if (inverted == 0) {
-      phase_lawson(g, P, S, 0, stamp, lc);
-    } else {
-      if (gtid == 0) P.st->c[C_INVERTED] += (unsigned long long)inverted;
-      // (1) revert until valid
-      bool ok = phase_fixpoint(g, P, lc);
-      g.sync();
-      if (ok) {
-        // removal list: reverted vertices that actually moved
-        const int stride = gridDim.x * blockDim.x;
-        if (gtid == 0) { P.st->vl_count[0] = 0; P.st->vl_count[1] = 0; }
-        g.sync();
-        for (int base = blockIdx.x * blockDim.x; base < P.V; base += stride) {
-          const int v = base + threadIdx.x;
-          int mine[1];
-          int k = 0;
-          if (v < P.V && ld_i(P.vmark + v) && !P.vfix[v]) {
-            const float2 pn = ldpos(P, v), po = P.pos_old[v];
-            if (__float_as_uint(pn.x) != __float_as_uint(po.x) || __float_as_uint(pn.y) != __float_as_uint(po.y)) {
-              P.target[v] = pn;
-              __stcg(P.pos + v, po);
-              mine[k++] = v;
-            }
-          }
-          stage_push<1>(S, mine, k, P.vl0, &P.st->vl_count[0], P.V, P.st);
-        }
-        stage_flush(S, P.vl0, &P.st->vl_count[0], P.V, P.st);
-        g.sync();
-        const int nrem = ld_i(&P.st->vl_count[0]);
-        if (gtid == 0) P.st->c[C_REVERTED] += (unsigned long long)nrem;
-        // (2) remove them (list ends in vl[0] or vl[1]; reinsertion needs the
-        // full list, so it is rebuilt from vmark afterwards)
-        ok = phase_remove(g, P, S, stamp, lc);
-        g.sync();
-        // (3) Lawson over every edge of the reduced mesh
-        if (gtid == 0) { P.st->wl_count[0] = 0; P.st->inverted = 0; }
-        g.sync();
-        const unsigned q1 = stamp++;
-        phase_classify(P, S, q1, lc);
-        g.sync();
-        phase_lawson(g, P, S, 0, stamp, lc);
-        g.sync();
-        // (4) reinsert at the new positions
-        if (gtid == 0) { P.st->vl_count[0] = 0; P.st->vl_count[1] = 0; }
-        g.sync();
-        for (int base = blockIdx.x * blockDim.x; base < P.V; base += stride) {
-          const int v = base + threadIdx.x;
-          int mine[1];
-          int k = 0;
-          if (v < P.V && ld_i(P.vhe + v) < 0 && ld_i(P.vmark + v)) {
-            __stcg(P.pos + v, __ldcg(P.target + v));
-            mine[k++] = v;
-          }
-          stage_push<1>(S, mine, k, P.vl0, &P.st->vl_count[0], P.V, P.st);
-        }
-        stage_flush(S, P.vl0, &P.st->vl_count[0], P.V, P.st);
-        g.sync();
-        if (ok) phase_insert(g, P, S, S2, stamp, lc);
-      }
-    }
-  }
+  timeline(P, 0);
+  const unsigned q0 = stamp++;
+  const unsigned sc0 = stamp++;
+  phase_classify<true>(g, P, q0, sc0, lc);
+  g.sync();
+  phase_classify_hard<true>(g, P, q0, sc0, lc);
+  timeline(P, 1);
+  const int inverted = ld_i(&P.st->inverted);
+  if (inverted == 0) phase_lawson<true>(g, P, 0, stamp, lc, sc0);
+  else stamp = repair_step(g, P, stamp);
   flush_counters(P, lc);
   g.sync();
-  if (gtid == 0) P.st->epoch = stamp;
+  timeline(P, kTimeline - 1);
+  if (gtid == 0) finish_launch(P, stamp);
+}
+
+// The initial triangulation: parallel insertion rounds from the bounding square.
+__global__ void __launch_bounds__(kThreads) k_build(KParams P) {
+  cg::grid_group g = cg::this_grid();
+  LocalCounters lc = {0, 0, 0, 0, 0, 0, 0};
+  unsigned stamp = ld_i(reinterpret_cast<const int*>(&P.st->epoch));
+  const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+  phase_insert(g, P, stamp, lc);
+  flush_counters(P, lc);
+  g.sync();
+  if (gtid == 0) finish_launch(P, stamp);
 }
 
 // ---------------------------------------------------------------------------
@@ -879,7 +1046,7 @@ static int cuda_fail(cudaError_t e, const char* what) {
 
 static void free_mesh(mcl_mesh* m) {
   if (!m) return;
-  void* ptrs[] = {m->pos[0], m->pos[1], m->ev, m->en, m->vhe, m->vfix, m->cand, m->win, m->qmark,
+  void* ptrs[] = {m->pos[0], m->pos[1], m->ev, m->en, m->vhe, m->vfix, m->cand, m->win, m->qmark, m->efa, m->hard,
                   m->wl[0], m->wl[1], m->vl[0], m->vl[1], m->vmark, m->claim, m->vfree, m->vhint,
                   m->vaux, m->vloc, m->vlocf, m->target, m->dstage, m->scratch, m->st};
   for (void* p : ptrs)
@@ -914,6 +1081,8 @@ static int alloc_mesh(int64_t V, int64_t E, mcl_mesh** out) {
   A((void**)&m->cand, 4 * E);
   A((void**)&m->win, 4 * E);
   A((void**)&m->qmark, 4 * E);
+  A((void**)&m->efa, 8 * E);
+  A((void**)&m->hard, 4 * E);
   A((void**)&m->wl[0], 4 * E);
   A((void**)&m->wl[1], 4 * E);
   A((void**)&m->vl[0], 4 * V);
@@ -940,6 +1109,7 @@ static int alloc_mesh(int64_t V, int64_t E, mcl_mesh** out) {
   if (e == cudaSuccess) e = cudaMemset(m->claim, 0, 16 * E);
   if (e == cudaSuccess) e = cudaMemset(m->vaux, 0xff, 4 * V);
   if (e == cudaSuccess) e = cudaMemset(m->vhint, 0xff, 4 * V);
+  if (e == cudaSuccess) e = cudaMemset(m->vmark, 0, 4 * V);
   DevState s;
   std::memset(&s, 0, sizeof(s));
   s.epoch = 1;
@@ -950,13 +1120,16 @@ static int alloc_mesh(int64_t V, int64_t E, mcl_mesh** out) {
   }
   int nsm = 0, per_sm = 0;
   e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_engine, kThreads, 0);
-  if (e != cudaSuccess || per_sm < 1) {
+  int per_sm2 = 0;
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_step, kThreads, 0);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm2, k_build, kThreads, 0);
+  if (e != cudaSuccess || per_sm < 1 || per_sm2 < 1) {
     free_mesh(m);
-    return cuda_fail(e == cudaSuccess ? cudaErrorInvalidConfiguration : e, "occupancy(k_engine)");
+    return cuda_fail(e == cudaSuccess ? cudaErrorInvalidConfiguration : e, "occupancy(k_step, k_build)");
   }
   m->coop_threads = kThreads;
   m->coop_blocks = nsm * per_sm;
+  m->repair_blocks = nsm * per_sm2;
   *out = m;
   return MCL_OK;
 }
@@ -1029,6 +1202,8 @@ static KParams make_params(mcl_mesh* m, int mode) {
   P.cand = m->cand;
   P.win = m->win;
   P.qmark = m->qmark;
+  P.efa = m->efa;
+  P.hard = m->hard;
   P.wl0 = m->wl[0];
   P.wl1 = m->wl[1];
   P.vl0 = m->vl[0];
@@ -1048,30 +1223,18 @@ static KParams make_params(mcl_mesh* m, int mode) {
   return P;
 }
 
-// Reset the per-call part of the device state (counters, lists, status).
-__global__ void k_reset_state(DevState* st) {
-  // fold the last call's counters into the running totals, then clear them
-  for (int i = 0; i < C_COUNT; ++i) st->tot[i] += st->c[i];
-  st->calls += 1;
-  const unsigned ep = st->epoch;
-  DevState z;
-  memset(&z, 0, sizeof(z));
-  z.epoch = ep;
-  for (int i = 0; i < C_COUNT; ++i) z.tot[i] = st->tot[i];
-  z.calls = st->calls;
-  *st = z;
-}
-
 static int launch_engine(mcl_mesh* m, KParams& P, cudaStream_t s) {
-  k_reset_state<<<1, 1, 0, s>>>(m->st);
-  CK(cudaGetLastError());
-  CK(cudaMemsetAsync(m->vmark, 0, 4 * m->V, s));
   void* args[] = {&P};
-  CK(cudaLaunchCooperativeKernel((void*)k_engine, dim3(m->coop_blocks), dim3(m->coop_threads), args, 0, s));
+  CK(cudaLaunchCooperativeKernel((void*)k_step, dim3(m->coop_blocks), dim3(m->coop_threads), args, 0, s));
   return MCL_OK;
 }
 
-static void fill_stats(const DevState& s, mcl_step_stats* o) {
+static void fill_stats_from(const unsigned long long* c, int status, int site, mcl_step_stats* o);
+
+static void fill_stats(const DevState& s, mcl_step_stats* o) { fill_stats_from(s.last, s.last_status, s.last_site, o); }
+
+static void fill_stats_from(const unsigned long long* c, int status, int site, mcl_step_stats* o) {
+  struct { const unsigned long long* c; } s{c};
   o->inverted_faces = (int64_t)s.c[C_INVERTED];
   o->reverted_vertices = (int64_t)s.c[C_REVERTED];
   o->removed_vertices = (int64_t)s.c[C_REMOVED];
@@ -1085,8 +1248,8 @@ static void fill_stats(const DevState& s, mcl_step_stats* o) {
   o->orient_fp64 = (int64_t)s.c[C_ORIENT_FP64];
   o->orient_exact = (int64_t)s.c[C_ORIENT_EXACT];
   o->sos_decisions = (int64_t)s.c[C_SOS];
-  o->status = s.status;
-  o->error_site = s.site;
+  o->status = status;
+  o->error_site = site;
 }
 
 static int finish(mcl_mesh* m, cudaStream_t s, mcl_step_stats* stats) {
@@ -1094,9 +1257,10 @@ static int finish(mcl_mesh* m, cudaStream_t s, mcl_step_stats* stats) {
   CK(cudaMemcpyAsync(m->st_host, m->st, sizeof(DevState), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   fill_stats(*m->st_host, stats);
-  m->last_status = m->st_host->status;
-  if (m->st_host->status != MCL_OK)
-    return fail(m->st_host->status, std::string("device status: ") + mcl_status_string(m->st_host->status));
+  m->last_status = m->st_host->last_status;
+  if (m->st_host->last_status != MCL_OK)
+    return fail(m->st_host->last_status,
+                std::string("device status: ") + mcl_status_string(m->st_host->last_status));
   return MCL_OK;
 }
 
@@ -1203,11 +1367,17 @@ int mcl_mesh_totals(mcl_mesh* m, mcl_step_stats* totals, int64_t* calls) {
   if (!m || !totals) return fail(MCL_ERR_INVALID_ARGUMENT, "null argument");
   CK(cudaDeviceSynchronize());
   CK(cudaMemcpy(m->st_host, m->st, sizeof(DevState), cudaMemcpyDeviceToHost));
-  DevState t = *m->st_host;
-  for (int i = 0; i < C_COUNT; ++i) t.c[i] = t.tot[i] + t.c[i];
-  fill_stats(t, totals);
-  totals->status = m->st_host->status;
+  const DevState& t = *m->st_host;
+  fill_stats_from(t.tot, t.last_status, t.last_site, totals);
   if (calls) *calls = (int64_t)t.calls;
+  return MCL_OK;
+}
+
+int mcl_debug_timeline(mcl_mesh* m, int64_t* out48) {
+  if (!m || !out48) return fail(MCL_ERR_INVALID_ARGUMENT, "null argument");
+  CK(cudaDeviceSynchronize());
+  CK(cudaMemcpy(m->st_host, m->st, sizeof(DevState), cudaMemcpyDeviceToHost));
+  for (int i = 0; i < kTimeline; ++i) out48[i] = (int64_t)m->st_host->ts[i];
   return MCL_OK;
 }
 
@@ -1461,18 +1631,17 @@ int mcl_mesh_build(mcl_float2* pts, int64_t n, mcl_mesh** out) {
   KParams P = make_params(m, ENGINE_BUILD);
   P.pos = m->pos[0];
   P.pos_old = m->pos[0];
-  k_reset_state<<<1, 1>>>(m->st);
   const int n32 = (int)n;
   e = cudaMemcpy(&m->st->vl_count[0], &n32, sizeof(int), cudaMemcpyHostToDevice);
   void* args[] = {&P};
   if (e == cudaSuccess)
-    e = cudaLaunchCooperativeKernel((void*)k_engine, dim3(m->coop_blocks), dim3(m->coop_threads), args, 0, 0);
+    e = cudaLaunchCooperativeKernel((void*)k_build, dim3(m->repair_blocks), dim3(m->coop_threads), args, 0, 0);
   if (e == cudaSuccess) e = cudaDeviceSynchronize();
   if (e == cudaSuccess) e = cudaMemcpy(m->st_host, m->st, sizeof(DevState), cudaMemcpyDeviceToHost);
   if (e == cudaSuccess) e = cudaMemcpy(m->pos[1], m->pos[0], 8 * V, cudaMemcpyDeviceToDevice);
   if (e != cudaSuccess) { free_mesh(m); return cuda_fail(e, "build"); }
-  if (m->st_host->status != MCL_OK) {
-    const int st = m->st_host->status;
+  if (m->st_host->last_status != MCL_OK) {
+    const int st = m->st_host->last_status;
     free_mesh(m);
     return fail(st, std::string("build failed: ") + mcl_status_string(st));
   }

@@ -50,19 +50,29 @@ enum Counter {
   C_COUNT
 };
 
+constexpr int kTimeline = 48;
+
 struct DevState {
+  // working state of the running launch; the launch leaves it cleared
   int wl_count[2];         // edge work-list sizes
   int vl_count[2];         // vertex work-list sizes
   int status;              // MCL_OK or the first error
+  int site;                // source line that set `status` (diagnostics)
   int inverted;            // faces with orientation <= 0 found by the last classification
+  int hard_count;          // edges the FP32 filters could not classify
   int fix_new[3];          // vertices newly reverted per fixpoint pass (triple-buffered)
   int fix_bad[3];          // non-positive faces seen per fixpoint pass
   unsigned int epoch;      // next unused stamp
-  int site;                // source line that set `status` (diagnostics)
-  int dbg[68];             // first failing vertex star: v, deg, then neighbour ids
-  unsigned long long tot[C_COUNT];  // running totals over all calls (never reset)
-  unsigned long long calls;
+  unsigned int tail_stamp; // stamp after a single-block flip tail
   unsigned long long c[C_COUNT];
+  // published by the last launch
+  int last_status;
+  int last_site;
+  unsigned long long last[C_COUNT];
+  unsigned long long tot[C_COUNT];  // running totals over all launches
+  unsigned long long calls;
+  int dbg[68];             // first failing vertex star: v, deg, then neighbour ids
+  unsigned long long ts[kTimeline];  // %globaltimer at phase boundaries of the last launch
 };
 
 enum MoveMode { MOVE_NONE = 0, MOVE_DISPLACE = 1, MOVE_INTEGRATE = 2 };
@@ -79,11 +89,13 @@ struct KParams {
   unsigned int* cand;      // per edge: stamp of the round in which it is a flip candidate
   unsigned int* win;       // per edge: stamp of the round in which it won
   unsigned int* qmark;     // per edge: stamp of the last work-list it was queued on
+  int2* efa;               // per edge: the two faces it claimed in the current round
+  int* hard;               // edges left to the full predicate ladder by the classification
   int* wl0;
   int* wl1;
   int* vl0;
   int* vl1;
-  int* vmark;              // per vertex: reverted flag
+  int* vmark;              // per vertex: stamp of the launch that reverted it
   unsigned long long* claim;  // per half-edge: face claims {stamp, ~priority}
   int* vfree;              // 3 per vertex: free edge slots for (re)insertion
   int* vhint;              // per vertex: half-edge to start point location from
@@ -149,13 +161,20 @@ __device__ __forceinline__ unsigned int mix32(unsigned int x) {
   return x;
 }
 
-struct LocalCounters {
-  unsigned long long orient_fp64, orient_exact, incircle_fp64, incircle_exact, sos;
-  unsigned long long incircle;
+struct LocalCounters {  // per-thread, folded into DevState at the end of a launch
+  unsigned orient_fp64, orient_exact, incircle_fp64, incircle_exact, sos;
+  unsigned incircle;
   int overflow;
 };
 
 __device__ __forceinline__ float2 ldpos(const KParams& P, int v) { return __ldcg(P.pos + v); }
+// Positions that stay fixed for the rest of the launch and were not read by
+// this SM before they were written may go through L1 (k_step after its move
+// pass); positions that change during the launch (k_repair) must not.
+template <bool kFixedPos>
+__device__ __forceinline__ float2 ldpos_t(const KParams& P, int v) {
+  return kFixedPos ? __ldca(P.pos + v) : __ldcg(P.pos + v);
+}
 
 __device__ __forceinline__ int orient_v(const KParams& P, float2 a, float2 b, float2 c, LocalCounters& lc) {
   return orient2d(a.x, a.y, b.x, b.y, c.x, c.y, &lc, &lc.overflow);
@@ -169,13 +188,15 @@ __device__ __forceinline__ void flag_error_at(const KParams& P, int code, int li
 #define flag_error(P, code) flag_error_at(P, code, __LINE__)
 
 // Is edge e locally non-Delaunay (d inside the circle of the left face a,b,c)?
+template <bool kFixedPos = false>
 __device__ __forceinline__ bool edge_illegal(const KParams& P, const int4 q, LocalCounters& lc) {
   if (q.x < 0 || q.z < 0 || q.w < 0) return false;
   if (bad_v(P, q.x) || bad_v(P, q.y) || bad_v(P, q.z) || bad_v(P, q.w)) {
     flag_error(P, MCL_ERR_DEGENERATE_INPUT);
     return false;
   }
-  const float2 a = ldpos(P, q.x), b = ldpos(P, q.y), c = ldpos(P, q.z), d = ldpos(P, q.w);
+  const float2 a = ldpos_t<kFixedPos>(P, q.x), b = ldpos_t<kFixedPos>(P, q.y), c = ldpos_t<kFixedPos>(P, q.z),
+               d = ldpos_t<kFixedPos>(P, q.w);
   lc.incircle++;
   return incircle_sos(a.x, a.y, b.x, b.y, c.x, c.y, d.x, d.y, q.x, q.y, q.z, q.w, &lc, &lc.overflow) > 0;
 }
@@ -220,6 +241,8 @@ struct mcl_mesh {
   unsigned int* cand;
   unsigned int* win;
   unsigned int* qmark;
+  int2* efa;
+  int* hard;
   int* wl[2];
   int* vl[2];
   int* vmark;
@@ -234,7 +257,8 @@ struct mcl_mesh {
   unsigned long long* scratch;  // small device scratch for query counters
   mcl::DevState* st;
   mcl::DevState* st_host;  // pinned mirror
-  int coop_blocks;
+  int coop_blocks;         // k_step grid
+  int repair_blocks;       // k_repair grid
   int coop_threads;
   int last_status;
 };

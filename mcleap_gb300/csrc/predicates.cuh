@@ -32,6 +32,7 @@
 
 #include <cstdint>
 #include <cmath>
+#include <cstring>
 
 #ifdef __CUDACC__
 #define MCL_HD __host__ __device__ __forceinline__
@@ -206,9 +207,11 @@ MCL_HD void exp_diff(double a, double b, Exp& h) {  // exact a - b
 }
 
 // ---------------------------------------------------------------------------
-// Exact stage.  Returns the sign; sets *overflow on capacity exhaustion.
-MCL_HD_NOINLINE int orient2d_exact_exp(float ax, float ay, float bx, float by, float cx, float cy,
-                                       int* overflow) {
+// Exact stage.  Returns the sign, or kExpOverflow when the expansion capacity
+// was exhausted.  (No pointer arguments: callers keep their state in registers.)
+constexpr int kExpOverflow = 3;
+
+MCL_HD_NOINLINE int orient2d_exact_exp(float ax, float ay, float bx, float by, float cx, float cy) {
   Exp acx, bcy, acy, bcx, l, r, t;
   exp_diff(ax, cx, acx);
   exp_diff(by, cy, bcy);
@@ -219,12 +222,12 @@ MCL_HD_NOINLINE int orient2d_exact_exp(float ax, float ay, float bx, float by, f
     exp_neg(r);
     ok = exp_add(l, r, l);
   }
-  if (!ok) { *overflow = 1; return 0; }
+  if (!ok) return kExpOverflow;
   return exp_sign(l);
 }
 
 MCL_HD_NOINLINE int incircle_exact_exp(float ax, float ay, float bx, float by, float cx, float cy,
-                                       float dx, float dy, int* overflow) {
+                                       float dx, float dy) {
   Exp adx, ady, bdx, bdy, cdx, cdy, lift, cr, t1, t2, acc;
   exp_diff(ax, dx, adx);
   exp_diff(ay, dy, ady);
@@ -245,17 +248,14 @@ MCL_HD_NOINLINE int incircle_exact_exp(float ax, float ay, float bx, float by, f
     const Exp& rx = *X[(k + 2) % 3];
     const Exp& ry = *Y[(k + 2) % 3];
     // lift = px^2 + py^2
-    if (!exp_mul(px, px, lift, t2) || !exp_mul(py, py, t1, t2) || !exp_add(lift, t1, lift)) {
-      *overflow = 1;
-      return 0;
-    }
+    if (!exp_mul(px, px, lift, t2) || !exp_mul(py, py, t1, t2) || !exp_add(lift, t1, lift)) return kExpOverflow;
     exp_compress(lift);
     // cross = qx*ry - qy*rx
-    if (!exp_mul(qx, ry, cr, t2) || !exp_mul(qy, rx, t1, t2)) { *overflow = 1; return 0; }
+    if (!exp_mul(qx, ry, cr, t2) || !exp_mul(qy, rx, t1, t2)) return kExpOverflow;
     exp_neg(t1);
-    if (!exp_add(cr, t1, cr)) { *overflow = 1; return 0; }
+    if (!exp_add(cr, t1, cr)) return kExpOverflow;
     exp_compress(cr);
-    if (!exp_mul(lift, cr, t1, t2) || !exp_add(acc, t1, acc)) { *overflow = 1; return 0; }
+    if (!exp_mul(lift, cr, t1, t2) || !exp_add(acc, t1, acc)) return kExpOverflow;
     exp_compress(acc);
   }
   return exp_sign(acc);
@@ -274,24 +274,18 @@ constexpr float kTinyF = 1e-30f;
 constexpr double kTinyD = 1e-250;
 
 // Returns 2 when undecided.
+// Branch-free form of the stage-A test: |det| >= (3+16e)e (|detleft|+|detright|).
+// (When detleft and detright differ in sign, |det| ~ detsum and the test
+// passes, which is the case Shewchuk's early exits handle.)
 MCL_HD int orient2d_fp32(float ax, float ay, float bx, float by, float cx, float cy) {
   const float detleft = fmul(fsub(ax, cx), fsub(by, cy));
   const float detright = fmul(fsub(ay, cy), fsub(bx, cx));
   const float det = fsub(detleft, detright);
-  float detsum;
-  if (detleft > 0.0f) {
-    if (detright <= 0.0f) return det > 0.0f ? 1 : (det < 0.0f ? -1 : 2);
-    detsum = fadd(detleft, detright);
-  } else if (detleft < 0.0f) {
-    if (detright >= 0.0f) return det > 0.0f ? 1 : (det < 0.0f ? -1 : 2);
-    detsum = fsub(-detleft, detright);
-  } else {
-    detsum = fabsf(detright);
-  }
-  if (!(detsum > kTinyF) || !(detsum < 1e37f)) return 2;
+  const float detsum = fadd(fabsf(detleft), fabsf(detright));
   const float err = fmul(kCcwErrF, detsum);
-  if (det >= err || -det >= err) return det > 0.0f ? 1 : (det < 0.0f ? -1 : 2);
-  return 2;
+  const bool ok = (detsum > kTinyF) & (detsum < 1e37f);
+  const int s = det > err ? 1 : (-det > err ? -1 : 2);
+  return ok ? s : 2;
 }
 
 MCL_HD int orient2d_fp64(float ax, float ay, float bx, float by, float cx, float cy) {
@@ -357,38 +351,176 @@ MCL_HD int incircle_fp64(float ax, float ay, float bx, float by, float cx, float
 }
 
 // ---------------------------------------------------------------------------
-// Full ladders.  `cnt` may be null.
-template <typename Counters>
-MCL_HD int orient2d(float ax, float ay, float bx, float by, float cx, float cy, Counters* cnt,
-                    int* overflow) {
-  int s = orient2d_fp32(ax, ay, bx, by, cx, cy);
-  if (s != 2) return s;
-  if (cnt) cnt->orient_fp64++;
+// Exact stage on integers.  Every float32 is an integer mantissa times a power
+// of two; after stripping trailing zero bits and aligning all coordinates of a
+// call to their smallest exponent, each coordinate is an integer of at most
+// 62 bits whenever the exponents span no more than ~38 binary orders (all
+// coordinates of one quad in practice, including the +-1e7 corners).  The
+// determinants are then evaluated exactly in 64-, 128- and 256-bit integer
+// arithmetic - no floating point, which on this GPU (FP64 at a small fraction
+// of FP32 / INT32 throughput) is much faster than the FP64 stage.  Returns
+// false when the coordinates do not fit; the caller then falls back to the
+// FP64 filter and the expansion arithmetic.
+typedef unsigned long long u64;
+typedef unsigned __int128 u128;
+typedef __int128 i128;
+
+MCL_HD unsigned f32_bits(float f) {
+#if defined(__CUDA_ARCH__)
+  return __float_as_uint(f);
+#else
+  unsigned u;
+  std::memcpy(&u, &f, 4);
+  return u;
+#endif
+}
+
+MCL_HD int ctz32(unsigned x) {
+#if defined(__CUDA_ARCH__)
+  return __ffs(x) - 1;
+#else
+  return __builtin_ctz(x);
+#endif
+}
+
+MCL_HD int clz64(u64 x) {
+#if defined(__CUDA_ARCH__)
+  return __clzll((long long)x);
+#else
+  return x ? __builtin_clzll(x) : 64;
+#endif
+}
+
+template <int N>
+MCL_HD bool to_fixed(const float (&v)[N], long long (&X)[N]) {
+  int e[N];
+  long long m[N];
+  int emin = 1 << 30;
+  for (int i = 0; i < N; ++i) {
+    const unsigned b = f32_bits(v[i]);
+    const unsigned ex = (b >> 23) & 0xFF;
+    unsigned mant = b & 0x7FFFFF;
+    int exp2;
+    if (ex == 0xFF) return false;  // inf / nan
+    if (ex == 0) exp2 = -149;
+    else { mant |= 0x800000u; exp2 = (int)ex - 150; }
+    if (mant == 0) { m[i] = 0; e[i] = 0; continue; }
+    const int tz = ctz32(mant);
+    mant >>= tz;
+    exp2 += tz;
+    m[i] = (b >> 31) ? -(long long)mant : (long long)mant;
+    e[i] = exp2;
+    if (exp2 < emin) emin = exp2;
+  }
+  for (int i = 0; i < N; ++i) {
+    if (m[i] == 0) { X[i] = 0; continue; }
+    const int sh = e[i] - emin;
+    const u64 mag = (u64)(m[i] < 0 ? -m[i] : m[i]);
+    if (sh > 61 || (64 - clz64(mag)) + sh > 61) return false;
+    X[i] = m[i] * (long long)(1ll << sh);
+  }
+  return true;
+}
+
+MCL_HD int orient2d_int(float ax, float ay, float bx, float by, float cx, float cy) {
+  const float v[6] = {ax, ay, bx, by, cx, cy};
+  long long X[6];
+  if (!to_fixed(v, X)) return 2;
+  const long long acx = X[0] - X[4], bcy = X[3] - X[5], acy = X[1] - X[5], bcx = X[2] - X[4];
+  const i128 l = (i128)acx * bcy, r = (i128)acy * bcx;
+  return l > r ? 1 : (l < r ? -1 : 0);
+}
+
+struct U256 {
+  u64 w[4];
+};
+
+MCL_HD void u256_add(U256& acc, const U256& x) {
+  u64 carry = 0;
+  for (int i = 0; i < 4; ++i) {
+    const u128 t = (u128)acc.w[i] + x.w[i] + carry;
+    acc.w[i] = (u64)t;
+    carry = (u64)(t >> 64);
+  }
+}
+
+MCL_HD U256 u128_mul(u128 a, u128 b) {
+  const u64 a0 = (u64)a, a1 = (u64)(a >> 64), b0 = (u64)b, b1 = (u64)(b >> 64);
+  U256 r;
+  const u128 t = (u128)a0 * b0;
+  r.w[0] = (u64)t;
+  const u128 p01 = (u128)a0 * b1, p10 = (u128)a1 * b0, p11 = (u128)a1 * b1;
+  u128 mid = (t >> 64) + (u64)p01;
+  mid += (u64)p10;
+  r.w[1] = (u64)mid;
+  u128 hi = (mid >> 64) + (p01 >> 64) + (p10 >> 64) + (u64)p11;
+  r.w[2] = (u64)hi;
+  r.w[3] = (u64)((hi >> 64) + (p11 >> 64));
+  return r;
+}
+
+MCL_HD int u256_cmp(const U256& a, const U256& b) {
+  for (int i = 3; i >= 0; --i)
+    if (a.w[i] != b.w[i]) return a.w[i] > b.w[i] ? 1 : -1;
+  return 0;
+}
+
+MCL_HD int incircle_int(float ax, float ay, float bx, float by, float cx, float cy, float dx, float dy) {
+  const float v[8] = {ax, ay, bx, by, cx, cy, dx, dy};
+  long long X[8];
+  if (!to_fixed(v, X)) return 2;
+  const long long adx = X[0] - X[6], ady = X[1] - X[7];
+  const long long bdx = X[2] - X[6], bdy = X[3] - X[7];
+  const long long cdx = X[4] - X[6], cdy = X[5] - X[7];
+  const u128 lift[3] = {(u128)((i128)adx * adx) + (u128)((i128)ady * ady),
+                        (u128)((i128)bdx * bdx) + (u128)((i128)bdy * bdy),
+                        (u128)((i128)cdx * cdx) + (u128)((i128)cdy * cdy)};
+  const i128 cross[3] = {(i128)bdx * cdy - (i128)bdy * cdx, (i128)cdx * ady - (i128)cdy * adx,
+                         (i128)adx * bdy - (i128)ady * bdx};
+  U256 pos = {{0, 0, 0, 0}}, neg = {{0, 0, 0, 0}};
+  for (int k = 0; k < 3; ++k) {
+    if (cross[k] == 0 || lift[k] == 0) continue;
+    const u128 mag = (u128)(cross[k] < 0 ? -cross[k] : cross[k]);
+    const U256 t = u128_mul(lift[k], mag);
+    if (cross[k] > 0) u256_add(pos, t);
+    else u256_add(neg, t);
+  }
+  return u256_cmp(pos, neg);
+}
+
+// ---------------------------------------------------------------------------
+// Full ladders.  Only the FP32 filter is inlined at the call site; the rest of
+// the ladder is one out-of-line call that returns the sign packed with flags
+// (so the hot loops keep a small register footprint and no local memory).
+enum : int { kUsedFp64 = 1, kUsedExact = 2, kUsedSos = 4, kOverflow = 8 };
+MCL_HD int pack_sign(int s, int flags) { return (s + 1) | (flags << 2); }
+MCL_HD int unpack_sign(int r) { return (r & 3) - 1; }
+MCL_HD int unpack_flags(int r) { return r >> 2; }
+
+MCL_HD_NOINLINE int orient2d_slow(float ax, float ay, float bx, float by, float cx, float cy) {
+  int s = orient2d_int(ax, ay, bx, by, cx, cy);
+  if (s != 2) return pack_sign(s, kUsedFp64 | kUsedExact);
   s = orient2d_fp64(ax, ay, bx, by, cx, cy);
-  if (s != 2) return s;
-  if (cnt) cnt->orient_exact++;
-  return orient2d_exact_exp(ax, ay, bx, by, cx, cy, overflow);
+  if (s != 2) return pack_sign(s, kUsedFp64);
+  s = orient2d_exact_exp(ax, ay, bx, by, cx, cy);
+  if (s == kExpOverflow) return pack_sign(0, kUsedFp64 | kUsedExact | kOverflow);
+  return pack_sign(s, kUsedFp64 | kUsedExact);
 }
 
-template <typename Counters>
-MCL_HD int incircle(float ax, float ay, float bx, float by, float cx, float cy, float dx, float dy,
-                    Counters* cnt, int* overflow) {
-  int s = incircle_fp32(ax, ay, bx, by, cx, cy, dx, dy);
-  if (s != 2) return s;
-  if (cnt) cnt->incircle_fp64++;
+MCL_HD_NOINLINE int incircle_slow(float ax, float ay, float bx, float by, float cx, float cy, float dx, float dy) {
+  int s = incircle_int(ax, ay, bx, by, cx, cy, dx, dy);
+  if (s != 2) return pack_sign(s, kUsedFp64 | kUsedExact);
   s = incircle_fp64(ax, ay, bx, by, cx, cy, dx, dy);
-  if (s != 2) return s;
-  if (cnt) cnt->incircle_exact++;
-  return incircle_exact_exp(ax, ay, bx, by, cx, cy, dx, dy, overflow);
+  if (s != 2) return pack_sign(s, kUsedFp64);
+  s = incircle_exact_exp(ax, ay, bx, by, cx, cy, dx, dy);
+  if (s == kExpOverflow) return pack_sign(0, kUsedFp64 | kUsedExact | kOverflow);
+  return pack_sign(s, kUsedFp64 | kUsedExact);
 }
 
-template <typename Counters>
-MCL_HD int incircle_sos(float ax, float ay, float bx, float by, float cx, float cy, float dx,
-                        float dy, int ia, int ib, int ic, int id, Counters* cnt, int* overflow) {
-  int s = incircle(ax, ay, bx, by, cx, cy, dx, dy, cnt, overflow);
-  if (s != 0) return s;
-  if (cnt) cnt->sos++;
-  // visit a, b, c, d in ascending id order
+// Exactly cocircular: decide by the symbolic perturbation (ascending ids).
+MCL_HD_NOINLINE int incircle_sos_tail(float ax, float ay, float bx, float by, float cx, float cy, float dx, float dy,
+                                      int ia, int ib, int ic, int id, int flags) {
+  flags |= kUsedSos;
   int ids[4] = {ia, ib, ic, id};
   int ord[4] = {0, 1, 2, 3};
   for (int i = 1; i < 4; ++i)
@@ -396,16 +528,66 @@ MCL_HD int incircle_sos(float ax, float ay, float bx, float by, float cx, float 
       int tmp = ord[j]; ord[j] = ord[j - 1]; ord[j - 1] = tmp;
     }
   for (int k = 0; k < 4; ++k) {
-    int c0 = 0;
+    int r;
+    int neg = 0;
     switch (ord[k]) {
-      case 0: c0 = orient2d(bx, by, cx, cy, dx, dy, cnt, overflow); break;
-      case 1: c0 = -orient2d(ax, ay, cx, cy, dx, dy, cnt, overflow); break;
-      case 2: c0 = orient2d(ax, ay, bx, by, dx, dy, cnt, overflow); break;
-      default: c0 = -orient2d(ax, ay, bx, by, cx, cy, cnt, overflow); break;
+      case 0: r = orient2d_fp32(bx, by, cx, cy, dx, dy); if (r == 2) r = orient2d_slow(bx, by, cx, cy, dx, dy); else r = pack_sign(r, 0); break;
+      case 1: r = orient2d_fp32(ax, ay, cx, cy, dx, dy); if (r == 2) r = orient2d_slow(ax, ay, cx, cy, dx, dy); else r = pack_sign(r, 0); neg = 1; break;
+      case 2: r = orient2d_fp32(ax, ay, bx, by, dx, dy); if (r == 2) r = orient2d_slow(ax, ay, bx, by, dx, dy); else r = pack_sign(r, 0); break;
+      default: r = orient2d_fp32(ax, ay, bx, by, cx, cy); if (r == 2) r = orient2d_slow(ax, ay, bx, by, cx, cy); else r = pack_sign(r, 0); neg = 1; break;
     }
-    if (c0 != 0) return c0;
+    flags |= unpack_flags(r) & kOverflow;
+    const int c0 = neg ? -unpack_sign(r) : unpack_sign(r);
+    if (c0 != 0) return pack_sign(c0, flags);
   }
-  return 0;
+  return pack_sign(0, flags);
+}
+
+template <typename Counters>
+MCL_HD void count_flags(int flags, Counters* cnt, int* overflow, bool incircle) {
+  if (cnt) {
+    if (incircle) {
+      if (flags & kUsedFp64) cnt->incircle_fp64++;
+      if (flags & kUsedExact) cnt->incircle_exact++;
+    } else {
+      if (flags & kUsedFp64) cnt->orient_fp64++;
+      if (flags & kUsedExact) cnt->orient_exact++;
+    }
+    if (flags & kUsedSos) cnt->sos++;
+  }
+  if (flags & kOverflow) *overflow = 1;
+}
+
+template <typename Counters>
+MCL_HD int orient2d(float ax, float ay, float bx, float by, float cx, float cy, Counters* cnt, int* overflow) {
+  const int s = orient2d_fp32(ax, ay, bx, by, cx, cy);
+  if (s != 2) return s;
+  const int r = orient2d_slow(ax, ay, bx, by, cx, cy);
+  count_flags(unpack_flags(r), cnt, overflow, false);
+  return unpack_sign(r);
+}
+
+template <typename Counters>
+MCL_HD int incircle(float ax, float ay, float bx, float by, float cx, float cy, float dx, float dy,
+                    Counters* cnt, int* overflow) {
+  const int s = incircle_fp32(ax, ay, bx, by, cx, cy, dx, dy);
+  if (s != 2) return s;
+  const int r = incircle_slow(ax, ay, bx, by, cx, cy, dx, dy);
+  count_flags(unpack_flags(r), cnt, overflow, true);
+  return unpack_sign(r);
+}
+
+template <typename Counters>
+MCL_HD int incircle_sos(float ax, float ay, float bx, float by, float cx, float cy, float dx, float dy,
+                        int ia, int ib, int ic, int id, Counters* cnt, int* overflow) {
+  const int s = incircle_fp32(ax, ay, bx, by, cx, cy, dx, dy);
+  if (s != 2) return s;
+  int r = incircle_slow(ax, ay, bx, by, cx, cy, dx, dy);
+  if (unpack_sign(r) == 0 && !(unpack_flags(r) & kOverflow))
+    r = incircle_sos_tail(ax, ay, bx, by, cx, cy, dx, dy, ia, ib, ic, id, unpack_flags(r));
+  const int f = unpack_flags(r);
+  count_flags(f, cnt, overflow, true);
+  return unpack_sign(r);
 }
 
 }  // namespace mcl
