@@ -36,8 +36,9 @@ UNIT = "pts*steps/s"
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--n", type=int, default=1_000_000)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
@@ -191,16 +192,19 @@ def run_ours(args, rank, world, dist):
     t_build = time.perf_counter() - t0
     V = dt.m_pos_size
     E = dt.m_he_size // 2
-    # displacements for warm-up + timed + e2e steps (host float64 Taylor-Green)
-    total = Wm + K + (0 if args.no_e2e else K)
-    disp = W.taylor_green_displacements(ht.m_pos, n, total)
+    # displacements for warm-up + timed + e2e steps (Taylor-Green, generated on
+    # the device; the e2e ones are staged in pinned host memory)
+    KE = 0 if args.no_e2e else min(args.e2e_steps, K)
+    dev_disp = W.taylor_green_displacements_device(ht.m_pos, n, Wm + K + KE, device=f"cuda:{local}")
+    host_e2e = [d.cpu().pin_memory() for d in dev_disp[Wm + K:]]
+    dev_disp = dev_disp[:Wm + K]
     stream = torch.cuda.Stream()
     sp = stream.cuda_stream
-    dev_disp = [torch.from_numpy(d).to(f"cuda:{local}") for d in disp[:Wm + K]]
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
     lib = L.lib()
     torch.cuda.synchronize()
 
+    cp, cf = clocks_start()
     # warm-up (untimed), with stats to check the status
     for k in range(Wm):
         st = L.StepStats()
@@ -214,7 +218,6 @@ def run_ours(args, rank, world, dist):
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
-    cp, cf = clocks_start()
     wall0 = time.perf_counter()
     with torch.cuda.stream(stream):
         for k in range(K):
@@ -225,7 +228,6 @@ def run_ours(args, rank, world, dist):
     stream.synchronize()
     torch.cuda.synchronize()
     wall = time.perf_counter() - wall0
-    clocks = clocks_stop(cp, cf, local)
     step_ms = np.array([s.elapsed_time(e) for s, e in zip(starts, ends)])
     st = dt.status(stream)
     if st["status"] != 0:
@@ -248,17 +250,21 @@ def run_ours(args, rank, world, dist):
     alg_bytes = 24 * V + 16 * E + 8 * V + 20 * max(wl_items, 0) / K + 96 * flips / K
     achieved = alg_bytes / (dev_s / K) / 1e9
     peak, peak_kind = peaks()
+    # DRAM traffic of one k_step launch measured by ncu on this workload
+    # (profiles/k_step_taylor_green_1M.md: 73.1 MB at 3,000,005 edges), scaled
+    # by the edge count for other sizes
+    traffic = 73.1e6 * E / 3000005
 
     # e2e: host displacements through the C ABI, per-step counters read back
     e2e = None
     if not args.no_e2e:
-        host_disp = [torch.from_numpy(d).pin_memory() for d in disp[Wm + K:Wm + 2 * K]]
+        host_disp = host_e2e
         stats = L.StepStats()
         torch.cuda.synchronize()
         if dist:
             dist.barrier()
         e0 = time.perf_counter()
-        for k in range(K):
+        for k in range(KE):
             L.check(lib.mcl_step_host(dt.handle, host_disp[k].data_ptr(), sp, C.byref(stats)))
         torch.cuda.synchronize()
         e_s = time.perf_counter() - e0
@@ -266,8 +272,9 @@ def run_ours(args, rank, world, dist):
             t = torch.tensor([e_s], device=f"cuda:{local}")
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
             e_s = float(t.item())
-        e2e = {"value": world * n * K / e_s, "unit": UNIT, "h2d_bytes_per_step": 8 * V,
-               "d2h_bytes_per_step": C.sizeof(L.StepStats), "ms_per_step": 1e3 * e_s / K}
+        e2e = {"value": world * n * KE / e_s, "unit": UNIT, "h2d_bytes_per_step": 8 * V,
+               "d2h_bytes_per_step": C.sizeof(L.StepStats), "ms_per_step": 1e3 * e_s / KE, "steps": KE}
+    clocks = clocks_stop(cp, cf, local)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -296,10 +303,10 @@ def run_ours(args, rank, world, dist):
             "predicates": {k: tot1[k] - tot0[k] for k in ("incircle_tests", "incircle_fp64", "incircle_exact",
                                                           "orient_fp64", "orient_exact", "sos_decisions")},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
-                         "kernel": "k_engine", "alg_bytes_per_launch": alg_bytes},
+                         "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                         "kernel": "k_step", "alg_bytes_per_launch": alg_bytes},
             "e2e": e2e, "cpu_baseline": cpu, "clocks": clocks,
-            "gpu_launches": 2 * K,
+            "gpu_launches": K,
             "wall_s": wall, "build_s": t_build,
         }
         print(json.dumps(line), flush=True)

@@ -191,6 +191,20 @@ int mcl_grid_update(mcl_grid* g, mcl_float2* pos_dev, mcl_float2* vel_dev, void*
 int mcl_grid_tables(mcl_grid* g, const int32_t** perm_dev, const int32_t** cell_start_dev,
                     const int32_t** cell_count_dev, int32_t* cells_x, int32_t* cells_y);
 
+/* Everything a header-side functor loop (apply_f_frnn) needs to visit cells:
+ * the cell of a point is (x, y) = floor((p - min) / cell), wrapped when
+ * periodic, else clamped to [0, cells); its table index is
+ * morton ? interleave(x, y) (x in the even bits) : y * cells_x + x. */
+typedef struct {
+  float min_x, min_y, cell_x, cell_y;
+  int32_t cells_x, cells_y, morton, periodic;
+  int64_t table_size, num_points;
+  const int32_t* perm_dev;        /* d_ind */
+  const int32_t* cell_start_dev;  /* first sorted index of each cell */
+  const int32_t* cell_count_dev;  /* points in each cell */
+} mcl_grid_desc;
+int mcl_grid_describe(mcl_grid* g, mcl_grid_desc* desc_host);
+
 /* apply_f_frnn with the reference tests' SaveNeighborsFunctor
  * (tests/grid2d_frnn.cu:26-60): for every sorted point i, the sorted indices j != i
  * with fl(fl(dx*dx)+fl(dy*dy)) <= fl(r*r), ascending; ROW layout without the

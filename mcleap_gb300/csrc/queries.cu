@@ -583,6 +583,16 @@ int mcl_grid_tables(mcl_grid* g, const int32_t** perm, const int32_t** start, co
   return MCL_OK;
 }
 
+int mcl_grid_describe(mcl_grid* g, mcl_grid_desc* d) {
+  if (!g || !d) return qfail(MCL_ERR_INVALID_ARGUMENT, "null argument");
+  d->min_x = g->minx; d->min_y = g->miny; d->cell_x = g->cx; d->cell_y = g->cy;
+  d->cells_x = g->nx; d->cells_y = g->ny; d->morton = g->morton;
+  d->periodic = (g->flags & MCL_GRID_PERIODIC) ? 1 : 0;
+  d->table_size = g->ncells; d->num_points = g->n;
+  d->perm_dev = g->perm; d->cell_start_dev = g->start; d->cell_count_dev = g->count;
+  return MCL_OK;
+}
+
 int mcl_grid_frnn(mcl_grid* g, const mcl_float2* pos, float r, int max_nb, int32_t* counts, int32_t* ids, void* stream,
                   int64_t* overflow) {
   if (!g || !pos || !counts || !ids || max_nb < 1 || !(r >= 0.f)) return qfail(MCL_ERR_INVALID_ARGUMENT, "bad args");

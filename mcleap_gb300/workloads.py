@@ -69,3 +69,29 @@ def gaussian_displacements(pos, sigma, seed, steps):
         p = (p + d).astype(np.float32)
         out.append(d)
     return out
+
+
+def taylor_green_displacements_device(pos, n, steps, frac=0.5, device="cuda"):
+    """taylor_green_displacements on the GPU with torch (velocity in float64,
+    positions and displacements in float32 with the same IEEE operations as
+    the engine's pos += d), for long benchmark runs.  Returns a list of
+    (V, 2) float32 device tensors."""
+    import torch
+
+    L = float(SCALE)
+    dt = frac * mean_spacing(n)
+    p = torch.as_tensor(pos, dtype=torch.float32, device=device).clone()
+    out = []
+    two_pi = 2.0 * np.pi
+    for _ in range(steps):
+        q = p[4:].double() / L
+        u = torch.sin(two_pi * q[:, 0]) * torch.cos(two_pi * q[:, 1])
+        v = -torch.cos(two_pi * q[:, 0]) * torch.sin(two_pi * q[:, 1])
+        new = torch.remainder(p[4:].double() + torch.stack([u, v], 1) * dt, L)
+        new32 = new.float()
+        new32[new32 >= L] = 0.0
+        d = torch.zeros_like(p)
+        d[4:] = new32 - p[4:]
+        p[4:] = p[4:] + d[4:]
+        out.append(d)
+    return out

@@ -1,0 +1,207 @@
+// C++ drop-in check: the reference's test drivers (tests/test_frnn.cu,
+// tests/test_closest_neighbors.cu, tests/grid2d_frnn.cu in the reference),
+// restated against include/mcleap/*.h and libmcl_gb300.so.  Prints one line per
+// check and exits non-zero on any failure.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <random>
+#include <set>
+#include <vector>
+
+#include "mcleap/Device_Triangulation.h"
+#include "mcleap/gridCount2d.h"
+
+static int g_fail = 0;
+#define CHECK(cond, ...)                 \
+  do {                                   \
+    if (!(cond)) {                       \
+      ++g_fail;                          \
+      std::printf("FAIL: " __VA_ARGS__); \
+      std::printf("\n");                 \
+    }                                    \
+  } while (0)
+
+static float sqdist(glm::vec2 a, glm::vec2 b) {
+  const float dx = a.x - b.x, dy = a.y - b.y;
+  const float dx2 = dx * dx, dy2 = dy * dy;
+  return dx2 + dy2;
+}
+
+static std::vector<glm::vec2> ref_points(int n, float bounds) {
+  std::mt19937 rng{3};
+  std::uniform_real_distribution<float> pos_r(-bounds, bounds);
+  std::vector<glm::vec2> p;
+  for (int i = 0; i < n; ++i) {
+    const float x = pos_r(rng), y = pos_r(rng);
+    p.push_back(glm::vec2(x, y));
+  }
+  return p;
+}
+
+// tests/test_frnn.cu: FRNN through oneRing + getFRNN, against brute force
+static void test_frnn(float radius) {
+  const int n = 1000, M = 20, F = 100;
+  auto pts = ref_points(n, 1000.f);
+  HostTriangulation* ht = new HostTriangulation();
+  ht->addDelaunayPoints(pts);
+  DeviceTriangulation dt(ht);
+  const int V = (int)ht->m_pos.size();
+  int *d_ring, *d_nb;
+  cudaMalloc(&d_ring, sizeof(int) * V * M);
+  cudaMalloc(&d_nb, sizeof(int) * V * F);
+  dt.oneRing<M>(d_ring);
+  dt.getFRNN<M, F>(radius, d_ring, d_nb);
+  std::vector<int> nb((size_t)V * F);
+  cudaMemcpy(nb.data(), d_nb, sizeof(int) * V * F, cudaMemcpyDeviceToHost);
+  const float rr = radius * radius;
+  int bad = 0;
+  for (int i = 0; i < V; ++i) {
+    std::vector<int> want;
+    for (int j = 0; j < V; ++j)
+      if (j != i && sqdist(ht->m_pos[i], ht->m_pos[j]) <= rr) want.push_back(j);
+    std::vector<int> got;
+    for (int k = 0; k < nb[i]; ++k) got.push_back(nb[(size_t)(k + 1) * V + i]);
+    std::sort(got.begin(), got.end());
+    if (got != want) ++bad;
+  }
+  CHECK(bad == 0, "frnn r=%g: %d vertices differ", radius, bad);
+  std::printf("frnn r=%g vertices=%d mismatching=%d\n", radius, V, bad);
+  cudaFree(d_ring);
+  cudaFree(d_nb);
+  delete ht;
+}
+
+// tests/test_closest_neighbors.cu
+static void test_closest(int n) {
+  const int M = 100;
+  auto pts = ref_points(n, 1000.f);
+  HostTriangulation ht;
+  ht.addDelaunayPoints(pts);
+  DeviceTriangulation dt(&ht);
+  const int V = (int)ht.m_pos.size();
+  int *d_ring, *d_cl;
+  cudaMalloc(&d_ring, sizeof(int) * V * M);
+  cudaMalloc(&d_cl, sizeof(int) * V);
+  dt.oneRing<M>(d_ring);
+  dt.closestNeighbors<M>(d_ring, d_cl);
+  std::vector<int> cl(V);
+  cudaMemcpy(cl.data(), d_cl, sizeof(int) * V, cudaMemcpyDeviceToHost);
+  int bad = 0;
+  for (int i = 0; i < V; ++i) {
+    int best = i == 0 ? 1 : 0;
+    float bd = sqdist(ht.m_pos[i], ht.m_pos[best]);
+    for (int j = 0; j < V; ++j) {
+      if (j == i) continue;
+      const float d = sqdist(ht.m_pos[i], ht.m_pos[j]);
+      if (d < bd) { bd = d; best = j; }
+    }
+    if (cl[i] != best) ++bad;
+  }
+  CHECK(bad == 0, "closest n=%d: %d differ", n, bad);
+  std::printf("closest n=%d mismatching=%d\n", n, bad);
+  cudaFree(d_ring);
+  cudaFree(d_cl);
+}
+
+// tests/grid2d_frnn.cu SaveNeighborsFunctor
+struct SaveNeighborsFunctor {
+  float rad;
+  int max_nb;
+  int* num;
+  int* ids;
+  __device__ void operator()(const int& i, const int& j, const glm::vec2 d, const double dist) {
+    if (i != j && dist <= rad) {
+      const int k = num[i]++;
+      if (k < max_nb) ids[i * max_nb + k] = j;
+    }
+  }
+};
+
+static void test_grid_lattice(int side, float step, float rad) {
+  const int n = side * side, max_nb = 40;
+  std::vector<glm::vec2> pos(n);
+  for (int x = 0; x < side; ++x)
+    for (int y = 0; y < side; ++y) pos[x + side * y] = glm::vec2(x * step, y * step);
+  glm::vec2* d_pos;
+  cudaMalloc(&d_pos, sizeof(glm::vec2) * n);
+  cudaMemcpy(d_pos, pos.data(), sizeof(glm::vec2) * n, cudaMemcpyHostToDevice);
+  GridCount2d gc(n, glm::vec2(0.f), glm::vec2(1.f), glm::ivec2(10));
+  gc.update(d_pos);
+  SaveNeighborsFunctor f{rad, max_nb, nullptr, nullptr};
+  cudaMalloc(&f.num, sizeof(int) * n);
+  cudaMalloc(&f.ids, sizeof(int) * n * max_nb);
+  cudaMemset(f.num, 0, sizeof(int) * n);
+  gc.apply_f_frnn<SaveNeighborsFunctor>(f, d_pos, rad);
+  cudaDeviceSynchronize();
+  std::vector<int> num(n);
+  cudaMemcpy(num.data(), f.num, sizeof(int) * n, cudaMemcpyDeviceToHost);
+  cudaMemcpy(pos.data(), d_pos, sizeof(glm::vec2) * n, cudaMemcpyDeviceToHost);
+  int bad = 0;
+  for (int i = 0; i < n; ++i) {
+    int want = 0;
+    for (int j = 0; j < n; ++j)
+      if (i != j && sqdist(pos[i], pos[j]) <= rad * rad) ++want;
+    if (num[i] != want) ++bad;
+  }
+  CHECK(bad == 0, "grid lattice %d x %d step %g: %d differ", side, side, step, bad);
+  std::printf("grid lattice %dx%d step=%g mismatching=%d\n", side, side, step, bad);
+  cudaFree(d_pos);
+  cudaFree(f.num);
+  cudaFree(f.ids);
+}
+
+// A few kinetic steps through movePoints + untangle2 + delonize2: every face
+// must stay positively oriented (checked in double on the host).
+static void test_kinetic() {
+  const int n = 5000;
+  std::mt19937 rng{7};
+  std::uniform_real_distribution<float> u(0.f, 8192.f);
+  std::normal_distribution<float> g(0.f, 0.3f * 8192.f / 70.7f);
+  std::vector<glm::vec2> pts(n);
+  for (auto& p : pts) p = glm::vec2(u(rng), u(rng));
+  HostTriangulation ht;
+  ht.addDelaunayPoints(pts);
+  DeviceTriangulation dt(&ht);
+  const int V = (int)ht.m_pos.size();
+  glm::vec2* d_move;
+  cudaMalloc(&d_move, sizeof(glm::vec2) * V);
+  for (int step = 0; step < 3; ++step) {
+    std::vector<glm::vec2> mv(V, glm::vec2(0.f));
+    dt.transferToHost();
+    for (int i = 4; i < V; ++i) {
+      glm::vec2 t = ht.m_pos[i] + glm::vec2(g(rng), g(rng));
+      t.x = std::min(std::max(t.x, 0.f), 8191.f);
+      t.y = std::min(std::max(t.y, 0.f), 8191.f);
+      mv[i] = t - ht.m_pos[i];
+    }
+    cudaMemcpy(d_move, mv.data(), sizeof(glm::vec2) * V, cudaMemcpyHostToDevice);
+    CHECK(dt.movePoints(d_move), "movePoints");
+    CHECK(dt.untangle2(), "untangle2: %s", mcl_last_error());
+    CHECK(dt.delonize2(), "delonize2: %s", mcl_last_error());
+    dt.transferToHost();
+    int inverted = 0;
+    for (size_t t = 0; t < ht.m_t.size(); ++t) {
+      const HalfEdge& h = ht.m_he[ht.m_t[t].he];
+      const glm::vec2 a = ht.m_pos[h.v], b = ht.m_pos[ht.m_he[ht.m_t[t].he ^ 1].v], c = ht.m_pos[h.op];
+      const double o = ((double)b.x - a.x) * ((double)c.y - a.y) - ((double)b.y - a.y) * ((double)c.x - a.x);
+      if (!(o > 0)) ++inverted;
+    }
+    CHECK(inverted == 0, "kinetic step %d: %d faces not positive", step, inverted);
+    std::printf("kinetic step %d removed=%lld flips=%lld inverted_after=%d\n", step,
+                (long long)dt.last_stats.removed_vertices, (long long)dt.last_stats.lawson_flips, inverted);
+  }
+  cudaFree(d_move);
+}
+
+int main() {
+  for (float r : {5.f, 10.f, 20.f, 30.f, 40.f, 50.f}) test_frnn(r);
+  for (int n : {10, 100, 1000}) test_closest(n);
+  test_grid_lattice(10, 1.f, 1.f);
+  test_grid_lattice(20, 0.5f, 1.f);
+  test_grid_lattice(40, 0.25f, 0.25f);
+  test_kinetic();
+  std::printf(g_fail ? "FAILED %d\n" : "ALL PASSED\n", g_fail);
+  return g_fail ? 1 : 0;
+}
