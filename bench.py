@@ -45,6 +45,7 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=20000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-queries", action="store_true")
     return ap.parse_args()
 
 
@@ -202,6 +203,19 @@ def run_ours(args, rank, world, dist):
     sp = stream.cuda_stream
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
     lib = L.lib()
+    # per-step queries on the moved mesh: one-ring of every vertex (column
+    # layout, 32 slots) and FRNN with r = 3 x spacing on the torus (periodic
+    # grid of 512 x 512 cells of 16 units, minimum-image distances) over the N
+    # moving points, answered in vertex-id order without permuting the mesh
+    do_q = not args.no_queries
+    RING_M, FRNN_MAX = 32, 64
+    h = W.mean_spacing(n)
+    r_q = 3.0 * h
+    if do_q:
+        ring = torch.empty(V * RING_M, dtype=torch.int32, device=f"cuda:{local}")
+        qcounts = torch.empty(n, dtype=torch.int32, device=f"cuda:{local}")
+        qids = torch.empty(n * FRNN_MAX, dtype=torch.int32, device=f"cuda:{local}")
+        grid = M.GridCount2d(n, (0.0, 0.0), (16.0, 16.0), (512, 512), periodic=True)
     torch.cuda.synchronize()
 
     cp, cf = clocks_start()
@@ -212,9 +226,19 @@ def run_ours(args, rank, world, dist):
     torch.cuda.synchronize()
     tot0 = dt.totals()
 
-    # timed region: K steps, device-resident inputs
+    def queries():
+        L.check(lib.mcl_one_ring(dt.handle, L.LAYOUT_COLUMN, RING_M, ring.data_ptr(), sp, None))
+        qa.record(stream)
+        pos_pts = dt.m_pos + 8 * 4  # the N moving points (ids 4..)
+        L.check(lib.mcl_grid_build(grid.handle, pos_pts, sp))
+        L.check(lib.mcl_grid_frnn_ids(grid.handle, r_q, FRNN_MAX, qcounts.data_ptr(), qids.data_ptr(), sp, None))
+
+    # timed region: K steps, device-resident inputs; each step is followed by
+    # its queries (timed separately, not part of the kinetic value)
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    q_ring = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    q_end = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
@@ -225,10 +249,34 @@ def run_ours(args, rank, world, dist):
             starts[k].record(stream)
             L.check(lib.mcl_step(dt.handle, dev_disp[Wm + k].data_ptr(), sp, None))
             ends[k].record(stream)
+            if do_q:
+                qa = q_ring[k]
+                queries()
+                q_end[k].record(stream)
     stream.synchronize()
     torch.cuda.synchronize()
     wall = time.perf_counter() - wall0
     step_ms = np.array([s.elapsed_time(e) for s, e in zip(starts, ends)])
+    qinfo = None
+    if do_q:
+        ring_ms = np.array([e.elapsed_time(a) for e, a in zip(ends, q_ring)])
+        frnn_ms = np.array([a.elapsed_time(b) for a, b in zip(q_ring, q_end)])
+        trunc = C.c_int64()
+        L.check(lib.mcl_one_ring(dt.handle, L.LAYOUT_COLUMN, RING_M, ring.data_ptr(), sp, C.byref(trunc)))
+        ovf = grid.frnn_ids(r_q, FRNN_MAX, qcounts, qids, stream=stream)
+        k_nb = int(qcounts.sum().item())
+        q_s = float(ring_ms.sum() + frnn_ms.sum()) / 1e3
+        ring_bytes, frnn_bytes = 52 * V, 28 * n + 4 * k_nb
+        qinfo = {
+            "one_ring": {"ms": float(ring_ms.mean()), "slots": RING_M, "truncated": trunc.value,
+                         "alg_bytes": ring_bytes, "gbs": ring_bytes / (ring_ms.mean() / 1e3) / 1e9},
+            "frnn": {"ms": float(frnn_ms.mean()), "r": r_q, "grid": "periodic 512x512 cells of 16",
+                     "neighbours": k_nb, "overflow": ovf, "alg_bytes": frnn_bytes,
+                     "gbs": frnn_bytes / (frnn_ms.mean() / 1e3) / 1e9},
+            "ms_per_step": 1e3 * q_s / K,
+            "pts_per_s": world * n * K / q_s,
+            "total_pts_steps_per_s": world * n * K / (q_s + float(step_ms.sum()) / 1e3),
+        }
     st = dt.status(stream)
     if st["status"] != 0:
         raise RuntimeError(f"engine status {st}")
@@ -305,8 +353,10 @@ def run_ours(args, rank, world, dist):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "kernel": "k_step", "alg_bytes_per_launch": alg_bytes},
+            "queries": qinfo,
             "e2e": e2e, "cpu_baseline": cpu, "clocks": clocks,
-            "gpu_launches": K,
+            # k_step per step, plus k_one_ring + 7 grid-build kernels + k_grid_frnn per step
+            "gpu_launches": K * (10 if do_q else 1),
             "wall_s": wall, "build_s": t_build,
         }
         print(json.dumps(line), flush=True)

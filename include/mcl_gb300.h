@@ -182,8 +182,9 @@ int mcl_grid_create(int64_t num_points, float min_x, float min_y, float cell_x, 
 int mcl_grid_destroy(mcl_grid* g);
 
 /* GridCount2d::update(pos[, vel]) (include/gridCount2d.h:119-135, :174-260): sorts
- * the points by cell (cells in Morton order, points inside a cell by their
- * previous index) and permutes pos_dev (and vel_dev when not NULL) in place. */
+ * the points by cell (cells row-major like the reference's hash y*nx + x,
+ * points inside a cell by their previous index) and permutes pos_dev (and
+ * vel_dev when not NULL) in place. */
 int mcl_grid_update(mcl_grid* g, mcl_float2* pos_dev, mcl_float2* vel_dev, void* stream);
 
 /* d_ind: perm_dev[i] = sorted position of the point that was at index i before
@@ -207,10 +208,25 @@ int mcl_grid_describe(mcl_grid* g, mcl_grid_desc* desc_host);
 
 /* apply_f_frnn with the reference tests' SaveNeighborsFunctor
  * (tests/grid2d_frnn.cu:26-60): for every sorted point i, the sorted indices j != i
- * with fl(fl(dx*dx)+fl(dy*dy)) <= fl(r*r), ascending; ROW layout without the
+ * with fl(fl(dx*dx)+fl(dy*dy)) <= fl(r*r), in the reference's stencil order
+ * (cell rows bottom to top, cells left to right, points of a cell in sorted
+ * order; gridCount2d.h:263-296); ROW layout without the
  * count slot: counts_dev[i], ids_dev[i*max_nb + k].  *overflow_host may be NULL. */
 int mcl_grid_frnn(mcl_grid* g, const mcl_float2* pos_dev, float r, int max_nb, int32_t* counts_dev,
                   int32_t* ids_dev, void* stream, int64_t* overflow_host);
+
+/* GridCount2d::update without the in-place permutation (the tables of
+ * include/gridCount2d.h:174-260 for positions the caller must keep in order,
+ * e.g. a mesh's vertex positions): builds the cell tables and keeps the sorted
+ * copy inside the grid; pos_dev is only read. */
+int mcl_grid_build(mcl_grid* g, const mcl_float2* pos_dev, void* stream);
+
+/* mcl_grid_frnn over the positions of the last mcl_grid_build / mcl_grid_update,
+ * in INPUT index space: counts_dev[i] and ids_dev[i*max_nb + k] for input point
+ * i, neighbour input indices in stencil order (the SaveNeighborsFunctor result of
+ * tests/grid2d_frnn.cu:26-60 mapped back through d_ind). */
+int mcl_grid_frnn_ids(mcl_grid* g, float r, int max_nb, int32_t* counts_dev, int32_t* ids_dev, void* stream,
+                      int64_t* overflow_host);
 
 /* mean_num_particle_in_cell (include/gridCount2d.h:314-334). */
 int mcl_grid_mean_occupancy(mcl_grid* g, float* mean_host);

@@ -33,6 +33,7 @@ EXPORTS = [
     "mcl_untangle", "mcl_delaunay_restore", "mcl_step", "mcl_step_host", "mcl_mesh_last_status", "mcl_mesh_totals",
     "mcl_one_ring", "mcl_closest_neighbors", "mcl_mesh_frnn",
     "mcl_grid_create", "mcl_grid_destroy", "mcl_grid_update", "mcl_grid_tables", "mcl_grid_describe", "mcl_grid_frnn",
+    "mcl_grid_build", "mcl_grid_frnn_ids",
     "mcl_grid_mean_occupancy", "mcl_debug_predicates_host", "mcl_debug_predicates_device", "mcl_mesh_validate", "mcl_debug_state", "mcl_debug_timeline", "mcl_grid_frnn_noalloc",
 ]
 
@@ -99,6 +100,8 @@ def lib():
             "mcl_grid_tables": ([vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp), C.POINTER(i32), C.POINTER(i32)], i32),
             "mcl_grid_frnn": ([vp, vp, f32, i32, vp, vp, vp, C.POINTER(i64)], i32),
             "mcl_grid_describe": ([vp, vp], i32),
+            "mcl_grid_build": ([vp, vp, vp], i32),
+            "mcl_grid_frnn_ids": ([vp, f32, i32, vp, vp, vp, C.POINTER(i64)], i32),
             "mcl_grid_mean_occupancy": ([vp, C.POINTER(f32)], i32),
             "mcl_debug_predicates_host": ([i32, vp, vp, i64, vp, vp], i32),
             "mcl_mesh_validate": ([vp, vp], i32),

@@ -5,7 +5,7 @@
 //   closest       DeviceTriangulation::closestNeighbors[2]  (include/kernels.cuh:129-165)
 //   mesh FRNN     DeviceTriangulation::getFRNN / getFRNN2   (include/kernels.cuh:169-272)
 //   grid          GridCount2d (include/gridCount2d.h): counting sort of points
-//                 into cells ordered along a Morton curve, stable inside a cell,
+//                 into row-major cells, stable inside a cell,
 //                 then fixed-radius queries over the (2w+1)^2 cell stencil.
 #include <cuda_runtime.h>
 
@@ -60,33 +60,55 @@ __device__ __forceinline__ int mv_rot(const MeshView& M, int h) { return mv_next
 constexpr int kMaxDeg = 4096;
 
 // ---------------------------------------------------------------------------
-__global__ void k_one_ring(MeshView M, int layout, int max_ring, int* ring, unsigned long long* truncated) {
+// Rings of up to kRegRing spokes are walked once and kept in registers (the
+// array is only ever indexed by unrolled constants), then written starting at
+// the spoke to the smallest neighbour; longer rings walk twice.
+constexpr int kRegRing = 16;
+
+__global__ void __launch_bounds__(256) k_one_ring(MeshView M, int layout, int max_ring, int* ring,
+                                                  unsigned long long* truncated) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= M.V) return;
   const int h0 = __ldg(M.vhe + i);
   if (h0 < 0) return;
-  // first pass: start at the spoke to the smallest neighbour id
-  int start = h0, best = 0x7fffffff, deg = 0;
+  const int cap = max_ring - 1;
+  const size_t stride = layout == MCL_LAYOUT_COLUMN ? (size_t)M.V : 1;
+  int* row = layout == MCL_LAYOUT_COLUMN ? ring + i : ring + (size_t)i * max_ring;
+  int reg[kRegRing];
+  int start = h0, best = 0x7fffffff, deg = 0, at = 0;
   int h = h0;
   do {
     const int w = mv_origin(M, h ^ 1);
-    if (w < best) { best = w; start = h; }
+    if (w < best) { best = w; start = h; at = deg; }
+#pragma unroll
+    for (int j = 0; j < kRegRing; ++j)
+      if (j == deg) reg[j] = w;
     h = mv_rot(M, h);
     ++deg;
   } while (h != h0 && deg < kMaxDeg);
-  const int cap = max_ring - 1;
-  int cnt = 0;
+  if (deg <= kRegRing && deg <= cap) {
+#pragma unroll
+    for (int k = 0; k < kRegRing; ++k) {
+      if (k < deg) {
+        int src = at + k;
+        if (src >= deg) src -= deg;
+        int w = reg[0];
+#pragma unroll
+        for (int j = 1; j < kRegRing; ++j)
+          if (j == src) w = reg[j];
+        row[(size_t)(k + 1) * stride] = w;
+      }
+    }
+    row[0] = deg;
+    return;
+  }
+  const int cnt = deg < cap ? deg : cap;
   h = start;
-  for (int k = 0; k < deg; ++k) {
-    if (cnt >= cap) break;
-    const int w = mv_origin(M, h ^ 1);
-    if (layout == MCL_LAYOUT_COLUMN) ring[(size_t)(cnt + 1) * M.V + i] = w;
-    else ring[(size_t)i * max_ring + cnt + 1] = w;
-    ++cnt;
+  for (int k = 0; k < cnt; ++k) {
+    row[(size_t)(k + 1) * stride] = mv_origin(M, h ^ 1);
     h = mv_rot(M, h);
   }
-  if (layout == MCL_LAYOUT_COLUMN) ring[i] = cnt;
-  else ring[(size_t)i * max_ring] = cnt;
+  row[0] = cnt;
   if (deg > cap) atomicAdd(truncated, 1ull);
 }
 
@@ -182,6 +204,7 @@ struct mcl_grid {
   float2* tmp2;
   void* scan_tmp;
   size_t scan_tmp_bytes;
+  int built;            // mcl_grid_build ran: tmp holds the sorted copy
 };
 
 namespace {
@@ -214,7 +237,7 @@ __device__ __forceinline__ int cell_coord(float p, float mn, float c, int n, int
 }
 
 __device__ __forceinline__ int cell_id(const GridView& G, int x, int y) {
-  return G.morton ? (int)(spread16((unsigned)x) | (spread16((unsigned)y) << 1)) : y * G.nx + x;
+  return y * G.nx + x;
 }
 
 __global__ void k_grid_hash(GridView G, int n, const float2* pos, int* cell, int* count) {
@@ -276,61 +299,151 @@ __global__ void k_gather(int n, const int* src, const float2* in, float2* out) {
   if (i < n) out[i] = in[src[i]];
 }
 
-constexpr int kGridLocal = 256;
+// Fixed-radius query, one thread per sorted slot i (threads of a warp are
+// neighbouring points of one cell row, so their candidates overlap in L1).
+// Cells are row-major, so each stencil row is one contiguous range of sorted
+// points (up to three with periodic wrap).  The stencil is the disk: for each
+// cell row the x extent comes from the query's own position and the row's
+// vertical distance, widened by a margin far above float rounding; cells it
+// skips hold no point within r, so the result and its order equal the full
+// (2w+1)^2 stencil's: rows bottom to top, cells left to right in stencil
+// order, points of a cell in sorted order (the reference's SaveNeighborsFunctor
+// order, gridCount2d.h:263-296).  Distances use the reference formula
+// fl(fl(dx*dx) + fl(dy*dy)) <= fl(r*r) without FMA; periodic grids take the
+// minimum image (|d| > L/2 -> d -= copysign(L, d)).  A candidate is tested
+// without branches: its sorted index is written to the thread's shared row at
+// slot nf and nf advances on a hit (a range takes this path only when the row
+// has room for all of it).  Rows hold up to kStageCap ids and are flushed one
+// warp per row (coalesced), ids and rows mapped through src when given;
+// entries past kStageCap go straight to global memory.
+constexpr int kStageCap = 48;
+constexpr int kFrnnThreads = 128;
 
-__global__ void k_grid_frnn(GridView G, int n, const float2* pos, const int* start, const int* count, float r2,
-                            int wx, int wy, float Lx, float Ly, int max_nb, int* counts, int* ids,
-                            unsigned long long* overflow) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const float2 p = pos[i];
-  const int x0 = cell_coord(p.x, G.minx, G.cx, G.nx, G.periodic);
-  const int y0 = cell_coord(p.y, G.miny, G.cy, G.ny, G.periodic);
-  int found[kGridLocal];
+template <bool kPeriodic>
+__global__ void __launch_bounds__(kFrnnThreads) k_grid_frnn(GridView G, int n, const float2* __restrict__ pos,
+                                                           const int* __restrict__ start,
+                                                           const int* __restrict__ count, float r, float Lx,
+                                                           float Ly, int max_nb, int* __restrict__ counts,
+                                                           int* __restrict__ ids, unsigned long long* overflow,
+                                                           const int* __restrict__ src) {
+  __shared__ int stage[kFrnnThreads * (kStageCap + 1)];
+  __shared__ int cnts[kFrnnThreads];
+  const int t = threadIdx.x, row0 = blockIdx.x * kFrnnThreads, i = row0 + t;
+  int* mine = stage + t * (kStageCap + 1);
+  const int scap = max_nb < kStageCap ? max_nb : kStageCap;
   int nf = 0;
-  bool over = false;
-  const float hx = 0.5f * Lx, hy = 0.5f * Ly;
-  // distinct stencil rows / columns (a periodic stencil wider than the grid
-  // visits every row or column once)
-  const bool allx = G.periodic && 2 * wx + 1 >= G.nx, ally = G.periodic && 2 * wy + 1 >= G.ny;
-  const int ylo = ally ? 0 : y0 - wy, yhi = ally ? G.ny - 1 : y0 + wy;
-  const int xlo = allx ? 0 : x0 - wx, xhi = allx ? G.nx - 1 : x0 + wx;
-  for (int yy = ylo; yy <= yhi; ++yy) {
-    int y = yy;
-    if (G.periodic) { y %= G.ny; if (y < 0) y += G.ny; }
-    else if (y < 0 || y >= G.ny) continue;
-    for (int xx = xlo; xx <= xhi; ++xx) {
-      int x = xx;
-      if (G.periodic) { x %= G.nx; if (x < 0) x += G.nx; }
-      else if (x < 0 || x >= G.nx) continue;
-      const int c = cell_id(G, x, y);
-      const int b = start[c], k = count[c];
-      for (int j = b; j < b + k; ++j) {
-        if (j == i) continue;
-        const float2 q = pos[j];
-        float dx = __fsub_rn(p.x, q.x), dy = __fsub_rn(p.y, q.y);
-        if (G.periodic) {
-          if (dx > hx) dx = __fsub_rn(dx, Lx); else if (dx < -hx) dx = __fadd_rn(dx, Lx);
-          if (dy > hy) dy = __fsub_rn(dy, Ly); else if (dy < -hy) dy = __fadd_rn(dy, Ly);
+  const float r2 = __fmul_rn(r, r);
+  if (i < n) {
+    const float2 p = pos[i];
+    const int row = src ? __ldg(src + i) : i;
+    int* direct = ids + (size_t)row * max_nb;
+    const float hx = 0.5f * Lx, hy = 0.5f * Ly;
+    const float ix = 1.0f / G.cx, iy = 1.0f / G.cy;
+    const float mx = 1e-3f * G.cx + 1e-5f * (fabsf(p.x) + fabsf(G.minx) + r);
+    const float my = 1e-3f * G.cy + 1e-5f * (fabsf(p.y) + fabsf(G.miny) + r);
+    const float px = p.x - G.minx, py = p.y - G.miny;
+    int ylo = (int)floorf(fmaxf(fminf((py - r - my) * iy, 1e9f), -1e9f));
+    int yhi = (int)floorf(fmaxf(fminf((py + r + my) * iy, 1e9f), -1e9f));
+    if (!kPeriodic) {
+      ylo = ylo < 0 ? 0 : (ylo >= G.ny ? G.ny - 1 : ylo);
+      yhi = yhi < 0 ? 0 : (yhi >= G.ny ? G.ny - 1 : yhi);
+    } else if (yhi - ylo + 1 > G.ny) {
+      ylo = 0; yhi = G.ny - 1;  // the disk covers every row: visit each once
+    }
+    for (int yy = ylo; yy <= yhi; ++yy) {
+      // vertical distance from p to the row's slab (0 inside), minus the margin;
+      // without wrap the border rows also hold the points clamped into them,
+      // so their slabs extend to infinity
+      float slo = yy * G.cy, shi = slo + G.cy;
+      if (!kPeriodic) {
+        if (yy == 0) slo = -INFINITY;
+        if (yy == G.ny - 1) shi = INFINITY;
+      }
+      const float dym = fmaxf(fmaxf(slo - py, py - shi) - my, 0.f);
+      const float hw = (kPeriodic && yhi - ylo + 1 >= G.ny) ? r + mx : sqrtf(fmaxf(r2 - dym * dym, 0.f)) * 1.0001f + mx;
+      int xlo = (int)floorf(fmaxf(fminf((px - hw) * ix, 1e9f), -1e9f));
+      int xhi = (int)floorf(fmaxf(fminf((px + hw) * ix, 1e9f), -1e9f));
+      int y = yy;
+      if (kPeriodic) {
+        y %= G.ny;
+        if (y < 0) y += G.ny;
+        if (xhi - xlo + 1 > G.nx) { xlo = 0; xhi = G.nx - 1; }
+      } else {
+        xlo = xlo < 0 ? 0 : (xlo >= G.nx ? G.nx - 1 : xlo);
+        xhi = xhi < 0 ? 0 : (xhi >= G.nx ? G.nx - 1 : xhi);
+      }
+      const int base = y * G.nx;
+#pragma unroll 1
+      for (int sgi = 0; sgi < 2; ++sgi) {
+        int sa, sb;
+        if (kPeriodic) {
+          // [xlo, xhi] (at most nx cells) in stencil order: from the wrapped
+          // start to the end of the row, then on from cell 0
+          const int s0 = (xlo % G.nx + G.nx) % G.nx, last = s0 + (xhi - xlo);
+          if (sgi == 0) { sa = s0; sb = last < G.nx ? last : G.nx - 1; }
+          else if (sgi == 1) { if (last < G.nx) continue; sa = 0; sb = last - G.nx; }
+          else continue;
+        } else {
+          if (sgi != 0) continue;
+          sa = xlo; sb = xhi;
         }
-        const float d = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
-        if (d <= r2) {
-          if (nf < kGridLocal) found[nf++] = j;
-          else over = true;
+        const int b = __ldg(start + base + sa);
+        const int e = __ldg(start + base + sb) + __ldg(count + base + sb);
+        if (nf + (e - b) <= scap) {
+#pragma unroll 4
+          for (int j = b; j < e; ++j) {
+            const float2 o = pos[j];
+            float dx = __fsub_rn(p.x, o.x), dy = __fsub_rn(p.y, o.y);
+            if (kPeriodic) {
+              dx = fabsf(dx) > hx ? __fsub_rn(dx, copysignf(Lx, dx)) : dx;
+              dy = fabsf(dy) > hy ? __fsub_rn(dy, copysignf(Ly, dy)) : dy;
+            }
+            const bool hit = (__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)) <= r2) & (j != i);
+            mine[nf] = j;
+            nf += hit ? 1 : 0;
+          }
+        } else {
+          for (int j = b; j < e; ++j) {
+            const float2 o = pos[j];
+            float dx = __fsub_rn(p.x, o.x), dy = __fsub_rn(p.y, o.y);
+            if (kPeriodic) {
+              dx = fabsf(dx) > hx ? __fsub_rn(dx, copysignf(Lx, dx)) : dx;
+              dy = fabsf(dy) > hy ? __fsub_rn(dy, copysignf(Ly, dy)) : dy;
+            }
+            if ((__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)) <= r2) & (j != i)) {
+              if (nf < scap) mine[nf] = j;
+              else if (nf < max_nb) direct[nf] = src ? __ldg(src + j) : j;
+              ++nf;
+            }
+          }
         }
       }
     }
+    counts[row] = nf < max_nb ? nf : max_nb;
+    if (nf > max_nb) atomicAdd(overflow, 1ull);
   }
-  for (int a = 1; a < nf; ++a) {
-    const int x = found[a];
-    int b = a - 1;
-    while (b >= 0 && found[b] > x) { found[b + 1] = found[b]; --b; }
-    found[b + 1] = x;
+  cnts[t] = nf < scap ? nf : scap;
+  __syncthreads();
+  const int lane = t & 31;
+  for (int rr = t >> 5; rr < kFrnnThreads && row0 + rr < n; rr += kFrnnThreads / 32) {
+    const int cr = cnts[rr];
+    const int row = src ? __ldg(src + row0 + rr) : row0 + rr;
+    int* dst = ids + (size_t)row * max_nb;
+    const int* from = stage + rr * (kStageCap + 1);
+    for (int k = lane; k < cr; k += 32) dst[k] = src ? __ldg(src + from[k]) : from[k];
   }
-  const int cnt = nf < max_nb ? nf : max_nb;
-  for (int k = 0; k < cnt; ++k) ids[(size_t)i * max_nb + k] = found[k];
-  counts[i] = cnt;
-  if (over || nf > max_nb) atomicAdd(overflow, 1ull);
+}
+
+int launch_grid_frnn(const GridView& G, int n, const float2* pos, const int* start, const int* count, float r,
+                     float Lx, float Ly, int max_nb, int* counts, int* ids, unsigned long long* ovf,
+                     const int* src, cudaStream_t s) {
+  const unsigned blocks = (unsigned)((n + kFrnnThreads - 1) / kFrnnThreads);
+  if (G.periodic)
+    k_grid_frnn<true><<<blocks, kFrnnThreads, 0, s>>>(G, n, pos, start, count, r, Lx, Ly, max_nb, counts, ids, ovf, src);
+  else
+    k_grid_frnn<false><<<blocks, kFrnnThreads, 0, s>>>(G, n, pos, start, count, r, Lx, Ly, max_nb, counts, ids, ovf, src);
+  QCK(cudaGetLastError());
+  return MCL_OK;
 }
 
 __global__ void k_mean_occupancy(int64_t ncells, const int* count, unsigned long long* acc) {
@@ -367,22 +480,15 @@ __global__ void k_scan_one_block(const int* in, int* out, int64_t n) {
   }
 }
 
-// Exclusive scan of n ints (device), with a temporary of per-block sums.
+// Exclusive scan of n ints, entirely on the device (no host round trip, so the
+// grid build can sit inside a captured CUDA graph): per-block scans, one block
+// scanning the block totals, then the block offsets added.  tmp holds nb ints
+// and tmp2 nb ints, nb = ceil(n / 1024).
 int scan_exclusive(const int* in, int* out, int64_t n, int* tmp, int* tmp2, cudaStream_t s) {
   const int64_t nb = (n + 1023) / 1024;
   k_scan_blocks<<<(unsigned)nb, 1024, 0, s>>>(in, out, tmp, n);
   if (nb > 1) {
-    std::vector<int> sums(nb);
-    QCK(cudaMemcpyAsync(sums.data(), tmp, 4 * nb, cudaMemcpyDeviceToHost, s));
-    QCK(cudaStreamSynchronize(s));
-    int64_t run = 0;
-    for (int64_t b = 0; b < nb; ++b) {
-      const int64_t x = sums[b];
-      sums[b] = (int)run;
-      run += x;
-    }
-    QCK(cudaMemcpyAsync(tmp2, sums.data(), 4 * nb, cudaMemcpyHostToDevice, s));
-    QCK(cudaStreamSynchronize(s));
+    k_scan_one_block<<<1, 1024, 0, s>>>(tmp, tmp2, nb);
     k_scan_add<<<(unsigned)nb, 1024, 0, s>>>(out, tmp2, n);
   }
   QCK(cudaGetLastError());
@@ -511,7 +617,7 @@ int mcl_grid_create(int64_t n, float minx, float miny, float cx, float cy, int32
   int side = 1, bits = 0;
   while (side < std::max(nx, ny)) { side <<= 1; ++bits; }
   const int64_t mcells = (int64_t)side * side;
-  g->morton = (side <= 65536 && mcells <= 4 * (int64_t)nx * ny + 1024) ? 1 : 0;
+  g->morton = 0;  // row-major: a stencil row of cells is one contiguous range of sorted points
   g->mbits = bits;
   g->ncells = g->morton ? mcells : (int64_t)nx * ny;
   const int64_t nn = std::max<int64_t>(n, 1);
@@ -546,14 +652,16 @@ int mcl_grid_destroy(mcl_grid* g) {
   return MCL_OK;
 }
 
-int mcl_grid_update(mcl_grid* g, mcl_float2* pos, mcl_float2* vel, void* stream) {
-  if (!g || !pos) return qfail(MCL_ERR_INVALID_ARGUMENT, "bad args");
-  cudaStream_t s = (cudaStream_t)stream;
+}  // extern "C"
+
+namespace {
+// Cell tables for the positions pos (input order) and their sorted copy in
+// g->tmp; pos itself is not written.
+int grid_build_tables(mcl_grid* g, const float2* pos, cudaStream_t s) {
   const int n = (int)g->n;
-  if (n == 0) return MCL_OK;
   const GridView G = view_of(g);
   QCK(cudaMemsetAsync(g->count, 0, 4 * g->ncells, s));
-  k_grid_hash<<<(n + 255) / 256, 256, 0, s>>>(G, n, (const float2*)pos, g->cell, g->count);
+  k_grid_hash<<<(n + 255) / 256, 256, 0, s>>>(G, n, pos, g->cell, g->count);
   int* tmp = (int*)g->scan_tmp;
   const int64_t nb = (g->ncells + 1023) / 1024;
   int rc = scan_exclusive(g->count, g->start, g->ncells, tmp, tmp + nb + 1, s);
@@ -562,13 +670,58 @@ int mcl_grid_update(mcl_grid* g, mcl_float2* pos, mcl_float2* vel, void* stream)
   k_grid_scatter<<<(n + 255) / 256, 256, 0, s>>>(n, g->cell, g->cursor, g->perm, g->src);
   k_grid_sort_cells<<<(unsigned)((g->ncells + 255) / 256), 256, 0, s>>>(g->ncells, g->start, g->count, g->src,
                                                                          g->perm);
-  k_gather<<<(n + 255) / 256, 256, 0, s>>>(n, g->src, (const float2*)pos, g->tmp);
+  k_gather<<<(n + 255) / 256, 256, 0, s>>>(n, g->src, pos, g->tmp);
+  QCK(cudaGetLastError());
+  return MCL_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int mcl_grid_update(mcl_grid* g, mcl_float2* pos, mcl_float2* vel, void* stream) {
+  if (!g || !pos) return qfail(MCL_ERR_INVALID_ARGUMENT, "bad args");
+  cudaStream_t s = (cudaStream_t)stream;
+  const int n = (int)g->n;
+  if (n == 0) return MCL_OK;
+  const int rc = grid_build_tables(g, (const float2*)pos, s);
+  if (rc != MCL_OK) return rc;
   QCK(cudaMemcpyAsync(pos, g->tmp, 8 * (size_t)n, cudaMemcpyDeviceToDevice, s));
   if (vel) {
     k_gather<<<(n + 255) / 256, 256, 0, s>>>(n, g->src, (const float2*)vel, g->tmp2);
     QCK(cudaMemcpyAsync(vel, g->tmp2, 8 * (size_t)n, cudaMemcpyDeviceToDevice, s));
   }
   QCK(cudaGetLastError());
+  g->built = 1;
+  return MCL_OK;
+}
+
+int mcl_grid_build(mcl_grid* g, const mcl_float2* pos, void* stream) {
+  if (!g || !pos) return qfail(MCL_ERR_INVALID_ARGUMENT, "bad args");
+  if (g->n == 0) return MCL_OK;
+  const int rc = grid_build_tables(g, (const float2*)pos, (cudaStream_t)stream);
+  if (rc == MCL_OK) g->built = 1;
+  return rc;
+}
+
+int mcl_grid_frnn_ids(mcl_grid* g, float r, int max_nb, int32_t* counts, int32_t* ids, void* stream,
+                      int64_t* overflow) {
+  if (!g || !counts || !ids || max_nb < 1 || !(r >= 0.f)) return qfail(MCL_ERR_INVALID_ARGUMENT, "bad args");
+  if (!g->built) return qfail(MCL_ERR_INVALID_ARGUMENT, "mcl_grid_frnn_ids: call mcl_grid_build first");
+  cudaStream_t s = (cudaStream_t)stream;
+  const int n = (int)g->n;
+  if (n == 0) return MCL_OK;
+  const GridView G = view_of(g);
+  unsigned long long* ovf = (unsigned long long*)g->scan_tmp;
+  QCK(cudaMemsetAsync(ovf, 0, 8, s));
+  const int rc = launch_grid_frnn(G, n, g->tmp, g->start, g->count, r, g->cx * g->nx, g->cy * g->ny, max_nb, counts,
+                                  ids, ovf, g->src, s);
+  if (rc != MCL_OK) return rc;
+  if (overflow) {
+    unsigned long long t = 0;
+    QCK(cudaMemcpyAsync(&t, ovf, 8, cudaMemcpyDeviceToHost, s));
+    QCK(cudaStreamSynchronize(s));
+    *overflow = (int64_t)t;
+  }
   return MCL_OK;
 }
 
@@ -600,12 +753,11 @@ int mcl_grid_frnn(mcl_grid* g, const mcl_float2* pos, float r, int max_nb, int32
   const int n = (int)g->n;
   if (n == 0) return MCL_OK;
   const GridView G = view_of(g);
-  const int wx = std::max(1, (int)std::ceil(r / g->cx)), wy = std::max(1, (int)std::ceil(r / g->cy));
   unsigned long long* ovf = (unsigned long long*)g->scan_tmp;
   QCK(cudaMemsetAsync(ovf, 0, 8, s));
-  k_grid_frnn<<<(n + 127) / 128, 128, 0, s>>>(G, n, (const float2*)pos, g->start, g->count, r * r, wx, wy,
-                                              g->cx * g->nx, g->cy * g->ny, max_nb, counts, ids, ovf);
-  QCK(cudaGetLastError());
+  const int rc = launch_grid_frnn(G, n, (const float2*)pos, g->start, g->count, r, g->cx * g->nx, g->cy * g->ny,
+                                  max_nb, counts, ids, ovf, nullptr, s);
+  if (rc != MCL_OK) return rc;
   if (overflow) {
     unsigned long long t = 0;
     QCK(cudaMemcpyAsync(&t, ovf, 8, cudaMemcpyDeviceToHost, s));
@@ -675,7 +827,7 @@ extern "C" int mcl_grid_frnn_noalloc(const mcl_float2* pos, int64_t n, float min
   int side = 1;
   while (side < std::max(cells_x, cells_y)) side <<= 1;
   const int64_t mcells = (int64_t)side * side;
-  const int morton = (side <= 65536 && mcells <= 4 * (int64_t)cells_x * cells_y + 1024) ? 1 : 0;
+  const int morton = 0;  // row-major cells, as mcl_grid_create
   const int64_t ncells = morton ? mcells : (int64_t)cells_x * cells_y;
   if (n > kNoAllocMaxPoints)
     return qfail(MCL_ERR_CAPACITY, "mcl_grid_frnn_noalloc: more than 262144 points");
@@ -705,10 +857,9 @@ extern "C" int mcl_grid_frnn_noalloc(const mcl_float2* pos, int64_t n, float min
   k_grid_scatter<<<(nn + 255) / 256, 256, 0, s>>>(nn, cell, cursor, perm, src);
   k_grid_sort_cells<<<(unsigned)((ncells + 255) / 256), 256, 0, s>>>(ncells, start, count, src, perm);
   k_gather<<<(nn + 255) / 256, 256, 0, s>>>(nn, src, (const float2*)pos, (float2*)sorted_pos);
-  const int wx = std::max(1, (int)std::ceil(r / cell_x)), wy = std::max(1, (int)std::ceil(r / cell_y));
-  k_grid_frnn<<<(nn + 127) / 128, 128, 0, s>>>(G, nn, (const float2*)sorted_pos, start, count, r * r, wx, wy,
-                                               cell_x * cells_x, cell_y * cells_y, max_nb, counts, ids, ovf);
-  QCK(cudaGetLastError());
+  const int rc2 = launch_grid_frnn(G, nn, (const float2*)sorted_pos, start, count, r, cell_x * cells_x,
+                                   cell_y * cells_y, max_nb, counts, ids, ovf, nullptr, s);
+  if (rc2 != MCL_OK) return rc2;
   if (overflow) {
     unsigned long long t = 0;
     QCK(cudaMemcpyAsync(&t, ovf, 8, cudaMemcpyDeviceToHost, s));

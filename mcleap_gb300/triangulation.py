@@ -267,6 +267,18 @@ class GridCount2d:
                                       _stream_ptr(stream), C.byref(ov)))
         return ov.value
 
+    def build(self, pos, stream=None):
+        """Cell tables for ``pos`` without permuting it (``pos`` is only read)."""
+        L.check(L.lib().mcl_grid_build(self.handle, L.ptr(pos), _stream_ptr(stream)))
+
+    def frnn_ids(self, rad, max_nb, counts, ids, stream=None, overflow=True):
+        """Neighbours of the last build/update in input index space; returns the
+        overflow count (or None when ``overflow`` is False: no host sync)."""
+        ov = C.c_int64()
+        L.check(L.lib().mcl_grid_frnn_ids(self.handle, float(rad), int(max_nb), L.ptr(counts), L.ptr(ids),
+                                          _stream_ptr(stream), C.byref(ov) if overflow else None))
+        return ov.value if overflow else None
+
     def tables(self):
         perm, start, count = C.c_void_p(), C.c_void_p(), C.c_void_p()
         nx, ny = C.c_int(), C.c_int()

@@ -240,7 +240,7 @@ def test_grid_reference_lattices(M):
         g, sp, c, rows, bc, bids, ov, _ = grid_check(M, pos, 1.0, ncell, (0.0, 0.0), rad, 40)
         assert ov == 0
         assert np.array_equal(c, bc)
-        assert np.array_equal(np.concatenate([rows[i, :c[i]] for i in range(len(pos))]), bids)
+        assert np.array_equal(np.concatenate([np.sort(rows[i, :c[i]]) for i in range(len(pos))]), bids)
 
 
 def test_grid_random_and_permutation(M):
@@ -248,7 +248,7 @@ def test_grid_random_and_permutation(M):
     pos = rng.uniform(-50, 50, (10000, 2)).astype(np.float32)
     g, sp, c, rows, bc, bids, ov, _ = grid_check(M, pos, 1.0, 100, (-50.0, -50.0), 1.0, 40)
     assert ov == 0 and np.array_equal(c, bc)
-    assert np.array_equal(np.concatenate([rows[i, :c[i]] for i in range(len(pos))]), bids)
+    assert np.array_equal(np.concatenate([np.sort(rows[i, :c[i]]) for i in range(len(pos))]), bids)
     from helpers import d2h
 
     t = g.tables()
@@ -267,7 +267,120 @@ def test_grid_periodic_torus(M):
     cell = 8192.0 / ncell
     g, sp, c, rows, bc, bids, ov, _ = grid_check(M, pos, cell, ncell, (0.0, 0.0), 3 * h, 64, periodic=True, L=8192.0)
     assert ov == 0 and np.array_equal(c, bc)
-    assert np.array_equal(np.concatenate([rows[i, :c[i]] for i in range(n)]), bids)
+    assert np.array_equal(np.concatenate([np.sort(rows[i, :c[i]]) for i in range(n)]), bids)
+
+
+def test_grid_build_keeps_input_order_and_answers_in_input_ids(M):
+    # the mesh's own positions, queried without permuting them (torus, r = 3h)
+    import torch
+
+    n = 30000
+    pos = uniform_points(n, 14)
+    h = spacing(n)
+    for periodic, ncell, max_nb in ((True, 256, 64), (False, 128, 64)):
+        cell = 8192.0 / ncell
+        r = 3 * h if periodic else 2.5 * h
+        g = M.GridCount2d(n, (0.0, 0.0), (cell, cell), (ncell, ncell), periodic=periodic)
+        d = cuda(pos)
+        g.build(d)
+        assert np.array_equal(d.cpu().numpy(), pos)
+        counts = torch.zeros(n, dtype=torch.int32, device="cuda")
+        ids = torch.full((n * max_nb,), -7, dtype=torch.int32, device="cuda")
+        assert g.frnn_ids(r, max_nb, counts, ids) == 0
+        c = counts.cpu().numpy()
+        rows = ids.cpu().numpy().reshape(n, max_nb)
+        bc, bids = O.frnn_brute(pos, r, periodic=periodic, L=8192.0)
+        assert np.array_equal(c, bc)
+        assert np.array_equal(np.concatenate([np.sort(rows[i, :c[i]]) for i in range(n)]), bids)
+        # a second build after the points moved reuses the grid
+        pos2 = np.mod(pos + np.float32(0.37 * h), np.float32(8192)).astype(np.float32)
+        g.build(cuda(pos2))
+        assert g.frnn_ids(r, max_nb, counts, ids) == 0
+        bc2, bids2 = O.frnn_brute(pos2, r, periodic=periodic, L=8192.0)
+        c2 = counts.cpu().numpy()
+        rows2 = ids.cpu().numpy().reshape(n, max_nb)
+        assert np.array_equal(c2, bc2)
+        assert np.array_equal(np.concatenate([np.sort(rows2[i, :c2[i]]) for i in range(n)]), bids2)
+        g.close()
+
+
+def stencil_order_lists(sp, start, count, nx, ny, cell, mn, r, periodic, L):
+    """Neighbour lists of every sorted point in the full (2w+1)^2 stencil order
+    (rows bottom to top, cells left to right, points of a cell in sorted
+    order), float32 distances as the reference formula."""
+    f = np.float32
+    w = int(np.ceil(r / cell))
+    r2 = f(f(r) * f(r))
+    h = f(0.5) * f(L)
+    out = []
+    for i, p in enumerate(sp):
+        x0 = int(np.floor((p[0] - mn[0]) / cell))
+        y0 = int(np.floor((p[1] - mn[1]) / cell))
+        if periodic:
+            x0 %= nx
+            y0 %= ny
+        else:
+            x0 = min(max(x0, 0), nx - 1)
+            y0 = min(max(y0, 0), ny - 1)
+        row = []
+        for yy in range(y0 - w, y0 + w + 1):
+            if periodic:
+                y = yy % ny
+            elif not 0 <= yy < ny:
+                continue
+            else:
+                y = yy
+            for xx in range(x0 - w, x0 + w + 1):
+                if periodic:
+                    x = xx % nx
+                elif not 0 <= xx < nx:
+                    continue
+                else:
+                    x = xx
+                c = y * nx + x
+                for j in range(start[c], start[c] + count[c]):
+                    if j == i:
+                        continue
+                    dx = f(p[0]) - f(sp[j][0])
+                    dy = f(p[1]) - f(sp[j][1])
+                    if periodic:
+                        if abs(dx) > h:
+                            dx = f(dx - f(np.copysign(f(L), dx)))
+                        if abs(dy) > h:
+                            dy = f(dy - f(np.copysign(f(L), dy)))
+                    if f(f(dx * dx) + f(dy * dy)) <= r2:
+                        row.append(j)
+        out.append(row)
+    return out
+
+
+@pytest.mark.parametrize("periodic", [False, True])
+def test_grid_frnn_order_is_the_stencil_order(M, periodic):
+    # the disk-shaped stencil visits fewer cells than the (2w+1)^2 square but
+    # must return the same neighbours in the same order
+    import torch
+
+    from helpers import d2h
+
+    rng = np.random.default_rng(21 + periodic)
+    n, nc, cell, r = 1500, 20, 50.0, 60.0
+    pos = (rng.random((n, 2), dtype=np.float32) * np.float32(1000)).astype(np.float32)
+    g = M.GridCount2d(n, (0.0, 0.0), (cell, cell), (nc, nc), periodic=periodic)
+    d = cuda(pos)
+    g.update(d)
+    sp = d.cpu().numpy()
+    t = g.tables()
+    start = d2h(t["start"], nc * nc)
+    count = d2h(t["count"], nc * nc)
+    max_nb = 64
+    counts = torch.zeros(n, dtype=torch.int32, device="cuda")
+    ids = torch.zeros(n * max_nb, dtype=torch.int32, device="cuda")
+    assert g.frnn(d, r, max_nb, counts, ids) == 0
+    c = counts.cpu().numpy()
+    rows = ids.cpu().numpy().reshape(n, max_nb)
+    want = stencil_order_lists(sp, start, count, nc, nc, cell, (0.0, 0.0), r, periodic, 1000.0)
+    for i in range(n):
+        assert rows[i, :c[i]].tolist() == want[i], i
 
 
 def test_device_predicates_match_host_and_golden(M):
