@@ -46,6 +46,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-queries", action="store_true")
+    ap.add_argument("--workload", default="taylor-green", choices=["taylor-green", "batched"])
+    ap.add_argument("--meshes", type=int, default=4096)
+    ap.add_argument("--plain-steps", type=int, default=3)
     return ap.parse_args()
 
 
@@ -362,6 +365,199 @@ def run_ours(args, rank, world, dist):
         print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------
+def run_batched(args, rank, world, dist):
+    """Batched form: many independent meshes (sizes log-uniform in [100, 1e5]),
+    each with its own Gaussian walk (sigma = 0.1 x its spacing, clamped to its
+    box) and FRNN at r = 2 x its spacing, all stepped by one launch per step;
+    against the plain form, the same meshes stepped one launch per mesh."""
+    import torch
+
+    from mcleap_gb300 import _lib as L
+    from mcleap_gb300 import autotune as AT
+    from mcleap_gb300 import batch as MB
+    from mcleap_gb300 import build as B
+    from mcleap_gb300 import workloads as W
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = f"cuda:{local}"
+    B.build()
+    K, Wm, nm = args.steps, args.warmup, args.meshes
+    rng = np.random.default_rng(4 + rank)
+    sizes = np.exp(rng.uniform(np.log(100), np.log(1e5), nm)).astype(np.int64)
+    t0 = time.perf_counter()
+    handles = [MB.build_mesh(W.uniform_points(int(n), 40000 + i)) for i, n in enumerate(sizes)]
+    t_build = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    batch = MB.MeshBatch.from_handles(handles, destroy_inputs=False)
+    verify = batch.clone()
+    t_batch = time.perf_counter() - t0
+    singles = [MB.MeshBatch(h) for h in handles]
+    V, E, npts = batch.V, batch.E, int(sizes.sum())
+    h = (8192.0 / np.sqrt(sizes)).astype(np.float32)
+    sigma = torch.tensor(0.1 * h, dtype=torch.float32, device=dev)
+    radius = torch.tensor(2.0 * h, dtype=torch.float32, device=dev)
+    F = 48
+    d = torch.zeros((V, 2), dtype=torch.float32, device=dev)
+    out = torch.empty(V * F, dtype=torch.int32, device=dev)
+    counter = torch.zeros(1, dtype=torch.int64, device=dev)
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+    lib = L.lib()
+    SEED = 1234
+
+    def pipeline_step(m, ctr, dd, outp, s, with_events=None):
+        m.walk(sigma, ctr, dd, seed=SEED, stream=s)
+        m.settle(dd, stream=s, sync=False)
+        if with_events:
+            with_events[0].record(s)
+        L.check(lib.mcl_step(m.handle, L.ptr(dd), s.cuda_stream, None))
+        if with_events:
+            with_events[1].record(s)
+        m.frnn(radius, F, outp, stream=s, sync=False)
+        if with_events:
+            with_events[2].record(s)
+
+    # autotune the launch shape on clones (walk + settle + step per candidate)
+    tune_ctr = torch.zeros(1, dtype=torch.int64, device=dev)
+
+    def tune_step(m, k, s):
+        with torch.cuda.stream(s):
+            tune_ctr.fill_(10_000 + k)
+        m.walk(sigma, tune_ctr, d, seed=SEED, stream=s)
+        m.settle(d, stream=s, sync=False)
+        L.check(lib.mcl_step(m.handle, L.ptr(d), s.cuda_stream, None))
+
+    t0 = time.perf_counter()
+    best, trials = AT.autotune(batch, tune_step, stream=stream)
+    t_tune = time.perf_counter() - t0
+
+    # warm-up, then K timed steps (inputs far larger than L2)
+    for k in range(Wm):
+        pipeline_step(batch, counter, d, out, stream)
+    stream.synchronize()
+    st = batch.status(stream)
+    if st["status"] != 0:
+        raise RuntimeError(f"batched warm-up failed: {st}")
+    tot0 = batch.totals()
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(K)]
+    cp, cf = clocks_start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    for k in range(K):
+        pipeline_step(batch, counter, d, out, stream, evs[k])
+    stream.synchronize()
+    st = batch.status(stream)
+    if st["status"] != 0:
+        raise RuntimeError(f"batched step failed: {st}")
+    tot1 = batch.totals()
+    step_ms = np.array([e[0].elapsed_time(e[1]) for e in evs])
+    frnn_ms = np.array([e[1].elapsed_time(e[2]) for e in evs])
+    kin_s = float(step_ms.sum()) / 1e3
+    if dist:
+        t = torch.tensor([kin_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        kin_s = float(t.item())
+    flips = tot1["lawson_flips"] - tot0["lawson_flips"] + tot1["removal_flips"] - tot0["removal_flips"]
+    wl_items = (tot1["incircle_tests"] - tot0["incircle_tests"]) - K * (E - 4 * nm)
+
+    # the whole per-step pipeline (walk, settle, step, FRNN) as a CUDA graph of two steps
+    graph = None
+    try:
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=stream):
+            for _ in range(2):
+                pipeline_step(batch, counter, d, out, stream)
+        reps = max(1, K // 2)
+        ge = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+        with torch.cuda.stream(stream):
+            for r in range(reps):
+                ge[r][0].record(stream)
+                g.replay()
+                ge[r][1].record(stream)
+        stream.synchronize()
+        st = batch.status(stream)
+        if st["status"] != 0:
+            raise RuntimeError(f"graph replay failed: {st}")
+        gms = np.array([a.elapsed_time(b) for a, b in ge]) / 2
+        graph = {"ms_per_step": float(gms.mean()), "p50": float(np.median(gms)), "p99": float(np.percentile(gms, 99)),
+                 "pts_steps_per_s": npts / (gms.mean() / 1e3), "steps": 2 * reps,
+                 "contents": "walk + settle + step + per-mesh FRNN, two steps per graph"}
+    except Exception as ex:  # noqa: BLE001 - reported, not fatal
+        graph = {"unavailable": str(ex)[:200]}
+    clocks = clocks_stop(cp, cf, local)
+
+    # plain form: the same meshes, one launch per mesh (device time of the
+    # steps only: host launch gaps are not counted against it)
+    KP = args.plain_steps
+    ctrs = torch.zeros(nm, dtype=torch.int64, device=dev)
+    pe = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(nm)]
+          for _ in range(KP)]
+    pw = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(KP)]
+    v0 = batch.v0
+    for i, m in enumerate(singles):  # first-call scratch allocation outside the timing
+        m.settle(d[int(v0[i]):int(v0[i] + batch.nv[i])], stream=stream, sync=False)
+    stream.synchronize()
+    for k in range(KP):
+        pw[k][0].record(stream)
+        for i, m in enumerate(singles):
+            di = d[int(v0[i]):int(v0[i] + batch.nv[i])]
+            m.walk(sigma[i:i + 1], ctrs[i:i + 1], di, seed=SEED + i, stream=stream)
+            m.settle(di, stream=stream, sync=False)
+            pe[k][i][0].record(stream)
+            L.check(lib.mcl_step(m.handle, L.ptr(di), sp, None))
+            pe[k][i][1].record(stream)
+            oi = out[int(v0[i]) * F:int(v0[i] + batch.nv[i]) * F]
+            m.frnn(radius[i:i + 1], F, oi, stream=stream, sync=False)
+        pw[k][1].record(stream)
+    stream.synchronize()
+    bad = [i for i, m in enumerate(singles[:64]) if m.status(stream)["status"] != 0]
+    plain_step_s = sum(a.elapsed_time(b) for row in pe for a, b in row) / 1e3
+    plain_wall_s = sum(a.elapsed_time(b) for a, b in pw) / 1e3
+
+    # the same steps through the batch (verify clone, fresh counter) must
+    # leave every mesh exactly as the plain form did
+    vctr = torch.zeros(1, dtype=torch.int64, device=dev)
+    vd = torch.zeros_like(d)
+    for k in range(KP):
+        pipeline_step(verify, vctr, vd, out, stream)
+    stream.synchronize()
+    check = sorted(set([0, nm - 1, int(np.argmax(sizes)), int(np.argmin(sizes))] +
+                       rng.choice(nm, size=min(nm, 12), replace=False).tolist()))
+    same = all(np.array_equal(verify.edges(i), singles[i].edges(0)) for i in check)
+
+    line = {
+        "metric": "batched kinetic pts*steps/s (move + untangle + Delaunay restore), one launch per step",
+        "value": world * npts * K / kin_s, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": Wm,
+        "ms_per_step": 1e3 * kin_s / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"batched: {nm} meshes, sizes log-uniform in [100, 1e5] (seed 4), Gaussian walk "
+                               "sigma = 0.1 x spacing clamped to each mesh's box, FRNN r = 2 x spacing",
+                   "meshes": nm, "points": npts, "vertices": V, "edges": E,
+                   "l2": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{world}"},
+        "flips_per_s": world * flips / kin_s,
+        "step_ms": {"p50": float(np.median(step_ms)), "p99": float(np.percentile(step_ms, 99)),
+                    "max": float(step_ms.max())},
+        "per_step": {"flips": flips / K, "worklist_items": wl_items / K},
+        "frnn": {"ms": float(frnn_ms.mean()), "max_nb": F, "pts_per_s": npts / (frnn_ms.mean() / 1e3)},
+        "pipeline_graph": graph,
+        "plain": {"steps": KP, "kinetic_pts_steps_per_s": npts * KP / plain_step_s,
+                  "launch_gaps_included_pts_steps_per_s": npts * KP / plain_wall_s,
+                  "ms_per_step": 1e3 * plain_step_s / KP, "failed_meshes": bad},
+        "speedup_vs_plain": (npts * K / kin_s) / (npts * KP / plain_step_s),
+        "same_as_plain": {"meshes_checked": len(check), "identical": same},
+        "autotune": {"best": best, "trials": len(trials), "seconds": t_tune},
+        "predicates": {k: tot1[k] - tot0[k] for k in ("incircle_tests", "incircle_fp64", "incircle_exact",
+                                                      "orient_fp64", "orient_exact", "sos_decisions")},
+        "clocks": clocks, "gpu_launches": K * 5,
+        "setup_s": {"build_meshes": t_build, "batch": t_batch},
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -378,6 +574,8 @@ def main():
     try:
         if args.impl == "reference":
             run_reference(args, rank, world)
+        elif args.workload == "batched":
+            run_batched(args, rank, world, dist)
         else:
             run_ours(args, rank, world, dist)
     finally:

@@ -249,6 +249,68 @@ int mcl_grid_frnn_noalloc(const mcl_float2* pos_dev, int64_t n, float min_x, flo
                           mcl_float2* sorted_pos_dev, int32_t* perm_dev, int32_t* counts_dev, int32_t* ids_dev,
                           void* stream, int64_t* overflow_host);
 
+/* ---- batches of meshes ---------------------------------------------------------
+ * No counterpart in the reference, which steps one DeviceTriangulation at a
+ * time.  A batch is an mcl_mesh whose connected components are independent
+ * meshes (each with its own bounding square): every mesh call above
+ * (mcl_step, mcl_one_ring, mcl_mesh_validate, ...) works on it and processes
+ * all meshes in one launch.  Vertex and edge ids are global in the batch;
+ * mcl_batch_range gives each mesh's slice. */
+
+/* Copy `count` meshes (their validated state) into a new batch; the inputs are
+ * unchanged and may be destroyed.  At most 2^30 vertices and 2^29 edges. */
+int mcl_batch_create(mcl_mesh* const* meshes, int64_t count, mcl_mesh** out);
+/* Number of meshes in a batch (1 for a plain mesh). */
+int mcl_batch_count(const mcl_mesh* m, int64_t* count);
+/* Mesh i of the batch: vertices [v0, v0 + nv), edges [e0, e0 + ne). */
+int mcl_batch_range(const mcl_mesh* m, int64_t i, int64_t* v0, int64_t* nv, int64_t* e0, int64_t* ne);
+/* Per vertex: index of its mesh (int32[V], device; NULL for a plain mesh). */
+int mcl_batch_vertex_mesh(const mcl_mesh* m, const int32_t** vcomp_dev);
+/* transferToHost for mesh i alone, renumbered from 0 (same layout as
+ * mcl_mesh_download_aos). */
+int mcl_batch_download_aos(mcl_mesh* m, int64_t i, mcl_float2* pos_host, int32_t* v_host, int32_t* he_host,
+                           int32_t* t_host);
+/* getFRNN (include/Device_Triangulation.h:529-557) with one radius per mesh:
+ * r_dev[i] for the vertices of mesh i (a plain mesh reads r_dev[0]). */
+int mcl_batch_frnn(mcl_mesh* m, const float* r_dev, int layout, int max_frnn, int32_t* out_dev, void* stream,
+                   int64_t* overflow_host);
+/* A copy of a mesh or batch at its validated state (for snapshots and tuning). */
+int mcl_mesh_clone(const mcl_mesh* src, mcl_mesh** out);
+
+/* Launch shape of the kinetic step: blocks_per_sm in [1, max] (0 = max), and
+ * the work-list size at or below which one block finishes the flip rounds
+ * (0 = 2048).  Results do not depend on either. */
+int mcl_mesh_set_tuning(mcl_mesh* m, int blocks_per_sm, int tail_items);
+int mcl_mesh_get_tuning(const mcl_mesh* m, int* blocks_per_sm, int* tail_items, int* max_blocks_per_sm);
+
+/* ---- motion models ----------------------------------------------------------- */
+/* Gaussian random walk, the motion of the reference's diffusion-limited
+ * aggregation experiment (experiments/diffusion_limited_aggregation.cu:51-60,
+ * :263-268): d_dev[v] = clamp(pos + sigma * N(0, I), lo, hi) - pos with
+ * sigma = sigma_dev[mesh of v], zero for the bounding corners and for vertices
+ * with frozen_dev[v] != 0 (frozen_dev may be NULL).  The normal draws of
+ * vertex v of mesh c are a function of (seed + c, *counter_dev, the id of v
+ * within mesh c) only (a counter-based generator), so a mesh draws the same
+ * numbers alone (with seed + c) as inside a batch; *counter_dev is
+ * incremented on the device after the draw, so a captured CUDA graph replays
+ * new steps. */
+int mcl_walk(mcl_mesh* m, const float* sigma_dev, const uint8_t* frozen_dev, uint64_t seed, uint64_t* counter_dev,
+             float lo, float hi, mcl_float2* d_dev, void* stream);
+/* Refuse moves that would put two vertices of one mesh at the same point: while
+ * two vertices sit at one point, each of them that moves is sent back (its
+ * displacement zeroed).  The result does not depend on thread order; vertices
+ * that do not move never yield.  No counterpart in the reference (duplicate
+ * points make its triangulation undefined).  *sent_back_host (may be NULL: no
+ * synchronisation) = displacements zeroed. */
+int mcl_settle_moves(mcl_mesh* m, mcl_float2* d_dev, void* stream, int64_t* sent_back_host);
+/* check_if_close_diffusion (experiments/diffusion_limited_aggregation.cu:51-60):
+ * frozen_out[v] = frozen_in[v], or 1 when a vertex with frozen_in != 0 lies
+ * within r_dev[mesh of v] of a free vertex v (fl(dx*dx + dy*dy) <= fl(r*r)).
+ * Reads only frozen_in, so the result does not depend on thread order.
+ * *newly_frozen_host may be NULL. */
+int mcl_dla_freeze(mcl_mesh* m, const float* r_dev, const uint8_t* frozen_in, uint8_t* frozen_out, void* stream,
+                   int64_t* newly_frozen_host);
+
 /* ---- diagnostics ------------------------------------------------------------ */
 /* Structural invariants of the device mesh; counts8[k] = violations of kind k:
  * 0 next/prev not inverse, 1 inner face not a 3-cycle, 2 apex != origin(prev),

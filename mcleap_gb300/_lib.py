@@ -34,6 +34,9 @@ EXPORTS = [
     "mcl_one_ring", "mcl_closest_neighbors", "mcl_mesh_frnn",
     "mcl_grid_create", "mcl_grid_destroy", "mcl_grid_update", "mcl_grid_tables", "mcl_grid_describe", "mcl_grid_frnn",
     "mcl_grid_build", "mcl_grid_frnn_ids",
+    "mcl_batch_create", "mcl_batch_count", "mcl_batch_range", "mcl_batch_vertex_mesh", "mcl_batch_download_aos",
+    "mcl_batch_frnn", "mcl_mesh_clone", "mcl_mesh_set_tuning", "mcl_mesh_get_tuning", "mcl_walk",
+    "mcl_settle_moves", "mcl_dla_freeze",
     "mcl_grid_mean_occupancy", "mcl_debug_predicates_host", "mcl_debug_predicates_device", "mcl_mesh_validate", "mcl_debug_state", "mcl_debug_timeline", "mcl_grid_frnn_noalloc",
 ]
 
@@ -110,6 +113,18 @@ def lib():
             "mcl_grid_frnn_noalloc": ([vp, i64, f32, f32, f32, f32, i32, i32, i32, f32, i32, vp, vp, vp, vp, vp,
                                        C.POINTER(i64)], i32),
             "mcl_debug_predicates_device": ([i32, vp, vp, i64, vp, vp, vp], i32),
+            "mcl_batch_create": ([vp, i64, C.POINTER(vp)], i32),
+            "mcl_batch_count": ([vp, C.POINTER(i64)], i32),
+            "mcl_batch_range": ([vp, i64, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64), C.POINTER(i64)], i32),
+            "mcl_batch_vertex_mesh": ([vp, C.POINTER(vp)], i32),
+            "mcl_batch_download_aos": ([vp, i64, vp, vp, vp, vp], i32),
+            "mcl_batch_frnn": ([vp, vp, i32, i32, vp, vp, C.POINTER(i64)], i32),
+            "mcl_mesh_clone": ([vp, C.POINTER(vp)], i32),
+            "mcl_mesh_set_tuning": ([vp, i32, i32], i32),
+            "mcl_mesh_get_tuning": ([vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)], i32),
+            "mcl_walk": ([vp, vp, vp, C.c_uint64, vp, f32, f32, vp, vp], i32),
+            "mcl_settle_moves": ([vp, vp, vp, C.POINTER(i64)], i32),
+            "mcl_dla_freeze": ([vp, vp, vp, vp, vp, C.POINTER(i64)], i32),
         }
         for name, (args, res) in sig.items():
             fn = getattr(L, name)

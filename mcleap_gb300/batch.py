@@ -1,0 +1,173 @@
+"""Batches of independent meshes stepped together, motion models, tuning.
+
+A batch is one device mesh whose components are the meshes (each with its own
+bounding square), so every engine call steps or queries all of them in one
+launch.  The reference has no counterpart: it steps one DeviceTriangulation at
+a time.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+from .triangulation import _stream_ptr
+
+
+def build_mesh(points):
+    """GPU Delaunay build of ``points`` (sorted in place into the reference's
+    Morton order, ids 4.. after the bounding corners); returns a raw handle."""
+    if not (isinstance(points, np.ndarray) and points.dtype == np.float32 and points.flags["C_CONTIGUOUS"]):
+        raise TypeError("points must be a C-contiguous float32 numpy array")
+    h = C.c_void_p()
+    L.check(L.lib().mcl_mesh_build(L.ptr(points), len(points), C.byref(h)))
+    return h
+
+
+class MeshBatch:
+    """Handle to a batch (or, with one mesh, a plain mesh) on the device."""
+
+    def __init__(self, handle):
+        self.handle = handle
+        V, HE, T = C.c_int64(), C.c_int64(), C.c_int64()
+        L.check(L.lib().mcl_mesh_sizes(self.handle, C.byref(V), C.byref(HE), C.byref(T)))
+        self.V, self.E, self.T = V.value, HE.value // 2, T.value
+        n = C.c_int64()
+        L.check(L.lib().mcl_batch_count(self.handle, C.byref(n)))
+        self.count = n.value
+        r = np.zeros((self.count, 4), np.int64)
+        a, b, c, d = C.c_int64(), C.c_int64(), C.c_int64(), C.c_int64()
+        for i in range(self.count):
+            L.check(L.lib().mcl_batch_range(self.handle, i, C.byref(a), C.byref(b), C.byref(c), C.byref(d)))
+            r[i] = (a.value, b.value, c.value, d.value)
+        self.v0, self.nv, self.e0, self.ne = r[:, 0], r[:, 1], r[:, 2], r[:, 3]
+
+    @classmethod
+    def from_handles(cls, handles, destroy_inputs=True):
+        arr = (C.c_void_p * len(handles))(*[h.value for h in handles])
+        out = C.c_void_p()
+        try:
+            L.check(L.lib().mcl_batch_create(arr, len(handles), C.byref(out)))
+        finally:
+            if destroy_inputs:
+                for h in handles:
+                    L.lib().mcl_mesh_destroy(h)
+        return cls(out)
+
+    @classmethod
+    def from_points(cls, point_sets):
+        """Build every mesh on the GPU (each array is Morton-sorted in place) and
+        batch them in the given order."""
+        return cls.from_handles([build_mesh(p) for p in point_sets])
+
+    def close(self):
+        if getattr(self, "handle", None) is not None and self.handle.value:
+            L.lib().mcl_mesh_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- state ------------------------------------------------------------------
+    @property
+    def positions_ptr(self):
+        p = C.c_void_p()
+        L.check(L.lib().mcl_mesh_positions(self.handle, C.byref(p)))
+        return p.value
+
+    def vertex_mesh_ptr(self):
+        p = C.c_void_p()
+        L.check(L.lib().mcl_batch_vertex_mesh(self.handle, C.byref(p)))
+        return p.value
+
+    def download(self, i):
+        """(pos, v, he, t) of mesh i in the reference's AoS layout, ids from 0."""
+        nv, ne = int(self.nv[i]), int(self.ne[i])
+        pos = np.zeros((nv, 2), np.float32)
+        v = np.zeros((nv, 2), np.int32)
+        he = np.zeros((2 * ne, 4), np.int32)
+        t = np.zeros((2 * (nv - 4) + 2, 1), np.int32)
+        L.check(L.lib().mcl_batch_download_aos(self.handle, i, L.ptr(pos), L.ptr(v), L.ptr(he), L.ptr(t)))
+        return pos, v, he, t
+
+    def edges(self, i):
+        """Sorted undirected edge list of mesh i (local ids)."""
+        he = self.download(i)[2]
+        a, b = he[0::2, 1], he[1::2, 1]
+        e = np.stack([np.minimum(a, b), np.maximum(a, b)], 1)
+        return e[np.lexsort((e[:, 1], e[:, 0]))]
+
+    def clone(self):
+        out = C.c_void_p()
+        L.check(L.lib().mcl_mesh_clone(self.handle, C.byref(out)))
+        return MeshBatch(out)
+
+    def set_tuning(self, blocks_per_sm=0, tail_items=0):
+        L.check(L.lib().mcl_mesh_set_tuning(self.handle, int(blocks_per_sm), int(tail_items)))
+
+    def tuning(self):
+        a, b, c = C.c_int(), C.c_int(), C.c_int()
+        L.check(L.lib().mcl_mesh_get_tuning(self.handle, C.byref(a), C.byref(b), C.byref(c)))
+        return dict(blocks_per_sm=a.value, tail_items=b.value, max_blocks_per_sm=c.value)
+
+    # -- stepping and motion -------------------------------------------------------
+    def step(self, d, stream=None, stats=True):
+        if stats:
+            st = L.StepStats()
+            L.check(L.lib().mcl_step(self.handle, L.ptr(d), _stream_ptr(stream), C.byref(st)))
+            return st.as_dict()
+        L.check(L.lib().mcl_step(self.handle, L.ptr(d), _stream_ptr(stream), None))
+        return None
+
+    def totals(self):
+        st = L.StepStats()
+        calls = C.c_int64()
+        L.check(L.lib().mcl_mesh_totals(self.handle, C.byref(st), C.byref(calls)))
+        d = st.as_dict()
+        d["calls"] = calls.value
+        return d
+
+    def status(self, stream=None):
+        st = L.StepStats()
+        L.check(L.lib().mcl_mesh_last_status(self.handle, _stream_ptr(stream), C.byref(st)))
+        return st.as_dict()
+
+    def validate(self):
+        out = np.zeros(8, np.int64)
+        L.check(L.lib().mcl_mesh_validate(self.handle, L.ptr(out)))
+        return out
+
+    def walk(self, sigma, counter, d, seed=0, frozen=None, lo=0.0, hi=float(np.nextafter(np.float32(8192), 0)),
+             stream=None):
+        """Gaussian random-walk displacements into ``d`` (sigma per mesh, device)."""
+        L.check(L.lib().mcl_walk(self.handle, L.ptr(sigma), L.ptr(frozen), int(seed), L.ptr(counter), float(lo),
+                                 float(hi), L.ptr(d), _stream_ptr(stream)))
+
+    def settle(self, d, stream=None, sync=True):
+        """Zero the displacements that would make two vertices of one mesh
+        coincide; returns how many were zeroed (None when sync is False)."""
+        n = C.c_int64()
+        L.check(L.lib().mcl_settle_moves(self.handle, L.ptr(d), _stream_ptr(stream), C.byref(n) if sync else None))
+        return n.value if sync else None
+
+    def dla_freeze(self, r, frozen_in, frozen_out, stream=None, sync=True):
+        n = C.c_int64()
+        L.check(L.lib().mcl_dla_freeze(self.handle, L.ptr(r), L.ptr(frozen_in), L.ptr(frozen_out),
+                                       _stream_ptr(stream), C.byref(n) if sync else None))
+        return n.value if sync else None
+
+    # -- queries ----------------------------------------------------------------------
+    def frnn(self, r, max_frnn, out, layout=L.LAYOUT_ROW, stream=None, sync=True):
+        """Mesh-walk FRNN with radius r[mesh] (device float array)."""
+        ov = C.c_int64()
+        L.check(L.lib().mcl_batch_frnn(self.handle, L.ptr(r), layout, int(max_frnn), L.ptr(out), _stream_ptr(stream),
+                                       C.byref(ov) if sync else None))
+        return ov.value if sync else None
+
+    def one_ring(self, max_ring, out, layout=L.LAYOUT_COLUMN, stream=None, sync=True):
+        tr = C.c_int64()
+        L.check(L.lib().mcl_one_ring(self.handle, layout, int(max_ring), L.ptr(out), _stream_ptr(stream),
+                                     C.byref(tr) if sync else None))
+        return tr.value if sync else None

@@ -337,7 +337,7 @@ __device__ void phase_lawson(cg::grid_group& g, const KParams& P, int src, unsig
       if (gtid == 0) set_error(P, MCL_ERR_NO_CONVERGENCE);
       break;
     }
-    if (n <= kTailItems && !(round == 0 && pre_sc)) {
+    if (n <= P.tail_items && !(round == 0 && pre_sc)) {
       // tail: block 0 finishes every remaining round on its own
       if (blockIdx.x == 0) {
         int s2 = src;
@@ -779,7 +779,8 @@ __device__ int insert_start(const KParams& P, int v) {
     h = ld_i(P.vhe + x);
     if (h >= 0 && h < 2 * P.E) return h;
   }
-  return 0;  // half-edge 0 is never freed: edge 0 is a side of the bounding square
+  // half-edge 0 of the vertex's mesh is never freed: a side of its bounding square
+  return P.vroot ? __ldg(P.vroot + v) : 0;
 }
 
 __device__ bool phase_insert(cg::grid_group& g, const KParams& P, unsigned& stamp,
@@ -1022,7 +1023,7 @@ __global__ void __launch_bounds__(kThreads) k_build(KParams P) {
 // Host side.
 static thread_local std::string g_last_error;
 
-static int fail(int code, const std::string& msg) {
+int fail(int code, const std::string& msg) {
   g_last_error = msg;
   return code;
 }
@@ -1033,7 +1034,7 @@ void mcl_set_last_error(const std::string& msg) { mcl::g_last_error = msg; }
 
 namespace mcl {
 
-static int cuda_fail(cudaError_t e, const char* what) {
+int cuda_fail(cudaError_t e, const char* what) {
   return fail(e == cudaErrorMemoryAllocation ? MCL_ERR_OUT_OF_MEMORY : MCL_ERR_CUDA,
               std::string(what) + ": " + cudaGetErrorString(e));
 }
@@ -1044,18 +1045,22 @@ static int cuda_fail(cudaError_t e, const char* what) {
     if (_e != cudaSuccess) return cuda_fail(_e, #call); \
   } while (0)
 
-static void free_mesh(mcl_mesh* m) {
+void free_mesh(mcl_mesh* m) {
   if (!m) return;
   void* ptrs[] = {m->pos[0], m->pos[1], m->ev, m->en, m->vhe, m->vfix, m->cand, m->win, m->qmark, m->efa, m->hard,
                   m->wl[0], m->wl[1], m->vl[0], m->vl[1], m->vmark, m->claim, m->vfree, m->vhint,
-                  m->vaux, m->vloc, m->vlocf, m->target, m->dstage, m->scratch, m->st};
+                  m->vaux, m->vloc, m->vlocf, m->target, m->dstage, m->scratch, m->st,
+                  m->vcomp, m->vroot, m->cbase, m->table, m->smark};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (m->st_host) cudaFreeHost(m->st_host);
+  delete[] m->comp_host;
   delete m;
 }
 
-static int alloc_mesh(int64_t V, int64_t E, mcl_mesh** out) {
+const float2* valid_positions(const mcl_mesh* m) { return m->valid_cur ? m->pos[m->cur] : m->pos[m->cur ^ 1]; }
+
+int alloc_mesh(int64_t V, int64_t E, mcl_mesh** out) {
   if (V < 4 || E < 5 || V > (1ll << 30) || E > (1ll << 29))
     return fail(MCL_ERR_INVALID_ARGUMENT, "mesh size out of range");
   int dev = 0;
@@ -1128,6 +1133,10 @@ static int alloc_mesh(int64_t V, int64_t E, mcl_mesh** out) {
     return cuda_fail(e == cudaSuccess ? cudaErrorInvalidConfiguration : e, "occupancy(k_step, k_build)");
   }
   m->coop_threads = kThreads;
+  m->nsm = nsm;
+  m->max_blocks_per_sm = per_sm;
+  m->tail_items = kTailItems;
+  m->ncomp = 1;
   m->coop_blocks = nsm * per_sm;
   m->repair_blocks = nsm * per_sm2;
   *out = m;
@@ -1190,6 +1199,81 @@ static int upload_soa(mcl_mesh* m, const mcl_float2* pos, const std::vector<int4
   return MCL_OK;
 }
 
+// transferToHost for the vertices [vb, vb + nv) and edges [eb, eb + ne) of one
+// component (the whole mesh, or one mesh of a batch), renumbered from 0.
+int download_range(mcl_mesh* m, int64_t vb, int64_t nv, int64_t eb, int64_t ne, int64_t T, mcl_float2* pos,
+                   int32_t* v, int32_t* he, int32_t* t) {
+  CK(cudaDeviceSynchronize());
+  const int64_t V = nv, E = ne, HE = 2 * E;
+  if (pos) CK(cudaMemcpy(pos, m->pos[m->cur] + vb, 8 * V, cudaMemcpyDeviceToHost));
+  if (!v && !he && !t) return MCL_OK;
+  std::vector<int4> ev(E), en(E);
+  std::vector<int> vhe(V);
+  CK(cudaMemcpy(ev.data(), m->ev + eb, 16 * E, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(en.data(), m->en + eb, 16 * E, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(vhe.data(), m->vhe + vb, 4 * V, cudaMemcpyDeviceToHost));
+  const int hb = (int)(2 * eb), vbi = (int)vb;
+  bool bad = false;
+  auto lv = [&](int x) {
+    if (x < 0) return -1;
+    x -= vbi;
+    if (x >= V || x < 0) bad = true;
+    return x;
+  };
+  auto lh = [&](int x) {
+    if (x < 0) return -1;
+    x -= hb;
+    if (x >= HE || x < 0) bad = true;
+    return x;
+  };
+  for (int64_t e = 0; e < E; ++e) {
+    ev[e] = make_int4(lv(ev[e].x), lv(ev[e].y), lv(ev[e].z), lv(ev[e].w));
+    en[e] = make_int4(lh(en[e].x), lh(en[e].y), lh(en[e].z), lh(en[e].w));
+  }
+  for (int64_t i = 0; i < V; ++i) vhe[i] = lh(vhe[i]);
+  if (bad) return fail(MCL_ERR_DEGENERATE_INPUT, "download: index outside the component");
+  auto org = [&](int64_t h) { const int4& q = ev[h >> 1]; return (h & 1) ? q.y : q.x; };
+  auto apex = [&](int64_t h) { const int4& q = ev[h >> 1]; return (h & 1) ? q.w : q.z; };
+  auto nxt = [&](int64_t h) { const int4& q = en[h >> 1]; return (h & 1) ? q.z : q.x; };
+  auto prv = [&](int64_t h) { const int4& q = en[h >> 1]; return (h & 1) ? q.w : q.y; };
+  std::vector<int> face(HE, -1);
+  int64_t nf = 0;
+  std::vector<int> owner;
+  owner.reserve(T);
+  for (int64_t h = 0; h < HE; ++h) {
+    if (apex(h) < 0 || org(h) < 0) continue;
+    const int64_t n = nxt(h), p = prv(h);
+    if (h < n && h < p) {
+      face[h] = (int)nf++;
+      owner.push_back((int)h);
+    }
+  }
+  for (int64_t h = 0; h < HE; ++h) {
+    if (apex(h) < 0 || org(h) < 0) continue;
+    const int64_t n = nxt(h), p = prv(h);
+    face[h] = face[std::min(h, std::min(n, p))];
+  }
+  if (he) {
+    for (int64_t h = 0; h < HE; ++h) {
+      he[4 * h] = nxt(h);
+      he[4 * h + 1] = org(h);
+      he[4 * h + 2] = face[h];
+      he[4 * h + 3] = apex(h) >= 0 ? apex(h) : -1;
+    }
+  }
+  if (v) {
+    for (int64_t i = 0; i < V; ++i) {
+      v[2 * i] = (int)i;
+      v[2 * i + 1] = vhe[i];
+    }
+  }
+  if (t) {
+    for (int64_t i = 0; i < (int64_t)owner.size() && i < T; ++i) t[i] = owner[i];
+  }
+  if (nf != T) return fail(MCL_ERR_DEGENERATE_INPUT, "face count mismatch on download");
+  return MCL_OK;
+}
+
 static KParams make_params(mcl_mesh* m, int mode) {
   KParams P;
   std::memset(&P, 0, sizeof(P));
@@ -1220,6 +1304,8 @@ static KParams make_params(mcl_mesh* m, int mode) {
   P.mode = mode;
   P.max_rounds = 1 << 16;
   P.walk_cap = 1 << 18;
+  P.tail_items = m->tail_items;
+  P.vroot = m->vroot;
   return P;
 }
 
@@ -1458,55 +1544,7 @@ int mcl_mesh_copy_positions(mcl_mesh* m, mcl_float2* dst, int to_host, void* str
 
 int mcl_mesh_download_aos(mcl_mesh* m, mcl_float2* pos, int32_t* v, int32_t* he, int32_t* t) {
   if (!m) return fail(MCL_ERR_INVALID_ARGUMENT, "null mesh");
-  CK(cudaDeviceSynchronize());
-  const int64_t V = m->V, E = m->E, HE = 2 * E;
-  if (pos) CK(cudaMemcpy(pos, m->pos[m->cur], 8 * V, cudaMemcpyDeviceToHost));
-  if (!v && !he && !t) return MCL_OK;
-  std::vector<int4> ev(E), en(E);
-  std::vector<int> vhe(V);
-  CK(cudaMemcpy(ev.data(), m->ev, 16 * E, cudaMemcpyDeviceToHost));
-  CK(cudaMemcpy(en.data(), m->en, 16 * E, cudaMemcpyDeviceToHost));
-  CK(cudaMemcpy(vhe.data(), m->vhe, 4 * V, cudaMemcpyDeviceToHost));
-  auto org = [&](int64_t h) { const int4& q = ev[h >> 1]; return (h & 1) ? q.y : q.x; };
-  auto apex = [&](int64_t h) { const int4& q = ev[h >> 1]; return (h & 1) ? q.w : q.z; };
-  auto nxt = [&](int64_t h) { const int4& q = en[h >> 1]; return (h & 1) ? q.z : q.x; };
-  auto prv = [&](int64_t h) { const int4& q = en[h >> 1]; return (h & 1) ? q.w : q.y; };
-  std::vector<int> face(HE, -1);
-  int64_t nf = 0;
-  std::vector<int> owner;
-  owner.reserve(m->T);
-  for (int64_t h = 0; h < HE; ++h) {
-    if (apex(h) < 0 || org(h) < 0) continue;
-    const int64_t n = nxt(h), p = prv(h);
-    if (h < n && h < p) {
-      face[h] = (int)nf++;
-      owner.push_back((int)h);
-    }
-  }
-  for (int64_t h = 0; h < HE; ++h) {
-    if (apex(h) < 0 || org(h) < 0) continue;
-    const int64_t n = nxt(h), p = prv(h);
-    face[h] = face[std::min(h, std::min(n, p))];
-  }
-  if (he) {
-    for (int64_t h = 0; h < HE; ++h) {
-      he[4 * h] = nxt(h);
-      he[4 * h + 1] = org(h);
-      he[4 * h + 2] = face[h];
-      he[4 * h + 3] = apex(h) >= 0 ? apex(h) : -1;
-    }
-  }
-  if (v) {
-    for (int64_t i = 0; i < V; ++i) {
-      v[2 * i] = (int)i;
-      v[2 * i + 1] = vhe[i];
-    }
-  }
-  if (t) {
-    for (int64_t i = 0; i < (int64_t)owner.size() && i < m->T; ++i) t[i] = owner[i];
-  }
-  if (nf != m->T) return fail(MCL_ERR_DEGENERATE_INPUT, "face count mismatch on download");
-  return MCL_OK;
+  return download_range(m, 0, m->V, 0, m->E, m->T, pos, v, he, t);
 }
 
 int mcl_move(mcl_mesh* m, const mcl_float2* d_dev, void* stream) {

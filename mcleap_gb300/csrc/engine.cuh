@@ -73,6 +73,9 @@ struct DevState {
   unsigned long long calls;
   int dbg[68];             // first failing vertex star: v, deg, then neighbour ids
   unsigned long long ts[kTimeline];  // %globaltimer at phase boundaries of the last launch
+  // mcl_settle_moves: [0] last stamp used, [1..3] moves sent back per pass
+  // (triple-buffered), [4] sent back by the last call, [5] status of the last call
+  unsigned int settle[8];
 };
 
 enum MoveMode { MOVE_NONE = 0, MOVE_DISPLACE = 1, MOVE_INTEGRATE = 2 };
@@ -112,6 +115,8 @@ struct KParams {
   int mode;
   int max_rounds;
   int walk_cap;
+  int tail_items;          // flip rounds with at most this many queued edges run in one block
+  const int* vroot;        // per vertex: a never-freed half-edge of its mesh (batches); NULL = half-edge 0
 };
 
 // ---------------------------------------------------------------------------
@@ -261,4 +266,30 @@ struct mcl_mesh {
   int repair_blocks;       // k_repair grid
   int coop_threads;
   int last_status;
+  // tuning (mcl_mesh_set_tuning)
+  int nsm;                 // SMs of the device
+  int max_blocks_per_sm;   // k_step occupancy limit
+  int tail_items;          // single-block flip-round threshold
+  // batches: a mesh made of independent components (mcl_batch_create)
+  int64_t ncomp;           // 1 for a plain mesh
+  int64_t* comp_host;      // [4 * ncomp]: first vertex, vertices, first edge, edges
+  int* vcomp;              // per vertex: component (NULL for a plain mesh)
+  int* vroot;              // per vertex: half-edge 0 of its component (NULL for a plain mesh)
+  int* cbase;              // per component: first vertex (NULL for a plain mesh)
+  // mcl_settle_moves
+  unsigned long long* table;  // hash table of positions, stamped entries
+  int64_t table_size;
+  int* smark;              // per vertex: stamp of the settle pass that found it coincident
+  int settle_blocks;       // k_settle grid (cooperative)
 };
+
+// Host-side helpers shared by the translation units of the library.
+namespace mcl {
+int alloc_mesh(int64_t V, int64_t E, mcl_mesh** out);
+void free_mesh(mcl_mesh* m);
+int fail(int code, const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what);
+int download_range(mcl_mesh* m, int64_t vb, int64_t nv, int64_t eb, int64_t ne, int64_t T, mcl_float2* pos,
+                   int32_t* v, int32_t* he, int32_t* t);
+const float2* valid_positions(const mcl_mesh* m);
+}  // namespace mcl

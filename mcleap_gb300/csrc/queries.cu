@@ -133,9 +133,16 @@ __global__ void k_closest(const float2* pos, int V, int layout, int max_ring, co
 // then written sorted ascending.
 constexpr int kFrnnLocal = 256;
 
-__global__ void k_mesh_frnn(MeshView M, float r2, int layout, int max_frnn, int* out, unsigned long long* overflow) {
+// With rcomp != nullptr the radius of vertex i is rcomp[vcomp[i]] (one radius
+// per mesh of a batch; a plain mesh has vcomp == nullptr and one radius).
+__global__ void k_mesh_frnn(MeshView M, float r2, int layout, int max_frnn, int* out, unsigned long long* overflow,
+                            const float* rcomp, const int* vcomp) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= M.V) return;
+  if (rcomp) {
+    const float rc = rcomp[vcomp ? vcomp[i] : 0];
+    r2 = __fmul_rn(rc, rc);
+  }
   int found[kFrnnLocal];
   int nf = 0;
   int top = 0;  // stack = found[top..nf): vertices whose rings are still to scan
@@ -180,6 +187,51 @@ __global__ void k_mesh_frnn(MeshView M, float r2, int layout, int max_frnn, int*
   if (layout == MCL_LAYOUT_COLUMN) out[i] = cnt;
   else out[(size_t)i * max_frnn] = cnt;
   if (over || nf > cap) atomicAdd(overflow, 1ull);
+}
+
+// Diffusion-limited aggregation contact (the reference's check_if_close_diffusion,
+// experiments/diffusion_limited_aggregation.cu:51-60, over mesh FRNN
+// neighbours): a free walker freezes when a vertex frozen before this call
+// lies within its mesh's radius.  Decisions read frozen_in only, so the result
+// does not depend on thread order.
+__global__ void k_dla_freeze(MeshView M, const unsigned char* vfix, const float* rcomp, const int* vcomp,
+                             const unsigned char* frozen_in, unsigned char* frozen_out,
+                             unsigned long long* newly) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= M.V) return;
+  unsigned char f = frozen_in[i];
+  if (!f && !vfix[i] && __ldg(M.vhe + i) >= 0) {
+    const float rc = rcomp[vcomp ? vcomp[i] : 0];
+    const float r2 = __fmul_rn(rc, rc);
+    int found[kFrnnLocal];
+    int nf = 0, top = 0;
+    const float2 pi = M.pos[i];
+    int cur = i;
+    for (int guard = 0; guard < (1 << 20) && !f; ++guard) {
+      const int h0 = __ldg(M.vhe + cur);
+      if (h0 >= 0) {
+        int h = h0, deg = 0;
+        do {
+          const int w = mv_origin(M, h ^ 1);
+          if (w != i) {
+            bool seen = false;
+            for (int k = 0; k < nf; ++k)
+              if (found[k] == w) { seen = true; break; }
+            if (!seen && sqdist(pi, M.pos[w]) <= r2) {
+              if (frozen_in[w]) { f = 1; break; }
+              if (nf < kFrnnLocal) found[nf++] = w;
+            }
+          }
+          h = mv_rot(M, h);
+          ++deg;
+        } while (h != h0 && deg < kMaxDeg);
+      }
+      if (f || top >= nf) break;
+      cur = found[top++];
+    }
+    if (f) atomicAdd(newly, 1ull);
+  }
+  frozen_out[i] = f;
 }
 
 }  // namespace
@@ -596,13 +648,52 @@ int mcl_mesh_frnn(mcl_mesh* m, float r, int layout, int max_frnn, int32_t* out, 
   unsigned long long* cnt = m->scratch;
   MeshView M{m->ev, m->en, m->vhe, m->pos[m->cur], (int)m->V, (int)m->E};
   QCK(cudaMemsetAsync(cnt, 0, 8, s));
-  k_mesh_frnn<<<(unsigned)((m->V + 127) / 128), 128, 0, s>>>(M, r * r, layout, max_frnn, out, cnt);
+  k_mesh_frnn<<<(unsigned)((m->V + 127) / 128), 128, 0, s>>>(M, r * r, layout, max_frnn, out, cnt, nullptr,
+                                                               nullptr);
   QCK(cudaGetLastError());
   if (overflow) {
     unsigned long long t = 0;
     QCK(cudaMemcpyAsync(&t, cnt, 8, cudaMemcpyDeviceToHost, s));
     QCK(cudaStreamSynchronize(s));
     *overflow = (int64_t)t;
+  }
+  return MCL_OK;
+}
+
+int mcl_batch_frnn(mcl_mesh* m, const float* r_dev, int layout, int max_frnn, int32_t* out, void* stream,
+                   int64_t* overflow) {
+  if (!m || !r_dev || !out || max_frnn < 2 || (layout != MCL_LAYOUT_COLUMN && layout != MCL_LAYOUT_ROW))
+    return qfail(MCL_ERR_INVALID_ARGUMENT, "bad args");
+  cudaStream_t s = (cudaStream_t)stream;
+  unsigned long long* cnt = m->scratch;
+  MeshView M{m->ev, m->en, m->vhe, m->pos[m->cur], (int)m->V, (int)m->E};
+  QCK(cudaMemsetAsync(cnt, 0, 8, s));
+  k_mesh_frnn<<<(unsigned)((m->V + 127) / 128), 128, 0, s>>>(M, 0.f, layout, max_frnn, out, cnt, r_dev, m->vcomp);
+  QCK(cudaGetLastError());
+  if (overflow) {
+    unsigned long long t = 0;
+    QCK(cudaMemcpyAsync(&t, cnt, 8, cudaMemcpyDeviceToHost, s));
+    QCK(cudaStreamSynchronize(s));
+    *overflow = (int64_t)t;
+  }
+  return MCL_OK;
+}
+
+int mcl_dla_freeze(mcl_mesh* m, const float* r_dev, const uint8_t* frozen_in, uint8_t* frozen_out, void* stream,
+                   int64_t* newly_frozen) {
+  if (!m || !r_dev || !frozen_in || !frozen_out || frozen_in == frozen_out)
+    return qfail(MCL_ERR_INVALID_ARGUMENT, "bad args (frozen_in and frozen_out must differ)");
+  cudaStream_t s = (cudaStream_t)stream;
+  unsigned long long* cnt = m->scratch + 1;
+  MeshView M{m->ev, m->en, m->vhe, m->pos[m->cur], (int)m->V, (int)m->E};
+  QCK(cudaMemsetAsync(cnt, 0, 8, s));
+  k_dla_freeze<<<(unsigned)((m->V + 127) / 128), 128, 0, s>>>(M, m->vfix, r_dev, m->vcomp, frozen_in, frozen_out, cnt);
+  QCK(cudaGetLastError());
+  if (newly_frozen) {
+    unsigned long long t = 0;
+    QCK(cudaMemcpyAsync(&t, cnt, 8, cudaMemcpyDeviceToHost, s));
+    QCK(cudaStreamSynchronize(s));
+    *newly_frozen = (int64_t)t;
   }
   return MCL_OK;
 }

@@ -254,3 +254,29 @@ def ring_sets_from_edges(edges, V):
     a, b = a[order], b[order]
     counts = np.bincount(a, minlength=V).astype(np.int32)
     return counts, b.astype(np.int32)
+
+
+def settle_moves(pos, d, comp=None, fixed=None):
+    """The coincident-move rule restated on the host: start with every vertex at
+    fl(pos + d) (fixed vertices at pos); while two vertices of one component sit
+    at the same point, every moving one among them gets d = 0; repeat.  Returns
+    the settled displacements."""
+    pos = np.ascontiguousarray(pos, np.float32)
+    d = np.array(d, np.float32, copy=True)
+    n = len(pos)
+    comp = np.zeros(n, np.int64) if comp is None else np.asarray(comp, np.int64)
+    fixed = np.zeros(n, bool) if fixed is None else np.asarray(fixed, bool)
+    d[fixed] = 0
+    for _ in range(n + 1):
+        cand = (pos + d).astype(np.float32)
+        cand[cand == 0] = 0  # -0 and +0 are one point
+        key = np.stack([comp, cand[:, 0].view(np.int32).astype(np.int64),
+                        cand[:, 1].view(np.int32).astype(np.int64)], 1)
+        _, inv, counts = np.unique(key, axis=0, return_inverse=True, return_counts=True)
+        shared = counts[inv.ravel()] > 1
+        moving = (d[:, 0] != 0) | (d[:, 1] != 0)
+        back = shared & moving & ~fixed
+        if not back.any():
+            return d
+        d[back] = 0
+    raise RuntimeError("settle_moves did not converge")

@@ -1,0 +1,246 @@
+"""Batches of meshes through the C ABI: one launch steps every mesh, and each
+mesh of the batch ends exactly where it ends when stepped alone (and equals the
+oracle's exact Delaunay triangulation).  Also the motion models (random walk,
+settling of coincident moves, aggregation contact) and per-mesh FRNN radii.
+"""
+import numpy as np
+import pytest
+
+from helpers import gaussian_disp, spacing, uniform_points
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+HI = float(np.nextafter(np.float32(8192), np.float32(0)))
+
+
+@pytest.fixture(scope="module")
+def M():
+    import torch
+
+    import mcleap_gb300 as M
+    from mcleap_gb300 import build as B
+
+    assert torch.cuda.is_available()
+    B.build()
+    M.lib()
+    return M
+
+
+def cuda(a):
+    import torch
+
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+SIZES = [100, 2000, 50, 3000, 800, 7]
+
+
+def make_points():
+    return [uniform_points(n, 500 + i) for i, n in enumerate(SIZES)]
+
+
+def test_batch_equals_meshes_stepped_alone(M):
+    pts = make_points()
+    batch = M.MeshBatch.from_points([p.copy() for p in pts])
+    assert batch.count == len(SIZES)
+    assert list(batch.nv) == [n + 4 for n in SIZES]
+    alone = []
+    for p in pts:
+        ht = M.HostTriangulation()
+        q = p.copy()
+        ht.addDelaunayPoints(q)
+        alone.append((ht, M.DeviceTriangulation(ht)))
+    for i, (ht, _) in enumerate(alone):
+        assert np.array_equal(batch.edges(i), ht.edges())
+    sigmas = [0.1, 0.3, 1.0, 0.2, 0.5, 0.3]
+    pos = [ht.m_pos.copy() for ht, _ in alone]
+    inverted = 0
+    for k in range(4):
+        ds = [gaussian_disp(len(pos[i]), sigmas[i] * spacing(SIZES[i]), 900 * k + i, clamp_pos=pos[i])
+              for i in range(len(SIZES))]
+        st = batch.step(cuda(np.concatenate(ds)))
+        assert st["status"] == 0, st
+        inverted += st["inverted_faces"]
+        assert not batch.validate().any()
+        for i, (ht, dt) in enumerate(alone):
+            assert dt.step(cuda(ds[i]))["status"] == 0
+            dt.transferToHost()
+            pos[i] = (pos[i] + ds[i]).astype(np.float32)
+            bpos = batch.download(i)[0]
+            assert np.array_equal(bpos, pos[i])
+            e = batch.edges(i)
+            assert np.array_equal(e, ht.edges()), (k, i)
+            assert np.array_equal(e, O.Mesh.build(pos[i][4:], exact=True).edges()), (k, i)
+    assert inverted > 0  # some mesh went through the repair path
+
+
+def test_clone_and_tuning_do_not_change_results(M):
+    pts = make_points()
+    a = M.MeshBatch.from_points([p.copy() for p in pts])
+    b = a.clone()
+    t = b.tuning()
+    assert t["max_blocks_per_sm"] >= 1
+    b.set_tuning(blocks_per_sm=1, tail_items=64)
+    assert b.tuning()["blocks_per_sm"] == 1 and b.tuning()["tail_items"] == 64
+    pos = [a.download(i)[0] for i in range(a.count)]
+    for k in range(3):
+        d = np.concatenate([gaussian_disp(len(pos[i]), 0.4 * spacing(SIZES[i]), 77 * k + i, clamp_pos=pos[i])
+                            for i in range(a.count)])
+        assert a.step(cuda(d))["status"] == 0
+        assert b.step(cuda(d))["status"] == 0
+        pos = [a.download(i)[0] for i in range(a.count)]
+    for i in range(a.count):
+        assert np.array_equal(a.edges(i), b.edges(i))
+
+
+def test_walk_is_counter_based_and_stays_in_the_box(M):
+    import torch
+
+    pts = make_points()
+    batch = M.MeshBatch.from_points([p.copy() for p in pts])
+    V = batch.V
+    sigma = cuda(np.array([5.0 * (i + 1) for i in range(batch.count)], np.float32))
+    counter = torch.zeros(1, dtype=torch.int64, device="cuda")
+    d1 = torch.zeros((V, 2), dtype=torch.float32, device="cuda")
+    d2 = torch.zeros_like(d1)
+    frozen = torch.zeros(V, dtype=torch.uint8, device="cuda")
+    frozen[4::2] = 1
+    batch.walk(sigma, counter, d1, seed=7, frozen=frozen)
+    assert counter.item() == 1
+    counter.zero_()
+    batch.walk(sigma, counter, d2, seed=7, frozen=frozen)
+    assert torch.equal(d1, d2)
+    batch.walk(sigma, counter, d2, seed=7, frozen=frozen)
+    assert not torch.equal(d1, d2)
+    d = d1.cpu().numpy()
+    fz = frozen.cpu().numpy().astype(bool)
+    pos = np.concatenate([batch.download(i)[0] for i in range(batch.count)])
+    corners = np.concatenate([np.arange(4) + v0 for v0 in batch.v0])
+    assert not d[corners].any() and not d[fz].any()
+    new = (pos + d).astype(np.float32)
+    free = np.ones(V, bool)
+    free[corners] = False
+    assert (new[free] >= 0).all() and (new[free] <= HI).all()
+    # a mesh draws the same numbers alone (seed + its index) as inside the batch
+    from mcleap_gb300.batch import build_mesh
+
+    one = M.MeshBatch(build_mesh(pts[1].copy()))
+    d_one = torch.zeros((one.V, 2), dtype=torch.float32, device="cuda")
+    c1 = torch.zeros(1, dtype=torch.int64, device="cuda")
+    one.walk(sigma[1:2], c1, d_one, seed=8, frozen=frozen[batch.v0[1]:batch.v0[1] + batch.nv[1]].contiguous())
+    assert torch.equal(d_one, d1[batch.v0[1]:batch.v0[1] + batch.nv[1]])
+    # per-mesh sigma: the spread grows with the mesh index
+    spread = [np.abs(d[batch.v0[i] + 4:batch.v0[i] + batch.nv[i]]).mean() for i in range(batch.count)
+              if batch.nv[i] > 200]
+    assert spread == sorted(spread)
+
+
+def test_settle_moves_matches_the_rule(M):
+    pts = make_points()
+    batch = M.MeshBatch.from_points([p.copy() for p in pts])
+    pos = np.concatenate([batch.download(i)[0] for i in range(batch.count)])
+    comp = np.concatenate([np.full(batch.nv[i], i) for i in range(batch.count)])
+    fixed = np.zeros(batch.V, bool)
+    for v0 in batch.v0:
+        fixed[v0:v0 + 4] = True
+    rng = np.random.default_rng(3)
+    d = (rng.standard_normal((batch.V, 2)) * 2.0).astype(np.float32)
+    d[fixed] = 0
+    b0, b1 = int(batch.v0[1]), int(batch.v0[3])  # meshes with 2000 and 3000 points
+
+    def window(v0, nv):
+        # vertices with both coordinates in [3000, 5000]: every difference of two
+        # such coordinates (and of 4000.5 / 4000.25) is exact in float32
+        # (Sterbenz), so pos + (target - pos) lands exactly on the target
+        p = pos[v0 + 4:v0 + nv]
+        return v0 + 4 + np.nonzero(((p >= 3000) & (p <= 5000)).all(1))[0]
+
+    w0, w1 = window(b0, int(batch.nv[1])), window(b1, int(batch.nv[3]))
+    assert len(w0) >= 8 and len(w1) >= 8
+    # a mover onto a vertex that stays
+    a, b = w0[0], w0[1]
+    d[a] = pos[b] - pos[a]
+    d[b] = 0
+    # two movers onto one point
+    tgt = np.float32([4000.5, 4000.25])
+    c0, c1 = w0[2], w0[3]
+    d[c0] = tgt - pos[c0]
+    d[c1] = tgt - pos[c1]
+    # a chain: x -> old(y), y -> z (z stays): y goes back, then x must too
+    x, y, z = w1[0], w1[1], w1[2]
+    d[y] = pos[z] - pos[y]
+    d[z] = 0
+    d[x] = pos[y] - pos[x]
+    # the same point in two different meshes is not a coincidence
+    e0, e1 = w0[4], w1[4]
+    d[e0] = pos[e1] - pos[e0]
+    d[e1] = 0
+    for v, t in ((a, pos[b]), (c0, tgt), (c1, tgt), (y, pos[z]), (x, pos[y]), (e0, pos[e1])):
+        assert np.array_equal((pos[v] + d[v]).astype(np.float32), t)
+    d = d.astype(np.float32)
+    want = O.settle_moves(pos, d, comp, fixed)
+    dd = cuda(d)
+    sent = batch.settle(dd)
+    got = dd.cpu().numpy()
+    assert np.array_equal(got, want)
+    assert sent == int(((want != d).any(1)).sum())
+    for v in (a, c0, c1, x, y):
+        assert not got[v].any(), v
+    assert got[e0].any()
+    # the settled move is then a valid step
+    assert batch.step(dd)["status"] == 0
+    assert not batch.validate().any()
+    # a second call on clean displacements changes nothing
+    d2 = np.zeros_like(d)
+    d2[w0[5]] = [0.5, 0.25]
+    dd2 = cuda(d2)
+    assert batch.settle(dd2) == 0
+    assert np.array_equal(dd2.cpu().numpy(), d2)
+
+
+def test_batch_frnn_per_mesh_radius(M):
+    import torch
+
+    from helpers import csr_from_table
+
+    pts = make_points()
+    batch = M.MeshBatch.from_points([p.copy() for p in pts])
+    radii = np.array([2.0 * spacing(n) for n in SIZES], np.float32)
+    F = 48
+    out = torch.zeros(batch.V * F, dtype=torch.int32, device="cuda")
+    assert batch.frnn(cuda(radii), F, out) == 0
+    c, rows = csr_from_table(out.cpu().numpy(), 1, batch.V, F)
+    for i in range(batch.count):
+        v0, nv = int(batch.v0[i]), int(batch.nv[i])
+        pos = batch.download(i)[0]
+        bc, bids = O.frnn_brute(pos, float(radii[i]))
+        assert np.array_equal(c[v0:v0 + nv], bc)
+        got = np.concatenate([rows[v0 + j] - v0 for j in range(nv)]) if nv else np.zeros(0, np.int32)
+        assert np.array_equal(got, bids), i
+
+
+def test_dla_freeze_matches_brute_force(M):
+    import torch
+
+    pts = make_points()
+    batch = M.MeshBatch.from_points([p.copy() for p in pts])
+    radii = np.array([1.0 * spacing(n) for n in SIZES], np.float32)
+    rng = np.random.default_rng(8)
+    fin = (rng.random(batch.V) < 0.2).astype(np.uint8)
+    for v0 in batch.v0:
+        fin[v0:v0 + 4] = 0
+    fi, fo = cuda(fin), torch.zeros(batch.V, dtype=torch.uint8, device="cuda")
+    newly = batch.dla_freeze(cuda(radii), fi, fo)
+    got = fo.cpu().numpy()
+    want = fin.copy()
+    for i in range(batch.count):
+        v0, nv = int(batch.v0[i]), int(batch.nv[i])
+        pos = batch.download(i)[0]
+        bc, bids = O.frnn_brute(pos, float(radii[i]))
+        offs = np.concatenate([[0], np.cumsum(bc)])
+        for j in range(4, nv):
+            if not fin[v0 + j] and fin[v0 + bids[offs[j]:offs[j + 1]]].any():
+                want[v0 + j] = 1
+    assert np.array_equal(got, want)
+    assert newly == int((want != fin).sum())
