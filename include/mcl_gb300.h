@@ -326,6 +326,15 @@ int mcl_debug_state(mcl_mesh* m, int32_t* out68);
  * [1] after the classification barrier, [2 + r] end of flip round r (r < 40),
  * [47] end; unused slots keep older values. */
 int mcl_debug_timeline(mcl_mesh* m, int64_t* out48);
+/* All counters of the last launch (engine order: flips, flip rounds, inverted
+ * faces, reverted, removed, removal flips, insertion rounds, incircle tests and
+ * stages, orientation stages, perturbation decisions, expansion overflows,
+ * fixpoint passes, removal
+ * rounds); returns how many exist. */
+int mcl_debug_counters(mcl_mesh* m, int64_t* out, int n);
+/* %globaltimer marks of the reinsertion rounds r < 16 of the last launch:
+ * [4r] located, [4r+1] winners known, [4r+2] split, [4r+3] flips done. */
+int mcl_debug_insert_timeline(mcl_mesh* m, int64_t* out64);
 
 /* The device predicate ladder evaluated on the host CPU (same source as the
  * device code), for testing without a GPU.  kind 0 = orient2d on n records of

@@ -37,7 +37,8 @@ EXPORTS = [
     "mcl_batch_create", "mcl_batch_count", "mcl_batch_range", "mcl_batch_vertex_mesh", "mcl_batch_download_aos",
     "mcl_batch_frnn", "mcl_mesh_clone", "mcl_mesh_set_tuning", "mcl_mesh_get_tuning", "mcl_walk",
     "mcl_settle_moves", "mcl_dla_freeze",
-    "mcl_grid_mean_occupancy", "mcl_debug_predicates_host", "mcl_debug_predicates_device", "mcl_mesh_validate", "mcl_debug_state", "mcl_debug_timeline", "mcl_grid_frnn_noalloc",
+    "mcl_grid_mean_occupancy", "mcl_debug_predicates_host", "mcl_debug_predicates_device", "mcl_mesh_validate", "mcl_debug_state", "mcl_debug_timeline", "mcl_grid_frnn_noalloc", "mcl_debug_counters",
+    "mcl_debug_insert_timeline",
 ]
 
 
@@ -110,6 +111,8 @@ def lib():
             "mcl_mesh_validate": ([vp, vp], i32),
             "mcl_debug_state": ([vp, vp], i32),
             "mcl_debug_timeline": ([vp, vp], i32),
+            "mcl_debug_counters": ([vp, vp, i32], i32),
+            "mcl_debug_insert_timeline": ([vp, vp], i32),
             "mcl_grid_frnn_noalloc": ([vp, i64, f32, f32, f32, f32, i32, i32, i32, f32, i32, vp, vp, vp, vp, vp,
                                        C.POINTER(i64)], i32),
             "mcl_debug_predicates_device": ([i32, vp, vp, i64, vp, vp, vp], i32),

@@ -261,6 +261,14 @@ __device__ __forceinline__ void timeline(const KParams& P, int slot) {
   }
 }
 
+__device__ __forceinline__ void timeline_insert(const KParams& P, int round, int k) {
+  if (blockIdx.x == 0 && threadIdx.x == 0 && round < 16) {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    P.st->ts_insert[4 * round + k] = t;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Lawson flip rounds starting from work-list `src`.  A round is two phases:
 //   A  every queued edge that is still non-Delaunay claims its two faces with
@@ -406,6 +414,29 @@ __device__ void mark_vertex(const KParams& P, int v, int& fresh, unsigned fs) {
   if (!marked(P, v, fs) && (unsigned)atomicExch(P.vmark + v, (int)fs) != fs) ++fresh;
 }
 
+// A non-positive face sends back one vertex per pass: the unmarked free vertex
+// that moved farthest (ties: smallest id).  A face whose vertices are all back
+// at their old positions is positive (the mesh was valid there), so every pass
+// that still sees a bad face marks a vertex and the fixpoint ends.  Sending
+// back fewer vertices means fewer removals and reinsertions; the result does
+// not depend on the choice (every sent-back vertex is reinserted at its
+// target).
+__device__ void mark_face(const KParams& P, int a, int b, int c, int& fresh, unsigned fs) {
+  const int t[3] = {a, b, c};
+  int pick = -1;
+  float best = -1.f;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const int v = t[k];
+    if (P.vfix[v] || marked(P, v, fs)) continue;
+    const float2 pn = ldpos(P, v), po = P.pos_old[v];
+    const float dx = __fsub_rn(pn.x, po.x), dy = __fsub_rn(pn.y, po.y);
+    const float m2 = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
+    if (m2 > best || (m2 == best && v < pick)) { best = m2; pick = v; }
+  }
+  if (pick >= 0) mark_vertex(P, pick, fresh, fs);
+}
+
 __device__ bool phase_fixpoint(cg::grid_group& g, const KParams& P, LocalCounters& lc, unsigned fs) {
   const int stride = gridDim.x * blockDim.x;
   const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -428,11 +459,11 @@ __device__ bool phase_fixpoint(cg::grid_group& g, const KParams& P, LocalCounter
       const float2 a = qpos(P, q.x, fs), b = qpos(P, q.y, fs);
       if (q.z >= 0 && orient_v(P, a, b, qpos(P, q.z, fs), lc) <= 0) {
         ++bad;
-        mark_vertex(P, q.x, fresh, fs); mark_vertex(P, q.y, fresh, fs); mark_vertex(P, q.z, fresh, fs);
+        mark_face(P, q.x, q.y, q.z, fresh, fs);
       }
       if (q.w >= 0 && orient_v(P, b, a, qpos(P, q.w, fs), lc) <= 0) {
         ++bad;
-        mark_vertex(P, q.x, fresh, fs); mark_vertex(P, q.y, fresh, fs); mark_vertex(P, q.w, fresh, fs);
+        mark_face(P, q.y, q.x, q.w, fresh, fs);
       }
     }
     if (fresh) atomicAdd(&P.st->fix_new[slot], fresh);
@@ -530,7 +561,12 @@ __device__ int remove_vertex_ears(const KParams& P, int v, LocalCounters& lc) {
     __stcg(P.ev + e, make_int4(-1, -1, -1, -1));
     __stcg(P.en + e, make_int4(-1, -1, -1, -1));
   }
-  __stcg(P.vaux + v, w[0]);
+  // the neighbour that later point location starts from: not a bounding
+  // corner (a corner's half-edges run along the hull, far from v)
+  int anchor = w[0];
+  for (int i = 0; i < k; ++i)
+    if (!P.vfix[w[i]]) { anchor = w[i]; break; }
+  __stcg(P.vaux + v, anchor);
   __stcg(P.vhe + v, -1);
   return MCL_OK;
 }
@@ -604,7 +640,8 @@ __device__ int remove_vertex(const KParams& P, int v, LocalCounters& lc, int& fl
     __stcg(P.en + es[k], make_int4(-1, -1, -1, -1));
   }
   P.vhint[v] = lxy;
-  P.vaux[v] = x;
+  // the neighbour that later point location starts from: not a bounding corner
+  P.vaux[v] = !P.vfix[x] ? x : (!P.vfix[y] ? y : z);
   __stcg(P.vhe + v, -1);
   return MCL_OK;
 }
@@ -704,10 +741,21 @@ __device__ int locate(const KParams& P, float2 p, int h, int* on, LocalCounters&
     int s[3] = {1, 1, 1};
     int cross = -1;
     const int start = it % 3;
-    for (int k = 0; k < 3 && cross < 0; ++k) {
+    // Every edge with p on its far side is a valid step; an edge with a
+    // bounding corner is taken only when no other is (stepping through a
+    // corner's fan of long hull triangles can take hundreds of steps).
+    bool corner_cross = false;
+    for (int k = 0; k < 3; ++k) {
       const int i = (start + k) % 3;
       s[i] = orient_v(P, q[i], q[(i + 1) % 3], p, lc);
-      if (s[i] < 0) cross = i;
+      if (s[i] < 0) {
+        const bool corner = P.vfix[o[i]] || P.vfix[o[(i + 1) % 3]];
+        if (cross < 0 || (corner_cross && !corner)) {
+          cross = i;
+          corner_cross = corner;
+        }
+        if (!corner) break;
+      }
     }
     if (cross >= 0) {
       const int t = hs[cross] ^ 1;
@@ -771,14 +819,38 @@ __device__ void split24(const KParams& P, int v, int g, const int* f) {
   if (ld_i(P.vhe + b) == h1) __stcg(P.vhe + b, n0);
 }
 
+// Start of the point location of a pending vertex: the hole half-edge recorded
+// at its removal when that edge is still live, else the neighbour recorded at
+// removal (vaux) and, when that one was removed too, its own recorded
+// neighbour, and so on: each hop stays about one spacing from the old
+// position, so the walk stays short instead of starting at the bounding square.
+__device__ __forceinline__ bool face_has_corner(const KParams& P, int h) {
+  const int a = he_origin(P, h), b = he_origin(P, h ^ 1), c = he_apex(P, h);
+  return (a >= 0 && P.vfix[a]) || (b >= 0 && P.vfix[b]) || (c >= 0 && P.vfix[c]);
+}
+
 __device__ int insert_start(const KParams& P, int v) {
   int h = __ldcg(P.vhint + v);
-  if (h >= 0 && h < 2 * P.E && he_origin(P, h) >= 0 && he_apex(P, h) >= 0) return h;
-  const int x = __ldcg(P.vaux + v);
-  if (x >= 0 && x < P.V) {
-    h = ld_i(P.vhe + x);
-    if (h >= 0 && h < 2 * P.E) return h;
+  const bool hint_ok = h >= 0 && h < 2 * P.E && he_origin(P, h) >= 0 && he_apex(P, h) >= 0;
+  // a start on a bounding corner's fan of long hull triangles makes the walk
+  // step along the hull one triangle at a time: prefer a face of the anchor
+  // neighbour that has no corner
+  if (hint_ok && !face_has_corner(P, h)) return h;
+  int x = __ldcg(P.vaux + v);
+  for (int hop = 0; hop < 64 && x >= 0 && x < P.V; ++hop) {
+    const int h0 = ld_i(P.vhe + x);
+    if (h0 >= 0 && h0 < 2 * P.E) {
+      int g = h0;
+      for (int k = 0; k < 64; ++k) {
+        if (he_apex(P, g) >= 0 && !face_has_corner(P, g)) return g;
+        g = he_next(P, g ^ 1);  // next outgoing half-edge of x
+        if (g < 0 || g >= 2 * P.E || g == h0) break;
+      }
+      return hint_ok ? h : h0;
+    }
+    x = __ldcg(P.vaux + x);
   }
+  if (hint_ok) return h;
   // half-edge 0 of the vertex's mesh is never freed: a side of its bounding square
   return P.vroot ? __ldg(P.vroot + v) : 0;
 }
@@ -826,6 +898,7 @@ __device__ bool phase_insert(cg::grid_group& g, const KParams& P, unsigned& stam
       }
     }
     g.sync();
+    timeline_insert(P, round, 0);
     for (int i = gtid; i < n; i += stride) {
       const int v = ld_i(in + i);
       const int fl = __ldcg(P.vlocf + v);
@@ -837,6 +910,7 @@ __device__ bool phase_insert(cg::grid_group& g, const KParams& P, unsigned& stam
       if (win) P.vlocf[v] = fl | 1;
     }
     g.sync();
+    timeline_insert(P, round, 1);
     int inserted = 0;
     for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
       const int i = base + threadIdx.x;
@@ -885,8 +959,10 @@ __device__ bool phase_insert(cg::grid_group& g, const KParams& P, unsigned& stam
     }
     (void)inserted;
     g.sync();
+    timeline_insert(P, round, 2);
     phase_lawson<false>(g, P, 0, stamp, lc, 0);
     g.sync();
+    timeline_insert(P, round, 3);
     src = dst;
   }
 }
@@ -929,6 +1005,7 @@ __device__ __noinline__ unsigned repair_step(cg::grid_group g, const KParams P, 
   // (1) revert until valid
   bool ok = phase_fixpoint(g, Q, lc, fs);
   g.sync();
+  timeline(P, 43);
   if (ok) {
     // removal list: reverted vertices that actually moved
     const int stride = gridDim.x * blockDim.x;
@@ -954,6 +1031,7 @@ __device__ __noinline__ unsigned repair_step(cg::grid_group g, const KParams P, 
     // (2) remove them
     ok = phase_remove(g, Q, stamp, lc);
     g.sync();
+    timeline(P, 44);
     // (3) Lawson over every edge of the reduced mesh
     if (gtid == 0) { P.st->wl_count[0] = 0; P.st->wl_count[1] = 0; P.st->inverted = 0; P.st->hard_count = 0; }
     g.sync();
@@ -964,6 +1042,7 @@ __device__ __noinline__ unsigned repair_step(cg::grid_group g, const KParams P, 
     phase_classify_hard<false>(g, Q, q1, sc1, lc);
     phase_lawson<false>(g, Q, 0, stamp, lc, sc1);
     g.sync();
+    timeline(P, 45);
     // (4) reinsert at the new positions
     if (gtid == 0) { P.st->vl_count[0] = 0; P.st->vl_count[1] = 0; }
     g.sync();
@@ -979,6 +1058,7 @@ __device__ __noinline__ unsigned repair_step(cg::grid_group g, const KParams P, 
     }
     g.sync();
     if (ok) phase_insert(g, Q, stamp, lc);
+    timeline(P, 46);
   }
   flush_counters(P, lc);
   return stamp;
@@ -1465,6 +1545,22 @@ int mcl_debug_timeline(mcl_mesh* m, int64_t* out48) {
   CK(cudaMemcpy(m->st_host, m->st, sizeof(DevState), cudaMemcpyDeviceToHost));
   for (int i = 0; i < kTimeline; ++i) out48[i] = (int64_t)m->st_host->ts[i];
   return MCL_OK;
+}
+
+int mcl_debug_insert_timeline(mcl_mesh* m, int64_t* out64) {
+  if (!m || !out64) return fail(MCL_ERR_INVALID_ARGUMENT, "null argument");
+  CK(cudaDeviceSynchronize());
+  CK(cudaMemcpy(m->st_host, m->st, sizeof(DevState), cudaMemcpyDeviceToHost));
+  for (int i = 0; i < 64; ++i) out64[i] = (int64_t)m->st_host->ts_insert[i];
+  return MCL_OK;
+}
+
+int mcl_debug_counters(mcl_mesh* m, int64_t* out, int n) {
+  if (!m || !out || n < 1) return fail(MCL_ERR_INVALID_ARGUMENT, "bad args");
+  CK(cudaDeviceSynchronize());
+  CK(cudaMemcpy(m->st_host, m->st, sizeof(DevState), cudaMemcpyDeviceToHost));
+  for (int i = 0; i < n && i < C_COUNT; ++i) out[i] = (int64_t)m->st_host->last[i];
+  return C_COUNT;
 }
 
 int mcl_debug_state(mcl_mesh* m, int32_t* out68) {
