@@ -401,7 +401,7 @@ def run_batched(args, rank, world, dist):
     F = 48
     d = torch.zeros((V, 2), dtype=torch.float32, device=dev)
     out = torch.empty(V * F, dtype=torch.int32, device=dev)
-    counter = torch.zeros(1, dtype=torch.int64, device=dev)
+    counter = torch.zeros(nm, dtype=torch.int64, device=dev)
     stream = torch.cuda.Stream()
     sp = stream.cuda_stream
     lib = L.lib()
@@ -420,7 +420,7 @@ def run_batched(args, rank, world, dist):
             with_events[2].record(s)
 
     # autotune the launch shape on clones (walk + settle + step per candidate)
-    tune_ctr = torch.zeros(1, dtype=torch.int64, device=dev)
+    tune_ctr = torch.zeros(nm, dtype=torch.int64, device=dev)
 
     def tune_step(m, k, s):
         with torch.cuda.stream(s):
@@ -519,7 +519,7 @@ def run_batched(args, rank, world, dist):
 
     # the same steps through the batch (verify clone, fresh counter) must
     # leave every mesh exactly as the plain form did
-    vctr = torch.zeros(1, dtype=torch.int64, device=dev)
+    vctr = torch.zeros(nm, dtype=torch.int64, device=dev)
     vd = torch.zeros_like(d)
     for k in range(KP):
         pipeline_step(verify, vctr, vd, out, stream)

@@ -274,6 +274,21 @@ int mcl_batch_download_aos(mcl_mesh* m, int64_t i, mcl_float2* pos_host, int32_t
  * r_dev[i] for the vertices of mesh i (a plain mesh reads r_dev[0]). */
 int mcl_batch_frnn(mcl_mesh* m, const float* r_dev, int layout, int max_frnn, int32_t* out_dev, void* stream,
                    int64_t* overflow_host);
+/* Mesh FRNN (getFRNN semantics) for a list of query vertices: row q of out_dev
+ * (n rows, COLUMN or ROW layout with the count slot) holds the neighbours of
+ * verts_dev[q] within r_dev[its mesh], ascending. */
+int mcl_batch_frnn_list(mcl_mesh* m, const float* r_dev, const int32_t* verts_dev, int64_t n, int layout,
+                        int max_frnn, int32_t* out_dev, void* stream, int64_t* overflow_host);
+/* oneRing (include/Device_Triangulation.h:499-517) for a list of query vertices. */
+int mcl_one_ring_list(mcl_mesh* m, const int32_t* verts_dev, int64_t n, int layout, int max_ring, int32_t* out_dev,
+                      void* stream, int64_t* truncated_host);
+/* Restrict the following mcl_step, mcl_untangle, mcl_delaunay_restore,
+ * mcl_walk, mcl_settle_moves and mcl_dla_freeze calls to the listed meshes of
+ * a batch (n == 0: every mesh again).  The other meshes are left exactly as
+ * they are, and a launch costs only what the listed meshes hold.
+ * Synchronises `stream` (the list is staged through one pinned buffer);
+ * mcl_move and mcl_integrate refuse to run while a subset is active. */
+int mcl_batch_set_active(mcl_mesh* m, const int32_t* meshes_host, int64_t n, void* stream);
 /* A copy of a mesh or batch at its validated state (for snapshots and tuning). */
 int mcl_mesh_clone(const mcl_mesh* src, mcl_mesh** out);
 
@@ -288,12 +303,13 @@ int mcl_mesh_get_tuning(const mcl_mesh* m, int* blocks_per_sm, int* tail_items, 
  * aggregation experiment (experiments/diffusion_limited_aggregation.cu:51-60,
  * :263-268): d_dev[v] = clamp(pos + sigma * N(0, I), lo, hi) - pos with
  * sigma = sigma_dev[mesh of v], zero for the bounding corners and for vertices
- * with frozen_dev[v] != 0 (frozen_dev may be NULL).  The normal draws of
- * vertex v of mesh c are a function of (seed + c, *counter_dev, the id of v
- * within mesh c) only (a counter-based generator), so a mesh draws the same
- * numbers alone (with seed + c) as inside a batch; *counter_dev is
- * incremented on the device after the draw, so a captured CUDA graph replays
- * new steps. */
+ * with frozen_dev[v] != 0 (frozen_dev may be NULL).  counter_dev holds one
+ * step counter per mesh (uint64[meshes]).  The normal draws of vertex v of
+ * mesh c are a function of (seed + c, counter_dev[c], the id of v within
+ * mesh c) only (a counter-based generator), so a mesh draws the same numbers
+ * alone (with seed + c) as inside a batch, whatever else runs; the counters
+ * of the walked meshes are incremented on the device after the draw, so a
+ * captured CUDA graph replays new steps. */
 int mcl_walk(mcl_mesh* m, const float* sigma_dev, const uint8_t* frozen_dev, uint64_t seed, uint64_t* counter_dev,
              float lo, float hi, mcl_float2* d_dev, void* stream);
 /* Refuse moves that would put two vertices of one mesh at the same point: while
@@ -303,13 +319,12 @@ int mcl_walk(mcl_mesh* m, const float* sigma_dev, const uint8_t* frozen_dev, uin
  * points make its triangulation undefined).  *sent_back_host (may be NULL: no
  * synchronisation) = displacements zeroed. */
 int mcl_settle_moves(mcl_mesh* m, mcl_float2* d_dev, void* stream, int64_t* sent_back_host);
-/* check_if_close_diffusion (experiments/diffusion_limited_aggregation.cu:51-60):
- * frozen_out[v] = frozen_in[v], or 1 when a vertex with frozen_in != 0 lies
- * within r_dev[mesh of v] of a free vertex v (fl(dx*dx + dy*dy) <= fl(r*r)).
- * Reads only frozen_in, so the result does not depend on thread order.
- * *newly_frozen_host may be NULL. */
-int mcl_dla_freeze(mcl_mesh* m, const float* r_dev, const uint8_t* frozen_in, uint8_t* frozen_out, void* stream,
-                   int64_t* newly_frozen_host);
+/* check_if_close_diffusion (experiments/diffusion_limited_aggregation.cu:51-60),
+ * in place: a free vertex v becomes frozen when a vertex that was frozen before
+ * the call lies within r_dev[mesh of v] (fl(dx*dx + dy*dy) <= fl(r*r)).  The
+ * decisions read the state before the call only, so the result does not
+ * depend on thread order.  *newly_frozen_host may be NULL. */
+int mcl_dla_freeze(mcl_mesh* m, const float* r_dev, uint8_t* frozen_dev, void* stream, int64_t* newly_frozen_host);
 
 /* ---- diagnostics ------------------------------------------------------------ */
 /* Structural invariants of the device mesh; counts8[k] = violations of kind k:

@@ -141,7 +141,8 @@ class MeshBatch:
 
     def walk(self, sigma, counter, d, seed=0, frozen=None, lo=0.0, hi=float(np.nextafter(np.float32(8192), 0)),
              stream=None):
-        """Gaussian random-walk displacements into ``d`` (sigma per mesh, device)."""
+        """Gaussian random-walk displacements into ``d`` (sigma and step counter
+        per mesh, device arrays)."""
         L.check(L.lib().mcl_walk(self.handle, L.ptr(sigma), L.ptr(frozen), int(seed), L.ptr(counter), float(lo),
                                  float(hi), L.ptr(d), _stream_ptr(stream)))
 
@@ -152,11 +153,34 @@ class MeshBatch:
         L.check(L.lib().mcl_settle_moves(self.handle, L.ptr(d), _stream_ptr(stream), C.byref(n) if sync else None))
         return n.value if sync else None
 
-    def dla_freeze(self, r, frozen_in, frozen_out, stream=None, sync=True):
+    def dla_freeze(self, r, frozen, stream=None, sync=True):
+        """Aggregation contact in place on ``frozen`` (uint8 per vertex)."""
         n = C.c_int64()
-        L.check(L.lib().mcl_dla_freeze(self.handle, L.ptr(r), L.ptr(frozen_in), L.ptr(frozen_out),
-                                       _stream_ptr(stream), C.byref(n) if sync else None))
+        L.check(L.lib().mcl_dla_freeze(self.handle, L.ptr(r), L.ptr(frozen), _stream_ptr(stream),
+                                       C.byref(n) if sync else None))
         return n.value if sync else None
+
+    def set_active(self, meshes=None, stream=None):
+        """Restrict the following steps and motion calls to these mesh indices
+        (None or empty: all meshes)."""
+        if meshes is None or len(meshes) == 0:
+            L.check(L.lib().mcl_batch_set_active(self.handle, None, 0, _stream_ptr(stream)))
+            return
+        a = np.ascontiguousarray(meshes, np.int32)
+        L.check(L.lib().mcl_batch_set_active(self.handle, L.ptr(a), len(a), _stream_ptr(stream)))
+
+    def frnn_list(self, r, verts, max_frnn, out, layout=L.LAYOUT_ROW, stream=None, sync=True):
+        ov = C.c_int64()
+        L.check(L.lib().mcl_batch_frnn_list(self.handle, L.ptr(r), L.ptr(verts), int(verts.numel()), layout,
+                                            int(max_frnn), L.ptr(out), _stream_ptr(stream),
+                                            C.byref(ov) if sync else None))
+        return ov.value if sync else None
+
+    def one_ring_list(self, verts, max_ring, out, layout=L.LAYOUT_ROW, stream=None, sync=True):
+        tr = C.c_int64()
+        L.check(L.lib().mcl_one_ring_list(self.handle, L.ptr(verts), int(verts.numel()), layout, int(max_ring),
+                                          L.ptr(out), _stream_ptr(stream), C.byref(tr) if sync else None))
+        return tr.value if sync else None
 
     # -- queries ----------------------------------------------------------------------
     def frnn(self, r, max_frnn, out, layout=L.LAYOUT_ROW, stream=None, sync=True):

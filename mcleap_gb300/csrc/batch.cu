@@ -92,17 +92,18 @@ __device__ __forceinline__ float2 normal2(unsigned long long seed, unsigned long
 // a displacement whose rounded sum would leave [lo, hi] is dropped.
 // The draws of vertex v of mesh c are keyed by (seed + c, local id of v), so a
 // mesh draws the same numbers alone (with seed + c) and inside a batch.
-__global__ void k_walk(int V, const float2* __restrict__ pos, const unsigned char* __restrict__ vfix,
+__global__ void k_walk(ActV A, const float2* __restrict__ pos, const unsigned char* __restrict__ vfix,
                        const int* __restrict__ vcomp, const int* __restrict__ cbase, const float* __restrict__ sigma,
                        const unsigned char* __restrict__ frozen, unsigned long long seed,
                        const unsigned long long* __restrict__ counter, float lo, float hi, float2* __restrict__ d) {
-  const int v = blockIdx.x * blockDim.x + threadIdx.x;
-  if (v >= V) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= A.V_it) return;
+  const int v = A.at(i);
   float2 out = make_float2(0.f, 0.f);
   if (!vfix[v] && !(frozen && frozen[v])) {
     const int c = vcomp ? vcomp[v] : 0;
     const float sg = sigma[c];
-    const float2 z = normal2(seed + (unsigned long long)c, *counter, cbase ? v - cbase[c] : v);
+    const float2 z = normal2(seed + (unsigned long long)c, counter[c], cbase ? v - cbase[c] : v);
     const float2 p = pos[v];
     const float tx = fminf(fmaxf(__fadd_rn(p.x, __fmul_rn(sg, z.x)), lo), hi);
     const float ty = fminf(fmaxf(__fadd_rn(p.y, __fmul_rn(sg, z.y)), lo), hi);
@@ -114,7 +115,11 @@ __global__ void k_walk(int V, const float2* __restrict__ pos, const unsigned cha
   d[v] = out;
 }
 
-__global__ void k_advance(unsigned long long* counter) { *counter += 1; }
+// counter[c] += 1 for every active mesh c (every mesh when n == 0)
+__global__ void k_advance(unsigned long long* counter, int n, const int* act, int ncomp) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n ? i < n : i < ncomp) counter[n ? act[i] : i] += 1;
+}
 
 // ---------------------------------------------------------------------------
 // Settling coincident moves.
@@ -139,7 +144,7 @@ __device__ __forceinline__ float2 cand_pos(const float2* pos, const float2* d, c
 }
 
 struct SettleArgs {
-  int V;
+  ActV A;
   const float2* pos;
   float2* d;
   const unsigned char* vfix;
@@ -164,7 +169,8 @@ __global__ void k_settle(SettleArgs A) {
     const unsigned stamp = base + 1 + (unsigned)pass;
     const int slot = 1 + pass % 3;
     if (gtid == 0) words[1 + (pass + 1) % 3] = 0;
-    for (int v = gtid; v < A.V; v += stride) {
+    for (int vi = gtid; vi < A.A.V_it; vi += stride) {
+      const int v = A.A.at(vi);
       const float2 p = cand_pos(A.pos, A.d, A.vfix, v);
       const int comp = A.vcomp ? A.vcomp[v] : 0;
       const unsigned long long key = ((unsigned long long)fbits(p.x) << 32) | fbits(p.y);
@@ -193,7 +199,8 @@ __global__ void k_settle(SettleArgs A) {
     }
     g.sync();
     int sent = 0;
-    for (int v = gtid; v < A.V; v += stride) {
+    for (int vi = gtid; vi < A.A.V_it; vi += stride) {
+      const int v = A.A.at(vi);
       if ((unsigned)__ldcg(A.smark + v) != stamp || A.vfix[v]) continue;
       const float2 q = A.d[v];
       if (q.x != 0.f || q.y != 0.f) {
@@ -280,6 +287,11 @@ int mcl_batch_create(mcl_mesh* const* meshes, int64_t count, mcl_mesh** out) {
   if (cudaMemcpy(b->cbase, base.data(), 4 * count, cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaDeviceSynchronize() != cudaSuccess)
     return bail(fail(MCL_ERR_CUDA, "mcl_batch_create: sync"));
+  b->dirty = new unsigned char[(size_t)count]();
+  b->act_list = new int[(size_t)count];
+  if (cudaMalloc((void**)&b->act_dev, 4 * (5 * count + 2)) != cudaSuccess ||
+      cudaMallocHost((void**)&b->act_host, 4 * (5 * count + 2)) != cudaSuccess)
+    return bail(fail(MCL_ERR_OUT_OF_MEMORY, "mcl_batch_create: active tables"));
   b->cur = 0;
   b->valid_cur = true;
   *out = b;
@@ -347,7 +359,59 @@ int mcl_mesh_clone(const mcl_mesh* src, mcl_mesh** out) {
   }
   m->tail_items = src->tail_items;
   m->coop_blocks = src->coop_blocks;
+  if (src->dirty) {
+    const int64_t nc = src->ncomp;
+    m->dirty = new unsigned char[(size_t)nc]();
+    m->act_list = new int[(size_t)nc];
+    if (cudaMalloc((void**)&m->act_dev, 4 * (5 * nc + 2)) != cudaSuccess ||
+        cudaMallocHost((void**)&m->act_host, 4 * (5 * nc + 2)) != cudaSuccess) {
+      free_mesh(m);
+      return fail(MCL_ERR_OUT_OF_MEMORY, "mcl_mesh_clone: active tables");
+    }
+  }
   *out = m;
+  return MCL_OK;
+}
+
+int mcl_batch_set_active(mcl_mesh* m, const int32_t* meshes_host, int64_t n, void* stream) {
+  if (!m || n < 0 || (n > 0 && !meshes_host)) return fail(MCL_ERR_INVALID_ARGUMENT, "bad args");
+  if (n == 0) {
+    m->nact = 0;
+    return MCL_OK;
+  }
+  if (!m->dirty) return fail(MCL_ERR_INVALID_ARGUMENT, "mcl_batch_set_active: not a batch");
+  if (n > m->ncomp) return fail(MCL_ERR_INVALID_ARGUMENT, "mcl_batch_set_active: more meshes than the batch has");
+  cudaStream_t s = (cudaStream_t)stream;
+  std::vector<unsigned char> seen((size_t)m->ncomp, 0);
+  // the staging buffer may still feed the previous call's copy
+  BCK(cudaStreamSynchronize(s));
+  const int64_t nc = m->ncomp;
+  int* epre = m->act_host;
+  int* e0 = epre + nc + 1;
+  int* vpre = e0 + nc;
+  int* v0 = vpre + nc + 1;
+  int* ids = v0 + nc;
+  int64_t E = 0, V = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    const int c = meshes_host[i];
+    if (c < 0 || c >= nc || seen[(size_t)c])
+      return fail(MCL_ERR_INVALID_ARGUMENT, "mcl_batch_set_active: mesh index out of range or repeated");
+    seen[(size_t)c] = 1;
+    m->act_list[i] = c;
+    ids[i] = c;
+    epre[i] = (int)E;
+    e0[i] = (int)m->comp_host[4 * c + 2];
+    vpre[i] = (int)V;
+    v0[i] = (int)m->comp_host[4 * c];
+    E += m->comp_host[4 * c + 3];
+    V += m->comp_host[4 * c + 1];
+  }
+  epre[n] = (int)E;
+  vpre[n] = (int)V;
+  BCK(cudaMemcpyAsync(m->act_dev, m->act_host, 4 * (5 * nc + 2), cudaMemcpyHostToDevice, s));
+  m->nact = (int)n;
+  m->act_E = (int)E;
+  m->act_V = (int)V;
   return MCL_OK;
 }
 
@@ -374,10 +438,16 @@ int mcl_walk(mcl_mesh* m, const float* sigma_dev, const uint8_t* frozen_dev, uin
   if (!m || !sigma_dev || !counter_dev || !d_dev || !(lo <= hi)) return fail(MCL_ERR_INVALID_ARGUMENT, "bad args");
   cudaStream_t s = (cudaStream_t)stream;
   const int V = (int)m->V;
-  k_walk<<<(V + 255) / 256, 256, 0, s>>>(V, m->pos[m->cur], m->vfix, m->vcomp, m->cbase, sigma_dev, frozen_dev, seed,
-                                         reinterpret_cast<const unsigned long long*>(counter_dev), lo, hi,
-                                         reinterpret_cast<float2*>(d_dev));
-  k_advance<<<1, 1, 0, s>>>(reinterpret_cast<unsigned long long*>(counter_dev));
+  const ActV A = act_of(m);
+  (void)V;
+  if (A.V_it > 0)
+    k_walk<<<(A.V_it + 255) / 256, 256, 0, s>>>(A, m->pos[m->cur], m->vfix, m->vcomp, m->cbase, sigma_dev, frozen_dev,
+                                                seed, reinterpret_cast<const unsigned long long*>(counter_dev), lo, hi,
+                                                reinterpret_cast<float2*>(d_dev));
+  const int na = m->nact ? m->nact : (int)m->ncomp;
+  k_advance<<<(na + 255) / 256, 256, 0, s>>>(reinterpret_cast<unsigned long long*>(counter_dev), m->nact,
+                                             m->nact ? m->act_dev + 4 * m->ncomp + 2 : nullptr,
+                                             (int)m->ncomp);
   BCK(cudaGetLastError());
   return MCL_OK;
 }
@@ -389,7 +459,7 @@ int mcl_settle_moves(mcl_mesh* m, mcl_float2* d_dev, void* stream, int64_t* sent
   if (rc != MCL_OK) return rc;
   cudaStream_t s = (cudaStream_t)stream;
   SettleArgs A;
-  A.V = (int)m->V;
+  A.A = act_of(m);
   A.pos = m->pos[m->cur];
   A.d = reinterpret_cast<float2*>(d_dev);
   A.vfix = m->vfix;

@@ -161,19 +161,23 @@ __device__ void phase_classify(cg::grid_group& g, const KParams& P, unsigned qst
                                LocalCounters& lc) {
   const int stride = gridDim.x * blockDim.x;
   if (P.move_mode != MOVE_NONE) {
-    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < P.V; v += stride) __stcg(P.pos + v, moved_pos(P, v));
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.V_it; i += stride) {
+      const int v = vert_at(P, i);
+      __stcg(P.pos + v, moved_pos(P, v));
+    }
     g.sync();
   }
   int bad = 0;
   unsigned ninc = 0;
   int def0 = -1, def1 = -1;  // edges deferred to the full ladder after the loop
-  for (int base = blockIdx.x * blockDim.x; base < P.E; base += stride) {
-    const int e = base + threadIdx.x;
+  for (int base = blockIdx.x * blockDim.x; base < P.E_it; base += stride) {
+    const int ei = base + threadIdx.x;
     int mine[1];
     int k = 0;
     int hard[1];
     int kh = 0;
-    if (e < P.E) {
+    if (ei < P.E_it) {
+      const int e = edge_at(P, ei);
       const int4 q = ld_ev(P, e);
       if (q.x >= 0 && (bad_v(P, q.x) || bad_v(P, q.y) || q.z >= P.V || q.w >= P.V)) {
         flag_error(P, MCL_ERR_DEGENERATE_INPUT);
@@ -449,7 +453,8 @@ __device__ bool phase_fixpoint(cg::grid_group& g, const KParams& P, LocalCounter
       P.st->c[C_FIX_PASSES] += 1;
     }
     int fresh = 0, bad = 0;
-    for (int e = gtid; e < P.E; e += stride) {
+    for (int ei = gtid; ei < P.E_it; ei += stride) {
+      const int e = edge_at(P, ei);
       const int4 q = ld_ev(P, e);
       if (q.x < 0) continue;
       if (bad_v(P, q.x) || bad_v(P, q.y) || q.z >= P.V || q.w >= P.V) {
@@ -1011,11 +1016,12 @@ __device__ __noinline__ unsigned repair_step(cg::grid_group g, const KParams P, 
     const int stride = gridDim.x * blockDim.x;
     if (gtid == 0) { P.st->vl_count[0] = 0; P.st->vl_count[1] = 0; }
     g.sync();
-    for (int base = blockIdx.x * blockDim.x; base < P.V; base += stride) {
-      const int v = base + threadIdx.x;
+    for (int base = blockIdx.x * blockDim.x; base < P.V_it; base += stride) {
+      const int vi = base + threadIdx.x;
+      const int v = vi < P.V_it ? vert_at(P, vi) : 0;
       int mine[1];
       int k = 0;
-      if (v < P.V && marked(Q, v, fs) && !P.vfix[v]) {
+      if (vi < P.V_it && marked(Q, v, fs) && !P.vfix[v]) {
         const float2 pn = ldpos(Q, v), po = P.pos_old[v];
         if (__float_as_uint(pn.x) != __float_as_uint(po.x) || __float_as_uint(pn.y) != __float_as_uint(po.y)) {
           __stcg(P.target + v, pn);
@@ -1046,11 +1052,12 @@ __device__ __noinline__ unsigned repair_step(cg::grid_group g, const KParams P, 
     // (4) reinsert at the new positions
     if (gtid == 0) { P.st->vl_count[0] = 0; P.st->vl_count[1] = 0; }
     g.sync();
-    for (int base = blockIdx.x * blockDim.x; base < P.V; base += stride) {
-      const int v = base + threadIdx.x;
+    for (int base = blockIdx.x * blockDim.x; base < P.V_it; base += stride) {
+      const int vi = base + threadIdx.x;
+      const int v = vi < P.V_it ? vert_at(P, vi) : 0;
       int mine[1];
       int k = 0;
-      if (v < P.V && ld_i(P.vhe + v) < 0 && marked(Q, v, fs)) {
+      if (vi < P.V_it && ld_i(P.vhe + v) < 0 && marked(Q, v, fs)) {
         __stcg(P.pos + v, __ldcg(P.target + v));
         mine[k++] = v;
       }
@@ -1130,15 +1137,27 @@ void free_mesh(mcl_mesh* m) {
   void* ptrs[] = {m->pos[0], m->pos[1], m->ev, m->en, m->vhe, m->vfix, m->cand, m->win, m->qmark, m->efa, m->hard,
                   m->wl[0], m->wl[1], m->vl[0], m->vl[1], m->vmark, m->claim, m->vfree, m->vhint,
                   m->vaux, m->vloc, m->vlocf, m->target, m->dstage, m->scratch, m->st,
-                  m->vcomp, m->vroot, m->cbase, m->table, m->smark};
+                  m->vcomp, m->vroot, m->cbase, m->table, m->smark, m->fnew, m->act_dev};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (m->st_host) cudaFreeHost(m->st_host);
+  if (m->act_host) cudaFreeHost(m->act_host);
   delete[] m->comp_host;
+  delete[] m->act_list;
+  delete[] m->dirty;
   delete m;
 }
 
 const float2* valid_positions(const mcl_mesh* m) { return m->valid_cur ? m->pos[m->cur] : m->pos[m->cur ^ 1]; }
+
+ActV act_of(const mcl_mesh* m) {
+  ActV a;
+  a.n = m->nact;
+  a.V_it = m->nact ? m->act_V : (int)m->V;
+  a.pre = m->nact ? m->act_dev + 2 * m->ncomp + 1 : nullptr;
+  a.v0 = m->nact ? m->act_dev + 3 * m->ncomp + 2 : nullptr;
+  return a;
+}
 
 int alloc_mesh(int64_t V, int64_t E, mcl_mesh** out) {
   if (V < 4 || E < 5 || V > (1ll << 30) || E > (1ll << 29))
@@ -1386,6 +1405,16 @@ static KParams make_params(mcl_mesh* m, int mode) {
   P.walk_cap = 1 << 18;
   P.tail_items = m->tail_items;
   P.vroot = m->vroot;
+  P.nact = m->nact;
+  P.E_it = m->nact ? m->act_E : (int)m->E;
+  P.V_it = m->nact ? m->act_V : (int)m->V;
+  if (m->nact) {
+    const int64_t nc = m->ncomp;
+    P.act_epre = m->act_dev;
+    P.act_e0 = m->act_dev + nc + 1;
+    P.act_vpre = m->act_dev + 2 * nc + 1;
+    P.act_v0 = m->act_dev + 3 * nc + 2;
+  }
   return P;
 }
 
@@ -1437,6 +1466,23 @@ static int finish(mcl_mesh* m, cudaStream_t s, mcl_step_stats* stats) {
 static int run_step(mcl_mesh* m, int move_mode, const float2* d, cudaStream_t s, mcl_step_stats* stats) {
   KParams P = make_params(m, ENGINE_STEP);
   if (move_mode != MOVE_NONE) {
+    if (m->dirty) {
+      // the launch writes the other position buffer for the active meshes
+      // only: the inactive meshes whose buffers differ are brought in step first
+      if (m->nact) {
+        std::vector<unsigned char> on((size_t)m->ncomp, 0);
+        for (int i = 0; i < m->nact; ++i) on[(size_t)m->act_list[i]] = 1;
+        for (int64_t c = 0; c < m->ncomp; ++c) {
+          if (on[(size_t)c] || !m->dirty[c]) continue;
+          const int64_t v0 = m->comp_host[4 * c], nv = m->comp_host[4 * c + 1];
+          CK(cudaMemcpyAsync(m->pos[m->cur ^ 1] + v0, m->pos[m->cur] + v0, 8 * nv, cudaMemcpyDeviceToDevice, s));
+          m->dirty[c] = 0;
+        }
+        for (int i = 0; i < m->nact; ++i) m->dirty[m->act_list[i]] = 1;
+      } else {
+        std::memset(m->dirty, 1, (size_t)m->ncomp);
+      }
+    }
     P.pos_old = m->pos[m->cur];
     P.pos = m->pos[m->cur ^ 1];
     P.move_mode = move_mode;
@@ -1645,6 +1691,8 @@ int mcl_mesh_download_aos(mcl_mesh* m, mcl_float2* pos, int32_t* v, int32_t* he,
 
 int mcl_move(mcl_mesh* m, const mcl_float2* d_dev, void* stream) {
   if (!m || !d_dev) return fail(MCL_ERR_INVALID_ARGUMENT, "null argument");
+  if (m->nact) return fail(MCL_ERR_INVALID_ARGUMENT, "mcl_move: a subset of the batch is active (use mcl_step)");
+  if (m->dirty) std::memset(m->dirty, 1, (size_t)m->ncomp);
   cudaStream_t s = (cudaStream_t)stream;
   const int src = m->cur, dst = m->valid_cur ? m->cur ^ 1 : m->cur;
   k_move_only<<<(unsigned)((m->V + 255) / 256), 256, 0, s>>>((int)m->V, m->vfix, m->pos[src], m->pos[dst],
@@ -1657,6 +1705,8 @@ int mcl_move(mcl_mesh* m, const mcl_float2* d_dev, void* stream) {
 
 int mcl_integrate(mcl_mesh* m, const float* dt_dev, const mcl_float2* v_dev, void* stream) {
   if (!m || !dt_dev || !v_dev) return fail(MCL_ERR_INVALID_ARGUMENT, "null argument");
+  if (m->nact) return fail(MCL_ERR_INVALID_ARGUMENT, "mcl_integrate: a subset of the batch is active (use mcl_step)");
+  if (m->dirty) std::memset(m->dirty, 1, (size_t)m->ncomp);
   cudaStream_t s = (cudaStream_t)stream;
   const int src = m->cur, dst = m->valid_cur ? m->cur ^ 1 : m->cur;
   k_move_only<<<(unsigned)((m->V + 255) / 256), 256, 0, s>>>((int)m->V, m->vfix, m->pos[src], m->pos[dst], nullptr,

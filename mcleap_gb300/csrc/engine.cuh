@@ -118,7 +118,40 @@ struct KParams {
   int walk_cap;
   int tail_items;          // flip rounds with at most this many queued edges run in one block
   const int* vroot;        // per vertex: a never-freed half-edge of its mesh (batches); NULL = half-edge 0
+  // active meshes of a batch (nact == 0: every edge and vertex): the full
+  // passes run over index spaces [0, E_it) and [0, V_it) that map to the
+  // edges and vertices of the active meshes
+  int nact;
+  int E_it, V_it;
+  const int* act_epre;     // [nact + 1] prefix sums of the active meshes' edge counts
+  const int* act_e0;       // [nact] first edge of each active mesh
+  const int* act_vpre;     // [nact + 1]
+  const int* act_v0;       // [nact]
 };
+
+__device__ __forceinline__ int act_map(const int* pre, const int* base, int n, int i) {
+  int lo = 0, hi = n - 1;  // largest c with pre[c] <= i
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(pre + mid) <= i) lo = mid;
+    else hi = mid - 1;
+  }
+  return __ldg(base + lo) + (i - __ldg(pre + lo));
+}
+// Index space of a pass over the active meshes' vertices (all when n == 0).
+struct ActV {
+  int n, V_it;
+  const int* pre;
+  const int* v0;
+  __device__ __forceinline__ int at(int i) const { return n ? act_map(pre, v0, n, i) : i; }
+};
+
+__device__ __forceinline__ int edge_at(const KParams& P, int i) {
+  return P.nact ? act_map(P.act_epre, P.act_e0, P.nact, i) : i;
+}
+__device__ __forceinline__ int vert_at(const KParams& P, int i) {
+  return P.nact ? act_map(P.act_vpre, P.act_v0, P.nact, i) : i;
+}
 
 // ---------------------------------------------------------------------------
 // Accessors.  Mesh records are mutated by other blocks inside the persistent
@@ -282,6 +315,14 @@ struct mcl_mesh {
   int64_t table_size;
   int* smark;              // per vertex: stamp of the settle pass that found it coincident
   int settle_blocks;       // k_settle grid (cooperative)
+  unsigned char* fnew;     // per vertex: newly frozen flags of mcl_dla_freeze
+  // active meshes (mcl_batch_set_active)
+  int nact;                // 0 = all
+  int act_E, act_V;
+  int* act_dev;            // device: epre[ncomp+1], e0[ncomp], vpre[ncomp+1], v0[ncomp], ids[ncomp]
+  int* act_host;           // pinned staging of the same
+  int* act_list;           // host: the active mesh ids
+  unsigned char* dirty;    // host, per mesh: its two position buffers differ
 };
 
 // Host-side helpers shared by the translation units of the library.
@@ -293,4 +334,5 @@ int cuda_fail(cudaError_t e, const char* what);
 int download_range(mcl_mesh* m, int64_t vb, int64_t nv, int64_t eb, int64_t ne, int64_t T, mcl_float2* pos,
                    int32_t* v, int32_t* he, int32_t* t);
 const float2* valid_positions(const mcl_mesh* m);
+ActV act_of(const mcl_mesh* m);
 }  // namespace mcl

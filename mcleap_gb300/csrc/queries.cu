@@ -194,11 +194,12 @@ __global__ void k_mesh_frnn(MeshView M, float r2, int layout, int max_frnn, int*
 // neighbours): a free walker freezes when a vertex frozen before this call
 // lies within its mesh's radius.  Decisions read frozen_in only, so the result
 // does not depend on thread order.
-__global__ void k_dla_freeze(MeshView M, const unsigned char* vfix, const float* rcomp, const int* vcomp,
+__global__ void k_dla_freeze(MeshView M, ActV A, const unsigned char* vfix, const float* rcomp, const int* vcomp,
                              const unsigned char* frozen_in, unsigned char* frozen_out,
                              unsigned long long* newly) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= M.V) return;
+  const int ii = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ii >= A.V_it) return;
+  const int i = A.at(ii);
   unsigned char f = frozen_in[i];
   if (!f && !vfix[i] && __ldg(M.vhe + i) >= 0) {
     const float rc = rcomp[vcomp ? vcomp[i] : 0];
@@ -232,6 +233,98 @@ __global__ void k_dla_freeze(MeshView M, const unsigned char* vfix, const float*
     if (f) atomicAdd(newly, 1ull);
   }
   frozen_out[i] = f;
+}
+
+// frozen[i] |= fnew[i] over the same vertices (second half of an in-place call)
+__global__ void k_dla_commit(ActV A, unsigned char* frozen, const unsigned char* fnew) {
+  const int ii = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ii >= A.V_it) return;
+  const int i = A.at(ii);
+  frozen[i] = fnew[i];
+}
+
+// Mesh FRNN / one-ring for a list of query vertices: row q is verts[q].
+__global__ void k_mesh_frnn_list(MeshView M, const float* rcomp, const int* vcomp, const int* verts, int n, int layout,
+                                 int max_frnn, int* out, unsigned long long* overflow) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const int i = verts[q];
+  const int cap = max_frnn - 1;
+  int* row = layout == MCL_LAYOUT_COLUMN ? out + q : out + (size_t)q * max_frnn;
+  const size_t stride = layout == MCL_LAYOUT_COLUMN ? (size_t)n : 1;
+  if (i < 0 || i >= M.V || __ldg(M.vhe + i) < 0) {
+    row[0] = 0;
+    return;
+  }
+  const float rc = rcomp[vcomp ? vcomp[i] : 0];
+  const float r2 = __fmul_rn(rc, rc);
+  int found[kFrnnLocal];
+  int nf = 0, top = 0;
+  bool over = false;
+  const float2 pi = M.pos[i];
+  int cur = i;
+  for (int guard = 0; guard < (1 << 20); ++guard) {
+    const int h0 = __ldg(M.vhe + cur);
+    if (h0 >= 0) {
+      int h = h0, deg = 0;
+      do {
+        const int w = mv_origin(M, h ^ 1);
+        if (w != i) {
+          bool seen = false;
+          for (int k = 0; k < nf; ++k)
+            if (found[k] == w) { seen = true; break; }
+          if (!seen && sqdist(pi, M.pos[w]) <= r2) {
+            if (nf < kFrnnLocal) found[nf++] = w;
+            else over = true;
+          }
+        }
+        h = mv_rot(M, h);
+        ++deg;
+      } while (h != h0 && deg < kMaxDeg);
+    }
+    if (top >= nf) break;
+    cur = found[top++];
+  }
+  for (int a = 1; a < nf; ++a) {
+    const int x = found[a];
+    int b = a - 1;
+    while (b >= 0 && found[b] > x) { found[b + 1] = found[b]; --b; }
+    found[b + 1] = x;
+  }
+  const int cnt = nf < cap ? nf : cap;
+  for (int k = 0; k < cnt; ++k) row[(size_t)(k + 1) * stride] = found[k];
+  row[0] = cnt;
+  if (over || nf > cap) atomicAdd(overflow, 1ull);
+}
+
+__global__ void k_one_ring_list(MeshView M, const int* verts, int n, int layout, int max_ring, int* out,
+                                unsigned long long* truncated) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const int i = verts[q];
+  int* row = layout == MCL_LAYOUT_COLUMN ? out + q : out + (size_t)q * max_ring;
+  const size_t stride = layout == MCL_LAYOUT_COLUMN ? (size_t)n : 1;
+  const int h0 = (i >= 0 && i < M.V) ? __ldg(M.vhe + i) : -1;
+  if (h0 < 0) {
+    row[0] = 0;
+    return;
+  }
+  int start = h0, best = 0x7fffffff, deg = 0, h = h0;
+  do {
+    const int w = mv_origin(M, h ^ 1);
+    if (w < best) { best = w; start = h; }
+    h = mv_rot(M, h);
+    ++deg;
+  } while (h != h0 && deg < kMaxDeg);
+  const int cap = max_ring - 1;
+  const int cnt = deg < cap ? deg : cap;
+  h = start;
+  for (int k = 0; k < cnt; ++k) {
+    row[(size_t)(k + 1) * stride] = mv_origin(M, h ^ 1);
+    h = mv_rot(M, h);
+  }
+  row[0] = cnt;
+  if (deg > cap) atomicAdd(truncated, 1ull);
 }
 
 }  // namespace
@@ -679,15 +772,64 @@ int mcl_batch_frnn(mcl_mesh* m, const float* r_dev, int layout, int max_frnn, in
   return MCL_OK;
 }
 
-int mcl_dla_freeze(mcl_mesh* m, const float* r_dev, const uint8_t* frozen_in, uint8_t* frozen_out, void* stream,
-                   int64_t* newly_frozen) {
-  if (!m || !r_dev || !frozen_in || !frozen_out || frozen_in == frozen_out)
-    return qfail(MCL_ERR_INVALID_ARGUMENT, "bad args (frozen_in and frozen_out must differ)");
+int mcl_batch_frnn_list(mcl_mesh* m, const float* r_dev, const int32_t* verts_dev, int64_t n, int layout,
+                        int max_frnn, int32_t* out_dev, void* stream, int64_t* overflow) {
+  if (!m || !r_dev || (n > 0 && (!verts_dev || !out_dev)) || n < 0 || max_frnn < 2 ||
+      (layout != MCL_LAYOUT_COLUMN && layout != MCL_LAYOUT_ROW))
+    return qfail(MCL_ERR_INVALID_ARGUMENT, "bad args");
   cudaStream_t s = (cudaStream_t)stream;
+  unsigned long long* cnt = m->scratch + 2;
+  QCK(cudaMemsetAsync(cnt, 0, 8, s));
+  if (n > 0) {
+    MeshView M{m->ev, m->en, m->vhe, m->pos[m->cur], (int)m->V, (int)m->E};
+    k_mesh_frnn_list<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(M, r_dev, m->vcomp, verts_dev, (int)n, layout,
+                                                                 max_frnn, out_dev, cnt);
+    QCK(cudaGetLastError());
+  }
+  if (overflow) {
+    unsigned long long t = 0;
+    QCK(cudaMemcpyAsync(&t, cnt, 8, cudaMemcpyDeviceToHost, s));
+    QCK(cudaStreamSynchronize(s));
+    *overflow = (int64_t)t;
+  }
+  return MCL_OK;
+}
+
+int mcl_one_ring_list(mcl_mesh* m, const int32_t* verts_dev, int64_t n, int layout, int max_ring, int32_t* out_dev,
+                      void* stream, int64_t* truncated) {
+  if (!m || (n > 0 && (!verts_dev || !out_dev)) || n < 0 || max_ring < 2 ||
+      (layout != MCL_LAYOUT_COLUMN && layout != MCL_LAYOUT_ROW))
+    return qfail(MCL_ERR_INVALID_ARGUMENT, "bad args");
+  cudaStream_t s = (cudaStream_t)stream;
+  unsigned long long* cnt = m->scratch + 3;
+  QCK(cudaMemsetAsync(cnt, 0, 8, s));
+  if (n > 0) {
+    MeshView M{m->ev, m->en, m->vhe, m->pos[m->cur], (int)m->V, (int)m->E};
+    k_one_ring_list<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(M, verts_dev, (int)n, layout, max_ring, out_dev, cnt);
+    QCK(cudaGetLastError());
+  }
+  if (truncated) {
+    unsigned long long t = 0;
+    QCK(cudaMemcpyAsync(&t, cnt, 8, cudaMemcpyDeviceToHost, s));
+    QCK(cudaStreamSynchronize(s));
+    *truncated = (int64_t)t;
+  }
+  return MCL_OK;
+}
+
+int mcl_dla_freeze(mcl_mesh* m, const float* r_dev, uint8_t* frozen, void* stream, int64_t* newly_frozen) {
+  if (!m || !r_dev || !frozen) return qfail(MCL_ERR_INVALID_ARGUMENT, "bad args");
+  cudaStream_t s = (cudaStream_t)stream;
+  if (!m->fnew && cudaMalloc((void**)&m->fnew, m->V) != cudaSuccess)
+    return qfail(MCL_ERR_OUT_OF_MEMORY, "mcl_dla_freeze: scratch");
   unsigned long long* cnt = m->scratch + 1;
   MeshView M{m->ev, m->en, m->vhe, m->pos[m->cur], (int)m->V, (int)m->E};
+  const ActV A = act_of(m);
   QCK(cudaMemsetAsync(cnt, 0, 8, s));
-  k_dla_freeze<<<(unsigned)((m->V + 127) / 128), 128, 0, s>>>(M, m->vfix, r_dev, m->vcomp, frozen_in, frozen_out, cnt);
+  if (A.V_it > 0) {
+    k_dla_freeze<<<(unsigned)((A.V_it + 127) / 128), 128, 0, s>>>(M, A, m->vfix, r_dev, m->vcomp, frozen, m->fnew, cnt);
+    k_dla_commit<<<(unsigned)((A.V_it + 255) / 256), 256, 0, s>>>(A, frozen, m->fnew);
+  }
   QCK(cudaGetLastError());
   if (newly_frozen) {
     unsigned long long t = 0;

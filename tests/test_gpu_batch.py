@@ -101,13 +101,13 @@ def test_walk_is_counter_based_and_stays_in_the_box(M):
     batch = M.MeshBatch.from_points([p.copy() for p in pts])
     V = batch.V
     sigma = cuda(np.array([5.0 * (i + 1) for i in range(batch.count)], np.float32))
-    counter = torch.zeros(1, dtype=torch.int64, device="cuda")
+    counter = torch.zeros(batch.count, dtype=torch.int64, device="cuda")
     d1 = torch.zeros((V, 2), dtype=torch.float32, device="cuda")
     d2 = torch.zeros_like(d1)
     frozen = torch.zeros(V, dtype=torch.uint8, device="cuda")
     frozen[4::2] = 1
     batch.walk(sigma, counter, d1, seed=7, frozen=frozen)
-    assert counter.item() == 1
+    assert counter.tolist() == [1] * batch.count
     counter.zero_()
     batch.walk(sigma, counter, d2, seed=7, frozen=frozen)
     assert torch.equal(d1, d2)
@@ -230,9 +230,9 @@ def test_dla_freeze_matches_brute_force(M):
     fin = (rng.random(batch.V) < 0.2).astype(np.uint8)
     for v0 in batch.v0:
         fin[v0:v0 + 4] = 0
-    fi, fo = cuda(fin), torch.zeros(batch.V, dtype=torch.uint8, device="cuda")
-    newly = batch.dla_freeze(cuda(radii), fi, fo)
-    got = fo.cpu().numpy()
+    fi = cuda(fin)
+    newly = batch.dla_freeze(cuda(radii), fi)
+    got = fi.cpu().numpy()
     want = fin.copy()
     for i in range(batch.count):
         v0, nv = int(batch.v0[i]), int(batch.nv[i])
@@ -244,3 +244,84 @@ def test_dla_freeze_matches_brute_force(M):
                 want[v0 + j] = 1
     assert np.array_equal(got, want)
     assert newly == int((want != fin).sum())
+
+
+def test_active_subset_steps_only_those_meshes(M):
+    """Steps restricted to some meshes of a batch leave the others untouched and
+    equal the same meshes stepped alone (the position double buffer of an
+    idle mesh is kept in step)."""
+    import torch
+
+    pts = make_points()
+    batch = M.MeshBatch.from_points([p.copy() for p in pts])
+    alone = []
+    for p in pts:
+        ht = M.HostTriangulation()
+        q = p.copy()
+        ht.addDelaunayPoints(q)
+        alone.append((ht, M.DeviceTriangulation(ht)))
+    pos = [ht.m_pos.copy() for ht, _ in alone]
+    plan = [[1, 3], [0, 1], [5, 2, 4], [], [3]]
+    for k, active in enumerate(plan):
+        batch.set_active(active)
+        ds = [np.zeros_like(pos[i]) for i in range(len(SIZES))]
+        for i in (active or range(len(SIZES))):
+            ds[i] = gaussian_disp(len(pos[i]), 0.3 * spacing(SIZES[i]), 31 * k + i, clamp_pos=pos[i])
+        st = batch.step(cuda(np.concatenate(ds)))
+        assert st["status"] == 0, st
+        for i in (active or range(len(SIZES))):
+            ht, dt = alone[i]
+            assert dt.step(cuda(ds[i]))["status"] == 0
+            dt.transferToHost()
+            pos[i] = (pos[i] + ds[i]).astype(np.float32)
+        batch.set_active(None)
+        assert not batch.validate().any()
+        for i, (ht, _) in enumerate(alone):
+            bpos = batch.download(i)[0]
+            assert np.array_equal(bpos, pos[i]), (k, i)
+            assert np.array_equal(batch.edges(i), ht.edges()), (k, i)
+    # the motion calls follow the active set too
+    counter = torch.zeros(batch.count, dtype=torch.int64, device="cuda")
+    d = torch.zeros((batch.V, 2), dtype=torch.float32, device="cuda")
+    sigma = cuda(np.full(batch.count, 3.0, np.float32))
+    batch.set_active([2, 4])
+    batch.walk(sigma, counter, d, seed=1)
+    assert counter.tolist() == [0, 0, 1, 0, 1, 0]
+    dn = d.cpu().numpy()
+    for i in range(batch.count):
+        sl = dn[batch.v0[i]:batch.v0[i] + batch.nv[i]]
+        assert sl.any() == (i in (2, 4))
+    assert batch.settle(d) == 0
+    assert batch.step(d)["status"] == 0
+    batch.set_active(None)
+    assert not batch.validate().any()
+
+
+def test_query_lists_match_full_queries(M):
+    import torch
+
+    from helpers import csr_from_table
+
+    pts = make_points()
+    batch = M.MeshBatch.from_points([p.copy() for p in pts])
+    radii = cuda(np.array([2.0 * spacing(n) for n in SIZES], np.float32))
+    F, RM = 48, 32
+    full = torch.zeros(batch.V * F, dtype=torch.int32, device="cuda")
+    batch.frnn(radii, F, full)
+    ring = torch.zeros(batch.V * RM, dtype=torch.int32, device="cuda")
+    batch.one_ring(RM, ring, layout=1)
+    rng = np.random.default_rng(2)
+    verts = rng.choice(batch.V, 500, replace=False).astype(np.int32)
+    vq = cuda(verts)
+    out = torch.zeros(len(verts) * F, dtype=torch.int32, device="cuda")
+    assert batch.frnn_list(radii, vq, F, out) == 0
+    c_full, rows_full = csr_from_table(full.cpu().numpy(), 1, batch.V, F)
+    c_l, rows_l = csr_from_table(out.cpu().numpy(), 1, len(verts), F)
+    for q, v in enumerate(verts):
+        assert np.array_equal(rows_l[q], rows_full[v])
+    outr = torch.zeros(len(verts) * RM, dtype=torch.int32, device="cuda")
+    assert batch.one_ring_list(vq, RM, outr) == 0
+    c_r, rows_r = csr_from_table(ring.cpu().numpy(), 1, batch.V, RM)
+    c_rl, rows_rl = csr_from_table(outr.cpu().numpy(), 1, len(verts), RM)
+    for q, v in enumerate(verts):
+        assert np.array_equal(rows_rl[q], rows_r[v])
