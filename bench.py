@@ -46,7 +46,11 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-queries", action="store_true")
-    ap.add_argument("--workload", default="taylor-green", choices=["taylor-green", "batched"])
+    ap.add_argument("--workload", default="taylor-green", choices=["taylor-green", "batched", "serving"])
+    ap.add_argument("--rate", type=float, default=2000.0)
+    ap.add_argument("--duration", type=float, default=10.0)
+    ap.add_argument("--drain-limit", type=float, default=60.0)
+    ap.add_argument("--budget-gb", type=float, default=150.0)
     ap.add_argument("--meshes", type=int, default=4096)
     ap.add_argument("--plain-steps", type=int, default=3)
     return ap.parse_args()
@@ -558,6 +562,67 @@ def run_batched(args, rank, world, dist):
         print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------
+def run_serving(args, rank, world, dist):
+    """Serving: meshes resident against an HBM budget, an open-loop Poisson
+    request stream (k-step aggregation updates and FRNN / one-ring query
+    batches), continuous batching vs the plain one-request-at-a-time form."""
+    import torch
+
+    from mcleap_gb300 import build as B
+    from mcleap_gb300 import serving as S
+    from mcleap_gb300 import workloads as W
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    B.build()
+    nm = args.meshes if args.meshes != 4096 else 512
+    rng = np.random.default_rng(5 + rank)
+    sizes = np.exp(rng.uniform(np.log(1e3), np.log(1e6), nm)).astype(np.int64)
+    t0 = time.perf_counter()
+    pts = [W.uniform_points(int(n), 60000 + i) for i, n in enumerate(sizes)]
+    server = S.MeshServer(pts, budget_bytes=args.budget_gb * 1e9, seed=99)
+    del pts
+    t_setup = time.perf_counter() - t0
+    sizes = server.sizes
+    reqs = S.poisson_requests(server.n, args.rate, args.duration, seed=77 + rank, mesh_sizes=sizes)
+    warm = S.poisson_requests(server.n, args.rate, 0.05, seed=1, mesh_sizes=sizes)
+    server.serve(warm, batched=True, realtime=False)  # warm-up (not reported)
+    cp, cf = clocks_start()
+    server.point_steps = 0
+    it0, l0 = server.iterations, server.launches
+    done = server.serve(reqs, batched=True, realtime=True, time_limit=args.duration + args.drain_limit)
+    served = S.latency_summary(done, server.wall, server.point_steps, len(reqs))
+    served["iterations"] = server.iterations - it0
+    launches = server.launches - l0
+    # plain form on the same request stream, same resident meshes
+    server.point_steps = 0
+    it1 = server.iterations
+    reqs2 = S.poisson_requests(server.n, args.rate, args.duration, seed=77 + rank, mesh_sizes=sizes)
+    done2 = server.serve(reqs2, batched=False, realtime=True, time_limit=args.duration + args.drain_limit)
+    plain = S.latency_summary(done2, server.wall, server.point_steps, len(reqs2))
+    plain["iterations"] = server.iterations - it1
+    clocks = clocks_stop(cp, cf, local)
+    line = {
+        "metric": "served kinetic pts*steps/s with p50/p99/p99.9 request latency (continuous batching)",
+        "value": served["pts_steps_per_s"], "unit": UNIT, "n_gpus": world, "steps": served["iterations"],
+        "warmup": len(warm), "ms_per_step": 1e3 * server.wall / max(1, served["iterations"]),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"serving: {server.n} resident meshes (sizes log-uniform in [1e3, 1e6], seed 5), "
+                               f"Poisson arrivals at {args.rate:g} req/s for {args.duration:g} s, half k-step "
+                               "aggregation updates (k in 1..16), half FRNN / one-ring batches of 1e3..1e5 "
+                               f"vertices; HBM budget {args.budget_gb:g} GB",
+                   "meshes": server.n, "points": int(sizes.sum()), "admitted": len(server.admitted),
+                   "rejected": len(server.rejected), "budget_used_gb": server.admission.used / 1e9,
+                   "parallelism": f"replicas x{world}"},
+        "served": served, "plain": plain,
+        "speedup_vs_plain": served["pts_steps_per_s"] / max(plain["pts_steps_per_s"], 1e-9),
+        "clocks": clocks, "gpu_launches": launches, "setup_s": t_setup,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -576,6 +641,8 @@ def main():
             run_reference(args, rank, world)
         elif args.workload == "batched":
             run_batched(args, rank, world, dist)
+        elif args.workload == "serving":
+            run_serving(args, rank, world, dist)
         else:
             run_ours(args, rank, world, dist)
     finally:
