@@ -156,6 +156,9 @@ __device__ __forceinline__ bool resolve_edge(const KParams& P, int e, LocalCount
 // whole filter.  Edges the filters cannot decide (a few per million) go to the
 // hard list, which is resolved with the full ladder after the barrier; the
 // caller must call phase_classify_hard before reading `inverted`.
+// Edges per thread and iteration of the classification pass.
+constexpr int kClassifyUnroll = 4;
+
 template <bool kFixedPos>
 __device__ void phase_classify(cg::grid_group& g, const KParams& P, unsigned qstamp, unsigned sc,
                                LocalCounters& lc) {
@@ -170,43 +173,67 @@ __device__ void phase_classify(cg::grid_group& g, const KParams& P, unsigned qst
   int bad = 0;
   unsigned ninc = 0;
   int def0 = -1, def1 = -1;  // edges deferred to the full ladder after the loop
-  for (int base = blockIdx.x * blockDim.x; base < P.E_it; base += stride) {
-    const int ei = base + threadIdx.x;
-    int mine[1];
-    int k = 0;
-    int hard[1];
-    int kh = 0;
-    if (ei < P.E_it) {
-      const int e = edge_at(P, ei);
-      const int4 q = ld_ev(P, e);
-      if (q.x >= 0 && (bad_v(P, q.x) || bad_v(P, q.y) || q.z >= P.V || q.w >= P.V)) {
+  // kClassifyUnroll edges per thread and iteration, their records and
+  // positions loaded before any is evaluated (memory-level parallelism: the
+  // pass is latency-bound on the position gathers); edge j of the iteration
+  // at base is base + j * blockDim.x + threadIdx.x, so every load stays
+  // coalesced across the warp.
+  constexpr int U = kClassifyUnroll;
+  for (int base = blockIdx.x * blockDim.x * U; base < P.E_it; base += stride * U) {
+    int4 q[U];
+    int e[U];
+#pragma unroll
+    for (int j = 0; j < U; ++j) {
+      const int ei = base + j * blockDim.x + threadIdx.x;
+      e[j] = ei < P.E_it ? edge_at(P, ei) : -1;
+      q[j] = e[j] >= 0 ? ld_ev(P, e[j]) : make_int4(-1, -1, -1, -1);
+    }
+    float2 pa[U], pb[U], pc[U], pd[U];
+#pragma unroll
+    for (int j = 0; j < U; ++j) {
+      const int4 r = q[j];
+      const bool ok = r.x >= 0 && !(bad_v(P, r.x) || bad_v(P, r.y) || r.z >= P.V || r.w >= P.V);
+      if (r.x >= 0 && !ok) {
         flag_error(P, MCL_ERR_DEGENERATE_INPUT);
-      } else if (q.x >= 0) {
-        const float2 a = ldpos_t<kFixedPos>(P, q.x), b = ldpos_t<kFixedPos>(P, q.y);
-        const float2 c = q.z >= 0 ? ldpos_t<kFixedPos>(P, q.z) : a;
-        const float2 d = q.w >= 0 ? ldpos_t<kFixedPos>(P, q.w) : a;
-        const int sa = q.z >= 0 ? orient2d_fp32(a.x, a.y, b.x, b.y, c.x, c.y) : 1;
-        const int sb = q.w >= 0 ? orient2d_fp32(b.x, b.y, a.x, a.y, d.x, d.y) : 1;
-        bool defer = false;
-        if (sa == 2 || sb == 2) {
+        q[j].x = -1;
+      }
+      if (ok) {
+        pa[j] = ldpos_t<kFixedPos>(P, r.x);
+        pb[j] = ldpos_t<kFixedPos>(P, r.y);
+        pc[j] = r.z >= 0 ? ldpos_t<kFixedPos>(P, r.z) : pa[j];
+        pd[j] = r.w >= 0 ? ldpos_t<kFixedPos>(P, r.w) : pa[j];
+      }
+    }
+    int mine[U];
+    int k = 0;
+    int hard[U];
+    int kh = 0;
+#pragma unroll
+    for (int j = 0; j < U; ++j) {
+      const int4 r = q[j];
+      if (r.x < 0) continue;
+      const float2 a = pa[j], b = pb[j], c = pc[j], d = pd[j];
+      const int sa = r.z >= 0 ? orient2d_fp32(a.x, a.y, b.x, b.y, c.x, c.y) : 1;
+      const int sb = r.w >= 0 ? orient2d_fp32(b.x, b.y, a.x, a.y, d.x, d.y) : 1;
+      bool defer = false;
+      if (sa == 2 || sb == 2) {
+        defer = true;
+      } else if (sa <= 0 || sb <= 0) {
+        bad += (sa <= 0) + (sb <= 0);
+      } else if (r.z >= 0 && r.w >= 0) {
+        ++ninc;
+        const int si = incircle_fp32(a.x, a.y, b.x, b.y, c.x, c.y, d.x, d.y);
+        if (si == 2) {
           defer = true;
-        } else if (sa <= 0 || sb <= 0) {
-          bad += (sa <= 0) + (sb <= 0);
-        } else if (q.z >= 0 && q.w >= 0) {
-          ++ninc;
-          const int si = incircle_fp32(a.x, a.y, b.x, b.y, c.x, c.y, d.x, d.y);
-          if (si == 2) {
-            defer = true;
-          } else if (si > 0 && enqueue_once(P, e, qstamp)) {
-            claim_edge(P, e, sc);
-            mine[k++] = e;
-          }
+        } else if (si > 0 && enqueue_once(P, e[j], qstamp)) {
+          claim_edge(P, e[j], sc);
+          mine[k++] = e[j];
         }
-        if (defer) {
-          if (def0 < 0) def0 = e;
-          else if (def1 < 0) def1 = e;
-          else hard[kh++] = e;
-        }
+      }
+      if (defer) {
+        if (def0 < 0) def0 = e[j];
+        else if (def1 < 0) def1 = e[j];
+        else hard[kh++] = e[j];
       }
     }
     if (__any_sync(kFull, k > 0)) warp_push(mine, k, P.wl0, &P.st->wl_count[0], P.E, P.st);

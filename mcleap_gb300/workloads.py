@@ -10,8 +10,20 @@ SCALE = np.float32(8192.0)
 
 
 def uniform_points(n, seed):
+    """n distinct float32 points i.i.d. uniform in [0, 8192)^2 (the unit square
+    scaled by 2^13); the rare exact duplicates of the 2^24-per-axis grid are
+    redrawn, since coincident points have no triangulation."""
     rng = np.random.default_rng(seed)
-    return (rng.random((n, 2), dtype=np.float32) * SCALE).astype(np.float32)
+    p = (rng.random((n, 2), dtype=np.float32) * SCALE).astype(np.float32)
+    for _ in range(64):
+        key = p.view(np.int64).ravel()
+        _, first = np.unique(key, return_index=True)
+        if len(first) == n:
+            return p
+        dup = np.ones(n, bool)
+        dup[first] = False
+        p[dup] = (rng.random((int(dup.sum()), 2), dtype=np.float32) * SCALE).astype(np.float32)
+    raise RuntimeError("could not draw distinct points")
 
 
 def mean_spacing(n):
