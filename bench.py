@@ -46,7 +46,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-queries", action="store_true")
-    ap.add_argument("--workload", default="taylor-green", choices=["taylor-green", "batched", "serving"])
+    ap.add_argument("--workload", default="taylor-green", choices=["taylor-green", "batched", "serving", "precision"])
     ap.add_argument("--rate", type=float, default=2000.0)
     ap.add_argument("--duration", type=float, default=10.0)
     ap.add_argument("--drain-limit", type=float, default=60.0)
@@ -623,6 +623,81 @@ def run_serving(args, rank, world, dist):
         print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------
+def run_precision(args, rank, world, dist):
+    """Precision stress: 4M float32 points (half on a jittered lattice, 30% in
+    tight clusters, 20% uniform), Gaussian walk sigma = 0.05 x spacing; the
+    predicate ladder's stage rates per step."""
+    import ctypes as C
+
+    import torch
+
+    from mcleap_gb300 import _lib as L
+    from mcleap_gb300 import batch as MB
+    from mcleap_gb300 import build as B
+    from mcleap_gb300 import workloads as W
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    B.build()
+    n = 4_000_000 if args.n == 1_000_000 else args.n
+    K = min(args.steps, 200)
+    t0 = time.perf_counter()
+    pts = W.precision_points(n, 3 + rank)
+    mesh = MB.MeshBatch(MB.build_mesh(pts))
+    t_build = time.perf_counter() - t0
+    V = mesh.V
+    h = 8192.0 / np.sqrt(n)
+    sigma = torch.tensor([0.05 * h], dtype=torch.float32, device="cuda")
+    counter = torch.zeros(1, dtype=torch.int64, device="cuda")
+    d = torch.zeros((V, 2), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.Stream()
+    lib = L.lib()
+    keys = ("incircle_tests", "incircle_fp64", "incircle_exact", "orient_fp64", "orient_exact", "sos_decisions",
+            "lawson_flips", "inverted_faces", "removed_vertices")
+    tot = {k: 0 for k in keys}
+
+    cp, cf = clocks_start()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    settled = 0
+    for k in range(K):
+        mesh.walk(sigma, counter, d, seed=21, stream=stream)
+        settled += mesh.settle(d, stream=stream)
+        ev[k][0].record(stream)
+        st = L.StepStats()
+        L.check(lib.mcl_step(mesh.handle, d.data_ptr(), stream.cuda_stream, C.byref(st)))
+        ev[k][1].record(stream)
+        sd = st.as_dict()
+        if sd["status"] != 0:
+            raise RuntimeError(f"precision step {k} failed: {sd}")
+        for key in keys:
+            tot[key] += sd[key]
+    stream.synchronize()
+    clocks = clocks_stop(cp, cf, local)
+    ms = np.array([a.elapsed_time(b) for a, b in ev])
+    inc = max(1, tot["incircle_tests"])
+    line = {
+        "metric": "precision stress: kinetic pts*steps/s and predicate stage rates",
+        "value": n * K / (ms.sum() / 1e3), "unit": UNIT, "n_gpus": world, "steps": K, "warmup": 0,
+        "ms_per_step": float(ms.mean()), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"precision: {n} points (50% jittered 2048x1024 lattice, 30% in 64 Gaussian "
+                               "clusters sigma 1e-3, 20% uniform), Gaussian walk sigma = 0.05 x spacing",
+                   "points": n, "parallelism": f"replicas x{world}"},
+        "rates": {"incircle_fp32_undecided": tot["incircle_fp64"] / inc,
+                  "incircle_fp64_undecided": tot["incircle_exact"] / inc,
+                  "sos_per_incircle": tot["sos_decisions"] / inc,
+                  "orient_fp32_undecided_per_step": tot["orient_fp64"] / K,
+                  "orient_fp64_undecided_per_step": tot["orient_exact"] / K},
+        "totals": tot, "settled_moves": settled,
+        "sign_check": "tests/test_gpu_precision.py compares sampled live-mesh predicate signs with the exact oracle",
+        "step_ms": {"p50": float(np.median(ms)), "p99": float(np.percentile(ms, 99))},
+        "clocks": clocks, "gpu_launches": K * 5, "build_s": t_build,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -643,6 +718,8 @@ def main():
             run_batched(args, rank, world, dist)
         elif args.workload == "serving":
             run_serving(args, rank, world, dist)
+        elif args.workload == "precision":
+            run_precision(args, rank, world, dist)
         else:
             run_ours(args, rank, world, dist)
     finally:

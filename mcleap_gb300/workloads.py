@@ -107,3 +107,36 @@ def taylor_green_displacements_device(pos, n, steps, frac=0.5, device="cuda"):
         p[4:] = p[4:] + d[4:]
         out.append(d)
     return out
+
+
+def precision_points(n, seed):
+    """Precision-stress point set (n float32 points, scaled by 2^13):
+    50% on distinct sites of the 2048 x 1024 lattice (i/2048, j/1024), each
+    coordinate jittered by U(-1e-7, 1e-7) in unit coordinates (about one ulp
+    near 0.5, so many land back on the lattice: exactly cocircular quads);
+    30% from 64 isotropic Gaussian clusters (sigma 1e-3, centres uniform,
+    clamped to the square); 20% uniform.  Exact duplicates are redrawn as
+    uniform points."""
+    rng = np.random.default_rng(seed)
+    n_lat = n // 2
+    n_clu = (3 * n) // 10
+    n_uni = n - n_lat - n_clu
+    sites = rng.choice(2048 * 1024, size=n_lat, replace=False)
+    i, j = sites % 2048, sites // 2048
+    lat = np.stack([i / 2048.0, j / 1024.0], 1) + rng.uniform(-1e-7, 1e-7, (n_lat, 2))
+    centres = rng.random((64, 2))
+    c = rng.integers(0, 64, n_clu)
+    clu = centres[c] + rng.normal(0.0, 1e-3, (n_clu, 2))
+    uni = rng.random((n_uni, 2))
+    hi = 1.0 - 2.0 ** -24
+    p = np.clip(np.concatenate([lat, clu, uni]), 0.0, hi).astype(np.float32) * SCALE
+    p = p.astype(np.float32)
+    for _ in range(64):
+        key = p.view(np.int64).ravel()
+        _, first = np.unique(key, return_index=True)
+        if len(first) == n:
+            return p
+        dup = np.ones(n, bool)
+        dup[first] = False
+        p[dup] = (rng.random((int(dup.sum()), 2), dtype=np.float32) * SCALE).astype(np.float32)
+    raise RuntimeError("could not draw distinct points")
