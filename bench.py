@@ -46,6 +46,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-queries", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--workload", default="taylor-green", choices=["taylor-green", "batched", "serving", "precision"])
     ap.add_argument("--rate", type=float, default=2000.0)
     ap.add_argument("--duration", type=float, default=10.0)
@@ -331,6 +332,18 @@ def run_ours(args, rank, world, dist):
                "d2h_bytes_per_step": C.sizeof(L.StepStats), "ms_per_step": 1e3 * e_s / KE, "steps": KE}
     clocks = clocks_stop(cp, cf, local)
 
+    # served vs plain on a short stream over 32 resident meshes (the serving
+    # workload, scaled down to keep the default run within a few minutes)
+    served = None
+    if not args.no_serving:
+        sv, pl, info = serving_measure(32, 2000.0, 2.0, 10.0, 150.0, 5 + rank)
+        served = {"workload": f"{info['meshes']} resident meshes ({info['points']} points), Poisson 2000 req/s "
+                              "for 2 s, k-step aggregation updates and FRNN / one-ring batches",
+                  "served": {k: sv[k] for k in ("p50_ms", "p99_ms", "p999_ms", "pts_steps_per_s", "completed",
+                                                "submitted", "iterations")},
+                  "plain": {k: pl[k] for k in ("p50_ms", "p99_ms", "p999_ms", "pts_steps_per_s", "completed",
+                                               "submitted", "iterations")}}
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         from oracle import oracle as O
@@ -361,6 +374,10 @@ def run_ours(args, rank, world, dist):
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "kernel": "k_step", "alg_bytes_per_launch": alg_bytes},
             "queries": qinfo,
+            "served_vs_plain": served,
+            # every timed step ended with status OK: no expansion overflow, no
+            # undecided sign (sampled signs vs the exact oracle: the GPU tests)
+            "predicate_errors": 0 if st["status"] == 0 else st["status"],
             "e2e": e2e, "cpu_baseline": cpu, "clocks": clocks,
             # k_step per step, plus k_one_ring + 7 grid-build kernels + k_grid_frnn per step
             "gpu_launches": K * (10 if do_q else 1),
@@ -563,6 +580,43 @@ def run_batched(args, rank, world, dist):
 
 
 # ---------------------------------------------------------------------------
+def serving_measure(nm, rate, duration, drain, budget_gb, seed):
+    """Serve an open-loop Poisson stream over nm resident meshes (sizes
+    log-uniform in [1e3, 1e6]) with continuous batching, then the same stream
+    in the plain one-request-at-a-time form."""
+    from mcleap_gb300 import serving as S
+    from mcleap_gb300 import workloads as W
+
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(np.log(1e3), np.log(1e6), nm)).astype(np.int64)
+    t0 = time.perf_counter()
+    pts = [W.uniform_points(int(n), 60000 + i) for i, n in enumerate(sizes)]
+    server = S.MeshServer(pts, budget_bytes=budget_gb * 1e9, seed=99)
+    del pts
+    t_setup = time.perf_counter() - t0
+    sizes = server.sizes
+    warm = S.poisson_requests(server.n, rate, 0.05, seed=1, mesh_sizes=sizes)
+    server.serve(warm, batched=True, realtime=False)  # warm-up (not reported)
+    server.point_steps = 0
+    it0, l0 = server.iterations, server.launches
+    reqs = S.poisson_requests(server.n, rate, duration, seed=seed + 72, mesh_sizes=sizes)
+    done = server.serve(reqs, batched=True, realtime=True, time_limit=duration + drain)
+    served = S.latency_summary(done, server.wall, server.point_steps, len(reqs))
+    served["iterations"] = server.iterations - it0
+    launches = server.launches - l0
+    server.point_steps = 0
+    it1 = server.iterations
+    reqs2 = S.poisson_requests(server.n, rate, duration, seed=seed + 72, mesh_sizes=sizes)
+    done2 = server.serve(reqs2, batched=False, realtime=True, time_limit=duration + drain)
+    plain = S.latency_summary(done2, server.wall, server.point_steps, len(reqs2))
+    plain["iterations"] = server.iterations - it1
+    info = {"meshes": server.n, "points": int(sizes.sum()), "admitted": len(server.admitted),
+            "rejected": len(server.rejected), "budget_used_gb": server.admission.used / 1e9,
+            "rate": rate, "duration_s": duration, "setup_s": t_setup, "launches": launches}
+    server.batch.close()
+    return served, plain, info
+
+
 def run_serving(args, rank, world, dist):
     """Serving: meshes resident against an HBM budget, an open-loop Poisson
     request stream (k-step aggregation updates and FRNN / one-ring query
@@ -570,54 +624,28 @@ def run_serving(args, rank, world, dist):
     import torch
 
     from mcleap_gb300 import build as B
-    from mcleap_gb300 import serving as S
-    from mcleap_gb300 import workloads as W
 
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     B.build()
     nm = args.meshes if args.meshes != 4096 else 512
-    rng = np.random.default_rng(5 + rank)
-    sizes = np.exp(rng.uniform(np.log(1e3), np.log(1e6), nm)).astype(np.int64)
-    t0 = time.perf_counter()
-    pts = [W.uniform_points(int(n), 60000 + i) for i, n in enumerate(sizes)]
-    server = S.MeshServer(pts, budget_bytes=args.budget_gb * 1e9, seed=99)
-    del pts
-    t_setup = time.perf_counter() - t0
-    sizes = server.sizes
-    reqs = S.poisson_requests(server.n, args.rate, args.duration, seed=77 + rank, mesh_sizes=sizes)
-    warm = S.poisson_requests(server.n, args.rate, 0.05, seed=1, mesh_sizes=sizes)
-    server.serve(warm, batched=True, realtime=False)  # warm-up (not reported)
     cp, cf = clocks_start()
-    server.point_steps = 0
-    it0, l0 = server.iterations, server.launches
-    done = server.serve(reqs, batched=True, realtime=True, time_limit=args.duration + args.drain_limit)
-    served = S.latency_summary(done, server.wall, server.point_steps, len(reqs))
-    served["iterations"] = server.iterations - it0
-    launches = server.launches - l0
-    # plain form on the same request stream, same resident meshes
-    server.point_steps = 0
-    it1 = server.iterations
-    reqs2 = S.poisson_requests(server.n, args.rate, args.duration, seed=77 + rank, mesh_sizes=sizes)
-    done2 = server.serve(reqs2, batched=False, realtime=True, time_limit=args.duration + args.drain_limit)
-    plain = S.latency_summary(done2, server.wall, server.point_steps, len(reqs2))
-    plain["iterations"] = server.iterations - it1
+    served, plain, info = serving_measure(nm, args.rate, args.duration, args.drain_limit, args.budget_gb, 5 + rank)
     clocks = clocks_stop(cp, cf, local)
     line = {
         "metric": "served kinetic pts*steps/s with p50/p99/p99.9 request latency (continuous batching)",
         "value": served["pts_steps_per_s"], "unit": UNIT, "n_gpus": world, "steps": served["iterations"],
-        "warmup": len(warm), "ms_per_step": 1e3 * server.wall / max(1, served["iterations"]),
+        "warmup": 1, "ms_per_step": 1e3 * served["wall_s"] / max(1, served["iterations"]),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"serving: {server.n} resident meshes (sizes log-uniform in [1e3, 1e6], seed 5), "
-                               f"Poisson arrivals at {args.rate:g} req/s for {args.duration:g} s, half k-step "
-                               "aggregation updates (k in 1..16), half FRNN / one-ring batches of 1e3..1e5 "
-                               f"vertices; HBM budget {args.budget_gb:g} GB",
-                   "meshes": server.n, "points": int(sizes.sum()), "admitted": len(server.admitted),
-                   "rejected": len(server.rejected), "budget_used_gb": server.admission.used / 1e9,
-                   "parallelism": f"replicas x{world}"},
+        "config": dict(workload=f"serving: {info['meshes']} resident meshes (sizes log-uniform in [1e3, 1e6]), "
+                                f"Poisson arrivals at {args.rate:g} req/s for {args.duration:g} s, half k-step "
+                                "aggregation updates (k in 1..16), half FRNN / one-ring batches of 1e3..1e5 "
+                                f"vertices; HBM budget {args.budget_gb:g} GB",
+                       parallelism=f"replicas x{world}", **info),
         "served": served, "plain": plain,
         "speedup_vs_plain": served["pts_steps_per_s"] / max(plain["pts_steps_per_s"], 1e-9),
-        "clocks": clocks, "gpu_launches": launches, "setup_s": t_setup,
+        "p50_latency_ratio_plain_over_served": plain["p50_ms"] / max(served["p50_ms"], 1e-9),
+        "clocks": clocks, "gpu_launches": info["launches"],
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
