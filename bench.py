@@ -307,9 +307,9 @@ def run_ours(args, rank, world, dist):
     achieved = alg_bytes / (dev_s / K) / 1e9
     peak, peak_kind = peaks()
     # DRAM traffic of one k_step launch measured by ncu on this workload
-    # (profiles/k_step_taylor_green_1M.md: 73.1 MB at 3,000,005 edges), scaled
+    # (profiles/k_step_taylor_green_1M.md: 71.1 MB at 3,000,005 edges), scaled
     # by the edge count for other sizes
-    traffic = 73.1e6 * E / 3000005
+    traffic = 71.06e6 * E / 3000005
 
     # e2e: host displacements through the C ABI, per-step counters read back
     e2e = None
