@@ -58,6 +58,17 @@ def parse():
 
 
 # ---------------------------------------------------------------------------
+def max_over_ranks(x, dist, device="cpu"):
+    """The largest value of x over all ranks (x itself without a process group)."""
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def clocks_start():
     try:
         f = open(os.path.join(ROOT, "gpurun_out", "clocks.csv") if os.path.isdir(os.path.join(ROOT, "gpurun_out"))
@@ -127,7 +138,8 @@ def cpu_reference(n, frac_n, seconds, seed, workers):
     wall = max(r[1] for r in res)
     flips = sum(r[2] for r in res)
     steps = sum(r[3] for r in res)
-    return pts_steps / wall, wall, flips, steps
+    capped = sum(r[4] for r in res)
+    return pts_steps / wall, wall, flips, steps, capped
 
 
 def _cpu_worker(n, frac_n, seconds, seed):
@@ -141,15 +153,16 @@ def _cpu_worker(n, frac_n, seconds, seed):
     # the same displacement per step relative to the local spacing as the GPU workload
     frac = 0.5
     t0 = time.perf_counter()
-    steps = flips = 0
+    steps = flips = capped = 0
     while time.perf_counter() - t0 < seconds or steps == 0:
         d = W.taylor_green_displacements(pos, n, 1, frac=frac)[0]
         r = m.kinetic_step_ref(d)
         flips += r["untangle_flips"] + r["delonize_flips"]
+        capped += r["capped"]
         pos = m.positions()
         steps += 1
     wall = time.perf_counter() - t0
-    return n * steps, wall, flips, steps
+    return n * steps, wall, flips, steps, capped
 
 
 def run_reference(args, rank, world):
@@ -162,7 +175,7 @@ def run_reference(args, rank, world):
     sample = min(args.cpu_sample, args.n)
     secs = max(3.0, args.cpu_seconds)
     t_all = time.perf_counter()
-    value, wall, flips, steps = cpu_reference(sample, args.n, secs, 1234, workers)
+    value, wall, flips, steps, capped = cpu_reference(sample, args.n, secs, 1234, workers)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
@@ -171,7 +184,8 @@ def run_reference(args, rank, world):
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": workers, "kind": "port",
                          "sample": f"{workers} independent Taylor-Green meshes of {sample} points, "
                                    f"{secs:.0f} s each; reference kinetic step = movePoint + untangle "
-                                   f"until false + delonize (restart scan), FP64 predicates"},
+                                   f"until false + delonize (restart scan), FP64 predicates; {steps} steps, "
+                                   f"{capped} stopped at the Lawson cap of 64 flips per edge (tangled)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "wall_s": time.perf_counter() - t_all,
     }
@@ -289,11 +303,7 @@ def run_ours(args, rank, world, dist):
     if st["status"] != 0:
         raise RuntimeError(f"engine status {st}")
     tot1 = dt.totals()
-    dev_s = float(step_ms.sum()) / 1e3
-    if dist:
-        t = torch.tensor([dev_s], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dev_s = float(t.item())
+    dev_s = max_over_ranks(float(step_ms.sum()) / 1e3, dist, f"cuda:{local}")
     value = world * n * K / dev_s
     flips = tot1["lawson_flips"] - tot0["lawson_flips"] + tot1["removal_flips"] - tot0["removal_flips"]
     wl_items = (tot1["incircle_tests"] - tot0["incircle_tests"]) - K * (E - 4)
@@ -323,11 +333,7 @@ def run_ours(args, rank, world, dist):
         for k in range(KE):
             L.check(lib.mcl_step_host(dt.handle, host_disp[k].data_ptr(), sp, C.byref(stats)))
         torch.cuda.synchronize()
-        e_s = time.perf_counter() - e0
-        if dist:
-            t = torch.tensor([e_s], device=f"cuda:{local}")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e_s = float(t.item())
+        e_s = max_over_ranks(time.perf_counter() - e0, dist, f"cuda:{local}")
         e2e = {"value": world * n * KE / e_s, "unit": UNIT, "h2d_bytes_per_step": 8 * V,
                "d2h_bytes_per_step": C.sizeof(L.StepStats), "ms_per_step": 1e3 * e_s / KE, "steps": KE}
     clocks = clocks_stop(cp, cf, local)
@@ -350,10 +356,11 @@ def run_ours(args, rank, world, dist):
 
         O.build()
         sample = min(args.cpu_sample, n)
-        v, w_s, fl, steps = cpu_reference(sample, n, args.cpu_seconds, 99, 1)
+        v, w_s, fl, steps, capped = cpu_reference(sample, n, args.cpu_seconds, 99, 1)
         cpu = {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
-               "sample": f"1 core, Taylor-Green mesh of {sample} points for {w_s:.1f} s ({steps} steps); "
-                         f"reference kinetic step = movePoint + untangle until false + delonize (restart scan)"}
+               "sample": f"1 core, Taylor-Green mesh of {sample} points for {w_s:.1f} s ({steps} steps, {capped} "
+                         f"stopped at the Lawson cap); reference kinetic step = movePoint + untangle until false "
+                         f"+ delonize (restart scan)"}
 
     if rank == 0:
         line = {
@@ -476,11 +483,7 @@ def run_batched(args, rank, world, dist):
     tot1 = batch.totals()
     step_ms = np.array([e[0].elapsed_time(e[1]) for e in evs])
     frnn_ms = np.array([e[1].elapsed_time(e[2]) for e in evs])
-    kin_s = float(step_ms.sum()) / 1e3
-    if dist:
-        t = torch.tensor([kin_s], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        kin_s = float(t.item())
+    kin_s = max_over_ranks(float(step_ms.sum()) / 1e3, dist, dev)
     flips = tot1["lawson_flips"] - tot0["lawson_flips"] + tot1["removal_flips"] - tot0["removal_flips"]
     wl_items = (tot1["incircle_tests"] - tot0["incircle_tests"]) - K * (E - 4 * nm)
 

@@ -145,11 +145,15 @@ void orc_ref_kinetic_step(void* h, const float* d, long long* out) {
   int passes = 0;
   while (passes < 64 && m->untangle_pass()) ++passes;
   long long f1 = m->flips;
-  m->delonize_restart_scan();
+  // cap the Lawson loop at 64 flips per edge: the reference never stops on a
+  // mesh its untangling left tangled
+  m->capped = false;
+  m->delonize_restart_scan(64ll * (long long)(m->he.size() / 2));
   long long f2 = m->flips;
   auto t1 = std::chrono::steady_clock::now();
   out[0] = passes; out[1] = f1 - f0; out[2] = f2 - f1;
   out[3] = (long long)std::chrono::duration<double, std::micro>(t1 - t0).count();
+  out[4] = m->capped ? 1 : 0;
 }
 
 long orc_ref_one_ring(void* h, int vi, int* out, long cap) {

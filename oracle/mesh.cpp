@@ -179,10 +179,17 @@ void Mesh::delonize_vertex(int vi) {
 
 // delonize (include/Host_Triangulation.h:305-319): restart the scan from edge 0
 // after every flip.  This is the reference CPU algorithm timed as the baseline.
-bool Mesh::delonize_restart_scan() {
+bool Mesh::delonize_restart_scan(long long max_flips) {
   bool flipped = false;
   bool ready = false;
+  long long n = 0;
   while (!ready) {
+    // the reference loops until no edge flips; on a mesh its untangling left
+    // tangled that may never happen, so the CPU baseline passes a cap
+    if (max_flips >= 0 && n++ >= max_flips) {
+      capped = true;
+      break;
+    }
     ready = true;
     for (int i = 0; i < (int)he.size(); i += 2) {
       if (delonize_edge(i)) {

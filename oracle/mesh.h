@@ -48,7 +48,8 @@ struct Mesh {
   bool add_delaunay_point_ref(P2 p);
   bool delonize_edge(int he_index);
   void delonize_vertex(int v_index);
-  bool delonize_restart_scan();
+  bool delonize_restart_scan(long long max_flips = -1);
+  bool capped = false;  // the last capped restart-scan stopped at its cap
   bool untangle_pass();
   bool untangle_edge(int he_index);
   bool is_ccw_face(int t_index) const;

@@ -204,10 +204,10 @@ class Mesh:
         return bool(lib().orc_ref_delonize(self.h))
 
     def kinetic_step_ref(self, d):
-        out = np.zeros(4, np.int64)
+        out = np.zeros(5, np.int64)
         lib().orc_ref_kinetic_step(self.h, np.ascontiguousarray(d, np.float32).ravel(), out)
         return dict(untangle_passes=int(out[0]), untangle_flips=int(out[1]),
-                    delonize_flips=int(out[2]), seconds=out[3] * 1e-6)
+                    delonize_flips=int(out[2]), seconds=out[3] * 1e-6, capped=bool(out[4]))
 
     def one_ring_ref(self, v):
         buf = np.zeros(4096, np.int32)
