@@ -757,10 +757,17 @@ __device__ bool phase_remove(cg::grid_group& g, const KParams& P, unsigned& stam
 // ---------------------------------------------------------------------------
 // Point location: visibility walk with exact orientation tests from half-edge h.
 // Returns a half-edge of the face containing p; *on is the half-edge p lies on
-// (or -1).  Errors are returned as negative MCL codes.
-__device__ int locate(const KParams& P, float2 p, int h, int* on, LocalCounters& lc) {
+// (or -1).  Errors are returned as negative MCL codes.  With max_steps > 0 the
+// walk stops after that many steps, returns -1 and leaves the face it reached
+// in *resume (a parallel round then waits for the longest walk only that long).
+__device__ int locate(const KParams& P, float2 p, int h, int* on, LocalCounters& lc, int max_steps = 0,
+                      int* resume = nullptr) {
   *on = -1;
   for (int it = 0; it < P.walk_cap; ++it) {
+    if (max_steps > 0 && it == max_steps) {
+      *resume = h;
+      return -1;
+    }
     if (h < 0 || h >= 2 * P.E) return -MCL_ERR_DEGENERATE_INPUT;
     const int hs[3] = {h, he_next(P, h), he_prev(P, h)};
     int o[3];
@@ -887,6 +894,10 @@ __device__ int insert_start(const KParams& P, int v) {
   return P.vroot ? __ldg(P.vroot + v) : 0;
 }
 
+// Steps a point location may take in one insertion round before it waits for
+// the next round (which starts where it stopped).
+constexpr int kWalkSlice = 48;
+
 __device__ bool phase_insert(cg::grid_group& g, const KParams& P, unsigned& stamp,
                              LocalCounters& lc) {
   const int stride = gridDim.x * blockDim.x;
@@ -913,7 +924,14 @@ __device__ bool phase_insert(cg::grid_group& g, const KParams& P, unsigned& stam
     for (int i = gtid; i < n; i += stride) {
       const int v = ld_i(in + i);
       int on = -1;
-      const int h = locate(P, ldpos(P, v), insert_start(P, v), &on, lc);
+      int resume = -1;
+      const int h = locate(P, ldpos(P, v), insert_start(P, v), &on, lc, kWalkSlice, &resume);
+      if (h == -1) {
+        // not there yet: go on from here in the next round
+        P.vloc[v] = resume;
+        P.vlocf[v] = 4;
+        continue;
+      }
       if (h < 0) {
         flag_error_at(P, (-h) & 0xff, 200000 + ((-h) >> 8));
         P.vlocf[v] = -1;
