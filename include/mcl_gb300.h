@@ -141,6 +141,15 @@ int mcl_step(mcl_mesh* m, const mcl_float2* d_dev, void* stream, mcl_step_stats*
 /* Same step with the displacement in host memory (copied in on `stream`). */
 int mcl_step_host(mcl_mesh* m, const mcl_float2* d_host, void* stream, mcl_step_stats* stats_host);
 
+/* Pipelined form of mcl_step_host: returns at once.  The host-to-device copy of
+ * d_host (pinned memory, kept unchanged until the copy is done) runs on a copy
+ * stream of the mesh into one of two staging buffers, overlapping the step in
+ * flight; the step runs on `stream` after its copy, and its counters are
+ * copied into *stats_pinned (pinned host memory, may be NULL) on `stream`.
+ * Synchronise `stream` (or an event recorded on it) before reading them.  No
+ * counterpart in the reference. */
+int mcl_step_host_async(mcl_mesh* m, const mcl_float2* d_host, void* stream, mcl_step_stats* stats_pinned);
+
 /* Counters summed over every call on this mesh since creation (synchronises
  * the device); *calls_host (may be NULL) = number of engine launches. */
 int mcl_mesh_totals(mcl_mesh* m, mcl_step_stats* totals_host, int64_t* calls_host);

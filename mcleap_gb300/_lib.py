@@ -30,7 +30,7 @@ EXPORTS = [
     "mcl_status_string", "mcl_last_error", "mcl_version",
     "mcl_mesh_create_from_aos", "mcl_mesh_build", "mcl_mesh_destroy", "mcl_mesh_sizes",
     "mcl_mesh_download_aos", "mcl_mesh_upload_aos", "mcl_mesh_positions", "mcl_mesh_copy_positions", "mcl_move", "mcl_integrate",
-    "mcl_untangle", "mcl_delaunay_restore", "mcl_step", "mcl_step_host", "mcl_mesh_last_status", "mcl_mesh_totals",
+    "mcl_untangle", "mcl_delaunay_restore", "mcl_step", "mcl_step_host", "mcl_step_host_async", "mcl_mesh_last_status", "mcl_mesh_totals",
     "mcl_one_ring", "mcl_closest_neighbors", "mcl_mesh_frnn",
     "mcl_grid_create", "mcl_grid_destroy", "mcl_grid_update", "mcl_grid_tables", "mcl_grid_describe", "mcl_grid_frnn",
     "mcl_grid_build", "mcl_grid_frnn_ids",
@@ -93,6 +93,7 @@ def lib():
             "mcl_delaunay_restore": ([vp, vp, C.POINTER(StepStats)], i32),
             "mcl_step": ([vp, vp, vp, C.POINTER(StepStats)], i32),
             "mcl_step_host": ([vp, vp, vp, C.POINTER(StepStats)], i32),
+            "mcl_step_host_async": ([vp, vp, vp, vp], i32),
             "mcl_mesh_last_status": ([vp, vp, C.POINTER(StepStats)], i32),
             "mcl_mesh_totals": ([vp, C.POINTER(StepStats), C.POINTER(i64)], i32),
             "mcl_one_ring": ([vp, i32, i32, vp, vp, C.POINTER(i64)], i32),

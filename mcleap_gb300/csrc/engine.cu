@@ -1185,6 +1185,16 @@ void free_mesh(mcl_mesh* m) {
                   m->vcomp, m->vroot, m->cbase, m->table, m->smark, m->fnew, m->act_dev};
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  if (m->dstage2) cudaFree(m->dstage2);
+  if (m->stats_dev) cudaFree(m->stats_dev);
+  if (m->copy_stream) {
+    cudaStreamSynchronize(m->copy_stream);
+    cudaStreamDestroy(m->copy_stream);
+    for (int i = 0; i < 2; ++i) {
+      cudaEventDestroy(m->ev_copied[i]);
+      cudaEventDestroy(m->ev_used[i]);
+    }
+  }
   if (m->st_host) cudaFreeHost(m->st_host);
   if (m->act_host) cudaFreeHost(m->act_host);
   delete[] m->comp_host;
@@ -1787,6 +1797,67 @@ int mcl_step_host(mcl_mesh* m, const mcl_float2* d_host, void* stream, mcl_step_
   cudaStream_t s = (cudaStream_t)stream;
   CK(cudaMemcpyAsync(m->dstage, d_host, 8 * m->V, cudaMemcpyHostToDevice, s));
   return mcl_step(m, reinterpret_cast<const mcl_float2*>(m->dstage), stream, stats);
+}
+
+}  // extern "C"
+
+namespace mcl {
+// the counters of the last launch as an mcl_step_stats, in device memory
+__global__ void k_publish_stats(const DevState* st, mcl_step_stats* out) {
+  if (threadIdx.x != 0) return;
+  const unsigned long long* c = st->last;
+  out->inverted_faces = (int64_t)c[C_INVERTED];
+  out->reverted_vertices = (int64_t)c[C_REVERTED];
+  out->removed_vertices = (int64_t)c[C_REMOVED];
+  out->lawson_flips = (int64_t)c[C_LAWSON_FLIPS];
+  out->lawson_rounds = (int64_t)c[C_LAWSON_ROUNDS];
+  out->removal_flips = (int64_t)c[C_REMOVAL_FLIPS];
+  out->insert_rounds = (int64_t)c[C_INSERT_ROUNDS];
+  out->incircle_tests = (int64_t)c[C_INCIRCLE];
+  out->incircle_fp64 = (int64_t)c[C_INCIRCLE_FP64];
+  out->incircle_exact = (int64_t)c[C_INCIRCLE_EXACT];
+  out->orient_fp64 = (int64_t)c[C_ORIENT_FP64];
+  out->orient_exact = (int64_t)c[C_ORIENT_EXACT];
+  out->sos_decisions = (int64_t)c[C_SOS];
+  out->status = st->last_status;
+  out->error_site = st->last_site;
+}
+}  // namespace mcl
+
+extern "C" {
+
+int mcl_step_host_async(mcl_mesh* m, const mcl_float2* d_host, void* stream, mcl_step_stats* stats_pinned) {
+  if (!m || !d_host) return fail(MCL_ERR_INVALID_ARGUMENT, "null argument");
+  if (!m->valid_cur || m->nact) return fail(MCL_ERR_INVALID_ARGUMENT, "mcl_step_host_async: needs a validated mesh "
+                                                                      "and every mesh of a batch active");
+  cudaStream_t s = (cudaStream_t)stream;
+  if (!m->copy_stream) {
+    CK(cudaMalloc((void**)&m->dstage2, 8 * m->V));
+    CK(cudaMalloc((void**)&m->stats_dev, 2 * sizeof(mcl_step_stats)));
+    CK(cudaStreamCreateWithFlags(&m->copy_stream, cudaStreamNonBlocking));
+    for (int i = 0; i < 2; ++i) {
+      CK(cudaEventCreateWithFlags(&m->ev_copied[i], cudaEventDisableTiming));
+      CK(cudaEventCreateWithFlags(&m->ev_used[i], cudaEventDisableTiming));
+      CK(cudaEventRecord(m->ev_used[i], m->copy_stream));
+    }
+  }
+  const int k = m->stage_idx;
+  m->stage_idx ^= 1;
+  float2* buf = k ? m->dstage2 : m->dstage;
+  // the copy into buffer k waits for the step that last read it, then runs on
+  // the copy stream, overlapping the step in flight on `stream`
+  CK(cudaStreamWaitEvent(m->copy_stream, m->ev_used[k], 0));
+  CK(cudaMemcpyAsync(buf, d_host, 8 * m->V, cudaMemcpyHostToDevice, m->copy_stream));
+  CK(cudaEventRecord(m->ev_copied[k], m->copy_stream));
+  CK(cudaStreamWaitEvent(s, m->ev_copied[k], 0));
+  const int rc = run_step(m, MOVE_DISPLACE, buf, s, nullptr);
+  if (rc != MCL_OK) return rc;
+  CK(cudaEventRecord(m->ev_used[k], s));
+  if (stats_pinned) {
+    k_publish_stats<<<1, 32, 0, s>>>(m->st, m->stats_dev + k);
+    CK(cudaMemcpyAsync(stats_pinned, m->stats_dev + k, sizeof(mcl_step_stats), cudaMemcpyDeviceToHost, s));
+  }
+  return MCL_OK;
 }
 
 int mcl_mesh_last_status(mcl_mesh* m, void* stream, mcl_step_stats* stats) {

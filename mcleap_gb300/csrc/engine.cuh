@@ -293,6 +293,12 @@ struct mcl_mesh {
   int* vlocf;
   float2* target;
   float2* dstage;          // device staging buffer for host displacements
+  // mcl_step_host_async: a second staging buffer, a copy stream, and events
+  float2* dstage2;
+  cudaStream_t copy_stream;
+  cudaEvent_t ev_copied[2], ev_used[2];
+  mcl_step_stats* stats_dev;  // [2] published counters of the pipelined steps
+  int stage_idx;
   unsigned long long* scratch;  // small device scratch for query counters
   mcl::DevState* st;
   mcl::DevState* st_host;  // pinned mirror

@@ -420,3 +420,43 @@ def test_errors_are_reported(M):
     ht.m_he[5, 0] = 10 ** 6
     with pytest.raises(McleapError):
         M.DeviceTriangulation(ht)
+
+
+def test_step_host_async_matches_step(M):
+    """The pipelined host-displacement call gives the same meshes and counters."""
+    import ctypes as C
+
+    import torch
+
+    from mcleap_gb300 import _lib as L
+
+    n = 8000
+    pts = uniform_points(n, 31)
+    ht1, _ = build_pair(M, pts)
+    ht2 = M.HostTriangulation()
+    ht2.m_pos, ht2.m_v, ht2.m_he, ht2.m_t = [a.copy() for a in (ht1.m_pos, ht1.m_v, ht1.m_he, ht1.m_t)]
+    a, b = M.DeviceTriangulation(ht1), M.DeviceTriangulation(ht2)
+    pos = ht1.m_pos.copy()
+    nstat = C.sizeof(L.StepStats)
+    pin = torch.empty(6 * nstat, dtype=torch.uint8, pin_memory=True)
+    hosts, want = [], []
+    stream = torch.cuda.Stream()
+    for k in range(6):
+        d = gaussian_disp(n + 4, 0.3 * spacing(n), 60 + k, clamp_pos=pos)
+        pos = (pos + d).astype(np.float32)
+        want.append(a.step(cuda(d)))
+        hosts.append(torch.from_numpy(d).pin_memory())
+    for k in range(6):
+        L.check(L.lib().mcl_step_host_async(b.handle, hosts[k].data_ptr(), stream.cuda_stream,
+                                            pin.data_ptr() + k * nstat))
+    stream.synchronize()
+    for k in range(6):
+        got = L.StepStats.from_address(pin.data_ptr() + k * nstat).as_dict()
+        # the classification's counts are deterministic; how many vertices the
+        # repair sends back depends on thread timing (the result does not)
+        assert got["status"] == 0 and got["inverted_faces"] == want[k]["inverted_faces"], k
+        assert got["incircle_tests"] > 0
+    a.transferToHost()
+    b.transferToHost()
+    assert np.array_equal(ht1.m_pos, ht2.m_pos)
+    assert np.array_equal(ht1.edges(), ht2.edges())
