@@ -77,12 +77,22 @@ __device__ __forceinline__ bool enqueue_once(const KParams& P, int e, unsigned s
   return atomicMax(P.qmark + e, stamp) < stamp;
 }
 
+// Called by every thread of the block (it holds a block barrier).
 __device__ void flush_counters(const KParams& P, LocalCounters& lc) {
-  // warp-reduce the common counter, atomics for the rare ones
+  // the common counter is reduced over the block (one atomic per block: one
+  // per warp on a single address cost microseconds at the end of every step),
+  // atomics for the rare ones
+  __shared__ unsigned long long part[kThreads / 32];
   unsigned long long inc = lc.incircle;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) inc += __shfl_down_sync(kFull, inc, o);
-  if ((threadIdx.x & 31) == 0 && inc) atomicAdd(&P.st->c[C_INCIRCLE], inc);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = inc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long t = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += part[w];
+    if (t) atomicAdd(&P.st->c[C_INCIRCLE], t);
+  }
   if (lc.incircle_fp64) atomicAdd(&P.st->c[C_INCIRCLE_FP64], (unsigned long long)lc.incircle_fp64);
   if (lc.incircle_exact) atomicAdd(&P.st->c[C_INCIRCLE_EXACT], (unsigned long long)lc.incircle_exact);
   if (lc.orient_fp64) atomicAdd(&P.st->c[C_ORIENT_FP64], (unsigned long long)lc.orient_fp64);
@@ -156,6 +166,23 @@ __device__ __forceinline__ bool resolve_edge(const KParams& P, int e, LocalCount
 // whole filter.  Edges the filters cannot decide (a few per million) go to the
 // hard list, which is resolved with the full ladder after the barrier; the
 // caller must call phase_classify_hard before reading `inverted`.
+__device__ __forceinline__ void timeline(const KParams& P, int slot) {
+  if (blockIdx.x == 0 && threadIdx.x == 0 && slot < kTimeline) {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    P.st->ts[slot] = t;
+  }
+}
+
+// the latest time any block reached this point
+__device__ __forceinline__ void timeline_max(const KParams& P, int slot) {
+  if (threadIdx.x == 0 && slot >= 43 && slot < 47) {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    atomicMax(&P.st->tsmax[slot - 43], t);
+  }
+}
+
 // Edges per thread and iteration of the classification pass.
 constexpr int kClassifyUnroll = 4;
 
@@ -168,7 +195,9 @@ __device__ void phase_classify(cg::grid_group& g, const KParams& P, unsigned qst
       const int v = vert_at(P, i);
       __stcg(P.pos + v, moved_pos(P, v));
     }
+    if (kFixedPos) timeline_max(P, 43);
     g.sync();
+    if (kFixedPos) timeline_max(P, 44);
   }
   int bad = 0;
   unsigned ninc = 0;
@@ -256,6 +285,7 @@ __device__ void phase_classify(cg::grid_group& g, const KParams& P, unsigned qst
   }
   lc.incircle += ninc;
   if (bad) atomicAdd(&P.st->inverted, bad);
+  if (kFixedPos) timeline_max(P, 45);
 }
 
 // Resolve the hard list of phase_classify (after its barrier) with the full
@@ -282,14 +312,6 @@ __device__ void phase_classify_hard(cg::grid_group& g, const KParams& P, unsigne
   }
   if (bad) atomicAdd(&P.st->inverted, bad);
   g.sync();
-}
-
-__device__ __forceinline__ void timeline(const KParams& P, int slot) {
-  if (blockIdx.x == 0 && threadIdx.x == 0 && slot < kTimeline) {
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    P.st->ts[slot] = t;
-  }
 }
 
 __device__ __forceinline__ void timeline_insert(const KParams& P, int round, int k) {
@@ -1029,6 +1051,10 @@ __device__ void finish_launch(const KParams& P, unsigned stamp) {
     st->c[i] = 0;
   }
   st->calls += 1;
+  for (int i = 0; i < 4; ++i) {
+    st->ts[43 + i] = st->tsmax[i];
+    st->tsmax[i] = 0;
+  }
   st->last_status = st->status;
   st->last_site = st->site;
   st->status = 0;

@@ -73,7 +73,8 @@ struct DevState {
   unsigned long long calls;
   int dbg[68];             // first failing vertex star: v, deg, then neighbour ids
   unsigned long long ts[kTimeline];  // %globaltimer at phase boundaries of the last launch
-  unsigned long long ts_insert[64];  // insertion round r < 16: [4r] located, [4r+1] won, [4r+2] split, [4r+3] flips done
+  unsigned long long ts_insert[64];
+  unsigned long long tsmax[4];      // latest block at marks of the running launch (published to ts[43..46])  // insertion round r < 16: [4r] located, [4r+1] won, [4r+2] split, [4r+3] flips done
   // mcl_settle_moves: [0] last stamp used, [1..3] moves sent back per pass
   // (triple-buffered), [4] sent back by the last call, [5] status of the last call
   unsigned int settle[8];
