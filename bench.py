@@ -303,6 +303,8 @@ def run_ours(args, rank, world, dist):
     if st["status"] != 0:
         raise RuntimeError(f"engine status {st}")
     tot1 = dt.totals()
+    if tot1["failed_launches"] != tot0["failed_launches"]:
+        raise RuntimeError(f"{tot1['failed_launches'] - tot0['failed_launches']} timed steps failed")
     dev_s = max_over_ranks(float(step_ms.sum()) / 1e3, dist, f"cuda:{local}")
     value = world * n * K / dev_s
     flips = tot1["lawson_flips"] - tot0["lawson_flips"] + tot1["removal_flips"] - tot0["removal_flips"]
@@ -366,7 +368,8 @@ def run_ours(args, rank, world, dist):
                   "served": {k: sv[k] for k in ("p50_ms", "p99_ms", "p999_ms", "pts_steps_per_s", "completed",
                                                 "submitted", "iterations")},
                   "plain": {k: pl[k] for k in ("p50_ms", "p99_ms", "p999_ms", "pts_steps_per_s", "completed",
-                                               "submitted", "iterations")}}
+                                               "submitted", "iterations")},
+                  "capacity": info["capacity"]}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -499,6 +502,8 @@ def run_batched(args, rank, world, dist):
     if st["status"] != 0:
         raise RuntimeError(f"batched step failed: {st}")
     tot1 = batch.totals()
+    if tot1["failed_launches"] != tot0["failed_launches"]:
+        raise RuntimeError(f"{tot1['failed_launches'] - tot0['failed_launches']} batched steps failed")
     step_ms = np.array([e[0].elapsed_time(e[1]) for e in evs])
     frnn_ms = np.array([e[1].elapsed_time(e[2]) for e in evs])
     kin_s = max_over_ranks(float(step_ms.sum()) / 1e3, dist, dev)
@@ -520,9 +525,8 @@ def run_batched(args, rank, world, dist):
                 g.replay()
                 ge[r][1].record(stream)
         stream.synchronize()
-        st = batch.status(stream)
-        if st["status"] != 0:
-            raise RuntimeError(f"graph replay failed: {st}")
+        if batch.totals()["failed_launches"] != tot1["failed_launches"]:
+            raise RuntimeError("a replayed step failed")
         gms = np.array([a.elapsed_time(b) for a, b in ge]) / 2
         graph = {"ms_per_step": float(gms.mean()), "p50": float(np.median(gms)), "p99": float(np.percentile(gms, 99)),
                  "pts_steps_per_s": npts / (gms.mean() / 1e3), "steps": 2 * reps,
@@ -555,7 +559,7 @@ def run_batched(args, rank, world, dist):
             m.frnn(radius[i:i + 1], F, oi, stream=stream, sync=False)
         pw[k][1].record(stream)
     stream.synchronize()
-    bad = [i for i, m in enumerate(singles[:64]) if m.status(stream)["status"] != 0]
+    bad = [i for i, m in enumerate(singles) if m.totals()["failed_launches"] != 0]
     plain_step_s = sum(a.elapsed_time(b) for row in pe for a, b in row) / 1e3
     plain_wall_s = sum(a.elapsed_time(b) for a, b in pw) / 1e3
 
@@ -631,9 +635,25 @@ def serving_measure(nm, rate, duration, drain, budget_gb, seed):
     done2 = server.serve(reqs2, batched=False, realtime=True, time_limit=duration + drain)
     plain = S.latency_summary(done2, server.wall, server.point_steps, len(reqs2))
     plain["iterations"] = server.iterations - it1
+    # capacity: the same requests all submitted at once (closed loop), served
+    # with continuous batching and in the plain form; work done / wall time
+    cap = {}
+    for mode, batched in (("served", True), ("plain", False)):
+        server.point_steps = 0
+        rq = S.poisson_requests(server.n, rate, duration, seed=seed + 72, mesh_sizes=sizes)
+        for r in rq:
+            r.t_arrival = 0.0
+        dn = server.serve(rq, batched=batched, realtime=False, time_limit=drain + duration)
+        summ = S.latency_summary(dn, server.wall, server.point_steps, len(rq))
+        cap[mode] = {k: summ[k] for k in ("completed", "submitted", "wall_s", "pts_steps_per_s",
+                                          "query_vertices_per_s", "requests_per_s")}
+    cap["speedup_pts_steps"] = cap["served"]["pts_steps_per_s"] / max(cap["plain"]["pts_steps_per_s"], 1e-9)
+    cap["speedup_requests"] = cap["served"]["requests_per_s"] / max(cap["plain"]["requests_per_s"], 1e-9)
+    frozen = float(server.frozen.float().mean().item())
     info = {"meshes": server.n, "points": int(sizes.sum()), "admitted": len(server.admitted),
             "rejected": len(server.rejected), "budget_used_gb": server.admission.used / 1e9,
-            "rate": rate, "duration_s": duration, "setup_s": t_setup, "launches": launches}
+            "rate": rate, "duration_s": duration, "setup_s": t_setup, "launches": launches,
+            "capacity": cap, "frozen_fraction_at_end": frozen}
     server.batch.close()
     return served, plain, info
 
@@ -653,6 +673,7 @@ def run_serving(args, rank, world, dist):
     cp, cf = clocks_start()
     served, plain, info = serving_measure(nm, args.rate, args.duration, args.drain_limit, args.budget_gb, 5 + rank)
     clocks = clocks_stop(cp, cf, local)
+    capacity = info.pop("capacity")
     line = {
         "metric": "served kinetic pts*steps/s with p50/p99/p99.9 request latency (continuous batching)",
         "value": served["pts_steps_per_s"], "unit": UNIT, "n_gpus": world, "steps": served["iterations"],
@@ -663,7 +684,7 @@ def run_serving(args, rank, world, dist):
                                 "aggregation updates (k in 1..16), half FRNN / one-ring batches of 1e3..1e5 "
                                 f"vertices; HBM budget {args.budget_gb:g} GB",
                        parallelism=f"replicas x{world}", **info),
-        "served": served, "plain": plain,
+        "served": served, "plain": plain, "capacity": capacity,
         "speedup_vs_plain": served["pts_steps_per_s"] / max(plain["pts_steps_per_s"], 1e-9),
         "p50_latency_ratio_plain_over_served": plain["p50_ms"] / max(served["p50_ms"], 1e-9),
         "clocks": clocks, "gpu_launches": info["launches"],

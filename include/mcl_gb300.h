@@ -74,6 +74,7 @@ typedef struct {
   int64_t sos_decisions;         /* exactly cocircular quads decided by perturbation */
   int64_t status;                /* MCL_OK or an error code */
   int64_t error_site;            /* engine source location that reported `status` */
+  int64_t failed_launches;       /* launches that ended with an error (totals: since creation) */
 } mcl_step_stats;
 
 /* ---- library ------------------------------------------------------------ */
@@ -151,7 +152,9 @@ int mcl_step_host(mcl_mesh* m, const mcl_float2* d_host, void* stream, mcl_step_
 int mcl_step_host_async(mcl_mesh* m, const mcl_float2* d_host, void* stream, mcl_step_stats* stats_pinned);
 
 /* Counters summed over every call on this mesh since creation (synchronises
- * the device); *calls_host (may be NULL) = number of engine launches. */
+ * the device); *calls_host (may be NULL) = number of engine launches.  Check
+ * failed_launches after a run of asynchronous steps: status reports only the
+ * last launch. */
 int mcl_mesh_totals(mcl_mesh* m, mcl_step_stats* totals_host, int64_t* calls_host);
 
 /* Status of the last asynchronous step on this mesh (synchronises the stream). */

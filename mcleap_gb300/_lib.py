@@ -55,7 +55,7 @@ class AosView(C.Structure):
 
 STAT_FIELDS = ["inverted_faces", "reverted_vertices", "removed_vertices", "lawson_flips", "lawson_rounds",
                "removal_flips", "insert_rounds", "incircle_tests", "incircle_fp64", "incircle_exact",
-               "orient_fp64", "orient_exact", "sos_decisions", "status", "error_site"]
+               "orient_fp64", "orient_exact", "sos_decisions", "status", "error_site", "failed_launches"]
 
 
 class StepStats(C.Structure):

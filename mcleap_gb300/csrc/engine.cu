@@ -890,12 +890,16 @@ __device__ __forceinline__ bool face_has_corner(const KParams& P, int h) {
   return (a >= 0 && P.vfix[a]) || (b >= 0 && P.vfix[b]) || (c >= 0 && P.vfix[c]);
 }
 
-__device__ int insert_start(const KParams& P, int v) {
+// In later rounds of an insertion phase the hint is where the vertex's last
+// walk ended (located, or paused): it is taken as it is, or a walk paused in a
+// corner's fan would be sent back to its anchor every round and never arrive.
+__device__ int insert_start(const KParams& P, int v, bool resume) {
   int h = __ldcg(P.vhint + v);
   const bool hint_ok = h >= 0 && h < 2 * P.E && he_origin(P, h) >= 0 && he_apex(P, h) >= 0;
-  // a start on a bounding corner's fan of long hull triangles makes the walk
-  // step along the hull one triangle at a time: prefer a face of the anchor
-  // neighbour that has no corner
+  if (resume && hint_ok) return h;
+  // a first start on a bounding corner's fan of long hull triangles makes the
+  // walk step along the hull one triangle at a time: prefer a face of the
+  // anchor neighbour that has no corner
   if (hint_ok && !face_has_corner(P, h)) return h;
   int x = __ldcg(P.vaux + v);
   for (int hop = 0; hop < 64 && x >= 0 && x < P.V; ++hop) {
@@ -947,7 +951,7 @@ __device__ bool phase_insert(cg::grid_group& g, const KParams& P, unsigned& stam
       const int v = ld_i(in + i);
       int on = -1;
       int resume = -1;
-      const int h = locate(P, ldpos(P, v), insert_start(P, v), &on, lc, kWalkSlice, &resume);
+      const int h = locate(P, ldpos(P, v), insert_start(P, v, round > 0), &on, lc, kWalkSlice, &resume);
       if (h == -1) {
         // not there yet: go on from here in the next round
         P.vloc[v] = resume;
@@ -1051,6 +1055,7 @@ __device__ void finish_launch(const KParams& P, unsigned stamp) {
     st->c[i] = 0;
   }
   st->calls += 1;
+  if (st->status != MCL_OK) st->failed += 1;
   for (int i = 0; i < 4; ++i) {
     st->ts[43 + i] = st->tsmax[i];
     st->tsmax[i] = 0;
@@ -1507,7 +1512,10 @@ static int launch_engine(mcl_mesh* m, KParams& P, cudaStream_t s) {
 
 static void fill_stats_from(const unsigned long long* c, int status, int site, mcl_step_stats* o);
 
-static void fill_stats(const DevState& s, mcl_step_stats* o) { fill_stats_from(s.last, s.last_status, s.last_site, o); }
+static void fill_stats(const DevState& s, mcl_step_stats* o) {
+  fill_stats_from(s.last, s.last_status, s.last_site, o);
+  o->failed_launches = s.last_status != MCL_OK ? 1 : 0;
+}
 
 static void fill_stats_from(const unsigned long long* c, int status, int site, mcl_step_stats* o) {
   struct { const unsigned long long* c; } s{c};
@@ -1526,6 +1534,7 @@ static void fill_stats_from(const unsigned long long* c, int status, int site, m
   o->sos_decisions = (int64_t)s.c[C_SOS];
   o->status = status;
   o->error_site = site;
+  o->failed_launches = 0;
 }
 
 static int finish(mcl_mesh* m, cudaStream_t s, mcl_step_stats* stats) {
@@ -1662,6 +1671,7 @@ int mcl_mesh_totals(mcl_mesh* m, mcl_step_stats* totals, int64_t* calls) {
   CK(cudaMemcpy(m->st_host, m->st, sizeof(DevState), cudaMemcpyDeviceToHost));
   const DevState& t = *m->st_host;
   fill_stats_from(t.tot, t.last_status, t.last_site, totals);
+  totals->failed_launches = (int64_t)t.failed;
   if (calls) *calls = (int64_t)t.calls;
   return MCL_OK;
 }
@@ -1847,6 +1857,7 @@ __global__ void k_publish_stats(const DevState* st, mcl_step_stats* out) {
   out->sos_decisions = (int64_t)c[C_SOS];
   out->status = st->last_status;
   out->error_site = st->last_site;
+  out->failed_launches = st->last_status != MCL_OK ? 1 : 0;
 }
 }  // namespace mcl
 

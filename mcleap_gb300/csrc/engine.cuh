@@ -71,6 +71,7 @@ struct DevState {
   unsigned long long last[C_COUNT];
   unsigned long long tot[C_COUNT];  // running totals over all launches
   unsigned long long calls;
+  unsigned long long failed;       // launches that ended with an error
   int dbg[68];             // first failing vertex star: v, deg, then neighbour ids
   unsigned long long ts[kTimeline];  // %globaltimer at phase boundaries of the last launch
   unsigned long long ts_insert[64];

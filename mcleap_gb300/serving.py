@@ -232,6 +232,8 @@ class MeshServer:
             if qs:
                 self._queries(qs, keep_results)
             self.stream.synchronize()
+            if stepping:
+                self.batch.status(self.stream)  # raises if this iteration's step failed
             self.iterations += 1
             t_end = time.perf_counter() - t0
             for r in stepping + qs:
