@@ -446,7 +446,8 @@ def run_batched(args, rank, world, dist):
     V, E, npts = batch.V, batch.E, int(sizes.sum())
     h = (8192.0 / np.sqrt(sizes)).astype(np.float32)
     sigma = torch.tensor(0.1 * h, dtype=torch.float32, device=dev)
-    radius = torch.tensor(2.0 * h, dtype=torch.float32, device=dev)
+    radius_host = (2.0 * h).astype(np.float32)
+    radius = torch.tensor(radius_host, dtype=torch.float32, device=dev)
     F = 48
     d = torch.zeros((V, 2), dtype=torch.float32, device=dev)
     out = torch.empty(V * F, dtype=torch.int32, device=dev)
@@ -464,7 +465,7 @@ def run_batched(args, rank, world, dist):
         L.check(lib.mcl_step(m.handle, L.ptr(dd), s.cuda_stream, None))
         if with_events:
             with_events[1].record(s)
-        m.frnn(radius, F, outp, stream=s, sync=False)
+        m.frnn_grid(radius_host, radius, F, outp, stream=s, sync=False)
         if with_events:
             with_events[2].record(s)
 
@@ -587,7 +588,8 @@ def run_batched(args, rank, world, dist):
         "step_ms": {"p50": float(np.median(step_ms)), "p99": float(np.percentile(step_ms, 99)),
                     "max": float(step_ms.max())},
         "per_step": {"flips": flips / K, "worklist_items": wl_items / K},
-        "frnn": {"ms": float(frnn_ms.mean()), "max_nb": F, "pts_per_s": npts / (frnn_ms.mean() / 1e3)},
+        "frnn": {"ms": float(frnn_ms.mean()), "max_nb": F, "pts_per_s": npts / (frnn_ms.mean() / 1e3),
+                 "method": "per-mesh grids (mcl_batch_frnn_grid); the plain loop uses the mesh walk per mesh"},
         "pipeline_graph": graph,
         "plain": {"steps": KP, "kinetic_pts_steps_per_s": npts * KP / plain_step_s,
                   "launch_gaps_included_pts_steps_per_s": npts * KP / plain_wall_s,
@@ -597,7 +599,10 @@ def run_batched(args, rank, world, dist):
         "autotune": {"best": best, "trials": len(trials), "seconds": t_tune},
         "predicates": {k: tot1[k] - tot0[k] for k in ("incircle_tests", "incircle_fp64", "incircle_exact",
                                                       "orient_fp64", "orient_exact", "sos_decisions")},
-        "clocks": clocks, "gpu_launches": K * 5,
+        # per step: k_walk + k_advance, k_settle, k_step, and the grid FRNN
+        # (k_bgrid_hash, 3 scan kernels, k_bgrid_scatter, k_grid_sort_cells,
+        # k_gather, k_bgrid_frnn)
+        "clocks": clocks, "gpu_launches": K * 12,
         "setup_s": {"build_meshes": t_build, "batch": t_batch},
     }
     if rank == 0:

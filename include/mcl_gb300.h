@@ -286,6 +286,13 @@ int mcl_batch_download_aos(mcl_mesh* m, int64_t i, mcl_float2* pos_host, int32_t
  * r_dev[i] for the vertices of mesh i (a plain mesh reads r_dev[0]). */
 int mcl_batch_frnn(mcl_mesh* m, const float* r_dev, int layout, int max_frnn, int32_t* out_dev, void* stream,
                    int64_t* overflow_host);
+/* mcl_batch_frnn (ROW layout) over per-mesh uniform grids instead of mesh
+ * walks: mesh c gets a grid over [lo, hi)^2 with cells of its radius r_host[c]
+ * (r_dev holds the same radii on the device); one counting sort of every
+ * point, one query kernel.  Same rows as mcl_batch_frnn (ascending vertex
+ * ids); max_frnn <= 49; every mesh of the batch (no active subset). */
+int mcl_batch_frnn_grid(mcl_mesh* m, const float* r_host, const float* r_dev, float lo, float hi, int max_frnn,
+                        int32_t* out_dev, void* stream, int64_t* overflow_host);
 /* Mesh FRNN (getFRNN semantics) for a list of query vertices: row q of out_dev
  * (n rows, COLUMN or ROW layout with the count slot) holds the neighbours of
  * verts_dev[q] within r_dev[its mesh], ascending. */

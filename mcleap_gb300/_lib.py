@@ -36,7 +36,7 @@ EXPORTS = [
     "mcl_grid_build", "mcl_grid_frnn_ids",
     "mcl_batch_create", "mcl_batch_count", "mcl_batch_range", "mcl_batch_vertex_mesh", "mcl_batch_download_aos",
     "mcl_batch_frnn", "mcl_mesh_clone", "mcl_mesh_set_tuning", "mcl_mesh_get_tuning", "mcl_walk",
-    "mcl_settle_moves", "mcl_dla_freeze", "mcl_batch_frnn_list", "mcl_one_ring_list", "mcl_batch_set_active",
+    "mcl_settle_moves", "mcl_dla_freeze", "mcl_batch_frnn_list", "mcl_one_ring_list", "mcl_batch_set_active", "mcl_batch_frnn_grid",
     "mcl_grid_mean_occupancy", "mcl_debug_predicates_host", "mcl_debug_predicates_device", "mcl_mesh_validate", "mcl_debug_state", "mcl_debug_timeline", "mcl_grid_frnn_noalloc", "mcl_debug_counters",
     "mcl_debug_insert_timeline",
 ]
@@ -132,6 +132,7 @@ def lib():
             "mcl_batch_frnn_list": ([vp, vp, vp, i64, i32, i32, vp, vp, C.POINTER(i64)], i32),
             "mcl_one_ring_list": ([vp, vp, i64, i32, i32, vp, vp, C.POINTER(i64)], i32),
             "mcl_batch_set_active": ([vp, vp, i64, vp], i32),
+            "mcl_batch_frnn_grid": ([vp, vp, vp, f32, f32, i32, vp, vp, C.POINTER(i64)], i32),
         }
         for name, (args, res) in sig.items():
             fn = getattr(L, name)

@@ -169,6 +169,15 @@ class MeshBatch:
         a = np.ascontiguousarray(meshes, np.int32)
         L.check(L.lib().mcl_batch_set_active(self.handle, L.ptr(a), len(a), _stream_ptr(stream)))
 
+    def frnn_grid(self, r_host, r, max_frnn, out, lo=0.0, hi=8192.0, stream=None, sync=True):
+        """The rows of ``frnn`` (ROW layout) from per-mesh grids; ``r_host`` and
+        ``r`` hold the same per-mesh radii on the host and the device."""
+        rh = np.ascontiguousarray(r_host, np.float32)
+        ov = C.c_int64()
+        L.check(L.lib().mcl_batch_frnn_grid(self.handle, L.ptr(rh), L.ptr(r), float(lo), float(hi), int(max_frnn),
+                                            L.ptr(out), _stream_ptr(stream), C.byref(ov) if sync else None))
+        return ov.value if sync else None
+
     def frnn_list(self, r, verts, max_frnn, out, layout=L.LAYOUT_ROW, stream=None, sync=True):
         ov = C.c_int64()
         L.check(L.lib().mcl_batch_frnn_list(self.handle, L.ptr(r), L.ptr(verts), int(verts.numel()), layout,

@@ -1213,7 +1213,9 @@ void free_mesh(mcl_mesh* m) {
   void* ptrs[] = {m->pos[0], m->pos[1], m->ev, m->en, m->vhe, m->vfix, m->cand, m->win, m->qmark, m->efa, m->hard,
                   m->wl[0], m->wl[1], m->vl[0], m->vl[1], m->vmark, m->claim, m->vfree, m->vhint,
                   m->vaux, m->vloc, m->vlocf, m->target, m->dstage, m->scratch, m->st,
-                  m->vcomp, m->vroot, m->cbase, m->table, m->smark, m->fnew, m->act_dev};
+                  m->vcomp, m->vroot, m->cbase, m->table, m->smark, m->fnew, m->act_dev,
+                  m->bg_cell, m->bg_src, m->bg_perm, m->bg_pos, m->bg_count, m->bg_start, m->bg_cursor,
+                  m->bg_tmp, m->bg_par};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (m->dstage2) cudaFree(m->dstage2);
@@ -1228,6 +1230,7 @@ void free_mesh(mcl_mesh* m) {
   }
   if (m->st_host) cudaFreeHost(m->st_host);
   if (m->act_host) cudaFreeHost(m->act_host);
+  if (m->bg_par_host) cudaFreeHost(m->bg_par_host);
   delete[] m->comp_host;
   delete[] m->act_list;
   delete[] m->dirty;

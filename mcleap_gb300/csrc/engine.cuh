@@ -324,6 +324,19 @@ struct mcl_mesh {
   int* smark;              // per vertex: stamp of the settle pass that found it coincident
   int settle_blocks;       // k_settle grid (cooperative)
   unsigned char* fnew;     // per vertex: newly frozen flags of mcl_dla_freeze
+  // mcl_batch_frnn_grid: one uniform grid per mesh, cells of all meshes in one table
+  int* bg_cell;            // per vertex: its cell (-1: bounding corner)
+  int* bg_src;             // per sorted slot: vertex
+  int* bg_perm;            // per vertex: sorted slot
+  float2* bg_pos;          // per sorted slot: position
+  int* bg_count;           // per cell
+  int* bg_start;
+  int* bg_cursor;
+  int* bg_tmp;             // scan scratch
+  int4* bg_par;            // per mesh: {cell size bits, cells per side, first cell, 0}
+  int4* bg_par_host;       // pinned copy of the uploaded grid parameters
+  int64_t bg_cap;          // cells the tables hold
+  int64_t bg_cells;        // cells of the uploaded parameters (0: none yet)
   // active meshes (mcl_batch_set_active)
   int nact;                // 0 = all
   int act_E, act_V;

@@ -1014,6 +1014,223 @@ int mcl_grid_mean_occupancy(mcl_grid* g, float* mean) {
 }  // extern "C"
 
 // ---------------------------------------------------------------------------
+// Batch FRNN over per-mesh grids (mcl_batch_frnn_grid): mesh c gets a uniform
+// grid over [lo, hi)^2 with cells of its own radius (so the disk touches at
+// most 3 x 3 cells), its cells numbered after those of the meshes before it;
+// one counting sort orders every point of every mesh, then one query kernel
+// answers every point with its own mesh's grid.  Same results as
+// mcl_batch_frnn (rows ascending), without walking the mesh.
+namespace {
+
+__device__ __forceinline__ int bg_coord(float p, float lo, float c, int n) {
+  float kf = floorf(__fdiv_rn(__fsub_rn(p, lo), c));
+  kf = fminf(fmaxf(kf, -1.0e9f), 1.0e9f);
+  const int k = (int)kf;
+  return k < 0 ? 0 : (k >= n ? n - 1 : k);
+}
+
+__global__ void k_bgrid_hash(int V, const float2* pos, const unsigned char* vfix, const int* vcomp, const int4* par,
+                             float lo, int* cell, int* count, int* out, int F) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= V) return;
+  if (vfix[v]) {  // bounding corners hold no neighbour within any radius
+    cell[v] = -1;
+    out[(size_t)v * F] = 0;
+    return;
+  }
+  const int4 q = par[vcomp ? vcomp[v] : 0];
+  const float c = __int_as_float(q.x);
+  const float2 p = pos[v];
+  const int x = bg_coord(p.x, lo, c, q.y), y = bg_coord(p.y, lo, c, q.y);
+  const int id = q.z + y * q.y + x;
+  cell[v] = id;
+  atomicAdd(count + id, 1);
+}
+
+__global__ void k_bgrid_scatter(int V, const int* cell, int* cursor, int* perm, int* src) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= V || cell[v] < 0) return;
+  const int slot = atomicAdd(cursor + cell[v], 1);
+  perm[v] = slot;
+  src[slot] = v;
+}
+
+// One thread per sorted slot (neighbouring points of one cell row of one
+// mesh); disk-culled rows of the mesh's grid, branch-free candidate test,
+// ids staged per thread in shared memory, sorted there and written out one row
+// per warp step.  Rows: out[v*F] = count, out[v*F + 1 + k] ascending.
+constexpr int kBStage = 48;
+
+__global__ void __launch_bounds__(kFrnnThreads) k_bgrid_frnn(int n, const float2* __restrict__ spos,
+                                                            const int* __restrict__ src, const int* __restrict__ vcomp,
+                                                            const int4* __restrict__ par, const float* __restrict__ rc,
+                                                            float lo, const int* __restrict__ start,
+                                                            const int* __restrict__ count, int F, int* __restrict__ out,
+                                                            unsigned long long* overflow) {
+  __shared__ int stage[kFrnnThreads * (kBStage + 1)];
+  __shared__ int cnts[kFrnnThreads];
+  __shared__ int rows[kFrnnThreads];
+  const int t = threadIdx.x, row0 = blockIdx.x * kFrnnThreads, i = row0 + t;
+  int* mine = stage + t * (kBStage + 1);
+  const int cap = F - 1;  // <= kBStage (checked by the host)
+  int nf = 0;
+  if (i < n) {
+    const int v = __ldg(src + i);
+    rows[t] = v;
+    const int mesh = vcomp ? __ldg(vcomp + v) : 0;
+    const int4 q = __ldg(par + mesh);
+    const float c = __int_as_float(q.x), inv = 1.0f / c;
+    const float r = __ldg(rc + mesh);
+    const float r2 = __fmul_rn(r, r);
+    const float2 p = spos[i];
+    const int nx = q.y;
+    const float mg = 1e-3f * c + 1e-5f * (fabsf(p.x) + fabsf(p.y) + fabsf(lo) + r);
+    const float px = p.x - lo, py = p.y - lo;
+    int ylo = (int)floorf(fmaxf(fminf((py - r - mg) * inv, 1e9f), -1e9f));
+    int yhi = (int)floorf(fmaxf(fminf((py + r + mg) * inv, 1e9f), -1e9f));
+    ylo = ylo < 0 ? 0 : (ylo >= nx ? nx - 1 : ylo);
+    yhi = yhi < 0 ? 0 : (yhi >= nx ? nx - 1 : yhi);
+    for (int yy = ylo; yy <= yhi; ++yy) {
+      float slo = yy * c, shi = slo + c;
+      if (yy == 0) slo = -INFINITY;
+      if (yy == nx - 1) shi = INFINITY;
+      const float dym = fmaxf(fmaxf(slo - py, py - shi) - mg, 0.f);
+      const float hw = sqrtf(fmaxf(r2 - dym * dym, 0.f)) * 1.0001f + mg;
+      int xlo = (int)floorf(fmaxf(fminf((px - hw) * inv, 1e9f), -1e9f));
+      int xhi = (int)floorf(fmaxf(fminf((px + hw) * inv, 1e9f), -1e9f));
+      xlo = xlo < 0 ? 0 : (xlo >= nx ? nx - 1 : xlo);
+      xhi = xhi < 0 ? 0 : (xhi >= nx ? nx - 1 : xhi);
+      const int base = q.z + yy * nx;
+      const int b = __ldg(start + base + xlo);
+      const int e = __ldg(start + base + xhi) + __ldg(count + base + xhi);
+      if (nf + (e - b) <= cap) {
+#pragma unroll 4
+        for (int j = b; j < e; ++j) {
+          const float2 o = spos[j];
+          const float dx = __fsub_rn(p.x, o.x), dy = __fsub_rn(p.y, o.y);
+          const bool hit = (__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)) <= r2) & (j != i);
+          mine[nf] = j;
+          nf += hit ? 1 : 0;
+        }
+      } else {
+        for (int j = b; j < e; ++j) {
+          const float2 o = spos[j];
+          const float dx = __fsub_rn(p.x, o.x), dy = __fsub_rn(p.y, o.y);
+          if ((__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)) <= r2) & (j != i)) {
+            if (nf < cap) mine[nf] = j;
+            ++nf;
+          }
+        }
+      }
+    }
+    if (nf > cap) atomicAdd(overflow, 1ull);
+    const int m = nf < cap ? nf : cap;
+    // vertex ids, ascending
+    for (int a = 0; a < m; ++a) mine[a] = __ldg(src + mine[a]);
+    for (int a = 1; a < m; ++a) {
+      const int x = mine[a];
+      int bb = a - 1;
+      while (bb >= 0 && mine[bb] > x) { mine[bb + 1] = mine[bb]; --bb; }
+      mine[bb + 1] = x;
+    }
+    nf = m;
+  }
+  cnts[t] = i < n ? nf : -1;
+  __syncthreads();
+  const int lane = t & 31;
+  for (int rr = t >> 5; rr < kFrnnThreads && row0 + rr < n; rr += kFrnnThreads / 32) {
+    const int cr = cnts[rr];
+    int* dst = out + (size_t)rows[rr] * F;
+    const int* from = stage + rr * (kBStage + 1);
+    if (lane == 0) dst[0] = cr;
+    for (int k = lane; k < cr; k += 32) dst[k + 1] = from[k];
+  }
+}
+
+}  // namespace
+
+extern "C" int mcl_batch_frnn_grid(mcl_mesh* m, const float* r_host, const float* r_dev, float lo, float hi,
+                                   int max_frnn, int32_t* out_dev, void* stream, int64_t* overflow) {
+  if (!m || !r_host || !r_dev || !out_dev || !(hi > lo) || max_frnn < 2)
+    return qfail(MCL_ERR_INVALID_ARGUMENT, "bad args");
+  if (max_frnn - 1 > kBStage) return qfail(MCL_ERR_CAPACITY, "mcl_batch_frnn_grid: max_frnn above 49");
+  if (m->nact) return qfail(MCL_ERR_INVALID_ARGUMENT, "mcl_batch_frnn_grid: runs over every mesh of the batch");
+  cudaStream_t s = (cudaStream_t)stream;
+  const int64_t nc = m->ncomp, V = m->V;
+  // per-mesh grids: cells of the mesh's radius, at most 4096 per side
+  std::vector<int4> par((size_t)nc);
+  int64_t cells = 0;
+  for (int64_t c = 0; c < nc; ++c) {
+    const float r = r_host[c];
+    if (!(r > 0.f)) return qfail(MCL_ERR_INVALID_ARGUMENT, "mcl_batch_frnn_grid: radius must be positive");
+    int side = (int)std::min<double>(4096.0, std::ceil((double)(hi - lo) / r));
+    side = std::max(side, 1);
+    float cell = (hi - lo) / (float)side;
+    if (cell < r) cell = r;  // a cell never narrower than the radius
+    int v;
+    std::memcpy(&v, &cell, 4);
+    par[(size_t)c] = make_int4(v, side, (int)cells, 0);
+    cells += (int64_t)side * side;
+    if (cells > (1ll << 30)) return qfail(MCL_ERR_CAPACITY, "mcl_batch_frnn_grid: more than 2^30 cells");
+  }
+  if (!m->bg_cell) {
+    auto A = [&](void** p, size_t b) { return cudaMalloc(p, b) == cudaSuccess; };
+    if (!A((void**)&m->bg_cell, 4 * V) || !A((void**)&m->bg_src, 4 * V) || !A((void**)&m->bg_perm, 4 * V) ||
+        !A((void**)&m->bg_pos, 8 * V) || !A((void**)&m->bg_par, sizeof(int4) * nc) ||
+        cudaMallocHost((void**)&m->bg_par_host, sizeof(int4) * nc) != cudaSuccess)
+      return qfail(MCL_ERR_OUT_OF_MEMORY, "mcl_batch_frnn_grid: point tables");
+  }
+  if (m->bg_cap < cells) {
+    if (m->bg_count) { cudaFree(m->bg_count); cudaFree(m->bg_start); cudaFree(m->bg_cursor); cudaFree(m->bg_tmp); }
+    m->bg_count = m->bg_start = m->bg_cursor = m->bg_tmp = nullptr;
+    const int64_t nb = (cells + 1023) / 1024 + 1;
+    if (cudaMalloc((void**)&m->bg_count, 4 * cells) != cudaSuccess ||
+        cudaMalloc((void**)&m->bg_start, 4 * cells) != cudaSuccess ||
+        cudaMalloc((void**)&m->bg_cursor, 4 * cells) != cudaSuccess ||
+        cudaMalloc((void**)&m->bg_tmp, 8 * nb) != cudaSuccess) {
+      m->bg_cap = 0;
+      return qfail(MCL_ERR_OUT_OF_MEMORY, "mcl_batch_frnn_grid: cell tables");
+    }
+    m->bg_cap = cells;
+  }
+  // the parameters are uploaded only when they change, from a pinned buffer the
+  // mesh keeps (a call captured in a CUDA graph then holds no host copy, or
+  // reads memory that outlives the call)
+  if (m->bg_cells != cells || std::memcmp(m->bg_par_host, par.data(), sizeof(int4) * nc) != 0) {
+    QCK(cudaStreamSynchronize(s));  // the previous upload has been read
+    std::memcpy(m->bg_par_host, par.data(), sizeof(int4) * nc);
+    QCK(cudaMemcpyAsync(m->bg_par, m->bg_par_host, sizeof(int4) * nc, cudaMemcpyHostToDevice, s));
+    m->bg_cells = cells;
+  }
+  const float2* pos = m->pos[m->cur];
+  const int Vi = (int)V;
+  QCK(cudaMemsetAsync(m->bg_count, 0, 4 * cells, s));
+  k_bgrid_hash<<<(Vi + 255) / 256, 256, 0, s>>>(Vi, pos, m->vfix, m->vcomp, m->bg_par, lo, m->bg_cell, m->bg_count,
+                                                out_dev, max_frnn);
+  const int64_t nb = (cells + 1023) / 1024;
+  int rc = scan_exclusive(m->bg_count, m->bg_start, cells, m->bg_tmp, m->bg_tmp + nb + 1, s);
+  if (rc != MCL_OK) return rc;
+  QCK(cudaMemcpyAsync(m->bg_cursor, m->bg_start, 4 * cells, cudaMemcpyDeviceToDevice, s));
+  k_bgrid_scatter<<<(Vi + 255) / 256, 256, 0, s>>>(Vi, m->bg_cell, m->bg_cursor, m->bg_perm, m->bg_src);
+  k_grid_sort_cells<<<(unsigned)((cells + 255) / 256), 256, 0, s>>>(cells, m->bg_start, m->bg_count, m->bg_src,
+                                                                     m->bg_perm);
+  const int npts = (int)(V - 4 * nc);
+  k_gather<<<(npts + 255) / 256, 256, 0, s>>>(npts, m->bg_src, pos, m->bg_pos);
+  unsigned long long* ovf = m->scratch + 4;
+  QCK(cudaMemsetAsync(ovf, 0, 8, s));
+  k_bgrid_frnn<<<(unsigned)((npts + kFrnnThreads - 1) / kFrnnThreads), kFrnnThreads, 0, s>>>(
+      npts, m->bg_pos, m->bg_src, m->vcomp, m->bg_par, r_dev, lo, m->bg_start, m->bg_count, max_frnn, out_dev, ovf);
+  QCK(cudaGetLastError());
+  if (overflow) {
+    unsigned long long t = 0;
+    QCK(cudaMemcpyAsync(&t, ovf, 8, cudaMemcpyDeviceToHost, s));
+    QCK(cudaStreamSynchronize(s));
+    *overflow = (int64_t)t;
+  }
+  return MCL_OK;
+}
+
+// ---------------------------------------------------------------------------
 // Grid neighbours without allocation.
 //
 // Some callers cannot allocate device memory at all: host frameworks that

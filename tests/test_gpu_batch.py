@@ -325,3 +325,32 @@ def test_query_lists_match_full_queries(M):
     c_rl, rows_rl = csr_from_table(outr.cpu().numpy(), 1, len(verts), RM)
     for q, v in enumerate(verts):
         assert np.array_equal(rows_rl[q], rows_r[v])
+
+
+def test_batch_frnn_grid_equals_mesh_walk(M):
+    import torch
+
+    pts = make_points()
+    batch = M.MeshBatch.from_points([p.copy() for p in pts])
+    radii = np.array([2.0 * spacing(n) for n in SIZES], np.float32)
+    rd = cuda(radii)
+    F = 48
+    a = torch.full((batch.V * F,), -5, dtype=torch.int32, device="cuda")
+    b = torch.full((batch.V * F,), -7, dtype=torch.int32, device="cuda")
+    assert batch.frnn(rd, F, a) == 0
+    assert batch.frnn_grid(radii, rd, F, b) == 0
+    ra, rb = a.view(batch.V, F).cpu().numpy(), b.view(batch.V, F).cpu().numpy()
+    assert np.array_equal(ra[:, 0], rb[:, 0])
+    for v in range(batch.V):
+        c = ra[v, 0]
+        assert np.array_equal(ra[v, 1:1 + c], rb[v, 1:1 + c]), v
+    # after some steps (points moved, grid rebuilt from the new positions)
+    pos = [batch.download(i)[0] for i in range(batch.count)]
+    d = np.concatenate([gaussian_disp(len(pos[i]), 0.3 * spacing(SIZES[i]), 3 + i, clamp_pos=pos[i])
+                        for i in range(batch.count)])
+    assert batch.step(cuda(d))["status"] == 0
+    batch.frnn(rd, F, a)
+    batch.frnn_grid(radii, rd, F, b)
+    ra, rb = a.view(batch.V, F).cpu().numpy(), b.view(batch.V, F).cpu().numpy()
+    assert np.array_equal(ra[:, 0], rb[:, 0])
+    assert all(np.array_equal(ra[v, 1:1 + ra[v, 0]], rb[v, 1:1 + ra[v, 0]]) for v in range(batch.V))
