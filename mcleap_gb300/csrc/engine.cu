@@ -73,6 +73,17 @@ __device__ __forceinline__ void warp_push(const int (&mine)[K], int k, int* gl, 
 
 #define set_error(P, code) flag_error_at(P, code, __LINE__)
 
+// This thread's position in the spread order used by whole-grid loops over a
+// work-list: warp slot w of block b has spread index w * gridDim.x + b, so a
+// short list is dealt out one warp per block (across every SM) instead of
+// filling the first blocks.  Its item chains are latency-bound, and packed
+// onto a few SMs their scattered loads, stores and atomics queue behind each
+// other in those SMs' memory pipelines.  A permutation of the global thread
+// ids; the warp's first lane has index spread_tid() - lane.
+__device__ __forceinline__ int spread_tid() {
+  return (int)(((threadIdx.x >> 5) * gridDim.x + blockIdx.x) << 5) + (int)(threadIdx.x & 31);
+}
+
 __device__ __forceinline__ bool enqueue_once(const KParams& P, int e, unsigned stamp) {
   return atomicMax(P.qmark + e, stamp) < stamp;
 }
@@ -108,32 +119,36 @@ __device__ void flush_counters(const KParams& P, LocalCounters& lc) {
 // New position of v for a fused move: pos_old + displacement (or + v*dt);
 // fixed vertices (bounding corners) stay.  pos_old, disp, vel and dt are
 // read-only for the whole launch, so they go through the read-only cache.
+// Every load is issued before the fixed-vertex test (no load waits on another).
 __device__ __forceinline__ float2 moved_pos(const KParams& P, int v) {
-  float2 p = __ldg(P.pos_old + v);
-  if (__ldg(P.vfix + v)) return p;
+  const float2 p = __ldg(P.pos_old + v);
+  const bool fixed = __ldg(P.vfix + v) != 0;
+  float2 q = p;
   if (P.move_mode == MOVE_DISPLACE) {
     const float2 d = __ldg(P.disp + v);
-    p.x = fadd(p.x, d.x);
-    p.y = fadd(p.y, d.y);
+    q.x = fadd(p.x, d.x);
+    q.y = fadd(p.y, d.y);
   } else if (P.move_mode == MOVE_INTEGRATE) {
     const float2 u = __ldg(P.vel + v);
     const float t = __ldg(P.dt + v);
-    p.x = fadd(p.x, fmul(u.x, t));
-    p.y = fadd(p.y, fmul(u.y, t));
+    q.x = fadd(p.x, fmul(u.x, t));
+    q.y = fadd(p.y, fmul(u.y, t));
   }
-  return p;
+  return fixed ? p : q;
 }
 
 // Phase A of a flip round for edge e (already known to be non-Delaunay): claim
 // both faces with a priority key, remember the face ids for phase B.
-__device__ __forceinline__ void claim_edge(const KParams& P, int e, unsigned sc) {
-  const int4 w = ld_en(P, e);
+__device__ __forceinline__ void claim_edge_with(const KParams& P, int e, int4 w, unsigned sc) {
   const int fa = min(2 * e, min(w.x, w.y)), fb = min(2 * e + 1, min(w.z, w.w));
   const unsigned long long key = ((unsigned long long)sc << 32) | (unsigned)(~mix32((unsigned)e ^ sc));
   atomicMax(P.claim + fa, key);
   atomicMax(P.claim + fb, key);
   __stcg(P.efa + e, make_int2(fa, fb));
   __stcg(P.cand + e, sc);
+}
+__device__ __forceinline__ void claim_edge(const KParams& P, int e, unsigned sc) {
+  claim_edge_with(P, e, ld_en(P, e), sc);
 }
 
 // Full predicate ladder for one edge: counts its non-positive faces into `bad`
@@ -183,17 +198,64 @@ __device__ __forceinline__ void timeline_max(const KParams& P, int slot) {
   }
 }
 
-// Edges per thread and iteration of the classification pass.
+// Edges per thread and iteration of the classification pass; vertices per
+// thread and iteration of its move pass.
 constexpr int kClassifyUnroll = 4;
+constexpr int kMoveUnroll = 4;
+
+// The classification streams the edge records through shared memory one
+// iteration ahead of their use (cp.async, 16 bytes per record, L2-coherent):
+// kEvStages iterations of kClassifyUnroll records per thread.  Each thread
+// copies and reads only its own slots, so completion is a cp.async.wait_group
+// of the thread itself and no block barrier is involved.  The first
+// iteration's records are requested before the move pass, which hides them.
+constexpr int kEvStages = 2;
+__shared__ int4 s_ev[kEvStages][kClassifyUnroll][kThreads];
+
+__device__ __forceinline__ void cp_async16(int4* smem, const int4* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// Request the records of the classification iteration at `base` into stage
+// `st` (one commit group, empty past the end).
+__device__ __forceinline__ void stage_edges(const KParams& P, int base, int st) {
+#pragma unroll
+  for (int j = 0; j < kClassifyUnroll; ++j) {
+    const int ei = base + j * blockDim.x + threadIdx.x;
+    if (ei < P.E_it) cp_async16(&s_ev[st][j][threadIdx.x], P.ev + edge_at(P, ei));
+  }
+  cp_async_commit();
+}
 
 template <bool kFixedPos>
 __device__ void phase_classify(cg::grid_group& g, const KParams& P, unsigned qstamp, unsigned sc,
                                LocalCounters& lc) {
   const int stride = gridDim.x * blockDim.x;
+  constexpr int U = kClassifyUnroll;
+  const int first = blockIdx.x * blockDim.x * U;
+  stage_edges(P, first, 0);
   if (P.move_mode != MOVE_NONE) {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.V_it; i += stride) {
-      const int v = vert_at(P, i);
-      __stcg(P.pos + v, moved_pos(P, v));
+    // kMoveUnroll vertices per thread and iteration, every load before any
+    // store (the pass is a stream: its loads must overlap)
+    constexpr int UM = kMoveUnroll;
+    for (int base = blockIdx.x * blockDim.x * UM; base < P.V_it; base += stride * UM) {
+      int v[UM];
+      float2 np[UM];
+#pragma unroll
+      for (int j = 0; j < UM; ++j) {
+        const int i = base + j * blockDim.x + threadIdx.x;
+        v[j] = i < P.V_it ? vert_at(P, i) : -1;
+        if (v[j] >= 0) np[j] = moved_pos(P, v[j]);
+      }
+#pragma unroll
+      for (int j = 0; j < UM; ++j)
+        if (v[j] >= 0) __stcg(P.pos + v[j], np[j]);
     }
     if (kFixedPos) timeline_max(P, 43);
     g.sync();
@@ -207,15 +269,17 @@ __device__ void phase_classify(cg::grid_group& g, const KParams& P, unsigned qst
   // pass is latency-bound on the position gathers); edge j of the iteration
   // at base is base + j * blockDim.x + threadIdx.x, so every load stays
   // coalesced across the warp.
-  constexpr int U = kClassifyUnroll;
-  for (int base = blockIdx.x * blockDim.x * U; base < P.E_it; base += stride * U) {
+  int it = 0;
+  for (int base = first; base < P.E_it; base += stride * U, ++it) {
+    stage_edges(P, base + stride * U, (it + 1) % kEvStages);
+    cp_async_wait<kEvStages - 1>();  // this iteration's records have landed
     int4 q[U];
     int e[U];
 #pragma unroll
     for (int j = 0; j < U; ++j) {
       const int ei = base + j * blockDim.x + threadIdx.x;
       e[j] = ei < P.E_it ? edge_at(P, ei) : -1;
-      q[j] = e[j] >= 0 ? ld_ev(P, e[j]) : make_int4(-1, -1, -1, -1);
+      q[j] = e[j] >= 0 ? s_ev[it % kEvStages][j][threadIdx.x] : make_int4(-1, -1, -1, -1);
     }
     float2 pa[U], pb[U], pc[U], pd[U];
 #pragma unroll
@@ -268,6 +332,7 @@ __device__ void phase_classify(cg::grid_group& g, const KParams& P, unsigned qst
     if (__any_sync(kFull, k > 0)) warp_push(mine, k, P.wl0, &P.st->wl_count[0], P.E, P.st);
     if (__any_sync(kFull, kh > 0)) warp_push(hard, kh, P.hard, &P.st->hard_count, P.E, P.st);
   }
+  cp_async_wait<0>();  // nothing left in flight into the staging slots
   // the deferred edges, with the full predicate ladder (out of the loop, so
   // the out-of-line calls do not weigh on the loop above)
   {
@@ -297,8 +362,9 @@ __device__ void phase_classify_hard(cg::grid_group& g, const KParams& P, unsigne
   if (n == 0) return;  // uniform: read after the classification barrier
   const int stride = gridDim.x * blockDim.x;
   int bad = 0;
-  for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
-    const int i = base + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  for (int base = spread_tid() - lane; base < n; base += stride) {
+    const int i = base + lane;
     int mine[1];
     int k = 0;
     if (i < n) {
@@ -340,7 +406,9 @@ __device__ __forceinline__ int lawson_round(const KParams& P, const int* in, int
   if (do_phase_a) {
     for (int i = t0; i < n; i += nt) {
       const int e = ld_i(in + i);
-      if (edge_illegal<kFixedPos>(P, ld_ev(P, e), lc)) claim_edge(P, e, sc);
+      const int4 q = ld_ev(P, e);
+      const int4 w = ld_en(P, e);  // loaded with q: no load waits for the predicate
+      if (edge_illegal<kFixedPos>(P, q, lc)) claim_edge_with(P, e, w, sc);
     }
     sync();
   }
@@ -352,12 +420,21 @@ __device__ __forceinline__ int lawson_round(const KParams& P, const int* in, int
     int k = 0;
     if (i < n) {
       const int e = ld_i(in + i);
-      if ((unsigned)ld_i(reinterpret_cast<const int*>(P.cand) + e) == sc) {
-        const int2 f = __ldcg(P.efa + e);
+      // Everything a winner needs is loaded together with its claim test: a
+      // winner shares no face with another winner, so no flip of this round
+      // writes its records, and only its own flip can move vhe[a] off 2e
+      // or vhe[b] off 2e+1.
+      const unsigned c = (unsigned)ld_i(reinterpret_cast<const int*>(P.cand) + e);
+      const int2 f = __ldcg(P.efa + e);
+      const int4 q = ld_ev(P, e);
+      const int4 w = ld_en(P, e);
+      if (c == sc) {
         const unsigned long long key = ((unsigned long long)sc << 32) | (unsigned)(~mix32((unsigned)e ^ sc));
-        if (__ldcg(P.claim + f.x) == key && __ldcg(P.claim + f.y) == key) {
-          const int4 w = ld_en(P, e);
-          if (flip_edge(P, e)) ++flips;
+        const unsigned long long ka = __ldcg(P.claim + f.x), kb = __ldcg(P.claim + f.y);
+        const int vha = bad_v(P, q.x) ? -1 : ld_i(P.vhe + q.x);
+        const int vhb = bad_v(P, q.y) ? -1 : ld_i(P.vhe + q.y);
+        if (ka == key && kb == key) {
+          if (flip_edge_with(P, e, q, w, vha, vhb)) ++flips;
           const int wing[4] = {w.x >> 1, w.y >> 1, w.z >> 1, w.w >> 1};
 #pragma unroll
           for (int j = 0; j < 4; ++j)
@@ -385,7 +462,10 @@ constexpr int kTailItems = 2048;
 // Winners share no face, so their writes never overlap; the candidate with the
 // highest priority always wins both faces, so every round flips at least once.
 // If pre_sc != 0 the first round's phase A was done by the classification.
-template <bool kFixedPos>
+// With kLast (the launch's final phase) the grid does not wait for a
+// single-block tail: the other blocks return at once and block 0 returns
+// when the tail is done; only block 0's `stamp` is then current.
+template <bool kFixedPos, bool kLast = false>
 __device__ void phase_lawson(cg::grid_group& g, const KParams& P, int src, unsigned& stamp,
                              LocalCounters& lc, unsigned pre_sc) {
   const int stride = gridDim.x * blockDim.x;
@@ -398,7 +478,7 @@ __device__ void phase_lawson(cg::grid_group& g, const KParams& P, int src, unsig
       if (gtid == 0) set_error(P, MCL_ERR_NO_CONVERGENCE);
       break;
     }
-    if (n <= P.tail_items && !(round == 0 && pre_sc)) {
+    if (n <= P.tail_items) {
       // tail: block 0 finishes every remaining round on its own
       if (blockIdx.x == 0) {
         int s2 = src;
@@ -407,22 +487,29 @@ __device__ void phase_lawson(cg::grid_group& g, const KParams& P, int src, unsig
           const int m = ld_i(&P.st->wl_count[s2]);
           if (m == 0) break;
           const int d2 = s2 ^ 1;
-          const unsigned sc = st2++, sq = st2++;
+          // the first round's phase A may have been done by the classification
+          // (then wl_count[d2] is still zero)
+          const bool pre = r2 == 0 && pre_sc;
+          const unsigned sc = pre ? pre_sc : st2++;
+          const unsigned sq = st2++;
           if (threadIdx.x == 0) {
-            P.st->wl_count[d2] = 0;
+            if (!pre) P.st->wl_count[d2] = 0;
             P.st->c[C_LAWSON_ROUNDS] += 1;
           }
           __syncthreads();
           flips += lawson_round<kFixedPos>(P, s2 ? P.wl1 : P.wl0, m, d2 ? P.wl1 : P.wl0, &P.st->wl_count[d2], sc, sq,
-                                           true, threadIdx.x, blockDim.x, lc, [] { __syncthreads(); });
+                                           !pre, threadIdx.x, blockDim.x, lc, [] { __syncthreads(); });
           __syncthreads();
           timeline(P, 2 + (r2 < 40 ? r2 : 40));
           s2 = d2;
         }
-        if (threadIdx.x == 0) P.st->tail_stamp = st2;
+        if (kLast) stamp = st2;
+        else if (threadIdx.x == 0) P.st->tail_stamp = st2;
       }
-      g.sync();
-      stamp = (unsigned)ld_i(reinterpret_cast<const int*>(&P.st->tail_stamp));
+      if (!kLast) {
+        g.sync();
+        stamp = (unsigned)ld_i(reinterpret_cast<const int*>(&P.st->tail_stamp));
+      }
       break;
     }
     const int dst = src ^ 1;
@@ -442,7 +529,7 @@ __device__ void phase_lawson(cg::grid_group& g, const KParams& P, int src, unsig
       }
     }
     const unsigned sq = stamp++;
-    flips += lawson_round<kFixedPos>(P, in, n, out, &P.st->wl_count[dst], sc, sq, phase_a, gtid, stride, lc,
+    flips += lawson_round<kFixedPos>(P, in, n, out, &P.st->wl_count[dst], sc, sq, phase_a, spread_tid(), stride, lc,
                                      [&] { g.sync(); });
     g.sync();
     timeline(P, 2 + (round < 40 ? round : 40));
@@ -735,13 +822,13 @@ __device__ bool phase_remove(cg::grid_group& g, const KParams& P, unsigned& stam
       P.st->c[C_REMOVE_ROUNDS] += 1;
     }
     // claim every face of the star
-    for (int i = gtid; i < n; i += stride) {
+    for (int i = spread_tid(); i < n; i += stride) {
       const int v = ld_i(in + i);
       const unsigned long long key = ((unsigned long long)sk << 32) | (unsigned)(~mix32((unsigned)v ^ sk));
       for_spokes(P, v, [&](int h) { atomicMax(P.claim + face_min(P, h), key); });
     }
     g.sync();
-    for (int i = gtid; i < n; i += stride) {
+    for (int i = spread_tid(); i < n; i += stride) {
       const int v = ld_i(in + i);
       const unsigned long long key = ((unsigned long long)sk << 32) | (unsigned)(~mix32((unsigned)v ^ sk));
       bool win = true;
@@ -753,8 +840,8 @@ __device__ bool phase_remove(cg::grid_group& g, const KParams& P, unsigned& stam
     }
     g.sync();
     int removed = 0, flips = 0;
-    for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
-      const int i = base + threadIdx.x;
+    for (int base = spread_tid() - (int)(threadIdx.x & 31); base < n; base += stride) {
+      const int i = base + (int)(threadIdx.x & 31);
       int mine[1];
       int k = 0;
       if (i < n) {
@@ -947,7 +1034,7 @@ __device__ bool phase_insert(cg::grid_group& g, const KParams& P, unsigned& stam
       P.st->c[C_INSERT_ROUNDS] += 1;
     }
     // locate and claim
-    for (int i = gtid; i < n; i += stride) {
+    for (int i = spread_tid(); i < n; i += stride) {
       const int v = ld_i(in + i);
       int on = -1;
       int resume = -1;
@@ -975,7 +1062,7 @@ __device__ bool phase_insert(cg::grid_group& g, const KParams& P, unsigned& stam
     }
     g.sync();
     timeline_insert(P, round, 0);
-    for (int i = gtid; i < n; i += stride) {
+    for (int i = spread_tid(); i < n; i += stride) {
       const int v = ld_i(in + i);
       const int fl = __ldcg(P.vlocf + v);
       if (fl < 0) continue;
@@ -988,8 +1075,8 @@ __device__ bool phase_insert(cg::grid_group& g, const KParams& P, unsigned& stam
     g.sync();
     timeline_insert(P, round, 1);
     int inserted = 0;
-    for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
-      const int i = base + threadIdx.x;
+    for (int base = spread_tid() - (int)(threadIdx.x & 31); base < n; base += stride) {
+      const int i = base + (int)(threadIdx.x & 31);
       int mine[8];
       int k = 0;
       int again[1];
@@ -1049,19 +1136,22 @@ __device__ bool phase_insert(cg::grid_group& g, const KParams& P, unsigned& stam
 // next launch (so no reset launch or memset precedes the next step).
 __device__ void finish_launch(const KParams& P, unsigned stamp) {
   DevState* st = P.st;
+  // L2-coherent reads: other blocks' atomics and stores are not in this SM's L1
   for (int i = 0; i < C_COUNT; ++i) {
-    st->last[i] = st->c[i];
-    st->tot[i] += st->c[i];
+    const unsigned long long c = __ldcg(&st->c[i]);
+    st->last[i] = c;
+    st->tot[i] += c;
     st->c[i] = 0;
   }
+  const int status = __ldcg(&st->status);
   st->calls += 1;
-  if (st->status != MCL_OK) st->failed += 1;
+  if (status != MCL_OK) st->failed += 1;
   for (int i = 0; i < 4; ++i) {
-    st->ts[43 + i] = st->tsmax[i];
+    st->ts[43 + i] = __ldcg(&st->tsmax[i]);
     st->tsmax[i] = 0;
   }
-  st->last_status = st->status;
-  st->last_site = st->site;
+  st->last_status = status;
+  st->last_site = __ldcg(&st->site);
   st->status = 0;
   st->site = 0;
   st->wl_count[0] = st->wl_count[1] = 0;
@@ -1153,7 +1243,6 @@ __global__ void __launch_bounds__(kThreads, 3) k_step(KParams P) {
   cg::grid_group g = cg::this_grid();
   LocalCounters lc = {0, 0, 0, 0, 0, 0, 0};
   unsigned stamp = ld_i(reinterpret_cast<const int*>(&P.st->epoch));
-  const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
   timeline(P, 0);
   const unsigned q0 = stamp++;
   const unsigned sc0 = stamp++;
@@ -1162,12 +1251,26 @@ __global__ void __launch_bounds__(kThreads, 3) k_step(KParams P) {
   phase_classify_hard<true>(g, P, q0, sc0, lc);
   timeline(P, 1);
   const int inverted = ld_i(&P.st->inverted);
-  if (inverted == 0) phase_lawson<true>(g, P, 0, stamp, lc, sc0);
+  if (inverted == 0) phase_lawson<true, true>(g, P, 0, stamp, lc, sc0);
   else stamp = repair_step(g, P, stamp);
   flush_counters(P, lc);
-  g.sync();
-  timeline(P, kTimeline - 1);
-  if (gtid == 0) finish_launch(P, stamp);
+  // No closing grid barrier: each block leaves when its own work is done and
+  // the last one to leave publishes the launch.
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    atomicMax(&P.st->stamp_max, stamp);
+    __threadfence();
+    if (atomicAdd(&P.st->arrived, 1u) == gridDim.x - 1) {
+      __threadfence();
+      unsigned long long t;
+      asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+      P.st->ts[kTimeline - 1] = t;
+      finish_launch(P, __ldcg(&P.st->stamp_max));
+      P.st->arrived = 0;
+      P.st->stamp_max = 0;
+    }
+  }
 }
 
 // The initial triangulation: parallel insertion rounds from the bounding square.

@@ -64,6 +64,8 @@ struct DevState {
   int fix_bad[3];          // non-positive faces seen per fixpoint pass
   unsigned int epoch;      // next unused stamp
   unsigned int tail_stamp; // stamp after a single-block flip tail
+  unsigned int arrived;    // blocks of k_step that have finished (the last one publishes)
+  unsigned int stamp_max;  // largest next-free stamp over those blocks
   unsigned long long c[C_COUNT];
   // published by the last launch
   int last_status;
@@ -245,6 +247,29 @@ __device__ __forceinline__ bool edge_illegal(const KParams& P, const int4 q, Loc
 // Edge flip of e = (a,b,c,d): the diagonal a-b becomes d-c.  Faces after the
 // flip: (d,c,a) left of 2e and (c,d,b) left of 2e+1.  Only e's own records and
 // the facing-side fields of its four wing half-edges are written.
+// flip_edge with e's records (q = ev[e], w = en[e]) and the one-ring anchors
+// of its endpoints (vha = vhe[a], vhb = vhe[b]) already loaded: valid when no
+// other thread writes them meanwhile, as for a flip-round winner.
+__device__ __forceinline__ bool flip_edge_with(const KParams& P, int e, int4 q, int4 w, int vha, int vhb) {
+  const int a = q.x, b = q.y, c = q.z, d = q.w;
+  const int n0 = w.x, p0 = w.y, n1 = w.z, p1 = w.w;
+  if (bad_v(P, a) || bad_v(P, b) || bad_v(P, c) || bad_v(P, d) || bad_h(P, n0) || bad_h(P, p0) ||
+      bad_h(P, n1) || bad_h(P, p1)) {
+    flag_error(P, MCL_ERR_DEGENERATE_INPUT);
+    return false;
+  }
+  const int h0 = 2 * e, h1 = 2 * e + 1;
+  __stcg(P.ev + e, make_int4(d, c, a, b));
+  __stcg(P.en + e, make_int4(p0, n1, p1, n0));
+  he_set_face(P, p0, d, n1, h0);
+  he_set_face(P, n1, c, h0, p0);
+  he_set_face(P, p1, c, n0, h1);
+  he_set_face(P, n0, d, h1, p1);
+  if (vha == h0) __stcg(P.vhe + a, n1);
+  if (vhb == h1) __stcg(P.vhe + b, n0);
+  return true;
+}
+
 __device__ __forceinline__ bool flip_edge(const KParams& P, int e) {
   const int4 q = ld_ev(P, e);
   const int4 w = ld_en(P, e);
