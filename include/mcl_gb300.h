@@ -75,6 +75,8 @@ typedef struct {
   int64_t status;                /* MCL_OK or an error code */
   int64_t error_site;            /* engine source location that reported `status` */
   int64_t failed_launches;       /* launches that ended with an error (totals: since creation) */
+  int64_t substep_vertices;      /* sent-back vertices brought to their targets by repair sub-steps
+                                    (without removal) */
 } mcl_step_stats;
 
 /* ---- library ------------------------------------------------------------ */
@@ -315,6 +317,14 @@ int mcl_mesh_clone(const mcl_mesh* src, mcl_mesh** out);
  * the work-list size at or below which one block finishes the flip rounds
  * (0 = 2048).  Results do not depend on either. */
 int mcl_mesh_set_tuning(mcl_mesh* m, int blocks_per_sm, int tail_items);
+
+/* Repair sub-steps per kinetic step (default 0: every vertex sent back while
+ * untangling is removed and reinserted at its target).  A sub-step moves the
+ * sent-back vertices toward their targets as far as their stars allow and
+ * restores the Delaunay property around them; those still short of their
+ * targets after the last sub-step are removed and reinserted.  The resulting
+ * mesh is the same Delaunay triangulation either way. */
+int mcl_mesh_set_substeps(mcl_mesh* m, int substeps);
 int mcl_mesh_get_tuning(const mcl_mesh* m, int* blocks_per_sm, int* tail_items, int* max_blocks_per_sm);
 
 /* ---- motion models ----------------------------------------------------------- */

@@ -35,7 +35,7 @@ EXPORTS = [
     "mcl_grid_create", "mcl_grid_destroy", "mcl_grid_update", "mcl_grid_tables", "mcl_grid_describe", "mcl_grid_frnn",
     "mcl_grid_build", "mcl_grid_frnn_ids",
     "mcl_batch_create", "mcl_batch_count", "mcl_batch_range", "mcl_batch_vertex_mesh", "mcl_batch_download_aos",
-    "mcl_batch_frnn", "mcl_mesh_clone", "mcl_mesh_set_tuning", "mcl_mesh_get_tuning", "mcl_walk",
+    "mcl_batch_frnn", "mcl_mesh_clone", "mcl_mesh_set_tuning", "mcl_mesh_get_tuning", "mcl_mesh_set_substeps", "mcl_walk",
     "mcl_settle_moves", "mcl_dla_freeze", "mcl_batch_frnn_list", "mcl_one_ring_list", "mcl_batch_set_active", "mcl_batch_frnn_grid",
     "mcl_grid_mean_occupancy", "mcl_debug_predicates_host", "mcl_debug_predicates_device", "mcl_mesh_validate", "mcl_debug_state", "mcl_debug_timeline", "mcl_grid_frnn_noalloc", "mcl_debug_counters",
     "mcl_debug_insert_timeline",
@@ -55,7 +55,8 @@ class AosView(C.Structure):
 
 STAT_FIELDS = ["inverted_faces", "reverted_vertices", "removed_vertices", "lawson_flips", "lawson_rounds",
                "removal_flips", "insert_rounds", "incircle_tests", "incircle_fp64", "incircle_exact",
-               "orient_fp64", "orient_exact", "sos_decisions", "status", "error_site", "failed_launches"]
+               "orient_fp64", "orient_exact", "sos_decisions", "status", "error_site", "failed_launches",
+               "substep_vertices"]
 
 
 class StepStats(C.Structure):
@@ -125,6 +126,7 @@ def lib():
             "mcl_batch_frnn": ([vp, vp, i32, i32, vp, vp, C.POINTER(i64)], i32),
             "mcl_mesh_clone": ([vp, C.POINTER(vp)], i32),
             "mcl_mesh_set_tuning": ([vp, i32, i32], i32),
+            "mcl_mesh_set_substeps": ([vp, i32], i32),
             "mcl_mesh_get_tuning": ([vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)], i32),
             "mcl_walk": ([vp, vp, vp, C.c_uint64, vp, f32, f32, vp, vp], i32),
             "mcl_settle_moves": ([vp, vp, vp, C.POINTER(i64)], i32),

@@ -107,6 +107,10 @@ class MeshBatch:
     def set_tuning(self, blocks_per_sm=0, tail_items=0):
         L.check(L.lib().mcl_mesh_set_tuning(self.handle, int(blocks_per_sm), int(tail_items)))
 
+    def set_substeps(self, substeps):
+        """Repair sub-steps per step (0: straight to removal and reinsertion)."""
+        L.check(L.lib().mcl_mesh_set_substeps(self.handle, int(substeps)))
+
     def tuning(self):
         a, b, c = C.c_int(), C.c_int(), C.c_int()
         L.check(L.lib().mcl_mesh_get_tuning(self.handle, C.byref(a), C.byref(b), C.byref(c)))

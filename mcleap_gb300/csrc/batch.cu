@@ -358,6 +358,7 @@ int mcl_mesh_clone(const mcl_mesh* src, mcl_mesh** out) {
     std::memcpy(m->comp_host, src->comp_host, sizeof(int64_t) * 4 * src->ncomp);
   }
   m->tail_items = src->tail_items;
+  m->substeps = src->substeps;
   m->coop_blocks = src->coop_blocks;
   if (src->dirty) {
     const int64_t nc = src->ncomp;
@@ -422,6 +423,12 @@ int mcl_mesh_set_tuning(mcl_mesh* m, int blocks_per_sm, int tail_items) {
     return fail(MCL_ERR_INVALID_ARGUMENT, "blocks per SM above the kernel's co-resident limit");
   m->coop_blocks = m->nsm * bps;
   m->tail_items = tail_items == 0 ? 2048 : tail_items;
+  return MCL_OK;
+}
+
+int mcl_mesh_set_substeps(mcl_mesh* m, int substeps) {
+  if (!m || substeps < 0 || substeps > 64) return fail(MCL_ERR_INVALID_ARGUMENT, "substeps must be in [0, 64]");
+  m->substeps = substeps;
   return MCL_OK;
 }
 

@@ -452,6 +452,13 @@ __device__ __forceinline__ int lawson_round(const KParams& P, const int* in, int
 // Rounds with at most this many queued edges run inside one block (block
 // barriers instead of grid barriers); the rest of the grid waits.
 constexpr int kTailItems = 2048;
+// Default repair sub-steps per kinetic step (phase_substeps).  Off: on the
+// uniform random-walk benchmarks (1M points, sigma = 0.1 x spacing; 512 meshes,
+// 8.5M points) 4 and 8 sub-steps leave 25% and 4% of the sent-back vertices
+// to removal, but each sub-step costs about as much as the removal and
+// reinsertion rounds it saves (latency-bound star walks and flip rounds), so
+// the step time does not improve.
+constexpr int kSubsteps = 0;
 
 // ---------------------------------------------------------------------------
 // Lawson flip rounds starting from work-list `src`.  A round is two phases:
@@ -1146,8 +1153,9 @@ __device__ void finish_launch(const KParams& P, unsigned stamp) {
   const int status = __ldcg(&st->status);
   st->calls += 1;
   if (status != MCL_OK) st->failed += 1;
+  const bool repaired = st->last[C_INVERTED] != 0;
   for (int i = 0; i < 4; ++i) {
-    st->ts[43 + i] = __ldcg(&st->tsmax[i]);
+    if (!repaired) st->ts[43 + i] = __ldcg(&st->tsmax[i]);
     st->tsmax[i] = 0;
   }
   st->last_status = status;
@@ -1160,6 +1168,213 @@ __device__ void finish_launch(const KParams& P, unsigned stamp) {
   st->hard_count = 0;
   for (int i = 0; i < 3; ++i) st->fix_new[i] = st->fix_bad[i] = 0;
   st->epoch = stamp;
+}
+
+// ---------------------------------------------------------------------------
+// Repair (1b): bring sent-back vertices to their targets in sub-steps, so that
+// most of them need no removal.  A Delaunay mesh whose vertex moves on a line
+// meets a flip (an incircle event) before any face around the vertex
+// degenerates, so moving part of the way, restoring the Delaunay property
+// around the vertex and moving on passes the obstruction that sent it back.
+// A sub-step moves every pending vertex toward its target (all the way, or
+// 9/10 of the way to the first face of its star that would degenerate, times
+// 2^-lvl after lvl send-backs in a row); sends back, pass by pass until every
+// face is positive, each mover with a non-positive face in its star (lvl + 1);
+// runs Lawson rounds over the stars of the movers that stayed; and keeps those
+// not yet at their targets pending (lvl 0).  Vertices sent back more than
+// kSubstepLevels times in a row, or still pending after P.substeps sub-steps,
+// are left on vl0 for removal and reinsertion.  The mesh ends as the Delaunay triangulation of
+// the targets either way; this path only saves removals.
+//
+// In: vl0 = pending vertices at valid positions (pos), targets in `target`,
+// vlocf = 0 for each, the mesh Delaunay.  Out: vl0 = vertices left for
+// removal (at their last valid positions), the mesh valid and Delaunay.
+constexpr int kSubstepLevels = 5;
+
+__device__ void phase_substeps(cg::grid_group& g, const KParams& P, unsigned& stamp, LocalCounters& lc) {
+  const int stride = gridDim.x * blockDim.x;
+  const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  int* const mv[2] = {P.vl2, P.vl2 + P.V};  // movers of a sub-step pass
+  int* const rv = P.vl2 + 2 * P.V;          // movers sent back in the current pass
+  int* const left = P.vl2 + 3 * P.V;        // past kSubstepLevels halvings
+  int src = 0;
+  int done = 0;
+  for (int s = 0; s < P.substeps; ++s) {
+    const int n = ld_i(&P.st->vl_count[src]);
+    if (n == 0) break;
+    const int dst = src ^ 1;
+    const int* in = src ? P.vl1 : P.vl0;
+    int* out = dst ? P.vl1 : P.vl0;
+    const unsigned qs = stamp++;
+    if (gtid == 0) {
+      P.st->vl_count[dst] = 0;
+      P.st->sub_count[0] = 0;
+      P.st->sub_count[1] = 0;
+      for (int k = 0; k < 3; ++k) P.st->sub_rev[k] = 0;
+      if (s == 0) P.st->sub_count[2] = 0;
+      P.st->wl_count[0] = 0;
+      P.st->wl_count[1] = 0;
+      P.st->c[C_SUBSTEPS] += 1;
+    }
+    g.sync();
+    // (a) move each pending vertex toward its target: all the way when no
+    // face of its star degenerates on the way, else 9/10 of the way to the
+    // first face that would (the flip that clears it comes before); after
+    // lvl consecutive send-backs, 2^-lvl of that
+    for (int base = spread_tid() - lane; base < n; base += stride) {
+      const int i = base + lane;
+      int mine[1];
+      int k = 0;
+      if (i < n) {
+        const int v = ld_i(in + i);
+        const float2 p = ldpos(P, v), t = __ldcg(P.target + v);
+        const int lvl = ld_i(P.vlocf + v);
+        double fmax = 1.0;
+        bool blocked = false;
+        for_spokes(P, v, [&](int h) {
+          const int d = he_origin(P, h ^ 1), a = he_apex(P, h);
+          if (bad_v(P, d) || a < 0 || bad_v(P, a)) return;
+          const float2 q = ldpos(P, d), r = ldpos(P, a);
+          // orientation of (x, q, r) is affine in x: its value at p and at t
+          const double o0 = ((double)q.x - p.x) * ((double)r.y - p.y) - ((double)q.y - p.y) * ((double)r.x - p.x);
+          const double o1 = ((double)q.x - t.x) * ((double)r.y - t.y) - ((double)q.y - t.y) * ((double)r.x - t.x);
+          if (o1 <= 0.0) {
+            blocked = true;
+            const double f = o0 > 0.0 ? o0 / (o0 - o1) : 0.0;
+            fmax = f < fmax ? f : fmax;
+          }
+        });
+        float2 c = t;
+        if (blocked || lvl > 0) {
+          const float f = (float)((blocked ? 0.9 * fmax : 1.0) * ldexp(1.0, -lvl));
+          c.x = fadd(p.x, fmul(fsub(t.x, p.x), f));
+          c.y = fadd(p.y, fmul(fsub(t.y, p.y), f));
+        }
+        __stcg(P.vprev + v, p);
+        __stcg(P.pos + v, c);
+        mine[k++] = v;
+      }
+      warp_push(mine, k, mv[0], &P.st->sub_count[0], P.V, P.st);
+    }
+    g.sync();
+    // (b) send back, pass by pass, every mover with a non-positive face in its
+    // star: every position is read (detect) before any is restored (apply)
+    int cur = 0;
+    for (int pass = 0;; ++pass) {
+      if (pass == 64) {
+        if (gtid == 0) set_error(P, MCL_ERR_NO_CONVERGENCE);
+        return;
+      }
+      const int m = ld_i(&P.st->sub_count[cur]);
+      const int nxt = cur ^ 1;
+      const int slot = pass % 3;
+      for (int base = spread_tid() - lane; base < m; base += stride) {
+        const int i = base + lane;
+        int stay[1], back[1], pend[1], gone[1];
+        int ks = 0, kb = 0, kp = 0, kg = 0;
+        if (i < m) {
+          const int v = ld_i(mv[cur] + i);
+          const float2 pv = ldpos(P, v);
+          bool good = true;
+          const bool ok = for_spokes(P, v, [&](int h) {
+            if (!good) return;
+            const int d = he_origin(P, h ^ 1), a = he_apex(P, h);
+            if (bad_v(P, d) || a < 0 || bad_v(P, a)) {
+              good = false;
+              return;
+            }
+            if (orient_v(P, pv, ldpos(P, d), ldpos(P, a), lc) <= 0) good = false;
+          });
+          if (!ok) flag_error(P, MCL_ERR_DEGENERATE_INPUT);
+          if (good) {
+            stay[ks++] = v;
+          } else {
+            const int lvl = ld_i(P.vlocf + v) + 1;
+            __stcg(P.vlocf + v, lvl);
+            back[kb++] = v;
+            if (lvl > kSubstepLevels) gone[kg++] = v;
+            else pend[kp++] = v;
+          }
+        }
+        warp_push(stay, ks, mv[nxt], &P.st->sub_count[nxt], P.V, P.st);
+        warp_push(back, kb, rv, &P.st->sub_rev[slot], P.V, P.st);
+        warp_push(pend, kp, out, &P.st->vl_count[dst], P.V, P.st);
+        warp_push(gone, kg, left, &P.st->sub_count[2], P.V, P.st);
+      }
+      g.sync();
+      const int nrev = ld_i(&P.st->sub_rev[slot]);
+      cur = nxt;
+      if (nrev == 0) break;
+      for (int i = spread_tid(); i < nrev; i += stride) {
+        const int v = ld_i(rv + i);
+        __stcg(P.pos + v, __ldcg(P.vprev + v));
+      }
+      if (gtid == 0) {
+        P.st->sub_count[nxt ^ 1] = 0;  // the list just read becomes the next survivors' list
+        P.st->sub_rev[(pass + 1) % 3] = 0;
+      }
+      g.sync();
+    }
+    // (c) movers that stayed: at their targets they are done, else they stay
+    // pending (lvl 0); (d) their stars are queued for Lawson rounds
+    const int m = ld_i(&P.st->sub_count[cur]);
+    for (int base = spread_tid() - lane; base < m; base += stride) {
+      const int i = base + lane;
+      int pend[1];
+      int kp = 0;
+      int h0 = -1;
+      if (i < m) {
+        const int v = ld_i(mv[cur] + i);
+        const float2 pv = ldpos(P, v), t = __ldcg(P.target + v);
+        if (__float_as_uint(pv.x) == __float_as_uint(t.x) && __float_as_uint(pv.y) == __float_as_uint(t.y)) {
+          ++done;
+        } else {
+          __stcg(P.vlocf + v, 0);
+          pend[kp++] = v;
+        }
+        h0 = ld_i(P.vhe + v);
+        if (h0 < 0 || h0 >= 2 * P.E) {
+          flag_error(P, MCL_ERR_DEGENERATE_INPUT);
+          h0 = -1;
+        }
+      }
+      warp_push(pend, kp, out, &P.st->vl_count[dst], P.V, P.st);
+      // the stars in lock step across the warp: spokes and link edges
+      int h = h0;
+      bool active = h0 >= 0;
+      for (int it = 0; it < 1024 && __any_sync(kFull, active); ++it) {
+        int mine[2];
+        int k = 0;
+        if (active) {
+          const int es = h >> 1, el = he_next(P, h) >> 1;
+          if (enqueue_once(P, es, qs)) mine[k++] = es;
+          if (el >= 0 && el < P.E && enqueue_once(P, el, qs)) mine[k++] = el;
+          h = he_prev(P, h) ^ 1;
+          if (h < 0 || h >= 2 * P.E || h == h0) active = false;
+        }
+        warp_push(mine, k, P.wl0, &P.st->wl_count[0], P.E, P.st);
+      }
+    }
+    g.sync();
+    phase_lawson<false>(g, P, 0, stamp, lc, 0);
+    src = dst;
+  }
+  // left for removal: still pending, and past the halving limit
+  const int np = ld_i(&P.st->vl_count[src]);
+  const int nl = ld_i(&P.st->sub_count[2]);
+  for (int i = gtid; i < np + nl; i += stride) {
+    const int v = i < np ? ld_i((src ? P.vl1 : P.vl0) + i) : ld_i(left + (i - np));
+    if (src || i >= np) __stcg(P.vl2 + i, v);  // staged through the first mover list
+  }
+  g.sync();
+  if (src || nl) {
+    for (int i = gtid; i < np + nl; i += stride)
+      if (src || i >= np) __stcg(P.vl0 + i, ld_i(P.vl2 + i));
+  }
+  if (gtid == 0) P.st->vl_count[0] = np + nl;
+  if (done) atomicAdd(&P.st->c[C_SUBSTEP_DONE], (unsigned long long)done);
+  g.sync();
 }
 
 // Repair of a step whose classification found inverted faces: revert, remove,
@@ -1192,15 +1407,40 @@ __device__ __noinline__ unsigned repair_step(cg::grid_group g, const KParams P, 
         if (__float_as_uint(pn.x) != __float_as_uint(po.x) || __float_as_uint(pn.y) != __float_as_uint(po.y)) {
           __stcg(P.target + v, pn);
           __stcg(P.pos + v, po);
+          __stcg(P.vlocf + v, 0);  // sub-step level
           mine[k++] = v;
         }
       }
       warp_push(mine, k, P.vl0, &P.st->vl_count[0], P.V, P.st);
     }
     g.sync();
+    const int nrev = ld_i(&P.st->vl_count[0]);
+    if (gtid == 0) P.st->c[C_REVERTED] += (unsigned long long)nrev;
+    if (nrev > 0) {
+      // (1b) Delaunay over every edge with the sent-back vertices at their old
+      // positions, then sub-steps toward their targets
+      if (gtid == 0) { P.st->wl_count[0] = 0; P.st->wl_count[1] = 0; P.st->inverted = 0; P.st->hard_count = 0; }
+      g.sync();
+      const unsigned q0 = stamp++;
+      const unsigned sc0 = stamp++;
+      phase_classify<false>(g, Q, q0, sc0, lc);
+      g.sync();
+      phase_classify_hard<false>(g, Q, q0, sc0, lc);
+      phase_lawson<false>(g, Q, 0, stamp, lc, sc0);
+      g.sync();
+      timeline_insert(P, 15, 0);
+      phase_substeps(g, Q, stamp, lc);
+      timeline_insert(P, 15, 1);
+    }
     const int nrem = ld_i(&P.st->vl_count[0]);
-    if (gtid == 0) P.st->c[C_REVERTED] += (unsigned long long)nrem;
-    // (2) remove them
+    if (nrem == 0) {
+      timeline(P, 44);
+      timeline(P, 45);
+      timeline(P, 46);
+      flush_counters(P, lc);
+      return stamp;
+    }
+    // (2) remove what is left
     ok = phase_remove(g, Q, stamp, lc);
     g.sync();
     timeline(P, 44);
@@ -1315,7 +1555,7 @@ void free_mesh(mcl_mesh* m) {
   if (!m) return;
   void* ptrs[] = {m->pos[0], m->pos[1], m->ev, m->en, m->vhe, m->vfix, m->cand, m->win, m->qmark, m->efa, m->hard,
                   m->wl[0], m->wl[1], m->vl[0], m->vl[1], m->vmark, m->claim, m->vfree, m->vhint,
-                  m->vaux, m->vloc, m->vlocf, m->target, m->dstage, m->scratch, m->st,
+                  m->vaux, m->vloc, m->vlocf, m->target, m->vprev, m->vl2, m->dstage, m->scratch, m->st,
                   m->vcomp, m->vroot, m->cbase, m->table, m->smark, m->fnew, m->act_dev,
                   m->bg_cell, m->bg_src, m->bg_perm, m->bg_pos, m->bg_count, m->bg_start, m->bg_cursor,
                   m->bg_tmp, m->bg_par};
@@ -1391,6 +1631,8 @@ int alloc_mesh(int64_t V, int64_t E, mcl_mesh** out) {
   A((void**)&m->vloc, 4 * V);
   A((void**)&m->vlocf, 4 * V);
   A((void**)&m->target, 8 * V);
+  A((void**)&m->vprev, 8 * V);
+  A((void**)&m->vl2, 16 * V);
   A((void**)&m->dstage, 8 * V);
   A((void**)&m->scratch, 64);
   A((void**)&m->st, sizeof(DevState));
@@ -1427,6 +1669,7 @@ int alloc_mesh(int64_t V, int64_t E, mcl_mesh** out) {
   m->nsm = nsm;
   m->max_blocks_per_sm = per_sm;
   m->tail_items = kTailItems;
+  m->substeps = kSubsteps;
   m->ncomp = 1;
   m->coop_blocks = nsm * per_sm;
   m->repair_blocks = nsm * per_sm2;
@@ -1591,11 +1834,14 @@ static KParams make_params(mcl_mesh* m, int mode) {
   P.vloc = m->vloc;
   P.vlocf = m->vlocf;
   P.target = m->target;
+  P.vprev = m->vprev;
+  P.vl2 = m->vl2;
   P.st = m->st;
   P.mode = mode;
   P.max_rounds = 1 << 16;
   P.walk_cap = 1 << 18;
   P.tail_items = m->tail_items;
+  P.substeps = m->substeps;
   P.vroot = m->vroot;
   P.nact = m->nact;
   P.E_it = m->nact ? m->act_E : (int)m->E;
@@ -1638,6 +1884,7 @@ static void fill_stats_from(const unsigned long long* c, int status, int site, m
   o->orient_fp64 = (int64_t)s.c[C_ORIENT_FP64];
   o->orient_exact = (int64_t)s.c[C_ORIENT_EXACT];
   o->sos_decisions = (int64_t)s.c[C_SOS];
+  o->substep_vertices = (int64_t)s.c[C_SUBSTEP_DONE];
   o->status = status;
   o->error_site = site;
   o->failed_launches = 0;

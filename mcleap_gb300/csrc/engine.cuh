@@ -47,6 +47,8 @@ enum Counter {
   C_OVERFLOW,
   C_FIX_PASSES,
   C_REMOVE_ROUNDS,
+  C_SUBSTEPS,       // sub-step rounds of the repair
+  C_SUBSTEP_DONE,   // sent-back vertices brought to their targets by sub-steps
   C_COUNT
 };
 
@@ -62,6 +64,8 @@ struct DevState {
   int hard_count;          // edges the FP32 filters could not classify
   int fix_new[3];          // vertices newly reverted per fixpoint pass (triple-buffered)
   int fix_bad[3];          // non-positive faces seen per fixpoint pass
+  int sub_count[3];        // repair sub-steps: mover lists (2), vertices left for removal
+  int sub_rev[3];          // movers sent back per sub-step pass (triple-buffered)
   unsigned int epoch;      // next unused stamp
   unsigned int tail_stamp; // stamp after a single-block flip tail
   unsigned int arrived;    // blocks of k_step that have finished (the last one publishes)
@@ -76,8 +80,12 @@ struct DevState {
   unsigned long long failed;       // launches that ended with an error
   int dbg[68];             // first failing vertex star: v, deg, then neighbour ids
   unsigned long long ts[kTimeline];  // %globaltimer at phase boundaries of the last launch
+  // insertion round r < 16: [4r] located, [4r+1] won, [4r+2] split, [4r+3] flips done
   unsigned long long ts_insert[64];
-  unsigned long long tsmax[4];      // latest block at marks of the running launch (published to ts[43..46])  // insertion round r < 16: [4r] located, [4r+1] won, [4r+2] split, [4r+3] flips done
+  // latest block at the move / classification marks of the running launch;
+  // published to ts[43..46] by a step without repair (a repair step keeps its
+  // own marks there)
+  unsigned long long tsmax[4];
   // mcl_settle_moves: [0] last stamp used, [1..3] moves sent back per pass
   // (triple-buffered), [4] sent back by the last call, [5] status of the last call
   unsigned int settle[8];
@@ -111,6 +119,8 @@ struct KParams {
   int* vloc;               // per vertex: located half-edge (+ on-edge flag in vlocf)
   int* vlocf;
   float2* target;          // per vertex: position to reinsert at
+  float2* vprev;           // per vertex: position before the current repair sub-step
+  int* vl2;                // 4 x V: repair sub-step lists (movers x2, sent back, left for removal)
   DevState* st;
   // move inputs
   const float2* disp;
@@ -121,6 +131,7 @@ struct KParams {
   int max_rounds;
   int walk_cap;
   int tail_items;          // flip rounds with at most this many queued edges run in one block
+  int substeps;            // repair sub-steps before removal
   const int* vroot;        // per vertex: a never-freed half-edge of its mesh (batches); NULL = half-edge 0
   // active meshes of a batch (nact == 0: every edge and vertex): the full
   // passes run over index spaces [0, E_it) and [0, V_it) that map to the
@@ -319,6 +330,8 @@ struct mcl_mesh {
   int* vloc;
   int* vlocf;
   float2* target;
+  float2* vprev;
+  int* vl2;
   float2* dstage;          // device staging buffer for host displacements
   // mcl_step_host_async: a second staging buffer, a copy stream, and events
   float2* dstage2;
@@ -337,6 +350,7 @@ struct mcl_mesh {
   int nsm;                 // SMs of the device
   int max_blocks_per_sm;   // k_step occupancy limit
   int tail_items;          // single-block flip-round threshold
+  int substeps;            // repair sub-steps before removal (mcl_mesh_set_substeps)
   // batches: a mesh made of independent components (mcl_batch_create)
   int64_t ncomp;           // 1 for a plain mesh
   int64_t* comp_host;      // [4 * ncomp]: first vertex, vertices, first edge, edges

@@ -94,6 +94,39 @@ def test_clone_and_tuning_do_not_change_results(M):
         assert np.array_equal(a.edges(i), b.edges(i))
 
 
+@pytest.mark.parametrize("sigma", [0.1, 0.5, 2.0])
+def test_repair_substeps_and_removal_give_the_same_mesh(M, sigma):
+    # sub-steps bring most sent-back vertices to their targets without
+    # removal; with none every one is removed and reinserted: the mesh must
+    # be the same exact Delaunay triangulation either way
+    pts = make_points()
+    a = M.MeshBatch.from_points([p.copy() for p in pts])
+    b = a.clone()
+    a.set_substeps(8)
+    b.set_substeps(0)
+    pos = [a.download(i)[0] for i in range(a.count)]
+    sub = removed_a = removed_b = 0
+    for k in range(3):
+        d = np.concatenate([gaussian_disp(len(pos[i]), sigma * spacing(SIZES[i]), 313 * k + i, clamp_pos=pos[i])
+                            for i in range(a.count)])
+        sa, sb = a.step(cuda(d)), b.step(cuda(d))
+        assert sa["status"] == 0 and sb["status"] == 0, (sa, sb)
+        # each sent-back vertex reaches its target by sub-steps or by reinsertion
+        assert sa["reverted_vertices"] == sa["substep_vertices"] + sa["removed_vertices"]
+        assert sb["substep_vertices"] == 0 and sb["removed_vertices"] == sb["reverted_vertices"]
+        sub += sa["substep_vertices"]
+        removed_a += sa["removed_vertices"]
+        removed_b += sb["removed_vertices"]
+        assert not a.validate().any() and not b.validate().any()
+        pos = [a.download(i)[0] for i in range(a.count)]
+        for i in range(a.count):
+            assert np.array_equal(b.download(i)[0], pos[i])
+            e = a.edges(i)
+            assert np.array_equal(e, b.edges(i)), (k, i)
+            assert np.array_equal(e, O.Mesh.build(pos[i][4:], exact=True).edges()), (k, i)
+    assert sub > 0 and removed_b > 0
+
+
 def test_walk_is_counter_based_and_stays_in_the_box(M):
     import torch
 
