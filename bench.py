@@ -319,11 +319,10 @@ def run_ours(args, rank, world, dist):
     achieved = alg_bytes / (dev_s / K) / 1e9
     peak, peak_kind = peaks()
     # DRAM traffic of one k_step launch measured by ncu on this workload
-    # (profiles/k_step_taylor_green_1M.md: 71.1 MB at 3,000,005 edges), scaled
-    # by the edge count for other sizes
-    traffic = 71.06e6 * E / 3000005
+    # (dram__bytes_read.sum + dram__bytes_write.sum = 73.0 MB at 3,000,005
+    # edges), scaled by the edge count for other sizes
+    traffic = 73.01e6 * E / 3000005
 
-    # e2e: host displacements through the C ABI, per-step counters read back
     # e2e: pinned host displacements through the pipelined C-ABI call (the
     # host-to-device copy of step k+1 overlaps step k); every step's counters
     # are copied back and checked by the host two steps later
