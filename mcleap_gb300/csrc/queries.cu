@@ -368,10 +368,11 @@ struct GridView {
   int nx, ny, morton, periodic;
 };
 
-__device__ __forceinline__ int cell_coord(float p, float mn, float c, int n, int periodic) {
+__device__ __forceinline__ int cell_coord(float p, float mn, float c, int n, int periodic, int* outside = nullptr) {
   float kf = floorf(__fdiv_rn(__fsub_rn(p, mn), c));
   kf = fminf(fmaxf(kf, -1.0e9f), 1.0e9f);  // also maps NaN to a border cell
   int k = (int)kf;
+  if (outside && (k < 0 || k >= n)) *outside = 1;
   if (periodic) {
     k %= n;
     if (k < 0) k += n;
@@ -385,14 +386,18 @@ __device__ __forceinline__ int cell_id(const GridView& G, int x, int y) {
   return y * G.nx + x;
 }
 
-__global__ void k_grid_hash(GridView G, int n, const float2* pos, int* cell, int* count) {
+// outside (may be NULL): set when a point's cell coordinate lies outside the
+// grid before wrapping or clamping (the point is outside the domain).
+__global__ void k_grid_hash(GridView G, int n, const float2* pos, int* cell, int* count, int* outside = nullptr) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float2 p = pos[i];
-  const int c = cell_id(G, cell_coord(p.x, G.minx, G.cx, G.nx, G.periodic),
-                        cell_coord(p.y, G.miny, G.cy, G.ny, G.periodic));
+  int out = 0;
+  const int c = cell_id(G, cell_coord(p.x, G.minx, G.cx, G.nx, G.periodic, &out),
+                        cell_coord(p.y, G.miny, G.cy, G.ny, G.periodic, &out));
   cell[i] = c;
   atomicAdd(count + c, 1);
+  if (out && outside) atomicOr(outside, 1);
 }
 
 // Exclusive scan of the cell counts, single-pass per block + block offsets.
@@ -470,7 +475,8 @@ __global__ void __launch_bounds__(kFrnnThreads) k_grid_frnn(GridView G, int n, c
                                                            const int* __restrict__ count, float r, float Lx,
                                                            float Ly, int max_nb, int* __restrict__ counts,
                                                            int* __restrict__ ids, unsigned long long* overflow,
-                                                           const int* __restrict__ src) {
+                                                           const int* __restrict__ src,
+                                                           const int* __restrict__ outside, int wrap_by_segment) {
   __shared__ int stage[kFrnnThreads * (kStageCap + 1)];
   __shared__ int cnts[kFrnnThreads];
   const int t = threadIdx.x, row0 = blockIdx.x * kFrnnThreads, i = row0 + t;
@@ -478,6 +484,12 @@ __global__ void __launch_bounds__(kFrnnThreads) k_grid_frnn(GridView G, int n, c
   const int scap = max_nb < kStageCap ? max_nb : kStageCap;
   int nf = 0;
   const float r2 = __fmul_rn(r, r);
+  // Minimum image by segment: with every point inside the domain and the
+  // stencil well under half the domain (checked by the caller), a candidate's
+  // |dx| exceeds half the domain exactly when its cell was reached across the
+  // wrap, so the per-candidate test "|dx| > Lx/2: dx -= copysign(Lx, dx)" is
+  // the constant shift of its row segment: dx + xs, with the same rounding.
+  const bool seg = kPeriodic && wrap_by_segment && outside && __ldg(outside) == 0;
   if (i < n) {
     const float2 p = pos[i];
     const int row = src ? __ldg(src + i) : i;
@@ -509,7 +521,11 @@ __global__ void __launch_bounds__(kFrnnThreads) k_grid_frnn(GridView G, int n, c
       int xlo = (int)floorf(fmaxf(fminf((px - hw) * ix, 1e9f), -1e9f));
       int xhi = (int)floorf(fmaxf(fminf((px + hw) * ix, 1e9f), -1e9f));
       int y = yy;
-      if (kPeriodic) {
+      float ys = 0.f;
+      if (kPeriodic && seg) {
+        if (y < 0) { y += G.ny; ys = Ly; }
+        else if (y >= G.ny) { y -= G.ny; ys = -Ly; }
+      } else if (kPeriodic) {
         y %= G.ny;
         if (y < 0) y += G.ny;
         if (xhi - xlo + 1 > G.nx) { xlo = 0; xhi = G.nx - 1; }
@@ -521,7 +537,13 @@ __global__ void __launch_bounds__(kFrnnThreads) k_grid_frnn(GridView G, int n, c
 #pragma unroll 1
       for (int sgi = 0; sgi < 2; ++sgi) {
         int sa, sb;
-        if (kPeriodic) {
+        float xs = 0.f;
+        if (kPeriodic && seg) {
+          // cells left of 0 are the row's end (+Lx), right of nx-1 its start (-Lx)
+          const int s0 = xlo < 0 ? xlo + G.nx : xlo, last = s0 + (xhi - xlo);
+          if (sgi == 0) { sa = s0; sb = last < G.nx ? last : G.nx - 1; xs = xlo < 0 ? Lx : 0.f; }
+          else { if (last < G.nx) continue; sa = 0; sb = last - G.nx; xs = xlo < 0 ? 0.f : -Lx; }
+        } else if (kPeriodic) {
           // [xlo, xhi] (at most nx cells) in stencil order: from the wrapped
           // start to the end of the row, then on from cell 0
           const int s0 = (xlo % G.nx + G.nx) % G.nx, last = s0 + (xhi - xlo);
@@ -534,7 +556,16 @@ __global__ void __launch_bounds__(kFrnnThreads) k_grid_frnn(GridView G, int n, c
         }
         const int b = __ldg(start + base + sa);
         const int e = __ldg(start + base + sb) + __ldg(count + base + sb);
-        if (nf + (e - b) <= scap) {
+        if (seg && nf + (e - b) <= scap) {
+#pragma unroll 4
+          for (int j = b; j < e; ++j) {
+            const float2 o = pos[j];
+            const float dx = __fadd_rn(__fsub_rn(p.x, o.x), xs), dy = __fadd_rn(__fsub_rn(p.y, o.y), ys);
+            const bool hit = (__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)) <= r2) & (j != i);
+            mine[nf] = j;
+            nf += hit ? 1 : 0;
+          }
+        } else if (nf + (e - b) <= scap) {
 #pragma unroll 4
           for (int j = b; j < e; ++j) {
             const float2 o = pos[j];
@@ -579,14 +610,25 @@ __global__ void __launch_bounds__(kFrnnThreads) k_grid_frnn(GridView G, int n, c
   }
 }
 
+// outside: the out-of-domain flag of the hashing of `pos` (NULL: unknown).
 int launch_grid_frnn(const GridView& G, int n, const float2* pos, const int* start, const int* count, float r,
                      float Lx, float Ly, int max_nb, int* counts, int* ids, unsigned long long* ovf,
-                     const int* src, cudaStream_t s) {
+                     const int* src, cudaStream_t s, const int* outside) {
   const unsigned blocks = (unsigned)((n + kFrnnThreads - 1) / kFrnnThreads);
+  // the minimum image by row segment is exact when every candidate cell lies
+  // within 0.45 of the domain of the query point (stencil half-width + a
+  // cell + the kernel's margins, with slack) and a row spans under nx cells
+  auto fits = [&](float c, float L, int cells, float mn) {
+    const double margin = 1e-3 * c + 1e-5 * (2.0 * std::fabs((double)mn) + L + r);
+    return cells >= 20 && (1.0001 * r + margin + c) * 1.01 <= 0.45 * L;
+  };
+  const int by_segment = G.periodic && outside && fits(G.cx, Lx, G.nx, G.minx) && fits(G.cy, Ly, G.ny, G.miny);
   if (G.periodic)
-    k_grid_frnn<true><<<blocks, kFrnnThreads, 0, s>>>(G, n, pos, start, count, r, Lx, Ly, max_nb, counts, ids, ovf, src);
+    k_grid_frnn<true><<<blocks, kFrnnThreads, 0, s>>>(G, n, pos, start, count, r, Lx, Ly, max_nb, counts, ids, ovf, src,
+                                                      outside, by_segment);
   else
-    k_grid_frnn<false><<<blocks, kFrnnThreads, 0, s>>>(G, n, pos, start, count, r, Lx, Ly, max_nb, counts, ids, ovf, src);
+    k_grid_frnn<false><<<blocks, kFrnnThreads, 0, s>>>(G, n, pos, start, count, r, Lx, Ly, max_nb, counts, ids, ovf,
+                                                       src, outside, 0);
   QCK(cudaGetLastError());
   return MCL_OK;
 }
@@ -858,7 +900,7 @@ int mcl_grid_create(int64_t n, float minx, float miny, float cx, float cy, int32
   cudaError_t e = cudaSuccess;
   auto A = [&](void** p, size_t b) { if (e == cudaSuccess) e = cudaMalloc(p, b); };
   A((void**)&g->cell, 4 * nn);
-  A((void**)&g->count, 4 * g->ncells);
+  A((void**)&g->count, 4 * (g->ncells + 1));  // + the out-of-domain flag of the last build
   A((void**)&g->start, 4 * g->ncells);
   A((void**)&g->cursor, 4 * g->ncells);
   A((void**)&g->perm, 4 * nn);
@@ -866,7 +908,7 @@ int mcl_grid_create(int64_t n, float minx, float miny, float cx, float cy, int32
   A((void**)&g->tmp, 8 * nn);
   A((void**)&g->tmp2, 8 * nn);
   A(&g->scan_tmp, 8 * nb);
-  if (e == cudaSuccess) e = cudaMemset(g->count, 0, 4 * g->ncells);
+  if (e == cudaSuccess) e = cudaMemset(g->count, 0, 4 * (g->ncells + 1));
   if (e == cudaSuccess) e = cudaMemset(g->start, 0, 4 * g->ncells);
   if (e != cudaSuccess) {
     mcl_grid_destroy(g);
@@ -893,8 +935,8 @@ namespace {
 int grid_build_tables(mcl_grid* g, const float2* pos, cudaStream_t s) {
   const int n = (int)g->n;
   const GridView G = view_of(g);
-  QCK(cudaMemsetAsync(g->count, 0, 4 * g->ncells, s));
-  k_grid_hash<<<(n + 255) / 256, 256, 0, s>>>(G, n, pos, g->cell, g->count);
+  QCK(cudaMemsetAsync(g->count, 0, 4 * (g->ncells + 1), s));
+  k_grid_hash<<<(n + 255) / 256, 256, 0, s>>>(G, n, pos, g->cell, g->count, g->count + g->ncells);
   int* tmp = (int*)g->scan_tmp;
   const int64_t nb = (g->ncells + 1023) / 1024;
   int rc = scan_exclusive(g->count, g->start, g->ncells, tmp, tmp + nb + 1, s);
@@ -947,7 +989,7 @@ int mcl_grid_frnn_ids(mcl_grid* g, float r, int max_nb, int32_t* counts, int32_t
   unsigned long long* ovf = (unsigned long long*)g->scan_tmp;
   QCK(cudaMemsetAsync(ovf, 0, 8, s));
   const int rc = launch_grid_frnn(G, n, g->tmp, g->start, g->count, r, g->cx * g->nx, g->cy * g->ny, max_nb, counts,
-                                  ids, ovf, g->src, s);
+                                  ids, ovf, g->src, s, g->count + g->ncells);
   if (rc != MCL_OK) return rc;
   if (overflow) {
     unsigned long long t = 0;
@@ -989,7 +1031,7 @@ int mcl_grid_frnn(mcl_grid* g, const mcl_float2* pos, float r, int max_nb, int32
   unsigned long long* ovf = (unsigned long long*)g->scan_tmp;
   QCK(cudaMemsetAsync(ovf, 0, 8, s));
   const int rc = launch_grid_frnn(G, n, (const float2*)pos, g->start, g->count, r, g->cx * g->nx, g->cy * g->ny,
-                                  max_nb, counts, ids, ovf, nullptr, s);
+                                  max_nb, counts, ids, ovf, nullptr, s, nullptr);
   if (rc != MCL_OK) return rc;
   if (overflow) {
     unsigned long long t = 0;
@@ -1308,7 +1350,7 @@ extern "C" int mcl_grid_frnn_noalloc(const mcl_float2* pos, int64_t n, float min
   k_grid_sort_cells<<<(unsigned)((ncells + 255) / 256), 256, 0, s>>>(ncells, start, count, src, perm);
   k_gather<<<(nn + 255) / 256, 256, 0, s>>>(nn, src, (const float2*)pos, (float2*)sorted_pos);
   const int rc2 = launch_grid_frnn(G, nn, (const float2*)sorted_pos, start, count, r, cell_x * cells_x,
-                                   cell_y * cells_y, max_nb, counts, ids, ovf, nullptr, s);
+                                   cell_y * cells_y, max_nb, counts, ids, ovf, nullptr, s, nullptr);
   if (rc2 != MCL_OK) return rc2;
   if (overflow) {
     unsigned long long t = 0;

@@ -354,6 +354,53 @@ def stencil_order_lists(sp, start, count, nx, ny, cell, mn, r, periodic, L):
     return out
 
 
+@pytest.mark.parametrize("outside", [False, True])
+def test_grid_frnn_ids_minimum_image_by_segment(M, outside):
+    # on the torus, mcl_grid_frnn_ids takes the minimum image per row segment
+    # when every point is inside the domain; it must return exactly the
+    # neighbours, in the same order, as the per-candidate minimum image of
+    # mcl_grid_frnn on the same sorted points (points outside the domain
+    # switch the segment form off)
+    import torch
+
+    from helpers import d2h
+
+    n, nc, L = 40000, 256, 8192.0
+    pos = uniform_points(n, 61 + outside)
+    hi = np.nextafter(np.float32(L), np.float32(0))
+    edge = np.array([[0, 0], [hi, hi], [0, hi], [hi, 0], [0, 4096], [hi, 17.5], [4096, hi]], np.float32)
+    pos[:len(edge)] = edge
+    if outside:
+        pos[10] = (-3.0, 100.0)
+        pos[11] = (L + 2.5, 8000.0)
+    r = 3 * spacing(n)
+    cell = L / nc
+    max_nb = 64
+    a = M.GridCount2d(n, (0.0, 0.0), (cell, cell), (nc, nc), periodic=True)
+    a.build(cuda(pos))
+    ca = torch.zeros(n, dtype=torch.int32, device="cuda")
+    ia = torch.zeros(n * max_nb, dtype=torch.int32, device="cuda")
+    assert a.frnn_ids(r, max_nb, ca, ia) == 0
+    b = M.GridCount2d(n, (0.0, 0.0), (cell, cell), (nc, nc), periodic=True)
+    d = cuda(pos)
+    b.update(d)
+    cb = torch.zeros(n, dtype=torch.int32, device="cuda")
+    ib = torch.zeros(n * max_nb, dtype=torch.int32, device="cuda")
+    assert b.frnn(d, r, max_nb, cb, ib) == 0
+    perm = d2h(b.tables()["perm"], n)  # sorted slot of input point i
+    src = np.empty(n, np.int64)
+    src[perm] = np.arange(n)
+    ca, ia = ca.cpu().numpy(), ia.cpu().numpy().reshape(n, max_nb)
+    cb, ib = cb.cpu().numpy(), ib.cpu().numpy().reshape(n, max_nb)
+    assert np.array_equal(ca, cb[perm])
+    for i in range(n):
+        k = ca[i]
+        assert ia[i, :k].tolist() == src[ib[perm[i], :k]].tolist(), i
+    assert ca[:len(edge)].min() > 0  # the corner points found neighbours across the wrap
+    a.close()
+    b.close()
+
+
 @pytest.mark.parametrize("periodic", [False, True])
 def test_grid_frnn_order_is_the_stencil_order(M, periodic):
     # the disk-shaped stencil visits fewer cells than the (2w+1)^2 square but
