@@ -227,7 +227,8 @@ def run_ours(args, rank, world, dist):
     lib = L.lib()
     # per-step queries on the moved mesh: one-ring of every vertex (column
     # layout, 32 slots) and FRNN with r = 3 x spacing on the torus (periodic
-    # grid of 512 x 512 cells of 16 units, minimum-image distances) over the N
+    # grid of 640 x 640 cells of 12.8 units = r / 1.92, the fastest of 256-1280
+    # cells per side; minimum-image distances) over the N
     # moving points, answered in vertex-id order without permuting the mesh
     do_q = not args.no_queries
     RING_M, FRNN_MAX = 32, 64
@@ -237,7 +238,7 @@ def run_ours(args, rank, world, dist):
         ring = torch.empty(V * RING_M, dtype=torch.int32, device=f"cuda:{local}")
         qcounts = torch.empty(n, dtype=torch.int32, device=f"cuda:{local}")
         qids = torch.empty(n * FRNN_MAX, dtype=torch.int32, device=f"cuda:{local}")
-        grid = M.GridCount2d(n, (0.0, 0.0), (16.0, 16.0), (512, 512), periodic=True)
+        grid = M.GridCount2d(n, (0.0, 0.0), (8192.0 / 640, 8192.0 / 640), (640, 640), periodic=True)
     torch.cuda.synchronize()
 
     cp, cf = clocks_start()
@@ -292,7 +293,7 @@ def run_ours(args, rank, world, dist):
         qinfo = {
             "one_ring": {"ms": float(ring_ms.mean()), "slots": RING_M, "truncated": trunc.value,
                          "alg_bytes": ring_bytes, "gbs": ring_bytes / (ring_ms.mean() / 1e3) / 1e9},
-            "frnn": {"ms": float(frnn_ms.mean()), "r": r_q, "grid": "periodic 512x512 cells of 16",
+            "frnn": {"ms": float(frnn_ms.mean()), "r": r_q, "grid": "periodic 640x640 cells of 12.8",
                      "neighbours": k_nb, "overflow": ovf, "alg_bytes": frnn_bytes,
                      "gbs": frnn_bytes / (frnn_ms.mean() / 1e3) / 1e9},
             "ms_per_step": 1e3 * q_s / K,
