@@ -85,3 +85,22 @@ def test_precision_stress_signs_and_edges(env):
     assert stages[1] + stages[2] + stages[3] > 0  # quads the FP32 filter could not decide
     print(f"sampled incircles: stage counts fp32/fp64/exact/sos {stages.tolist()}, exactly cocircular "
           f"{cocircular}, reference FP64 incircle wrong on {ref_wrong}")
+
+
+@pytest.mark.parametrize("exponent,rotation", [(23, 0.0), (30, 0.0), (22, 0.3)])
+def test_sign_map_is_exact(env, exponent, rotation):
+    # the reference's precision experiment as counts: every cell of the
+    # engine's map has the exact sign; near the circle the FP32 filter hands
+    # the cells to the later stages
+    from mcleap_gb300 import signmap as S
+
+    R = 128
+    counts, grid = S.sign_map(R, exponent, rotation)
+    exact = O.incircle(S.quad_points(R, exponent, rotation), mode=1)
+    assert np.array_equal(grid.ravel(), exact)
+    assert counts["positive"] + counts["zero"] + counts["negative"] == R * R
+    assert sum(counts["stages"].values()) == R * R
+    assert counts["stages"]["fp32"] < R * R
+    if rotation == 0.0:
+        assert counts["zero"] > 0  # d itself is on the circle
+    print(counts)
