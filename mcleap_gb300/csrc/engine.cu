@@ -547,6 +547,21 @@ __device__ void phase_lawson(cg::grid_group& g, const KParams& P, int src, unsig
   if ((threadIdx.x & 31) == 0 && flips) atomicAdd(&P.st->c[C_LAWSON_FLIPS], (unsigned long long)flips);
 }
 
+// Iterate the outgoing half-edges of v counter-clockwise.
+template <typename F>
+__device__ bool for_spokes(const KParams& P, int v, F f) {
+  const int s0 = ld_i(P.vhe + v);
+  if (s0 < 0 || s0 >= 2 * P.E) return false;
+  int h = s0;
+  for (int k = 0; k < 1024; ++k) {
+    f(h);
+    h = he_prev(P, h) ^ 1;
+    if (h < 0 || h >= 2 * P.E) return false;
+    if (h == s0) return true;
+  }
+  return false;
+}
+
 // ---------------------------------------------------------------------------
 // Repair (1): revert vertices of non-positive faces until all faces are positive.
 __device__ __forceinline__ bool marked(const KParams& P, int v, unsigned fs) {
@@ -557,8 +572,13 @@ __device__ __forceinline__ float2 qpos(const KParams& P, int v, unsigned fs) {
   return marked(P, v, fs) ? P.pos_old[v] : ldpos(P, v);
 }
 
-__device__ void mark_vertex(const KParams& P, int v, int& fresh, unsigned fs) {
-  if (!marked(P, v, fs) && (unsigned)atomicExch(P.vmark + v, (int)fs) != fs) ++fresh;
+// A newly marked vertex records the pass that marked it in vloc (free until
+// the insertion rounds): the next pass checks only the faces of its star.
+__device__ void mark_vertex(const KParams& P, int v, int& fresh, unsigned fs, int pass) {
+  if (!marked(P, v, fs) && (unsigned)atomicExch(P.vmark + v, (int)fs) != fs) {
+    __stcg(P.vloc + v, pass);
+    ++fresh;
+  }
 }
 
 // A non-positive face sends back one vertex per pass: the unmarked free vertex
@@ -568,20 +588,32 @@ __device__ void mark_vertex(const KParams& P, int v, int& fresh, unsigned fs) {
 // back fewer vertices means fewer removals and reinsertions; the result does
 // not depend on the choice (every sent-back vertex is reinserted at its
 // target).
-__device__ void mark_face(const KParams& P, int a, int b, int c, int& fresh, unsigned fs) {
+// A bad face whose free vertices all turned out marked (by other faces of the
+// same pass, after its orientation was read) is checked again next pass
+// through the star of one of them.
+__device__ void mark_face(const KParams& P, int a, int b, int c, int& fresh, unsigned fs, int pass) {
   const int t[3] = {a, b, c};
-  int pick = -1;
+  int pick = -1, any = -1;
   float best = -1.f;
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     const int v = t[k];
-    if (P.vfix[v] || marked(P, v, fs)) continue;
+    if (P.vfix[v]) continue;
+    if (marked(P, v, fs)) {
+      any = v;
+      continue;
+    }
     const float2 pn = ldpos(P, v), po = P.pos_old[v];
     const float dx = __fsub_rn(pn.x, po.x), dy = __fsub_rn(pn.y, po.y);
     const float m2 = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
     if (m2 > best || (m2 == best && v < pick)) { best = m2; pick = v; }
   }
-  if (pick >= 0) mark_vertex(P, pick, fresh, fs);
+  if (pick >= 0) {
+    mark_vertex(P, pick, fresh, fs, pass);
+  } else if (any >= 0) {
+    __stcg(P.vloc + any, pass);
+    ++fresh;
+  }
 }
 
 __device__ bool phase_fixpoint(cg::grid_group& g, const KParams& P, LocalCounters& lc, unsigned fs) {
@@ -596,22 +628,42 @@ __device__ bool phase_fixpoint(cg::grid_group& g, const KParams& P, LocalCounter
       P.st->c[C_FIX_PASSES] += 1;
     }
     int fresh = 0, bad = 0;
-    for (int ei = gtid; ei < P.E_it; ei += stride) {
-      const int e = edge_at(P, ei);
-      const int4 q = ld_ev(P, e);
-      if (q.x < 0) continue;
-      if (bad_v(P, q.x) || bad_v(P, q.y) || q.z >= P.V || q.w >= P.V) {
-        flag_error(P, MCL_ERR_DEGENERATE_INPUT);
-        continue;
+    if (pass == 0) {
+      // every face, once per edge side
+      for (int ei = gtid; ei < P.E_it; ei += stride) {
+        const int e = edge_at(P, ei);
+        const int4 q = ld_ev(P, e);
+        if (q.x < 0) continue;
+        if (bad_v(P, q.x) || bad_v(P, q.y) || q.z >= P.V || q.w >= P.V) {
+          flag_error(P, MCL_ERR_DEGENERATE_INPUT);
+          continue;
+        }
+        const float2 a = qpos(P, q.x, fs), b = qpos(P, q.y, fs);
+        if (q.z >= 0 && orient_v(P, a, b, qpos(P, q.z, fs), lc) <= 0) {
+          ++bad;
+          mark_face(P, q.x, q.y, q.z, fresh, fs, pass);
+        }
+        if (q.w >= 0 && orient_v(P, b, a, qpos(P, q.w, fs), lc) <= 0) {
+          ++bad;
+          mark_face(P, q.y, q.x, q.w, fresh, fs, pass);
+        }
       }
-      const float2 a = qpos(P, q.x, fs), b = qpos(P, q.y, fs);
-      if (q.z >= 0 && orient_v(P, a, b, qpos(P, q.z, fs), lc) <= 0) {
-        ++bad;
-        mark_face(P, q.x, q.y, q.z, fresh, fs);
-      }
-      if (q.w >= 0 && orient_v(P, b, a, qpos(P, q.w, fs), lc) <= 0) {
-        ++bad;
-        mark_face(P, q.y, q.x, q.w, fresh, fs);
+    } else {
+      // only a face with a vertex sent back in the last pass can have changed
+      // sign: the stars of those vertices
+      for (int vi = gtid; vi < P.V_it; vi += stride) {
+        const int v = vert_at(P, vi);
+        if (!marked(P, v, fs) || __ldcg(P.vloc + v) != pass - 1) continue;
+        const float2 pv = qpos(P, v, fs);
+        const bool ok = for_spokes(P, v, [&](int h) {
+          const int d = he_origin(P, h ^ 1), a = he_apex(P, h);
+          if (bad_v(P, d) || a < 0 || bad_v(P, a)) return;  // hull side: no face
+          if (orient_v(P, pv, qpos(P, d, fs), qpos(P, a, fs), lc) <= 0) {
+            ++bad;
+            mark_face(P, v, d, a, fresh, fs, pass);
+          }
+        });
+        if (!ok) flag_error(P, MCL_ERR_DEGENERATE_INPUT);
       }
     }
     if (fresh) atomicAdd(&P.st->fix_new[slot], fresh);
@@ -792,21 +844,6 @@ __device__ int remove_vertex(const KParams& P, int v, LocalCounters& lc, int& fl
   P.vaux[v] = !P.vfix[x] ? x : (!P.vfix[y] ? y : z);
   __stcg(P.vhe + v, -1);
   return MCL_OK;
-}
-
-// Iterate the outgoing half-edges of v counter-clockwise.
-template <typename F>
-__device__ bool for_spokes(const KParams& P, int v, F f) {
-  const int s0 = ld_i(P.vhe + v);
-  if (s0 < 0 || s0 >= 2 * P.E) return false;
-  int h = s0;
-  for (int k = 0; k < 1024; ++k) {
-    f(h);
-    h = he_prev(P, h) ^ 1;
-    if (h < 0 || h >= 2 * P.E) return false;
-    if (h == s0) return true;
-  }
-  return false;
 }
 
 __device__ bool phase_remove(cg::grid_group& g, const KParams& P, unsigned& stamp, LocalCounters& lc) {
@@ -1416,7 +1453,7 @@ __device__ __noinline__ unsigned repair_step(cg::grid_group g, const KParams P, 
     g.sync();
     const int nrev = ld_i(&P.st->vl_count[0]);
     if (gtid == 0) P.st->c[C_REVERTED] += (unsigned long long)nrev;
-    if (nrev > 0) {
+    if (nrev > 0 && P.substeps > 0) {
       // (1b) Delaunay over every edge with the sent-back vertices at their old
       // positions, then sub-steps toward their targets
       if (gtid == 0) { P.st->wl_count[0] = 0; P.st->wl_count[1] = 0; P.st->inverted = 0; P.st->hard_count = 0; }
