@@ -350,15 +350,6 @@ struct mcl_grid {
 
 namespace {
 
-__device__ __forceinline__ unsigned spread16(unsigned w) {
-  w &= 0xffff;
-  w = (w | (w << 8)) & 0x00FF00FFu;
-  w = (w | (w << 4)) & 0x0F0F0F0Fu;
-  w = (w | (w << 2)) & 0x33333333u;
-  w = (w | (w << 1)) & 0x55555555u;
-  return w;
-}
-
 struct GridView {
   float minx, miny, cx, cy;
   int nx, ny, morton, periodic;
