@@ -70,9 +70,10 @@ def max_over_ranks(x, dist, device="cpu"):
 
 
 def clocks_start():
+    """Sample SM clocks and throttle reasons every 200 ms while a timed region
+    runs; the raw samples go to $MCL_CLOCKS_CSV when set."""
     try:
-        f = open(os.path.join(ROOT, "gpurun_out", "clocks.csv") if os.path.isdir(os.path.join(ROOT, "gpurun_out"))
-                 else os.devnull, "w")
+        f = open(os.environ.get("MCL_CLOCKS_CSV") or os.devnull, "w")
         p = subprocess.Popen(
             ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
