@@ -761,11 +761,21 @@ __device__ int remove_vertex_ears(const KParams& P, int v, LocalCounters& lc) {
     __stcg(P.ev + e, make_int4(-1, -1, -1, -1));
     __stcg(P.en + e, make_int4(-1, -1, -1, -1));
   }
-  // the neighbour that later point location starts from: not a bounding
-  // corner (a corner's half-edges run along the hull, far from v)
+  // the neighbour that later point location starts from: the nearest that is
+  // not a bounding corner (a corner's half-edges run along the hull, far from
+  // v; so do the edges between consecutive hull points)
   int anchor = w[0];
-  for (int i = 0; i < k; ++i)
-    if (!P.vfix[w[i]]) { anchor = w[i]; break; }
+  {
+    const float2 pv = ldpos(P, v);
+    float best = INFINITY;
+    for (int i = 0; i < k; ++i) {
+      if (P.vfix[w[i]]) continue;
+      const float2 q = ldpos(P, w[i]);
+      const float dx = __fsub_rn(q.x, pv.x), dy = __fsub_rn(q.y, pv.y);
+      const float d2 = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
+      if (d2 < best) { best = d2; anchor = w[i]; }
+    }
+  }
   __stcg(P.vaux + v, anchor);
   __stcg(P.vhe + v, -1);
   return MCL_OK;
@@ -777,6 +787,8 @@ __device__ int remove_vertex_ears(const KParams& P, int v, LocalCounters& lc) {
 // thread; the caller owns every face of the vertex's star.
 __device__ int remove_vertex(const KParams& P, int v, LocalCounters& lc, int& flips) {
   const float2 pv = ldpos(P, v);
+  int nearest = -1;  // the nearest neighbour that is not a bounding corner
+  float nearest_d2 = INFINITY;
   for (int guard = 0; guard < 4096; ++guard) {
     const int s0 = ld_i(P.vhe + v);
     if (s0 < 0 || s0 >= 2 * P.E) return MCL_ERR_DEGENERATE_INPUT | (__LINE__ << 8);
@@ -785,6 +797,15 @@ __device__ int remove_vertex(const KParams& P, int v, LocalCounters& lc, int& fl
     int flipped = -1;
     do {
       ++deg;
+      if (guard == 0) {
+        const int w = he_origin(P, h ^ 1);
+        if (!bad_v(P, w) && !P.vfix[w]) {
+          const float2 q = ldpos(P, w);
+          const float dx = __fsub_rn(q.x, pv.x), dy = __fsub_rn(q.y, pv.y);
+          const float d2 = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
+          if (d2 < nearest_d2) { nearest_d2 = d2; nearest = w; }
+        }
+      }
       if (flipped < 0) {
         // flipping spoke h = v->w replaces faces (v,w,*) and (w,v,*) by (d,c,a), (c,d,b)
         const int e = h >> 1;
@@ -840,8 +861,10 @@ __device__ int remove_vertex(const KParams& P, int v, LocalCounters& lc, int& fl
     __stcg(P.en + es[k], make_int4(-1, -1, -1, -1));
   }
   P.vhint[v] = lxy;
-  // the neighbour that later point location starts from: not a bounding corner
-  P.vaux[v] = !P.vfix[x] ? x : (!P.vfix[y] ? y : z);
+  // the neighbour that later point location starts from: the nearest of the
+  // star it had when its removal began that is not a bounding corner (the
+  // last three can be far: consecutive points on the hull)
+  P.vaux[v] = nearest >= 0 ? nearest : (!P.vfix[x] ? x : (!P.vfix[y] ? y : z));
   __stcg(P.vhe + v, -1);
   return MCL_OK;
 }
@@ -1028,23 +1051,35 @@ __device__ int insert_start(const KParams& P, int v, bool resume) {
   int h = __ldcg(P.vhint + v);
   const bool hint_ok = h >= 0 && h < 2 * P.E && he_origin(P, h) >= 0 && he_apex(P, h) >= 0;
   if (resume && hint_ok) return h;
-  // a first start on a bounding corner's fan of long hull triangles makes the
-  // walk step along the hull one triangle at a time: prefer a face of the
-  // anchor neighbour that has no corner
-  if (hint_ok && !face_has_corner(P, h)) return h;
-  int x = __ldcg(P.vaux + v);
+  // the live anchor: the neighbour recorded at removal, or its own anchor if
+  // that one was removed too
+  int x = __ldcg(P.vaux + v), h0 = -1;
   for (int hop = 0; hop < 64 && x >= 0 && x < P.V; ++hop) {
-    const int h0 = ld_i(P.vhe + x);
-    if (h0 >= 0 && h0 < 2 * P.E) {
-      int g = h0;
-      for (int k = 0; k < 64; ++k) {
-        if (he_apex(P, g) >= 0 && !face_has_corner(P, g)) return g;
-        g = he_next(P, g ^ 1);  // next outgoing half-edge of x
-        if (g < 0 || g >= 2 * P.E || g == h0) break;
-      }
-      return hint_ok ? h : h0;
-    }
+    h0 = ld_i(P.vhe + x);
+    if (h0 >= 0 && h0 < 2 * P.E) break;
+    h0 = -1;
     x = __ldcg(P.vaux + x);
+  }
+  // a first start on a bounding corner's fan of long hull triangles makes the
+  // walk step along the hull one triangle at a time: prefer a face with no
+  // corner.  The hint's edge slot may have been freed by a later removal and
+  // reused far away, so it is taken only when it is not farther from the
+  // target than the anchor.
+  if (hint_ok && !face_has_corner(P, h)) {
+    if (h0 < 0) return h;
+    const float2 t = ldpos(P, v), ph = ldpos(P, he_origin(P, h)), px = ldpos(P, x);
+    const float dh = __fadd_rn(__fmul_rn(ph.x - t.x, ph.x - t.x), __fmul_rn(ph.y - t.y, ph.y - t.y));
+    const float dx = __fadd_rn(__fmul_rn(px.x - t.x, px.x - t.x), __fmul_rn(px.y - t.y, px.y - t.y));
+    if (dh <= dx) return h;
+  }
+  if (h0 >= 0) {
+    int g = h0;
+    for (int k = 0; k < 64; ++k) {
+      if (he_apex(P, g) >= 0 && !face_has_corner(P, g)) return g;
+      g = he_next(P, g ^ 1);  // next outgoing half-edge of x
+      if (g < 0 || g >= 2 * P.E || g == h0) break;
+    }
+    return hint_ok ? h : h0;
   }
   if (hint_ok) return h;
   // half-edge 0 of the vertex's mesh is never freed: a side of its bounding square
@@ -1082,7 +1117,11 @@ __device__ bool phase_insert(cg::grid_group& g, const KParams& P, unsigned& stam
       const int v = ld_i(in + i);
       int on = -1;
       int resume = -1;
-      const int h = locate(P, ldpos(P, v), insert_start(P, v, round > 0), &on, lc, kWalkSlice, &resume);
+      // a walk paused in the last round goes on from where it stopped; any
+      // other start is the closer of the hint (the face located last round,
+      // which can reach far along the hull) and the anchor
+      const bool paused = round > 0 && __ldcg(P.vlocf + v) == 4;
+      const int h = locate(P, ldpos(P, v), insert_start(P, v, paused), &on, lc, kWalkSlice, &resume);
       if (h == -1) {
         // not there yet: go on from here in the next round
         P.vloc[v] = resume;
