@@ -782,10 +782,22 @@ __device__ int remove_vertex_ears(const KParams& P, int v, LocalCounters& lc) {
 }
 
 // ---------------------------------------------------------------------------
-// Repair (2): removal of a vertex from a valid triangulation by flipping its
-// spokes until it has degree 3, then merging its three faces.  Runs in one
-// thread; the caller owns every face of the vertex's star.
+// Repair (2): removal of a vertex from a valid triangulation: ear clipping of
+// its star polygon, or, for stars above kEarMax spokes, flipping its spokes
+// until it has degree 3, then merging its three faces.  Runs in one thread;
+// the caller owns every face of the vertex's star.
 __device__ int remove_vertex(const KParams& P, int v, LocalCounters& lc, int& flips) {
+  {
+    // Ear clipping first: one walk around the star, then local work on the
+    // loaded polygon (the spoke flips below walk the star again after every
+    // flip, a chain of dependent loads per flip).  Stars of more than
+    // kEarMax spokes take the flips.
+    const int rc = remove_vertex_ears(P, v, lc);
+    if ((rc & 0xff) != MCL_ERR_CAPACITY) {
+      ++flips;  // counted as one repair operation
+      return rc;
+    }
+  }
   const float2 pv = ldpos(P, v);
   int nearest = -1;  // the nearest neighbour that is not a bounding corner
   float nearest_d2 = INFINITY;
