@@ -1583,8 +1583,9 @@ __global__ void __launch_bounds__(kThreads, 3) k_step(KParams P) {
   else stamp = repair_step(g, P, stamp);
   flush_counters(P, lc);
   // No closing grid barrier: each block leaves when its own work is done and
-  // the last one to leave publishes the launch.
-  __threadfence();
+  // the last one to leave publishes the launch.  The block barrier orders its
+  // threads' counter updates before thread 0's fence, and the fence (which is
+  // cumulative) orders them before the block's arrival.
   __syncthreads();
   if (threadIdx.x == 0) {
     atomicMax(&P.st->stamp_max, stamp);
