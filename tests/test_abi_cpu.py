@@ -53,6 +53,35 @@ def test_status_strings(L):
         assert lib.mcl_status_string(code) != b"unknown status"
 
 
+# entry points taking a mesh, with the argument list after the mesh (all NULL /
+# zero): each must refuse a NULL mesh with MCL_ERR_INVALID_ARGUMENT before it
+# touches the device, so this runs without a GPU
+NULL_MESH_CALLS = {
+    "mcl_batch_count": 1, "mcl_batch_range": 5, "mcl_batch_vertex_mesh": 1, "mcl_batch_download_aos": 5,
+    "mcl_batch_set_active": 3, "mcl_mesh_set_tuning": 2, "mcl_mesh_set_substeps": 1, "mcl_mesh_get_tuning": 3,
+    "mcl_settle_moves": 3, "mcl_mesh_totals": 2, "mcl_debug_timeline": 1, "mcl_debug_insert_timeline": 1,
+    "mcl_debug_counters": 2, "mcl_debug_state": 1, "mcl_mesh_validate": 1, "mcl_mesh_upload_aos": 1,
+    "mcl_mesh_sizes": 3, "mcl_mesh_positions": 1, "mcl_mesh_copy_positions": 3, "mcl_mesh_download_aos": 4,
+    "mcl_move": 2, "mcl_integrate": 3, "mcl_untangle": 2, "mcl_delaunay_restore": 2, "mcl_step": 3,
+    "mcl_step_host": 3, "mcl_step_host_async": 3, "mcl_mesh_last_status": 2,
+}
+
+
+def test_null_mesh_is_refused(L):
+    import ctypes as C
+
+    lib = L.lib()
+    scalars = (C.c_int, C.c_int32, C.c_int64, C.c_uint64, C.c_float, C.c_double)
+    for name, nargs in NULL_MESH_CALLS.items():
+        fn = getattr(lib, name)
+        types = fn.argtypes or [C.c_void_p] * (nargs + 1)
+        assert len(types) == nargs + 1, name
+        args = [0 if t in scalars else None for t in types]
+        assert args[0] is None
+        assert fn(*args) == L.MCL_ERR_INVALID_ARGUMENT, name
+    assert lib.mcl_mesh_destroy(None) == 0
+
+
 def test_host_ladder_orient_matches_golden(L):
     g = np.load(os.path.join(G, "predicates.npz"))
     sign, stage = L.predicates_host(0, g["orient_pts"])
