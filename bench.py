@@ -166,6 +166,22 @@ def _cpu_worker(n, frac_n, seconds, seed):
     return n * steps, wall, flips, steps, capped
 
 
+def _cpu_rebuild_seconds(n, seed):
+    """One exact Delaunay rebuild (the oracle's insertion with exact
+    predicates) of an n-point Taylor-Green mesh after one step, in seconds."""
+    sys.path.insert(0, ROOT)
+    from mcleap_gb300 import workloads as W
+    from oracle import oracle as O
+
+    pts = O.morton_sort(W.uniform_points(n, seed))
+    m = O.Mesh.build(pts, exact=False)
+    d = W.taylor_green_displacements(m.positions(), n, 1, frac=0.5)[0]
+    pos = (m.positions() + d).astype(np.float32)
+    t0 = time.perf_counter()
+    O.Mesh.build(pos[4:], exact=True)
+    return time.perf_counter() - t0
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -389,7 +405,9 @@ def run_ours(args, rank, world, dist):
         O.build()
         sample = min(args.cpu_sample, n)
         v, w_s, fl, steps, capped = cpu_reference(sample, n, args.cpu_seconds, 99, 1)
+        rebuild_s = _cpu_rebuild_seconds(sample, 99)
         cpu = {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
+               "oracle_rebuild_pts_per_s": sample / rebuild_s,
                "sample": f"1 core, Taylor-Green mesh of {sample} points for {w_s:.1f} s ({steps} steps, {capped} "
                          f"stopped at the Lawson cap); reference kinetic step = movePoint + untangle until false "
                          f"+ delonize (restart scan)"}
