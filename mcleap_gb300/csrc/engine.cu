@@ -1229,6 +1229,28 @@ __device__ bool phase_insert(cg::grid_group& g, const KParams& P, unsigned& stam
 // End of a launch: publish this launch's counters and status for the host,
 // add them to the running totals, and leave the working state clean for the
 // next launch (so no reset launch or memset precedes the next step).
+// The step counters of the last launch in the public record layout.
+__device__ void publish_stats(const DevState* st, mcl_step_stats* out) {
+  const unsigned long long* c = st->last;
+  out->inverted_faces = (int64_t)c[C_INVERTED];
+  out->reverted_vertices = (int64_t)c[C_REVERTED];
+  out->removed_vertices = (int64_t)c[C_REMOVED];
+  out->lawson_flips = (int64_t)c[C_LAWSON_FLIPS];
+  out->lawson_rounds = (int64_t)c[C_LAWSON_ROUNDS];
+  out->removal_flips = (int64_t)c[C_REMOVAL_FLIPS];
+  out->insert_rounds = (int64_t)c[C_INSERT_ROUNDS];
+  out->incircle_tests = (int64_t)c[C_INCIRCLE];
+  out->incircle_fp64 = (int64_t)c[C_INCIRCLE_FP64];
+  out->incircle_exact = (int64_t)c[C_INCIRCLE_EXACT];
+  out->orient_fp64 = (int64_t)c[C_ORIENT_FP64];
+  out->orient_exact = (int64_t)c[C_ORIENT_EXACT];
+  out->sos_decisions = (int64_t)c[C_SOS];
+  out->status = st->last_status;
+  out->error_site = st->last_site;
+  out->failed_launches = st->last_status != MCL_OK ? 1 : 0;
+  out->substep_vertices = (int64_t)c[C_SUBSTEP_DONE];
+}
+
 __device__ void finish_launch(const KParams& P, unsigned stamp) {
   DevState* st = P.st;
   // L2-coherent reads: other blocks' atomics and stores are not in this SM's L1
@@ -1248,6 +1270,7 @@ __device__ void finish_launch(const KParams& P, unsigned stamp) {
   }
   st->last_status = status;
   st->last_site = __ldcg(&st->site);
+  if (P.stats_out) publish_stats(st, P.stats_out);  // host-mapped: no copy launch
   st->status = 0;
   st->site = 0;
   st->wl_count[0] = st->wl_count[1] = 0;
@@ -1995,8 +2018,12 @@ static int finish(mcl_mesh* m, cudaStream_t s, mcl_step_stats* stats) {
 // must be repaired to; when valid_cur is false (points were moved since the
 // last validated state) pos[cur^1] holds the validated positions.  A fused move
 // (valid_cur true) reads pos[cur] and writes pos[cur^1].
-static int run_step(mcl_mesh* m, int move_mode, const float2* d, cudaStream_t s, mcl_step_stats* stats) {
+// stats_mapped (may be NULL): device-visible pinned host record the launch
+// itself fills at its end.
+static int run_step(mcl_mesh* m, int move_mode, const float2* d, cudaStream_t s, mcl_step_stats* stats,
+                    mcl_step_stats* stats_mapped = nullptr) {
   KParams P = make_params(m, ENGINE_STEP);
+  P.stats_out = stats_mapped;
   if (move_mode != MOVE_NONE) {
     if (m->dirty) {
       // the launch writes the other position buffer for the active meshes
@@ -2282,24 +2309,7 @@ int mcl_step_host(mcl_mesh* m, const mcl_float2* d_host, void* stream, mcl_step_
 namespace mcl {
 // the counters of the last launch as an mcl_step_stats, in device memory
 __global__ void k_publish_stats(const DevState* st, mcl_step_stats* out) {
-  if (threadIdx.x != 0) return;
-  const unsigned long long* c = st->last;
-  out->inverted_faces = (int64_t)c[C_INVERTED];
-  out->reverted_vertices = (int64_t)c[C_REVERTED];
-  out->removed_vertices = (int64_t)c[C_REMOVED];
-  out->lawson_flips = (int64_t)c[C_LAWSON_FLIPS];
-  out->lawson_rounds = (int64_t)c[C_LAWSON_ROUNDS];
-  out->removal_flips = (int64_t)c[C_REMOVAL_FLIPS];
-  out->insert_rounds = (int64_t)c[C_INSERT_ROUNDS];
-  out->incircle_tests = (int64_t)c[C_INCIRCLE];
-  out->incircle_fp64 = (int64_t)c[C_INCIRCLE_FP64];
-  out->incircle_exact = (int64_t)c[C_INCIRCLE_EXACT];
-  out->orient_fp64 = (int64_t)c[C_ORIENT_FP64];
-  out->orient_exact = (int64_t)c[C_ORIENT_EXACT];
-  out->sos_decisions = (int64_t)c[C_SOS];
-  out->status = st->last_status;
-  out->error_site = st->last_site;
-  out->failed_launches = st->last_status != MCL_OK ? 1 : 0;
+  if (threadIdx.x == 0) publish_stats(st, out);
 }
 }  // namespace mcl
 
@@ -2329,10 +2339,17 @@ int mcl_step_host_async(mcl_mesh* m, const mcl_float2* d_host, void* stream, mcl
   CK(cudaMemcpyAsync(buf, d_host, 8 * m->V, cudaMemcpyHostToDevice, m->copy_stream));
   CK(cudaEventRecord(m->ev_copied[k], m->copy_stream));
   CK(cudaStreamWaitEvent(s, m->ev_copied[k], 0));
-  const int rc = run_step(m, MOVE_DISPLACE, buf, s, nullptr);
+  // a pinned record the device can address is filled by the step itself
+  // (no publishing kernel and copy between steps); otherwise it is copied
+  mcl_step_stats* mapped = nullptr;
+  if (stats_pinned && cudaHostGetDevicePointer((void**)&mapped, stats_pinned, 0) != cudaSuccess) {
+    (void)cudaGetLastError();
+    mapped = nullptr;
+  }
+  const int rc = run_step(m, MOVE_DISPLACE, buf, s, nullptr, mapped);
   if (rc != MCL_OK) return rc;
   CK(cudaEventRecord(m->ev_used[k], s));
-  if (stats_pinned) {
+  if (stats_pinned && !mapped) {
     k_publish_stats<<<1, 32, 0, s>>>(m->st, m->stats_dev + k);
     CK(cudaMemcpyAsync(stats_pinned, m->stats_dev + k, sizeof(mcl_step_stats), cudaMemcpyDeviceToHost, s));
   }

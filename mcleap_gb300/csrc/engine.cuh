@@ -132,6 +132,7 @@ struct KParams {
   int walk_cap;
   int tail_items;          // flip rounds with at most this many queued edges run in one block
   int substeps;            // repair sub-steps before removal
+  mcl_step_stats* stats_out;  // device-visible host record the launch fills at its end (or NULL)
   const int* vroot;        // per vertex: a never-freed half-edge of its mesh (batches); NULL = half-edge 0
   // active meshes of a batch (nact == 0: every edge and vertex): the full
   // passes run over index spaces [0, E_it) and [0, V_it) that map to the
