@@ -147,10 +147,11 @@ int mcl_step_host(mcl_mesh* m, const mcl_float2* d_host, void* stream, mcl_step_
 /* Pipelined form of mcl_step_host: returns at once.  The host-to-device copy of
  * d_host (pinned memory, kept unchanged until the copy is done) runs on a copy
  * stream of the mesh into one of two staging buffers, overlapping the step in
- * flight; the step runs on `stream` after its copy, and its counters are
- * copied into *stats_pinned (pinned host memory, may be NULL) on `stream`.
- * Synchronise `stream` (or an event recorded on it) before reading them.  No
- * counterpart in the reference. */
+ * flight; the step runs on `stream` after its copy, and its counters land in
+ * *stats_pinned (pinned host memory, may be NULL): written by the step's last
+ * block when the device can address the record (cudaHostGetDevicePointer),
+ * else copied on `stream`.  Synchronise `stream` (or an event recorded on it)
+ * before reading them.  No counterpart in the reference. */
 int mcl_step_host_async(mcl_mesh* m, const mcl_float2* d_host, void* stream, mcl_step_stats* stats_pinned);
 
 /* Counters summed over every call on this mesh since creation (synchronises
