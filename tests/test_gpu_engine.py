@@ -564,3 +564,14 @@ def test_step_host_async_matches_step(M):
     b.transferToHost()
     assert np.array_equal(ht1.m_pos, ht2.m_pos)
     assert np.array_equal(ht1.edges(), ht2.edges())
+    # a pageable record (not addressable by the device) is copied instead of
+    # written by the step: the same counters arrive
+    page = np.zeros(nstat, np.uint8)
+    d = gaussian_disp(n + 4, 0.3 * spacing(n), 99, clamp_pos=pos)
+    hd = torch.from_numpy(d).pin_memory()
+    want2 = a.step(cuda(d))
+    L.check(L.lib().mcl_step_host_async(b.handle, hd.data_ptr(), stream.cuda_stream, page.ctypes.data))
+    stream.synchronize()
+    got = L.StepStats.from_buffer(page).as_dict()
+    assert got["status"] == 0 and got["inverted_faces"] == want2["inverted_faces"]
+    assert got["incircle_tests"] > 0
