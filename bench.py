@@ -389,7 +389,9 @@ def run_ours(args, rank, world, dist):
                "d2h_bytes_per_step": nstat, "ms_per_step": 1e3 * e_s / SEG, "steps": SEG * len(seg_s),
                "segments_ms_per_step": [1e3 * x / SEG for x in seg_s],
                "path": "mcl_step_host_async (pinned host displacements, copy overlapped with the previous step); "
-                       f"{KEW} untimed warm-up steps, then the median of {len(seg_s)} segments of {SEG} steps"}
+                       f"{KEW} untimed warm-up steps, then the median of {len(seg_s)} segments of {SEG} steps; "
+                       "steps back to back as an application runs them (no L2 flush in between, unlike the "
+                       "device-timed value)"}
     clocks = clocks_stop(cp, cf, local)
 
     # served vs plain on a short stream over 32 resident meshes (the serving
