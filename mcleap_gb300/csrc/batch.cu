@@ -358,8 +358,11 @@ int mcl_mesh_clone(const mcl_mesh* src, mcl_mesh** out) {
     std::memcpy(m->comp_host, src->comp_host, sizeof(int64_t) * 4 * src->ncomp);
   }
   m->tail_items = src->tail_items;
-  m->substeps = src->substeps;
   m->coop_blocks = src->coop_blocks;
+  if (src->substeps > 0 && (rc = mcl_mesh_set_substeps(m, src->substeps)) != MCL_OK) {
+    free_mesh(m);
+    return rc;
+  }
   if (src->dirty) {
     const int64_t nc = src->ncomp;
     m->dirty = new unsigned char[(size_t)nc]();
@@ -428,6 +431,16 @@ int mcl_mesh_set_tuning(mcl_mesh* m, int blocks_per_sm, int tail_items) {
 
 int mcl_mesh_set_substeps(mcl_mesh* m, int substeps) {
   if (!m || substeps < 0 || substeps > 64) return fail(MCL_ERR_INVALID_ARGUMENT, "substeps must be in [0, 64]");
+  if (substeps > 0 && !m->vl2) {
+    // the sub-step scratch (24 B per vertex) exists only for meshes that use it
+    BCK(cudaMalloc((void**)&m->vprev, 8 * m->V));
+    const cudaError_t e = cudaMalloc((void**)&m->vl2, 16 * m->V);
+    if (e != cudaSuccess) {
+      cudaFree(m->vprev);
+      m->vprev = nullptr;
+      return cuda_fail(e, "cudaMalloc(sub-step scratch)");
+    }
+  }
   m->substeps = substeps;
   return MCL_OK;
 }

@@ -1743,8 +1743,6 @@ int alloc_mesh(int64_t V, int64_t E, mcl_mesh** out) {
   A((void**)&m->vloc, 4 * V);
   A((void**)&m->vlocf, 4 * V);
   A((void**)&m->target, 8 * V);
-  A((void**)&m->vprev, 8 * V);
-  A((void**)&m->vl2, 16 * V);
   A((void**)&m->dstage, 8 * V);
   A((void**)&m->scratch, 64);
   A((void**)&m->st, sizeof(DevState));
@@ -1953,7 +1951,7 @@ static KParams make_params(mcl_mesh* m, int mode) {
   P.max_rounds = 1 << 16;
   P.walk_cap = 1 << 18;
   P.tail_items = m->tail_items;
-  P.substeps = m->substeps;
+  P.substeps = m->vl2 ? m->substeps : 0;  // no scratch, no sub-steps
   P.vroot = m->vroot;
   P.nact = m->nact;
   P.E_it = m->nact ? m->act_E : (int)m->E;

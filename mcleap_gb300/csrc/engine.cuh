@@ -120,7 +120,8 @@ struct KParams {
   int* vlocf;
   float2* target;          // per vertex: position to reinsert at
   float2* vprev;           // per vertex: position before the current repair sub-step
-  int* vl2;                // 4 x V: repair sub-step lists (movers x2, sent back, left for removal)
+  int* vl2;                // 4 x V: repair sub-step lists (movers x2, sent back, left for removal);
+                           // vprev and vl2 exist only after mcl_mesh_set_substeps(m, n > 0)
   DevState* st;
   // move inputs
   const float2* disp;

@@ -39,7 +39,7 @@ BOX_HI = float(np.nextafter(np.float32(8192), np.float32(0)))
 # Device bytes per vertex and per edge of a resident mesh: the engine's arrays
 # (positions x2, work lists, marks, reinsertion scratch; edge records, claims,
 # stamps), the batch tables, the settle table and the server's own state.
-BYTES_PER_VERTEX = 16 + 4 + 1 + 8 + 4 + 12 + 4 + 4 + 4 + 4 + 8 + 8 + 4 + 4 + 16 + 4 + 1 + 1 + 8 + 8 + 16
+BYTES_PER_VERTEX = 16 + 4 + 1 + 8 + 4 + 12 + 4 + 4 + 4 + 4 + 8 + 8 + 4 + 4 + 16 + 4 + 1 + 1 + 8
 BYTES_PER_EDGE = 16 + 16 + 4 + 4 + 4 + 8 + 4 + 8 + 16
 
 
