@@ -223,7 +223,7 @@ def run_ours(args, rank, world, dist):
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     B.build()
-    n, K, Wm = args.n, args.steps, args.warmup
+    n, K, Wm = args.n, args.steps, max(3, args.warmup)  # at least 3 untimed warm-up steps
     pts = W.uniform_points(n, 2026 + rank)
     t0 = time.perf_counter()
     ht = M.HostTriangulation()
@@ -470,7 +470,7 @@ def run_batched(args, rank, world, dist):
     torch.cuda.set_device(local)
     dev = f"cuda:{local}"
     B.build()
-    K, Wm, nm = args.steps, args.warmup, args.meshes
+    K, Wm, nm = args.steps, max(3, args.warmup), args.meshes
     rng = np.random.default_rng(4 + rank)
     sizes = np.exp(rng.uniform(np.log(100), np.log(1e5), nm)).astype(np.int64)
     t0 = time.perf_counter()
