@@ -411,8 +411,8 @@ def stencil_order_lists(sp, start, count, nx, ny, cell, mn, r, periodic, L):
     return out
 
 
-@pytest.mark.parametrize("outside", [False, True])
-def test_grid_frnn_ids_minimum_image_by_segment(M, outside):
+@pytest.mark.parametrize("outside,nc", [(False, 256), (True, 256), (False, 640)])
+def test_grid_frnn_ids_minimum_image_by_segment(M, outside, nc):
     # on the torus, mcl_grid_frnn_ids takes the minimum image per row segment
     # when every point is inside the domain; it must return exactly the
     # neighbours, in the same order, as the per-candidate minimum image of
@@ -422,7 +422,7 @@ def test_grid_frnn_ids_minimum_image_by_segment(M, outside):
 
     from helpers import d2h
 
-    n, nc, L = 40000, 256, 8192.0
+    n, L = 40000, 8192.0
     pos = uniform_points(n, 61 + outside)
     hi = np.nextafter(np.float32(L), np.float32(0))
     edge = np.array([[0, 0], [hi, hi], [0, hi], [hi, 0], [0, 4096], [hi, 17.5], [4096, hi]], np.float32)
