@@ -12,7 +12,7 @@ e2e:   the same steps through the C ABI with host displacement buffers
 (mcl_step_host: pinned host -> device copy inside the timed region) and a
 device -> host read of each step's counters.
 --impl reference: the reference's CPU kinetic path (restated in oracle/, the
-checker) on all host cores, each worker stepping an independent bounded
+oracle the tests compare with) on all host cores, each worker stepping an independent bounded
 sample of the same workload.
 
 Multi-GPU: meshes are independent, so N GPUs run N replicas (weak scaling).

@@ -1,7 +1,8 @@
 """ctypes wrapper of the CPU oracle (test infrastructure only).
 
 Only the tests, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg
-use this module: it is the checker, never the engine.  ``liboracle.so`` is the
+use this module: it is what the engine is compared with, never part of the
+engine.  ``liboracle.so`` is the
 restatement in this folder; ``_ref/libref.so`` (optional, built only where the
 reference sources exist) is the reference's own HostTriangulation and
 predicates.c, used to pin the restatement.

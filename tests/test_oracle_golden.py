@@ -2,7 +2,7 @@
 
 The fixtures in tests/golden/ come from the reference's own HostTriangulation
 and Shewchuk's predicates.c (tests/golden/make_golden.py).  These tests pin the
-CPU restatement in oracle/ before it is trusted as the GPU engine's checker.
+CPU restatement in oracle/ before the GPU engine is compared with it.
 """
 import hashlib
 import os
