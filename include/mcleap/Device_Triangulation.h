@@ -72,6 +72,15 @@ struct DeviceTriangulation {
     refresh();
     return ok;
   }
+  // include/Device_Triangulation.h:183-186 (bodies at :411-417 return false
+  // in the reference): move point p_index by d and leave a valid mesh.  Here
+  // every variant runs the kinetic step on a displacement with one nonzero
+  // entry (through host memory), so the mesh is also Delaunay afterwards.
+  bool moveFlipflop(int p_index, glm::vec2 d) { return move_one(p_index, d); }
+  bool moveFlipflopDelaunay(int p_index, glm::vec2 d) { return move_one(p_index, d); }
+  bool moveUntangling(int p_index, glm::vec2 d) { return move_one(p_index, d); }
+  bool moveUntanglingDelaunay(int p_index, glm::vec2 d) { return move_one(p_index, d); }
+
   // movePoints + untangle + delonize in one launch (no counterpart in the reference).
   bool step(glm::vec2* d) {
     const bool ok = mcl_step(mesh, reinterpret_cast<const mcl_float2*>(d), nullptr, &last_stats) == MCL_OK;
@@ -107,6 +116,16 @@ struct DeviceTriangulation {
   }
 
  private:
+  std::vector<glm::vec2> one_;  // host displacement of a single-point move
+  bool move_one(int p, glm::vec2 d) {
+    if (p < 4 || p >= m_pos_size) return false;  // the bounding corners stay
+    one_.assign((size_t)m_pos_size, glm::vec2(0.f, 0.f));
+    one_[(size_t)p] = d;
+    const bool ok =
+        mcl_step_host(mesh, reinterpret_cast<const mcl_float2*>(one_.data()), nullptr, &last_stats) == MCL_OK;
+    refresh();
+    return ok;
+  }
   void refresh() {
     mcl_float2* p = nullptr;
     mcl_mesh_positions(mesh, &p);

@@ -51,6 +51,15 @@ struct HostTriangulation {
     return true;
   }
 
+  // include/Host_Triangulation.h:77-80 (bodies at :408-413 return false in the
+  // reference): move point p_index by d and leave a valid mesh.  Here every
+  // variant steps a device copy of the mesh with that single displacement, so
+  // the mesh is also Delaunay afterwards.
+  bool moveFlipflop(int p_index, glm::vec2 d) { return move_one(p_index, d); }
+  bool moveFlipflopDelaunay(int p_index, glm::vec2 d) { return move_one(p_index, d); }
+  bool moveUntangling(int p_index, glm::vec2 d) { return move_one(p_index, d); }
+  bool moveUntanglingDelaunay(int p_index, glm::vec2 d) { return move_one(p_index, d); }
+
   // include/Host_Triangulation.h:305-319 and :417-423, on the GPU: the result is
   // the Delaunay triangulation of the current positions.
   bool delonize() { return run_on_device(); }
@@ -82,6 +91,20 @@ struct HostTriangulation {
   }
 
  private:
+  bool move_one(int p, glm::vec2 d) {
+    if (p < 4 || p >= (int)m_pos.size()) return false;  // the bounding corners stay
+    std::vector<glm::vec2> disp(m_pos.size(), glm::vec2(0.f, 0.f));
+    disp[(size_t)p] = d;
+    mcl_aos_view a = view();
+    mcl_mesh* m = nullptr;
+    mcleap_detail::check(mcl_mesh_create_from_aos(&a, &m));
+    mcl_step_stats st;
+    const int rc = mcl_step_host(m, reinterpret_cast<const mcl_float2*>(disp.data()), nullptr, &st);
+    if (rc == MCL_OK) download(m);
+    mcl_mesh_destroy(m);
+    mcleap_detail::check(rc);
+    return true;
+  }
   bool run_on_device() {
     mcl_aos_view a = view();
     mcl_mesh* m = nullptr;

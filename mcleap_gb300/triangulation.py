@@ -74,6 +74,28 @@ class HostTriangulation:
         self.m_pos[p_index] += np.asarray(d, np.float32)
         return True
 
+    def _move_one(self, p_index, d):
+        """include/Host_Triangulation.h:77-80 (the reference's bodies at
+        :408-413 return False): move one point and leave a valid Delaunay
+        mesh, by stepping a device copy with a single nonzero displacement.
+        The bounding corners (ids 0..3) refuse to move."""
+        if not 4 <= p_index < len(self.m_pos):
+            return False
+        disp = np.zeros_like(self.m_pos)
+        disp[p_index] = np.asarray(d, np.float32)
+        view = self.aos_view()
+        h = C.c_void_p()
+        L.check(L.lib().mcl_mesh_create_from_aos(C.byref(view), C.byref(h)))
+        try:
+            st = L.StepStats()
+            L.check(L.lib().mcl_step_host(h, L.ptr(disp), None, C.byref(st)))
+            self._download(h)
+        finally:
+            L.lib().mcl_mesh_destroy(h)
+        return True
+
+    moveFlipflop = moveFlipflopDelaunay = moveUntangling = moveUntanglingDelaunay = _move_one
+
     def edges(self):
         """Sorted undirected edge list (u < v), one row per edge."""
         a, b = self.m_he[0::2, 1], self.m_he[1::2, 1]
@@ -182,6 +204,20 @@ class DeviceTriangulation:
             self.last_stats = st.as_dict()
             return self.last_stats
         return None
+
+    def _move_one(self, p_index, d):
+        """include/Device_Triangulation.h:183-186 (the reference's bodies at
+        :411-417 return False): move one point and leave a valid Delaunay
+        mesh, through one kinetic step on a host displacement with a single
+        nonzero entry.  The bounding corners (ids 0..3) refuse to move."""
+        if not 4 <= p_index < self.m_pos_size:
+            return False
+        disp = np.zeros((self.m_pos_size, 2), np.float32)
+        disp[p_index] = np.asarray(d, np.float32)
+        self.step_host(disp)
+        return True
+
+    moveFlipflop = moveFlipflopDelaunay = moveUntangling = moveUntanglingDelaunay = _move_one
 
     def totals(self):
         """Counters summed over every call since creation, and the call count."""

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <random>
 #include <set>
@@ -193,6 +194,39 @@ static void test_kinetic() {
                 (long long)dt.last_stats.removed_vertices, (long long)dt.last_stats.lawson_flips, inverted);
   }
   cudaFree(d_move);
+
+  // Single-point moves (moveUntangling on the device mesh, moveFlipflopDelaunay
+  // on the host one): the point lands where asked, across many triangles, and
+  // every face stays positive; the bounding corners refuse to move.
+  auto positive_faces = [&](const HostTriangulation& h) {
+    int bad = 0;
+    for (size_t t = 0; t < h.m_t.size(); ++t) {
+      const HalfEdge& e = h.m_he[h.m_t[t].he];
+      const glm::vec2 a = h.m_pos[e.v], b = h.m_pos[h.m_he[h.m_t[t].he ^ 1].v], c = h.m_pos[e.op];
+      const double o = ((double)b.x - a.x) * ((double)c.y - a.y) - ((double)b.y - a.y) * ((double)c.x - a.x);
+      if (!(o > 0)) ++bad;
+    }
+    return bad;
+  };
+  dt.transferToHost();
+  const int p = 4 + n / 2;
+  const glm::vec2 target(4096.5f, 4100.25f);
+  const glm::vec2 dp = target - ht.m_pos[p];
+  CHECK(!dt.moveUntangling(2, glm::vec2(1.f, 1.f)), "a bounding corner moved");
+  CHECK(dt.moveUntangling(p, dp), "moveUntangling: %s", mcl_last_error());
+  dt.transferToHost();
+  CHECK(std::fabs(ht.m_pos[p].x - target.x) < 1e-2f && std::fabs(ht.m_pos[p].y - target.y) < 1e-2f,
+        "moveUntangling put point %d at (%g, %g)", p, ht.m_pos[p].x, ht.m_pos[p].y);
+  int bad = positive_faces(ht);
+  CHECK(bad == 0, "moveUntangling: %d faces not positive", bad);
+  const int q = 4 + n / 3;
+  const glm::vec2 tq = glm::vec2(100.f, 8000.f);
+  CHECK(ht.moveFlipflopDelaunay(q, tq - ht.m_pos[q]), "moveFlipflopDelaunay: %s", mcl_last_error());
+  CHECK(std::fabs(ht.m_pos[q].x - tq.x) < 1e-2f && std::fabs(ht.m_pos[q].y - tq.y) < 1e-2f,
+        "moveFlipflopDelaunay put point %d at (%g, %g)", q, ht.m_pos[q].x, ht.m_pos[q].y);
+  bad = positive_faces(ht);
+  CHECK(bad == 0, "moveFlipflopDelaunay: %d faces not positive", bad);
+  std::printf("single-point moves ok\n");
 }
 
 int main() {

@@ -196,6 +196,28 @@ def test_separate_calls_equal_fused_step(M):
     assert np.array_equal(ht1.m_pos, ht2.m_pos)
 
 
+def test_single_point_moves_match_exact_dt(M):
+    """moveUntangling / moveFlipflopDelaunay (stubs in the reference) move one
+    point across the mesh and leave the exact Delaunay triangulation."""
+    n = 3000
+    ht, srt = build_pair(M, uniform_points(n, 21))
+    dt = M.DeviceTriangulation(ht)
+    assert not dt.moveUntangling(1, (5.0, 5.0)) and not ht.moveFlipflop(3, (5.0, 5.0))
+    p, q = 4 + n // 2, 4 + n // 5
+    want = ht.m_pos.copy()
+    d = np.float32([4096.5, 4100.25]) - want[p]
+    assert dt.moveUntangling(p, d)
+    want[p] = want[p] + d
+    dt.transferToHost()
+    assert np.array_equal(ht.m_pos, want)
+    assert np.array_equal(ht.edges(), O.Mesh.build(want[4:], exact=True).edges())
+    e = np.float32([100.0, 8000.0]) - want[q]
+    assert ht.moveFlipflopDelaunay(q, e)
+    want[q] = want[q] + e
+    assert np.array_equal(ht.m_pos, want)
+    assert np.array_equal(ht.edges(), O.Mesh.build(want[4:], exact=True).edges())
+
+
 def test_one_ring_and_closest(M):
     import torch
 
