@@ -124,3 +124,29 @@ def test_host_ladder_near_degenerate(L):
     sign, stage = L.predicates_host(1, p)
     assert np.array_equal(sign, O.incircle(p, 1))
     assert (stage >= 0).all()
+
+
+def test_cpp_dropin_headers_compile_and_link(L, tmp_path):
+    """The C++ drop-in headers compile with nvcc against the C ABI, and the
+    reference-style driver program links against the library (not run here)."""
+    from mcleap_gb300 import build as B
+
+    exe = str(tmp_path / "test_dropin")
+    cmd = [B.nvcc(), "-std=c++17", "-O0", "-gencode", "arch=compute_103a,code=sm_103a",
+           "-I", os.path.join(ROOT, "include"), os.path.join(ROOT, "tests", "cpp", "test_dropin.cu"),
+           "-L", os.path.dirname(L.LIB_PATH), "-lmcl_gb300", "-o", exe]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert os.path.getsize(exe) > 0
+
+
+def test_single_point_moves_refuse_the_bounding_corners():
+    """moveFlipflop & co. leave ids 0..3 (the bounding square) alone and
+    report False, before any device work."""
+    import mcleap_gb300 as M
+
+    ht = M.HostTriangulation()
+    before = ht.m_pos.copy()
+    for f in (ht.moveFlipflop, ht.moveFlipflopDelaunay, ht.moveUntangling, ht.moveUntanglingDelaunay):
+        assert f(0, (1.0, 1.0)) is False and f(3, (1.0, 1.0)) is False and f(4, (1.0, 1.0)) is False
+    assert np.array_equal(ht.m_pos, before)
