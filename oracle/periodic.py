@@ -93,3 +93,93 @@ def shift_edges(edges, wrapped):
     e = np.array(edges, np.int64)
     e[:, 2:] += w[e[:, 1]] - w[e[:, 0]]
     return canonical(e)
+
+
+def _byte(o):
+    o = np.asarray(o, np.int64)
+    return (o[..., 0] + 8) | ((o[..., 1] + 8) << 4)
+
+
+def eo_pack(B, C, X1):
+    """Edge words in the engine's periodic encoding: one byte per offset
+    (B, C, X1), a nibble per component biased by 8."""
+    return (_byte(B) | (_byte(C) << 8) | (_byte(X1) << 16)).astype(np.uint32)
+
+
+def eo_unpack(eo):
+    w = np.asarray(eo, np.int64)
+    out = []
+    for k in range(3):
+        b = (w >> (8 * k)) & 0xFF
+        out.append(np.stack([(b & 15) - 8, ((b >> 4) & 15) - 8], -1))
+    return out
+
+
+def periodic_mesh(xy, L):
+    """The periodic Delaunay triangulation of xy as a mesh in the engine's
+    layout: ev[e] = (a, b, c, d), en[e] = (next(h0), prev(h0), next(h1),
+    prev(h1)), eo[e] = (B, C, X1) offsets; vertex ids 0..n-1, 3n edges.
+
+    Faces come from the 3 x 3 cover's exact triangulation: a cover face stands
+    for its torus face when the copy of its smallest-id vertex is the central
+    one.  Half-edges pair up as (u -> v, t) with (v -> u, -t)."""
+    n = len(xy)
+    pos, _, he, _ = O.Mesh.build(cover(xy, L), exact=True).aos()
+    h = np.arange(len(he))
+    f = he[:, 2]
+    keep = f >= 0
+    # one half-edge per face, then its two successors
+    first = np.full(f.max() + 1, -1, np.int64)
+    first[f[keep]] = h[keep]
+    first = first[first >= 0]
+    tri = np.stack([first, he[first, 0], he[he[first, 0], 0]], 1)
+    cv = he[tri, 1].astype(np.int64) - 4        # cover vertex ids of each face's origins
+    tri, cv = tri[(cv >= 0).all(1)], cv[(cv >= 0).all(1)]
+    k, i = cv // n, cv % n
+    rep = k[np.arange(len(k)), np.argmin(i, 1)] == CENTER
+    k, i = k[rep], i[rep]
+    si = np.sort(i, 1)
+    if not ((si[:, 0] < si[:, 1]) & (si[:, 1] < si[:, 2])).all():
+        raise ValueError("a face uses two copies of one vertex: too few points for the period")
+    F = len(i)
+    if F != 2 * n:
+        raise ValueError("the cover does not give a torus triangulation (%d faces for %d points)" % (F, n))
+    off = OFFSETS[k]                              # (F, 3, 2) copy of each corner
+    # half-edge (f, j): origin corner j, target corner j+1, apex corner j+2
+    j0, j1, j2 = np.arange(3), (np.arange(3) + 1) % 3, (np.arange(3) + 2) % 3
+    org, tgt, apx = i[:, j0].ravel(), i[:, j1].ravel(), i[:, j2].ravel()
+    t = (off[:, j1] - off[:, j0]).reshape(-1, 2)
+    x = (off[:, j2] - off[:, j0]).reshape(-1, 2)
+    # h0 of each edge: org < tgt, or org == tgt with t > 0
+    first_side = (org < tgt) | ((org == tgt) & ((t[:, 0] > 0) | ((t[:, 0] == 0) & (t[:, 1] > 0))))
+    key_u = np.where(first_side, org, tgt)
+    key_v = np.where(first_side, tgt, org)
+    key_t = np.where(first_side[:, None], t, -t)
+    keys = np.column_stack([key_u, key_v, key_t])
+    uniq, inv, cnt = np.unique(keys, axis=0, return_inverse=True, return_counts=True)
+    inv = inv.ravel()
+    if len(uniq) != 3 * n or (cnt != 2).any():
+        raise ValueError("half-edges do not pair into 3n edges")
+    hid = 2 * inv + (~first_side).astype(np.int64)   # half-edge id of (f, j)
+    if len(np.unique(hid)) != 6 * n:
+        raise ValueError("two half-edges of one side")
+    hf = hid.reshape(F, 3)
+    nxt = np.empty(6 * n, np.int64)
+    prv = np.empty(6 * n, np.int64)
+    nxt[hf[:, j0].ravel()] = hf[:, j1].ravel()
+    prv[hf[:, j0].ravel()] = hf[:, j2].ravel()
+    origin = np.empty(6 * n, np.int64)
+    apex = np.empty(6 * n, np.int64)
+    tt = np.empty((6 * n, 2), np.int64)
+    xx = np.empty((6 * n, 2), np.int64)
+    origin[hid], apex[hid], tt[hid], xx[hid] = org, apx, t, x
+    ev = np.stack([origin[0::2], origin[1::2], apex[0::2], apex[1::2]], 1).astype(np.int32)
+    en = np.stack([nxt[0::2], prv[0::2], nxt[1::2], prv[1::2]], 1).astype(np.int32)
+    eo = eo_pack(tt[0::2], xx[0::2], xx[1::2])
+    return ev, en, eo
+
+
+def mesh_edges(ev, eo):
+    """Canonical (u, v, ox, oy) edges of a periodic mesh in the engine layout."""
+    B = eo_unpack(eo)[0]
+    return canonical(np.column_stack([ev[:, 0], ev[:, 1], B]))
