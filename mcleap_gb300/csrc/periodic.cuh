@@ -28,6 +28,7 @@
 #pragma once
 
 #include "predicates.cuh"
+#include "../../include/mcl_gb300.h"
 
 namespace mcl {
 
@@ -146,6 +147,215 @@ MCL_HD Off wrap_position(F2& p, float lo, float L) {
   p.x = wrap_axis(p.x, lo, L, w.x);
   p.y = wrap_axis(p.y, lo, L, w.y);
   return w;
+}
+
+// ---------------------------------------------------------------------------
+// The periodic step's per-thread bodies.  Each kernel of the step is one of
+// these over a flat index; they compile for host and device, so the CPU test
+// suite runs the very same code serially (a serial run of a launch gives the
+// GPU's result: claims are max-reductions and the flips of one round write
+// disjoint fields).
+
+struct alignas(8) PF2 {
+  float x, y;
+};
+struct alignas(16) PI4 {
+  int x, y, z, w;
+};
+
+// step counters, reset by the host before each step (nondelaunay before each round)
+struct PCount {
+  unsigned long long wrapped, inverted, nondelaunay, flips, incircle, incircle_fp64, incircle_exact, orient_fp64,
+      orient_exact, sos, overflow, error, error_site;
+};
+
+struct PView {
+  int n;          // vertices
+  int E;          // edges (3n)
+  float L, lo;    // period, lower side of the domain (2L)
+  PF2* pos;       // canonical positions, in [lo, lo + L)^2
+  PI4* ev;        // (a, b, c, d)
+  PI4* en;        // (next h0, prev h0, next h1, prev h1)
+  unsigned* eo;   // offsets (B, C, X1)
+  unsigned char* wv;          // this step's wrap of each vertex (an offset byte)
+  unsigned* cand;             // round stamp of the non-Delaunay edges
+  unsigned long long* claim;  // face claims, by the smallest half-edge id of the face
+  PCount* cnt;
+};
+
+MCL_HD void p_add(unsigned long long* p, unsigned long long v) {
+#if defined(__CUDA_ARCH__)
+  atomicAdd(p, v);
+#else
+  *p += v;
+#endif
+}
+MCL_HD void p_max(unsigned long long* p, unsigned long long v) {
+#if defined(__CUDA_ARCH__)
+  atomicMax(p, v);
+#else
+  if (v > *p) *p = v;
+#endif
+}
+MCL_HD void p_error(const PView& V, int code, int site) {
+#if defined(__CUDA_ARCH__)
+  atomicCAS(&V.cnt->error, 0ull, (unsigned long long)code);
+  atomicCAS(&V.cnt->error_site, 0ull, (unsigned long long)site);
+#else
+  if (!V.cnt->error) V.cnt->error = (unsigned long long)code;
+  if (!V.cnt->error_site) V.cnt->error_site = (unsigned long long)site;
+#endif
+}
+
+MCL_HD bool p_vertices_ok(const PView& V, PI4 q) {
+  return (unsigned)q.x < (unsigned)V.n && (unsigned)q.y < (unsigned)V.n && (unsigned)q.z < (unsigned)V.n &&
+         (unsigned)q.w < (unsigned)V.n;
+}
+MCL_HD bool p_halfedges_ok(const PView& V, PI4 w) {
+  const unsigned H = 2u * (unsigned)V.E;
+  return (unsigned)w.x < H && (unsigned)w.y < H && (unsigned)w.z < H && (unsigned)w.w < H;
+}
+
+// a bijective 32-bit mix (xor-shift / multiply rounds) for claim priorities
+MCL_HD unsigned p_mix(unsigned x) {
+  x ^= x >> 16;
+  x *= 0x7feb352du;
+  x ^= x >> 15;
+  x *= 0x846ca68bu;
+  x ^= x >> 16;
+  return x;
+}
+MCL_HD unsigned long long p_key(int e, unsigned stamp) {
+  return ((unsigned long long)stamp << 32) | (unsigned)(~p_mix((unsigned)e ^ stamp));
+}
+MCL_HD int p_min(int a, int b) { return a < b ? a : b; }
+MCL_HD int p_face_a(int e, PI4 w) { return p_min(2 * e, p_min(w.x, w.y)); }
+MCL_HD int p_face_b(int e, PI4 w) { return p_min(2 * e + 1, p_min(w.z, w.w)); }
+
+struct PLocal {
+  int incircle_fp64 = 0, incircle_exact = 0, orient_fp64 = 0, orient_exact = 0, sos = 0, overflow = 0;
+};
+MCL_HD void p_flush(const PView& V, const PLocal& lc) {
+  if (lc.incircle_fp64) p_add(&V.cnt->incircle_fp64, lc.incircle_fp64);
+  if (lc.incircle_exact) p_add(&V.cnt->incircle_exact, lc.incircle_exact);
+  if (lc.orient_fp64) p_add(&V.cnt->orient_fp64, lc.orient_fp64);
+  if (lc.orient_exact) p_add(&V.cnt->orient_exact, lc.orient_exact);
+  if (lc.sos) p_add(&V.cnt->sos, lc.sos);
+  if (lc.overflow) p_add(&V.cnt->overflow, 1);
+}
+
+// vertex v: move by d[v], wrap into the domain, record the wrap
+MCL_HD void p_body_move(const PView& V, const PF2* d, int v) {
+  PF2 p = V.pos[v];
+  const PF2 dv = d[v];
+  p.x = fadd(p.x, dv.x);
+  p.y = fadd(p.y, dv.y);
+  const Off w = wrap_position(p, V.lo, V.L);
+  if (!(p.x >= V.lo && p.x < V.lo + V.L && p.y >= V.lo && p.y < V.lo + V.L)) {
+    p_error(V, MCL_ERR_INVALID_ARGUMENT, 1);  // a move of a period or more, or not finite
+    V.wv[v] = (unsigned char)off_byte(Off{0, 0});
+    return;
+  }
+  V.pos[v] = p;
+  V.wv[v] = (unsigned char)off_byte(w);
+  if (!off_zero(w)) p_add(&V.cnt->wrapped, 1);
+}
+
+// edge e: the wraps of its quad's vertices into its offset word
+MCL_HD void p_body_wrap(const PView& V, int e) {
+  const PI4 q = V.ev[e];
+  if (!p_vertices_ok(V, q)) {
+    p_error(V, MCL_ERR_DEGENERATE_INPUT, 2);
+    return;
+  }
+  const int r[4] = {q.x, q.y, q.z, q.w};
+  int delta = 0;
+  for (int k = 0; k < 4; ++k) {
+    const Off w = off_from_byte(V.wv[r[k]]);
+    if (!off_zero(w)) delta += eo_wrap_delta(k, w);
+  }
+  if (delta) V.eo[e] = V.eo[e] + (unsigned)delta;
+}
+
+// edge e: orientation of its two faces and, when both are positive, the
+// incircle test; a non-Delaunay edge claims both faces for this round
+MCL_HD void p_body_classify(const PView& V, int e, unsigned stamp) {
+  const PI4 q = V.ev[e];
+  const PI4 w = V.en[e];
+  const unsigned o = V.eo[e];
+  if (!p_vertices_ok(V, q) || !p_halfedges_ok(V, w)) {
+    p_error(V, MCL_ERR_DEGENERATE_INPUT, 3);
+    return;
+  }
+  PF2 qb, qc, qd;
+  if (!quad_frame(o, V.pos[q.y], V.pos[q.z], V.pos[q.w], V.L, qb, qc, qd)) {
+    p_error(V, MCL_ERR_DEGENERATE_INPUT, 4);  // an offset outside -1..+1
+    return;
+  }
+  const PF2 pa = V.pos[q.x];
+  PLocal lc;
+  const int sa = orient2d(pa.x, pa.y, qb.x, qb.y, qc.x, qc.y, &lc, &lc.overflow);
+  const int sb = orient2d(qb.x, qb.y, pa.x, pa.y, qd.x, qd.y, &lc, &lc.overflow);
+  if (sa <= 0 || sb <= 0) {
+    p_add(&V.cnt->inverted, (unsigned long long)((sa <= 0) + (sb <= 0)));
+    p_flush(V, lc);
+    return;
+  }
+  p_add(&V.cnt->incircle, 1);
+  const bool nd =
+      incircle_sos(pa.x, pa.y, qb.x, qb.y, qc.x, qc.y, qd.x, qd.y, q.x, q.y, q.z, q.w, &lc, &lc.overflow) > 0;
+  p_flush(V, lc);
+  if (!nd) return;
+  p_add(&V.cnt->nondelaunay, 1);
+  const unsigned long long key = p_key(e, stamp);
+  p_max(V.claim + p_face_a(e, w), key);
+  p_max(V.claim + p_face_b(e, w), key);
+  V.cand[e] = stamp;
+}
+
+// one side of a wing half-edge h: its apex, next and prev, and its apex offset byte
+MCL_HD void p_set_face(const PView& V, int h, int apex, int next, int prev, unsigned char apex_off) {
+  const int e = h >> 1;
+  PI4* q = V.ev + e;
+  PI4* w = V.en + e;
+  unsigned char* ob = reinterpret_cast<unsigned char*>(V.eo + e);
+  if (h & 1) {
+    q->w = apex;
+    w->z = next;
+    w->w = prev;
+    ob[2] = apex_off;
+  } else {
+    q->z = apex;
+    w->x = next;
+    w->y = prev;
+    ob[1] = apex_off;
+  }
+}
+
+// edge e: flip when it holds the claims of both its faces (the planar
+// engine's flip, plus the offsets)
+MCL_HD void p_body_flip(const PView& V, int e, unsigned stamp) {
+  if (V.cand[e] != stamp) return;
+  const PI4 q = V.ev[e];
+  const PI4 w = V.en[e];
+  if (!p_vertices_ok(V, q) || !p_halfedges_ok(V, w)) {
+    p_error(V, MCL_ERR_DEGENERATE_INPUT, 5);
+    return;
+  }
+  const unsigned long long key = p_key(e, stamp);
+  if (V.claim[p_face_a(e, w)] != key || V.claim[p_face_b(e, w)] != key) return;
+  const FlipOffsets f = flip_offsets(V.eo[e]);
+  const int a = q.x, b = q.y, c = q.z, d = q.w;
+  const int n0 = w.x, p0 = w.y, n1 = w.z, p1 = w.w;
+  const int h0 = 2 * e, h1 = 2 * e + 1;
+  V.ev[e] = PI4{d, c, a, b};
+  V.en[e] = PI4{p0, n1, p1, n0};
+  V.eo[e] = f.eo;
+  p_set_face(V, p0, d, n1, h0, f.p0);
+  p_set_face(V, n1, c, h0, p0, f.n1);
+  p_set_face(V, p1, c, n0, h1, f.p1);
+  p_set_face(V, n0, d, h1, p1, f.n0);
+  p_add(&V.cnt->flips, 1);
 }
 
 }  // namespace mcl

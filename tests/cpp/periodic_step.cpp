@@ -1,0 +1,98 @@
+// Serial run, on the CPU, of the periodic step's kernel bodies
+// (mcleap_gb300/csrc/periodic.cuh) in the order the GPU launches them: move +
+// wrap every vertex, fold the wraps into every edge word, then rounds of
+// classify-all / flip-winners until no edge is non-Delaunay.  A serial run of
+// one launch gives the GPU's result (claims are max-reductions, one round's
+// flips write disjoint fields), so this checks the device code's logic and
+// indexing without a GPU.
+//
+//   periodic_step IN OUT
+//   IN : int32 n, int32 E, float L, float pos[n][2], float d[n][2],
+//        int32 ev[E][4], int32 en[E][4], uint32 eo[E]
+//   OUT: int32 status, int32 flips, int32 wrapped, int32 inverted, int32 rounds,
+//        int32 nonpositive_after, float pos[n][2], int32 ev[E][4], int32 en[E][4],
+//        uint32 eo[E]
+// status: an MCL_* code from the bodies (0 ok), 100 + an I/O failure.
+#include <cstdint>
+#include <cstdio>
+#include <vector>
+
+#include "periodic.cuh"
+
+using mcl::PF2;
+using mcl::PI4;
+
+namespace {
+
+template <typename T>
+bool rd(FILE* f, T* p, size_t k) { return fread(p, sizeof(T), k, f) == k; }
+template <typename T>
+void wr(FILE* f, const T* p, size_t k) { fwrite(p, sizeof(T), k, f); }
+
+struct NoCount {
+  int incircle_fp64, incircle_exact, orient_fp64, orient_exact, sos;
+};
+
+// orientation of the face of half-edge h, in its origin's frame
+int face_sign(const mcl::PView& V, int h) {
+  const int e = h >> 1, s = h & 1;
+  const PI4 q = V.ev[e];
+  const int o = s ? q.y : q.x, t = s ? q.x : q.y, x = s ? q.w : q.z;
+  const PF2 pt = mcl::off_translate(V.pos[t], mcl::eo_target(V.eo[e], s), V.L);
+  const PF2 px = mcl::off_translate(V.pos[x], mcl::eo_apex(V.eo[e], s), V.L);
+  int overflow = 0;
+  return mcl::orient2d(V.pos[o].x, V.pos[o].y, pt.x, pt.y, px.x, px.y, (NoCount*)nullptr, &overflow);
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+  if (argc != 3) return 1;
+  int n = 0, E = 0;
+  float L = 0;
+  FILE* in = fopen(argv[1], "rb");
+  if (!in || !rd(in, &n, 1) || !rd(in, &E, 1) || !rd(in, &L, 1)) return 2;
+  std::vector<PF2> pos(n), d(n);
+  std::vector<PI4> ev(E), en(E);
+  std::vector<uint32_t> eo(E), cand(E, 0);
+  std::vector<unsigned char> wv(n, 0);
+  std::vector<unsigned long long> claim(2 * (size_t)E, 0);
+  if (!rd(in, pos.data(), n) || !rd(in, d.data(), n) || !rd(in, ev.data(), E) || !rd(in, en.data(), E) ||
+      !rd(in, eo.data(), E))
+    return 3;
+  fclose(in);
+
+  mcl::PCount cnt{};
+  mcl::PView V{n, E, L, 2.0f * L, pos.data(), ev.data(), en.data(), eo.data(), wv.data(), cand.data(),
+               claim.data(), &cnt};
+  int rounds = 0;
+  unsigned long long inverted = 0;
+  for (int v = 0; v < n; ++v) mcl::p_body_move(V, d.data(), v);
+  if (!cnt.error)
+    for (int e = 0; e < E; ++e) mcl::p_body_wrap(V, e);
+  for (unsigned stamp = 1; !cnt.error && stamp <= 4096; ++stamp) {
+    cnt.nondelaunay = 0;
+    cnt.inverted = 0;
+    for (int e = 0; e < E; ++e) mcl::p_body_classify(V, e, stamp);
+    ++rounds;
+    if (cnt.error) break;
+    if (stamp == 1) inverted = cnt.inverted;
+    if (cnt.inverted || !cnt.nondelaunay) break;
+    for (int e = 0; e < E; ++e) mcl::p_body_flip(V, e, stamp);
+  }
+  int after = 0;
+  if (!cnt.error)
+    for (int h = 0; h < 2 * E; ++h) after += face_sign(V, h) <= 0;
+
+  FILE* out = fopen(argv[2], "wb");
+  if (!out) return 4;
+  const int32_t head[6] = {(int32_t)cnt.error, (int32_t)cnt.flips, (int32_t)cnt.wrapped, (int32_t)inverted, rounds,
+                           after};
+  wr(out, head, 6);
+  wr(out, pos.data(), n);
+  wr(out, ev.data(), E);
+  wr(out, en.data(), E);
+  wr(out, eo.data(), E);
+  fclose(out);
+  return 0;
+}

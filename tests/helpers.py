@@ -102,3 +102,75 @@ def d2h(ptr, count, dtype=np.int32):
     rc = cudart().cudaMemcpy(out.ctypes.data, ptr, out.nbytes, 2)
     assert rc == 0, rc
     return out
+
+
+# -- the torus [2L, 3L)^2 of the periodic meshes (L = 8192) --------------------------
+
+TORUS_L = 8192.0
+
+
+def torus_points(n, seed, L=TORUS_L):
+    """n distinct float32 points uniform in [2L, 3L)^2."""
+    rng = np.random.default_rng(seed)
+    x0 = 2.0 * L
+    p = (x0 + rng.random((n, 2)) * L).astype(np.float32)
+    p[p >= x0 + L] = np.nextafter(np.float32(x0 + L), np.float32(0))
+    assert len(np.unique(p, axis=0)) == n
+    return p
+
+
+def torus_wrap(q, L=TORUS_L):
+    """The engine's wrap of moved float32 coordinates into [2L, 3L)."""
+    lo, hi = np.float32(2 * L), np.float32(3 * L)
+    q = q.astype(np.float32).copy()
+    up = q >= hi
+    q[up] = q[up] - np.float32(L)
+    dn = q < lo
+    r = (q[dn] + np.float32(L)).astype(np.float32)
+    r[r >= hi] = lo
+    q[dn] = r
+    return q
+
+
+def eo_fields(eo):
+    """(B, C, X1) offsets of periodic edge words (a nibble per component, bias 8)."""
+    w = np.asarray(eo, np.int64)
+    return [np.stack([((w >> (8 * k)) & 15) - 8, ((w >> (8 * k + 4)) & 15) - 8], -1) for k in range(3)]
+
+
+def torus_settle(xy, d, ev, eo, drift, L=TORUS_L):
+    """Reset to the common drift the moves of the vertices of faces the move
+    would turn (or nearly turn) over, until none would: the periodic step
+    restores Delaunay by flips only."""
+    B, C, X1 = eo_fields(eo)
+    D = B + X1
+    a, b, c, dd = (ev[:, k] for k in range(4))
+    d = d.copy()
+
+    def orient(p, q, r):
+        return (q[:, 0] - p[:, 0]) * (r[:, 1] - p[:, 1]) - (q[:, 1] - p[:, 1]) * (r[:, 0] - p[:, 0])
+
+    tol = 1e-6 * L * L / len(xy)
+    for _ in range(100):
+        p = (xy + d).astype(np.float32).astype(np.float64)
+        pa, pb, pc, pd = p[a], p[b] + B * L, p[c] + C * L, p[dd] + D * L
+        bad = (orient(pa, pb, pc) <= tol) | (orient(pb, pa, pd) <= tol)
+        if not bad.any():
+            return d
+        d[np.unique(ev[bad])] = drift
+    raise RuntimeError("torus_settle did not converge")
+
+
+def torus_faces_consistent(ev, en, eo):
+    """t(h) + t(next h) + t(prev h) = 0 around every face and x(h) = t(h) + t(next h)."""
+    B, C, X1 = eo_fields(eo)
+    h = np.arange(2 * len(ev))
+    e, s = h // 2, h % 2
+
+    def t_of(hh):
+        return np.where((hh % 2 == 1)[:, None], -B[hh // 2], B[hh // 2])
+
+    nx = np.where(s == 0, en[e, 0], en[e, 2])
+    pv = np.where(s == 0, en[e, 1], en[e, 3])
+    x = np.where((s == 0)[:, None], C[e], X1[e])
+    return bool((t_of(h) + t_of(nx) + t_of(pv) == 0).all() and (x == t_of(h) + t_of(nx)).all())
