@@ -392,6 +392,62 @@ int mcl_debug_predicates_host(int kind, const float* pts, const int32_t* ids, in
 int mcl_debug_predicates_device(int kind, const float* pts_dev, const int32_t* ids_dev, int64_t n,
                                 int32_t* sign_dev, int32_t* stage_dev, void* stream);
 
+/* ---- periodic (flat torus) meshes ------------------------------------------
+ * The reference's periodic triangulation is a stub
+ * (include/Host_PeriodicTriangulation.h: the constructor at :101-104 keeps a
+ * CGAL periodic domain, commented out; the rest is the bounding-square code).
+ * Here: n points on the torus [2L, 3L)^2, L a power of two (so every
+ * translate by one period is an exact float), point ids 0..n-1 in the
+ * caller's order, 3n edges, 2n faces, no bounding square.  Edge e holds
+ * ev[e] = (a, b, c, d) and en[e] = (next h0, prev h0, next h1, prev h1) as in
+ * the planar engine (h0 = 2e: a -> b with apex c; h1 = 2e + 1: b -> a with apex
+ * d) and one offset word eo[e]: bytes 0, 1, 2 hold, in periods, the copy of b
+ * relative to a, of c relative to a, and of d relative to b, a nibble per
+ * component biased by 8 (x low, y high). */
+typedef struct mcl_periodic mcl_periodic;
+
+/* Exact periodic Delaunay triangulation of pts_host (n points in
+ * [2L, 3L)^2, in general position), built on the GPU as the planar
+ * triangulation of the points and their copies within a band around the
+ * domain, restricted to the torus.  Fails with MCL_ERR_DEGENERATE_INPUT when
+ * the points are too sparse for the period (a face would use two copies of
+ * one point). */
+int mcl_periodic_build(const mcl_float2* pts_host, int64_t n, float L, mcl_periodic** out);
+
+/* A periodic mesh from host arrays in the layout above (validated). */
+int mcl_periodic_create(const mcl_float2* pos_host, int64_t n, float L, const int32_t* ev_host,
+                        const int32_t* en_host, const uint32_t* eo_host, mcl_periodic** out);
+int mcl_periodic_destroy(mcl_periodic* m);
+int mcl_periodic_sizes(const mcl_periodic* m, int64_t* n, int64_t* E, float* L);
+/* Any pointer may be NULL. */
+int mcl_periodic_download(mcl_periodic* m, mcl_float2* pos_host, int32_t* ev_host, int32_t* en_host,
+                          uint32_t* eo_host);
+/* The device positions (float2[n], canonical, in [2L, 3L)^2). */
+int mcl_periodic_positions(mcl_periodic* m, mcl_float2** pos_dev);
+
+/* One kinetic step on the torus: every point moves by d_dev[i] (device,
+ * float2[n]; shorter than a period) and wraps into the domain, then parallel
+ * Lawson flip rounds restore the periodic Delaunay triangulation.  Restoring
+ * is by flips only: a move that turns a face over returns
+ * MCL_ERR_DEGENERATE_INPUT with the positions moved.  stats (may be NULL):
+ * inverted_faces, lawson_flips, lawson_rounds, the predicate counters, status;
+ * wrapped (may be NULL): points that crossed a side. */
+int mcl_periodic_step(mcl_periodic* m, const mcl_float2* d_dev, void* stream, mcl_step_stats* stats,
+                      int64_t* wrapped);
+
+/* Host conversion behind mcl_periodic_build, for meshes built elsewhere: the
+ * periodic mesh that a planar triangulation of a cover of the torus stands
+ * for.  vertex_point[v] / vertex_copy[v] give, for each vertex of the planar
+ * AoS mesh, the point id it is a copy of and the copy k = 3 (oy + 1) + (ox + 1)
+ * of its translate (ox, oy) periods (-1 for vertices that are no copy, like
+ * the bounding corners).  A face stands for its torus face when the copy of its
+ * smallest point id is the untranslated one (k = 4).  Output: ev, en (int32[3n][4])
+ * and eo (uint32[3n]), edges numbered by (u, v, offset) in ascending order.
+ * No device work. */
+int mcl_periodic_from_planar(const mcl_aos_view* planar_host, const int32_t* vertex_point,
+                             const int32_t* vertex_copy, int64_t n, int32_t* ev_host, int32_t* en_host,
+                             uint32_t* eo_host);
+
 #ifdef __cplusplus
 }
 #endif

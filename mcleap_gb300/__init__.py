@@ -7,6 +7,7 @@ include/mcl_gb300.h); this package is its Python binding.
 """
 from ._lib import McleapError, lib  # noqa: F401
 from .batch import MeshBatch  # noqa: F401
+from .periodic import PeriodicTriangulation  # noqa: F401
 from .triangulation import DeviceTriangulation, GridCount2d, HostTriangulation  # noqa: F401
 
 __all__ = ["HostTriangulation", "DeviceTriangulation", "GridCount2d", "MeshBatch", "McleapError", "lib"]

@@ -39,6 +39,8 @@ EXPORTS = [
     "mcl_settle_moves", "mcl_dla_freeze", "mcl_batch_frnn_list", "mcl_one_ring_list", "mcl_batch_set_active", "mcl_batch_frnn_grid",
     "mcl_grid_mean_occupancy", "mcl_debug_predicates_host", "mcl_debug_predicates_device", "mcl_mesh_validate", "mcl_debug_state", "mcl_debug_timeline", "mcl_grid_frnn_noalloc", "mcl_debug_counters",
     "mcl_debug_insert_timeline",
+    "mcl_periodic_build", "mcl_periodic_create", "mcl_periodic_destroy", "mcl_periodic_sizes", "mcl_periodic_download",
+    "mcl_periodic_positions", "mcl_periodic_step", "mcl_periodic_from_planar",
 ]
 
 
@@ -135,6 +137,14 @@ def lib():
             "mcl_one_ring_list": ([vp, vp, i64, i32, i32, vp, vp, C.POINTER(i64)], i32),
             "mcl_batch_set_active": ([vp, vp, i64, vp], i32),
             "mcl_batch_frnn_grid": ([vp, vp, vp, f32, f32, i32, vp, vp, C.POINTER(i64)], i32),
+            "mcl_periodic_build": ([vp, i64, f32, C.POINTER(vp)], i32),
+            "mcl_periodic_create": ([vp, i64, f32, vp, vp, vp, C.POINTER(vp)], i32),
+            "mcl_periodic_destroy": ([vp], i32),
+            "mcl_periodic_sizes": ([vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(f32)], i32),
+            "mcl_periodic_download": ([vp, vp, vp, vp, vp], i32),
+            "mcl_periodic_positions": ([vp, C.POINTER(vp)], i32),
+            "mcl_periodic_step": ([vp, vp, vp, C.POINTER(StepStats), C.POINTER(i64)], i32),
+            "mcl_periodic_from_planar": ([C.POINTER(AosView), vp, vp, i64, vp, vp, vp], i32),
         }
         for name, (args, res) in sig.items():
             fn = getattr(L, name)

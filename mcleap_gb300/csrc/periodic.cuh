@@ -15,9 +15,9 @@
 // are shorter than half a period.  They are packed one byte per offset into a
 // u32 per edge (byte 0 = B, byte 1 = C, byte 2 = X1), a nibble per component
 // biased by 8: x(h) of half-edge 2e + s is byte 1 + s of eo[e], so a flip can
-// rewrite the apex offset of a wing half-edge with a byte store, and a wrap of
-// a vertex updates offsets with one signed atomic add per edge (the bias keeps
-// every nibble in 0..15, so no borrow crosses a field).
+// rewrite the apex offset of a wing half-edge with a byte store, and the wraps
+// of an edge's vertices update its word with signed adds (the bias keeps every
+// nibble in 0..15, so no borrow crosses a field).
 //
 // Exact translates: with positions in [2L, 3L), x + L stays in the binade
 // [2L, 4L) and x - L lands in [L, 2L), whose grid is finer, so every
@@ -107,9 +107,8 @@ MCL_HD FlipOffsets flip_offsets(unsigned w) {
 // Signed addend to an edge word when one of its quad's vertices changes its
 // canonical copy: the vertex's new position is old - w periods.  `role` is the
 // vertex's place in ev[e]: 0 = a (origin of h0), 1 = b, 2 = c, 3 = d.  Adding
-// the results for every role a wrapped vertex holds (in any order, with
-// atomicAdd on the GPU) gives B' = B + w_b - w_a, C' = C + w_c - w_a,
-// X1' = X1 + w_d - w_b.
+// the results for the four roles (in any order) gives B' = B + w_b - w_a,
+// C' = C + w_c - w_a, X1' = X1 + w_d - w_b.
 MCL_HD int eo_wrap_delta(int role, Off w) {
   auto field = [](int byte, Off o) { return o.x * (1 << (8 * byte)) + o.y * (1 << (8 * byte + 4)); };
   switch (role) {
@@ -165,8 +164,8 @@ struct alignas(16) PI4 {
 
 // step counters, reset by the host before each step (nondelaunay before each round)
 struct PCount {
-  unsigned long long wrapped, inverted, nondelaunay, flips, incircle, incircle_fp64, incircle_exact, orient_fp64,
-      orient_exact, sos, overflow, error, error_site;
+  unsigned long long wrapped, inverted, nondelaunay, flips, incircle_fp64, incircle_exact, orient_fp64, orient_exact,
+      sos, overflow, error, error_site;
 };
 
 struct PView {
@@ -301,7 +300,6 @@ MCL_HD void p_body_classify(const PView& V, int e, unsigned stamp) {
     p_flush(V, lc);
     return;
   }
-  p_add(&V.cnt->incircle, 1);
   const bool nd =
       incircle_sos(pa.x, pa.y, qb.x, qb.y, qc.x, qc.y, qd.x, qd.y, q.x, q.y, q.z, q.w, &lc, &lc.overflow) > 0;
   p_flush(V, lc);

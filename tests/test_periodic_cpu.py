@@ -11,6 +11,7 @@ import pytest
 
 from helpers import TORUS_L as L
 from helpers import torus_faces_consistent, torus_points, torus_settle, torus_wrap
+from oracle import oracle as O
 from oracle import periodic as P
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -111,3 +112,75 @@ def test_a_face_turned_over_is_reported(harness, tmp_path):
 def eo_b_vec(w):
     w = int(w)
     return np.array([(w & 15) - 8, ((w >> 4) & 15) - 8], np.float32)
+
+
+# -- the library's host side of the periodic meshes (no device work) -------------------
+
+@pytest.fixture(scope="module")
+def lib():
+    from mcleap_gb300 import _lib
+    from mcleap_gb300 import build as B
+
+    B.build()
+    return _lib
+
+
+def test_from_planar_equals_the_oracle_mesh(lib):
+    """The host conversion behind mcl_periodic_build, fed the oracle's planar
+    triangulation of the 3 x 3 cover, gives the oracle's periodic mesh, edge
+    numbering included."""
+    from mcleap_gb300 import periodic as MP
+
+    n = 2500
+    xy = torus_points(n, 21)
+    pos, v, he, t = O.Mesh.build(P.cover(xy, L), exact=True).aos()
+    row = np.arange(len(pos)) - 4
+    vpoint = np.where(row >= 0, row % n, -1).astype(np.int32)
+    vcopy = np.where(row >= 0, row // n, -1).astype(np.int32)
+    keep = [np.ascontiguousarray(a) for a in (pos, v, he, t)]
+    view = lib.AosView(*(lib.ptr(a) for a in keep), len(pos), len(he), len(t))
+    ev, en, eo = MP.from_planar(view, vpoint, vcopy, n)
+    ev0, en0, eo0 = P.periodic_mesh(xy, L)
+    assert np.array_equal(ev, ev0) and np.array_equal(en, en0) and np.array_equal(eo, eo0)
+    assert np.array_equal(MP.canonical_edges(ev, eo), P.periodic_edges(xy, L))
+
+
+def test_from_planar_refuses_a_sparse_cover(lib):
+    """Too few points for the period: some face would use two copies of one point."""
+    from mcleap_gb300 import periodic as MP
+
+    n = 3
+    xy = torus_points(n, 5)
+    pos, v, he, t = O.Mesh.build(P.cover(xy, L), exact=True).aos()
+    row = np.arange(len(pos)) - 4
+    keep = [np.ascontiguousarray(a) for a in (pos, v, he, t)]
+    view = lib.AosView(*(lib.ptr(a) for a in keep), len(pos), len(he), len(t))
+    with pytest.raises(lib.McleapError) as err:
+        MP.from_planar(view, np.where(row >= 0, row % n, -1), np.where(row >= 0, row // n, -1), n)
+    assert err.value.code == lib.MCL_ERR_DEGENERATE_INPUT
+
+
+def test_periodic_arguments_are_checked_before_device_work(lib):
+    import ctypes as C
+
+    h = C.c_void_p()
+    pts = torus_points(100, 1)
+    L_ = lib.lib()
+    assert L_.mcl_periodic_build(lib.ptr(pts), 100, 1000.0, C.byref(h)) == lib.MCL_ERR_INVALID_ARGUMENT
+    bad = pts.copy()
+    bad[7] = (1.0, 1.0)
+    assert L_.mcl_periodic_build(lib.ptr(bad), 100, L, C.byref(h)) == lib.MCL_ERR_DEGENERATE_INPUT
+    ev = np.zeros((300, 4), np.int32)
+    en = np.zeros((300, 4), np.int32)
+    eo = np.full(300, 0x888888, np.uint32)
+    ev[5, 2] = 100  # a vertex id out of range
+    rc = L_.mcl_periodic_create(lib.ptr(pts), 100, L, lib.ptr(ev), lib.ptr(en), lib.ptr(eo), C.byref(h))
+    assert rc == lib.MCL_ERR_INVALID_ARGUMENT and b"ev out of range" in L_.mcl_last_error()
+    ev[5, 2] = 0
+    eo[9] = 0x8A8888  # an offset of +2
+    rc = L_.mcl_periodic_create(lib.ptr(pts), 100, L, lib.ptr(ev), lib.ptr(en), lib.ptr(eo), C.byref(h))
+    assert rc == lib.MCL_ERR_INVALID_ARGUMENT and b"eo out of range" in L_.mcl_last_error()
+    for name in ("mcl_periodic_destroy",):
+        assert getattr(L_, name)(None) == lib.MCL_OK
+    st = lib.StepStats()
+    assert L_.mcl_periodic_step(None, None, None, C.byref(st), None) == lib.MCL_ERR_INVALID_ARGUMENT

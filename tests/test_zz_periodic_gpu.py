@@ -1,0 +1,106 @@
+"""Periodic (flat torus) meshes on the GPU against the torus oracle: the exact
+build (edge numbering included) and kinetic steps with wraps and flips."""
+import numpy as np
+import pytest
+
+from helpers import TORUS_L as L
+from helpers import torus_faces_consistent, torus_points, torus_settle, torus_wrap
+from oracle import periodic as P
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def M():
+    import torch
+
+    import mcleap_gb300 as M
+    from mcleap_gb300 import build as B
+
+    assert torch.cuda.is_available()
+    B.build()
+    M.lib()
+    return M
+
+
+def cuda(a):
+    import torch
+
+    return torch.from_numpy(np.ascontiguousarray(a, np.float32)).cuda()
+
+
+@pytest.mark.parametrize("n,seed", [(500, 1), (20000, 2)])
+def test_build_is_the_oracle_mesh(M, n, seed):
+    xy = torus_points(n, seed)
+    pt = M.PeriodicTriangulation(xy, L)
+    assert (pt.n, pt.E, pt.L) == (n, 3 * n, L)
+    pos, ev, en, eo = pt.download()
+    assert np.array_equal(pos, xy)
+    ev0, en0, eo0 = P.periodic_mesh(xy, L)
+    assert np.array_equal(ev, ev0) and np.array_equal(en, en0) and np.array_equal(eo, eo0)
+
+
+def test_identity_step_changes_nothing(M):
+    xy = torus_points(3000, 4)
+    pt = M.PeriodicTriangulation(xy, L)
+    before = pt.download()
+    st = pt.step(cuda(np.zeros_like(xy)))
+    assert st["status"] == 0 and st["lawson_flips"] == 0 and st["wrapped"] == 0 and st["lawson_rounds"] == 1
+    after = pt.download()
+    assert all(np.array_equal(a, b) for a, b in zip(before, after))
+
+
+def test_steps_with_wraps_match_the_oracle(M):
+    n = 20000
+    xy = torus_points(n, 3)
+    pt = M.PeriodicTriangulation(xy, L)
+    h = L / np.sqrt(n)
+    rng = np.random.default_rng(7)
+    pos = xy
+    wrapped = flips = 0
+    for shift in [(0.0, 0.0), (0.37, -0.61), (-0.9, 0.45), (0.2, 0.2)]:
+        _, ev, _, eo = pt.download()
+        drift = (np.array(shift) * h).astype(np.float32)
+        d = (rng.normal(0, 0.08 * h, (n, 2)) + drift).astype(np.float32)
+        d = torus_settle(pos, d, ev, eo, drift)
+        st = pt.step(cuda(d))
+        assert st["status"] == 0 and st["inverted_faces"] == 0, st
+        want = torus_wrap(pos + d)
+        pos2, ev2, en2, eo2 = pt.download()
+        assert np.array_equal(pos2, want)
+        assert torus_faces_consistent(ev2, en2, eo2)
+        assert np.array_equal(M.periodic.canonical_edges(ev2, eo2), P.periodic_edges(want, L))
+        wrapped += st["wrapped"]
+        flips += st["lawson_flips"]
+        pos = want
+    assert wrapped > 0 and flips > 0
+
+
+def test_mesh_from_arrays_steps_like_the_built_one(M):
+    n = 3000
+    xy = torus_points(n, 5)
+    ev, en, eo = P.periodic_mesh(xy, L)
+    a = M.PeriodicTriangulation(xy, L)
+    b = M.periodic.PeriodicTriangulation.from_arrays(xy, L, ev, en, eo)
+    h = L / np.sqrt(n)
+    drift = np.float32([0.3 * h, 0.1 * h])
+    d = (np.random.default_rng(2).normal(0, 0.05 * h, (n, 2)) + drift).astype(np.float32)
+    d = torus_settle(xy, d, ev, eo, drift)
+    a.step(cuda(d))
+    b.step(cuda(d))
+    assert all(np.array_equal(x, y) for x, y in zip(a.download(), b.download()))
+
+
+def test_a_face_turned_over_is_reported(M):
+    """Flips only on the torus: a move that turns a face over is an error, with
+    the count of faces turned."""
+    xy = torus_points(2000, 12)
+    pt = M.PeriodicTriangulation(xy, L)
+    _, ev, _, eo = pt.download()
+    a, b = ev[0, 0], ev[0, 1]
+    B = M.periodic.eo_offsets(eo[:1])[0][0].astype(np.float32)
+    d = np.zeros_like(xy)
+    d[a] = 2.0 * (xy[b] + B * np.float32(L) - xy[a])
+    with pytest.raises(M.McleapError) as err:
+        pt.step(cuda(d))
+    assert err.value.code == 6 and pt.last_stats["inverted_faces"] > 0
