@@ -184,3 +184,42 @@ def test_periodic_arguments_are_checked_before_device_work(lib):
         assert getattr(L_, name)(None) == lib.MCL_OK
     st = lib.StepStats()
     assert L_.mcl_periodic_step(None, None, None, C.byref(st), None) == lib.MCL_ERR_INVALID_ARGUMENT
+
+
+def band_cover(xy, band):
+    """The cover mcl_periodic_build triangulates: the points (copy 4), then
+    their translates within `band` of the domain, copies 0..3 and 5..8."""
+    lo, hi = 2 * L, 3 * L
+    pts, point, copy = [], [], []
+    for k in [4, 0, 1, 2, 3, 5, 6, 7, 8]:
+        ox, oy = k % 3 - 1, k // 3 - 1
+        q = (xy.astype(np.float64) + np.array([ox * L, oy * L])).astype(np.float32)
+        inside = ((q >= lo - band) & (q < hi + band)).all(1)
+        pts.append(q[inside])
+        point.append(np.nonzero(inside)[0])
+        copy.append(np.full(inside.sum(), k))
+    return np.concatenate(pts), np.concatenate(point), np.concatenate(copy)
+
+
+@pytest.mark.parametrize("n,seed", [(500, 1), (800, 31), (6000, 32)])
+def test_band_cover_build_equals_the_oracle_mesh(lib, n, seed):
+    """mcl_periodic_build's host logic with the oracle's exact builder standing
+    in for the GPU build (equal edge sets, shown by the GPU parity tests): the
+    quarter-period band cover, Morton-sorted like mcl_mesh_build, ids recovered
+    by position, converted by the library, gives the oracle's periodic mesh."""
+    from mcleap_gb300 import periodic as MP
+
+    xy = torus_points(n, seed)
+    cp, cpoint, ccopy = band_cover(xy, 0.25 * L)
+    assert len(cp) < 2.5 * n
+    srt = O.morton_sort(cp)
+    pos, v, he, t = O.Mesh.build(srt, exact=True).aos()
+    where = {(a.tobytes()): i for i, a in enumerate(cp)}
+    idx = np.array([where[p.tobytes()] for p in pos[4:]])
+    vpoint = np.concatenate([[-1] * 4, cpoint[idx]]).astype(np.int32)
+    vcopy = np.concatenate([[-1] * 4, ccopy[idx]]).astype(np.int32)
+    keep = [np.ascontiguousarray(a) for a in (pos, v, he, t)]
+    view = lib.AosView(*(lib.ptr(a) for a in keep), len(pos), len(he), len(t))
+    ev, en, eo = MP.from_planar(view, vpoint, vcopy, n)
+    ev0, en0, eo0 = P.periodic_mesh(xy, L)
+    assert np.array_equal(ev, ev0) and np.array_equal(en, en0) and np.array_equal(eo, eo0)
