@@ -435,6 +435,22 @@ int mcl_periodic_positions(mcl_periodic* m, mcl_float2** pos_dev);
 int mcl_periodic_step(mcl_periodic* m, const mcl_float2* d_dev, void* stream, mcl_step_stats* stats,
                       int64_t* wrapped);
 
+/* oneRing<M> / oneRing2<M> (include/Device_Triangulation.h:500-517) on a
+ * periodic mesh: each vertex's neighbours clockwise, starting at the smallest
+ * (id, offset), at most max_ring - 1 of them, slot 0 the count; layout
+ * MCL_LAYOUT_COLUMN (ring[(k+1) n + i]) or MCL_LAYOUT_ROW (ring[i max_ring + k]).
+ * offs_dev (may be NULL; same layout, one byte per slot) receives each
+ * neighbour's copy offset relative to the vertex (an offset byte as in eo).
+ * truncated (may be NULL): vertices with more than max_ring - 1 neighbours. */
+int mcl_periodic_one_ring(mcl_periodic* m, int max_ring, int layout, int32_t* ring_dev, uint8_t* offs_dev,
+                          void* stream, int64_t* truncated);
+
+/* closestNeighbors<M> (include/Device_Triangulation.h:520-528) on a periodic
+ * mesh, from a ring table and its offsets: the neighbour nearest on the torus
+ * (the reference's float squared distance; smallest id among equals). */
+int mcl_periodic_closest(mcl_periodic* m, int max_ring, int layout, const int32_t* ring_dev,
+                         const uint8_t* offs_dev, int32_t* closest_dev, void* stream);
+
 /* Host conversion behind mcl_periodic_build, for meshes built elsewhere: the
  * periodic mesh that a planar triangulation of a cover of the torus stands
  * for.  vertex_point[v] / vertex_copy[v] give, for each vertex of the planar

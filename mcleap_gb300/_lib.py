@@ -40,7 +40,8 @@ EXPORTS = [
     "mcl_grid_mean_occupancy", "mcl_debug_predicates_host", "mcl_debug_predicates_device", "mcl_mesh_validate", "mcl_debug_state", "mcl_debug_timeline", "mcl_grid_frnn_noalloc", "mcl_debug_counters",
     "mcl_debug_insert_timeline",
     "mcl_periodic_build", "mcl_periodic_create", "mcl_periodic_destroy", "mcl_periodic_sizes", "mcl_periodic_download",
-    "mcl_periodic_positions", "mcl_periodic_step", "mcl_periodic_from_planar",
+    "mcl_periodic_positions", "mcl_periodic_step", "mcl_periodic_from_planar", "mcl_periodic_one_ring",
+    "mcl_periodic_closest",
 ]
 
 
@@ -145,6 +146,8 @@ def lib():
             "mcl_periodic_positions": ([vp, C.POINTER(vp)], i32),
             "mcl_periodic_step": ([vp, vp, vp, C.POINTER(StepStats), C.POINTER(i64)], i32),
             "mcl_periodic_from_planar": ([C.POINTER(AosView), vp, vp, i64, vp, vp, vp], i32),
+            "mcl_periodic_one_ring": ([vp, i32, i32, vp, vp, vp, C.POINTER(i64)], i32),
+            "mcl_periodic_closest": ([vp, i32, i32, vp, vp, vp, vp], i32),
         }
         for name, (args, res) in sig.items():
             fn = getattr(L, name)

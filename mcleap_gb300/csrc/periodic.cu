@@ -43,6 +43,7 @@ struct mcl_periodic {
   unsigned char* wv;
   unsigned* cand;
   unsigned long long* claim;
+  int* vhe;          // one outgoing half-edge per vertex (queries)
   PCount* cnt;
   PCount* cnt_host;  // pinned
   unsigned stamp;    // last round stamp used
@@ -76,6 +77,18 @@ __global__ void k_pflip(PView V, unsigned stamp) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < V.E) mcl::p_body_flip(V, i, stamp);
 }
+__global__ void k_pvhe(PView V, int* vhe) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < 2 * V.E) mcl::p_body_vhe(V, vhe, i);
+}
+__global__ void k_pring(PView V, const int* vhe, bool column, int max_ring, int* ring, unsigned char* offs) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < V.n) mcl::p_body_ring(V, vhe, i, column, max_ring, ring, offs);
+}
+__global__ void k_pclosest(PView V, bool column, int max_ring, const int* ring, const unsigned char* offs, int* out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < V.n) mcl::p_body_closest(V, i, column, max_ring, ring, offs, out);
+}
 
 unsigned blocks(int64_t k) { return (unsigned)((k + kThreads - 1) / kThreads); }
 
@@ -92,6 +105,7 @@ void free_periodic(mcl_periodic* m) {
   cudaFree(m->wv);
   cudaFree(m->cand);
   cudaFree(m->claim);
+  cudaFree(m->vhe);
   cudaFree(m->cnt);
   if (m->cnt_host) cudaFreeHost(m->cnt_host);
   delete m;
@@ -279,6 +293,7 @@ int alloc_upload(const mcl_float2* pos, int64_t n, float L, const int32_t* ev, c
   A((void**)&m->wv, (size_t)n);
   A((void**)&m->cand, 4 * (size_t)E);
   A((void**)&m->claim, 16 * (size_t)E);
+  A((void**)&m->vhe, 4 * (size_t)n);
   A((void**)&m->cnt, sizeof(PCount));
   if (e == cudaSuccess) e = cudaMallocHost((void**)&m->cnt_host, sizeof(PCount));
   if (e == cudaSuccess) e = cudaMemcpy(m->pos, pos, 8 * (size_t)n, cudaMemcpyHostToDevice);
@@ -493,6 +508,37 @@ int mcl_periodic_step(mcl_periodic* m, const mcl_float2* d_dev, void* stream, mc
     msg = "mcl_periodic_step: exact predicate capacity exceeded";
   }
   return rc == MCL_OK ? MCL_OK : mcl::fail(rc, msg);
+}
+
+int mcl_periodic_one_ring(mcl_periodic* m, int max_ring, int layout, int32_t* ring_dev, uint8_t* offs_dev,
+                          void* stream, int64_t* truncated) {
+  if (!m || !ring_dev || max_ring < 1 || (layout != MCL_LAYOUT_COLUMN && layout != MCL_LAYOUT_ROW))
+    return mcl::fail(MCL_ERR_INVALID_ARGUMENT, "mcl_periodic_one_ring: bad arguments");
+  cudaStream_t s = (cudaStream_t)stream;
+  const PView V = view(m);
+  PCK(cudaMemsetAsync(m->cnt, 0, sizeof(PCount), s));
+  k_pvhe<<<blocks(2 * m->E), kThreads, 0, s>>>(V, m->vhe);
+  k_pring<<<blocks(m->n), kThreads, 0, s>>>(V, m->vhe, layout == MCL_LAYOUT_COLUMN, max_ring, ring_dev, offs_dev);
+  PCK(cudaGetLastError());
+  PCK(cudaMemcpyAsync(m->cnt_host, m->cnt, sizeof(PCount), cudaMemcpyDeviceToHost, s));
+  PCK(cudaStreamSynchronize(s));
+  if (m->cnt_host->error)
+    return mcl::fail((int)m->cnt_host->error,
+                     "mcl_periodic_one_ring: malformed mesh (site " + std::to_string(m->cnt_host->error_site) + ")");
+  if (truncated) *truncated = (int64_t)m->cnt_host->truncated;
+  return MCL_OK;
+}
+
+int mcl_periodic_closest(mcl_periodic* m, int max_ring, int layout, const int32_t* ring_dev, const uint8_t* offs_dev,
+                         int32_t* closest_dev, void* stream) {
+  if (!m || !ring_dev || !offs_dev || !closest_dev || max_ring < 1 ||
+      (layout != MCL_LAYOUT_COLUMN && layout != MCL_LAYOUT_ROW))
+    return mcl::fail(MCL_ERR_INVALID_ARGUMENT, "mcl_periodic_closest: bad arguments");
+  cudaStream_t s = (cudaStream_t)stream;
+  k_pclosest<<<blocks(m->n), kThreads, 0, s>>>(view(m), layout == MCL_LAYOUT_COLUMN, max_ring, ring_dev, offs_dev,
+                                               closest_dev);
+  PCK(cudaGetLastError());
+  return MCL_OK;
 }
 
 }  // extern "C"

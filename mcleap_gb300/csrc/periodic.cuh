@@ -165,7 +165,7 @@ struct alignas(16) PI4 {
 // step counters, reset by the host before each step (nondelaunay before each round)
 struct PCount {
   unsigned long long wrapped, inverted, nondelaunay, flips, incircle_fp64, incircle_exact, orient_fp64, orient_exact,
-      sos, overflow, error, error_site;
+      sos, overflow, error, error_site, truncated;
 };
 
 struct PView {
@@ -354,6 +354,108 @@ MCL_HD void p_body_flip(const PView& V, int e, unsigned stamp) {
   p_set_face(V, p1, c, n0, h1, f.p1);
   p_set_face(V, n0, d, h1, p1, f.n0);
   p_add(&V.cnt->flips, 1);
+}
+
+// ---------------------------------------------------------------------------
+// Queries on a periodic mesh.
+
+// half-edge h: make it its origin's outgoing half-edge (any one will do; the
+// ring below starts at its smallest neighbour whatever the walk's start)
+MCL_HD void p_body_vhe(const PView& V, int* vhe, int h) {
+  const PI4 q = V.ev[h >> 1];
+  const int o = (h & 1) ? q.y : q.x;
+  if ((unsigned)o >= (unsigned)V.n) {
+    p_error(V, MCL_ERR_DEGENERATE_INPUT, 6);
+    return;
+  }
+  vhe[o] = h;
+}
+
+MCL_HD int p_origin(const PView& V, int h) {
+  const PI4 q = V.ev[h >> 1];
+  return (h & 1) ? q.y : q.x;
+}
+// next outgoing half-edge clockwise around the origin: next(twin(h))
+MCL_HD int p_rot(const PView& V, int h) {
+  const PI4 w = V.en[(h ^ 1) >> 1];
+  return ((h ^ 1) & 1) ? w.z : w.x;
+}
+// neighbour key for the ring's start: smallest id, then smallest offset byte
+MCL_HD long long p_ring_key(int id, unsigned off) { return ((long long)id << 8) | off; }
+
+constexpr int kPeriodicMaxDeg = 4096;
+
+// vertex v: its neighbours clockwise, starting at the smallest (id, offset),
+// at most max_ring - 1 of them; slot 0 holds the count (the reference's ring
+// layout, include/kernels.cuh:54-84).  offs (may be null) receives, in the same
+// layout, each neighbour's copy offset relative to v (an offset byte).
+MCL_HD void p_body_ring(const PView& V, const int* vhe, int v, bool column, int max_ring, int* ring,
+                        unsigned char* offs) {
+  const int h0 = vhe[v];
+  const unsigned H = 2u * (unsigned)V.E;
+  if ((unsigned)h0 >= H || p_origin(V, h0) != v) {
+    p_error(V, MCL_ERR_DEGENERATE_INPUT, 7);
+    return;
+  }
+  const size_t stride = column ? (size_t)V.n : 1;
+  int* row = column ? ring + v : ring + (size_t)v * max_ring;
+  unsigned char* orow = offs ? (column ? offs + v : offs + (size_t)v * max_ring) : nullptr;
+  int start = h0, deg = 0, h = h0;
+  long long best = 0;
+  do {
+    const int nb = p_origin(V, h ^ 1);
+    const unsigned ob = off_byte(eo_target(V.eo[h >> 1], h & 1));
+    const long long key = p_ring_key(nb, ob);
+    if (deg == 0 || key < best) {
+      best = key;
+      start = h;
+    }
+    h = p_rot(V, h);
+    ++deg;
+    if ((unsigned)h >= H) {
+      p_error(V, MCL_ERR_DEGENERATE_INPUT, 8);
+      return;
+    }
+  } while (h != h0 && deg < kPeriodicMaxDeg);
+  if (h != h0) {
+    p_error(V, MCL_ERR_DEGENERATE_INPUT, 9);
+    return;
+  }
+  const int cap = max_ring - 1;
+  const int cnt = deg < cap ? deg : cap;
+  h = start;
+  for (int k = 0; k < cnt; ++k) {
+    row[(size_t)(k + 1) * stride] = p_origin(V, h ^ 1);
+    if (orow) orow[(size_t)(k + 1) * stride] = (unsigned char)off_byte(eo_target(V.eo[h >> 1], h & 1));
+    h = p_rot(V, h);
+  }
+  row[0] = cnt;
+  if (orow) orow[0] = 0;
+  if (deg > cap) p_add(&V.cnt->truncated, 1);
+}
+
+// vertex v: the ring neighbour nearest to v on the torus (smallest id among
+// equals), by the reference's float squared distance (include/kernels.cuh:125-127)
+// between v and the neighbour's copy; -1 for an empty ring.
+MCL_HD void p_body_closest(const PView& V, int v, bool column, int max_ring, const int* ring,
+                           const unsigned char* offs, int* out) {
+  const int cnt = column ? ring[v] : ring[(size_t)v * max_ring];
+  const PF2 p = V.pos[v];
+  int best = -1;
+  float bd = 0.f;
+  for (int k = 0; k < cnt && k < max_ring - 1; ++k) {
+    const size_t at = column ? (size_t)(k + 1) * V.n + v : (size_t)v * max_ring + k + 1;
+    const int j = ring[at];
+    if ((unsigned)j >= (unsigned)V.n) continue;
+    const PF2 q = off_translate(V.pos[j], off_from_byte(offs[at]), V.L);
+    const float dx = fsub(p.x, q.x), dy = fsub(p.y, q.y);
+    const float d = fadd(fmul(dx, dx), fmul(dy, dy));
+    if (best < 0 || d < bd || (d == bd && j < best)) {
+      best = j;
+      bd = d;
+    }
+  }
+  out[v] = best;
 }
 
 }  // namespace mcl

@@ -101,6 +101,21 @@ class PeriodicTriangulation:
         _, ev, _, eo = self.download()
         return canonical_edges(ev, eo)
 
+    def oneRing(self, maxRingSize, ring_neighbors, offsets=None, stream=None, layout=L.LAYOUT_COLUMN):
+        """Clockwise neighbours from the smallest (id, offset); slot 0 the
+        count.  offsets (optional uint8 device tensor, same layout): each
+        neighbour's copy offset byte.  Returns the number of truncated rings."""
+        trunc = C.c_int64()
+        L.check(L.lib().mcl_periodic_one_ring(self.handle, maxRingSize, layout, L.ptr(ring_neighbors), L.ptr(offsets),
+                                              _stream_ptr(stream), C.byref(trunc)))
+        return trunc.value
+
+    def closestNeighbors(self, maxRingSize, ring_neighbors, offsets, closest_neighbors, stream=None,
+                         layout=L.LAYOUT_COLUMN):
+        L.check(L.lib().mcl_periodic_closest(self.handle, maxRingSize, layout, L.ptr(ring_neighbors), L.ptr(offsets),
+                                             L.ptr(closest_neighbors), _stream_ptr(stream)))
+        return True
+
 
 def from_planar(aos_view, vertex_point, vertex_copy, n):
     """The periodic mesh a planar triangulation of a cover stands for (host

@@ -10,8 +10,9 @@
 //   IN : int32 n, int32 E, float L, float pos[n][2], float d[n][2],
 //        int32 ev[E][4], int32 en[E][4], uint32 eo[E]
 //   OUT: int32 status, int32 flips, int32 wrapped, int32 inverted, int32 rounds,
-//        int32 nonpositive_after, float pos[n][2], int32 ev[E][4], int32 en[E][4],
-//        uint32 eo[E]
+//        int32 nonpositive_after, int32 truncated, float pos[n][2], int32 ev[E][4],
+//        int32 en[E][4], uint32 eo[E], then the queries on the final mesh:
+//        int32 ring[kRing][n] and uint8 offs[kRing][n] (column layout), int32 closest[n]
 // status: an MCL_* code from the bodies (0 ok), 100 + an I/O failure.
 #include <cstdint>
 #include <cstdio>
@@ -28,6 +29,8 @@ template <typename T>
 bool rd(FILE* f, T* p, size_t k) { return fread(p, sizeof(T), k, f) == k; }
 template <typename T>
 void wr(FILE* f, const T* p, size_t k) { fwrite(p, sizeof(T), k, f); }
+
+constexpr int kRing = 8;  // small enough that some rings are truncated
 
 struct NoCount {
   int incircle_fp64, incircle_exact, orient_fp64, orient_exact, sos;
@@ -84,15 +87,28 @@ int main(int argc, char** argv) {
   if (!cnt.error)
     for (int h = 0; h < 2 * E; ++h) after += face_sign(V, h) <= 0;
 
+  // queries, in launch order: outgoing half-edges, rings, closest neighbours
+  std::vector<int> vhe(n, -1), ring((size_t)kRing * n, -1), closest(n, -2);
+  std::vector<unsigned char> offs((size_t)kRing * n, 0);
+  if (!cnt.error) {
+    for (int h = 0; h < 2 * E; ++h) mcl::p_body_vhe(V, vhe.data(), h);
+    for (int v = 0; v < n && !cnt.error; ++v) mcl::p_body_ring(V, vhe.data(), v, true, kRing, ring.data(), offs.data());
+    for (int v = 0; v < n && !cnt.error; ++v)
+      mcl::p_body_closest(V, v, true, kRing, ring.data(), offs.data(), closest.data());
+  }
+
   FILE* out = fopen(argv[2], "wb");
   if (!out) return 4;
-  const int32_t head[6] = {(int32_t)cnt.error, (int32_t)cnt.flips, (int32_t)cnt.wrapped, (int32_t)inverted, rounds,
-                           after};
-  wr(out, head, 6);
+  const int32_t head[7] = {(int32_t)cnt.error, (int32_t)cnt.flips, (int32_t)cnt.wrapped, (int32_t)inverted, rounds,
+                           after, (int32_t)cnt.truncated};
+  wr(out, head, 7);
   wr(out, pos.data(), n);
   wr(out, ev.data(), E);
   wr(out, en.data(), E);
   wr(out, eo.data(), E);
+  wr(out, ring.data(), ring.size());
+  wr(out, offs.data(), offs.size());
+  wr(out, closest.data(), closest.size());
   fclose(out);
   return 0;
 }

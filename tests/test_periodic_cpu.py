@@ -15,6 +15,7 @@ from oracle import oracle as O
 from oracle import periodic as P
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+RING = 8  # ring slots of the harness (kRing)
 
 
 @pytest.fixture(scope="module")
@@ -35,8 +36,8 @@ def run(harness, tmp_path, pos, d, ev, en, eo):
             f.write(np.ascontiguousarray(a).tobytes())
     subprocess.run([harness, src, dst], check=True)
     raw = open(dst, "rb").read()
-    head = [int(x) for x in np.frombuffer(raw[:24], np.int32)]
-    o = 24
+    head = [int(x) for x in np.frombuffer(raw[:28], np.int32)]
+    o = 28
     pos2 = np.frombuffer(raw[o:o + 8 * n], np.float32).reshape(n, 2)
     o += 8 * n
     ev2 = np.frombuffer(raw[o:o + 16 * E], np.int32).reshape(E, 4)
@@ -44,7 +45,14 @@ def run(harness, tmp_path, pos, d, ev, en, eo):
     en2 = np.frombuffer(raw[o:o + 16 * E], np.int32).reshape(E, 4)
     o += 16 * E
     eo2 = np.frombuffer(raw[o:o + 4 * E], np.uint32)
-    st = dict(zip(["status", "flips", "wrapped", "inverted", "rounds", "nonpositive_after"], head))
+    o += 4 * E
+    ring = np.frombuffer(raw[o:o + 4 * RING * n], np.int32).reshape(RING, n)
+    o += 4 * RING * n
+    offs = np.frombuffer(raw[o:o + RING * n], np.uint8).reshape(RING, n)
+    o += RING * n
+    closest = np.frombuffer(raw[o:o + 4 * n], np.int32)
+    run.queries = (ring, offs, closest)
+    st = dict(zip(["status", "flips", "wrapped", "inverted", "rounds", "nonpositive_after", "truncated"], head))
     return st, pos2, ev2, en2, eo2
 
 
@@ -81,7 +89,8 @@ def test_identity_step_changes_nothing(harness, tmp_path):
     xy = torus_points(2000, 9)
     ev, en, eo = P.periodic_mesh(xy, L)
     st, pos, ev2, en2, eo2 = run(harness, tmp_path, xy, np.zeros_like(xy), ev, en, eo)
-    assert st == dict(status=0, flips=0, wrapped=0, inverted=0, rounds=1, nonpositive_after=0)
+    assert {k: st[k] for k in ("status", "flips", "wrapped", "inverted", "rounds", "nonpositive_after")} == dict(
+        status=0, flips=0, wrapped=0, inverted=0, rounds=1, nonpositive_after=0)
     assert np.array_equal(ev2, ev) and np.array_equal(en2, en) and np.array_equal(eo2, eo)
 
 
@@ -184,6 +193,8 @@ def test_periodic_arguments_are_checked_before_device_work(lib):
         assert getattr(L_, name)(None) == lib.MCL_OK
     st = lib.StepStats()
     assert L_.mcl_periodic_step(None, None, None, C.byref(st), None) == lib.MCL_ERR_INVALID_ARGUMENT
+    assert L_.mcl_periodic_one_ring(None, 8, 0, None, None, None, None) == lib.MCL_ERR_INVALID_ARGUMENT
+    assert L_.mcl_periodic_closest(None, 8, 0, None, None, None, None) == lib.MCL_ERR_INVALID_ARGUMENT
 
 
 def band_cover(xy, band):
@@ -223,3 +234,52 @@ def test_band_cover_build_equals_the_oracle_mesh(lib, n, seed):
     ev, en, eo = MP.from_planar(view, vpoint, vcopy, n)
     ev0, en0, eo0 = P.periodic_mesh(xy, L)
     assert np.array_equal(ev, ev0) and np.array_equal(en, en0) and np.array_equal(eo, eo0)
+
+
+def ring_reference(edges, n):
+    """Directed (neighbour, ox, oy) sets of every vertex from canonical edges."""
+    out = [set() for _ in range(n)]
+    for u, v, ox, oy in edges:
+        out[u].add((v, ox, oy))
+        out[v].add((u, -ox, -oy))
+    return out
+
+
+def test_ring_and_closest_on_a_stepped_mesh(harness, tmp_path):
+    """One-ring (clockwise from the smallest neighbour, truncated at RING - 1)
+    and closest neighbour on the torus, by the query bodies, after a step."""
+    n = 3000
+    xy = torus_points(n, 41)
+    ev, en, eo = P.periodic_mesh(xy, L)
+    h = L / np.sqrt(n)
+    drift = np.float32([0.45 * h, -0.2 * h])
+    d = (np.random.default_rng(4).normal(0, 0.05 * h, (n, 2)) + drift).astype(np.float32)
+    d = torus_settle(xy, d, ev, eo, drift)
+    st, pos, ev2, _, eo2 = run(harness, tmp_path, xy, d, ev, en, eo)
+    assert st["status"] == 0 and st["wrapped"] > 0
+    ring, offs, closest = run.queries
+    want = ring_reference(P.periodic_edges(pos, L), n)
+    deg = np.array([len(w) for w in want])
+    assert st["truncated"] == int((deg > RING - 1).sum()) > 0
+    p64 = pos.astype(np.float64)
+    for v in range(n):
+        cnt = ring[0, v]
+        assert cnt == min(deg[v], RING - 1)
+        nb = ring[1:cnt + 1, v]
+        ob = offs[1:cnt + 1, v].astype(np.int64)
+        o = np.stack([(ob & 15) - 8, ((ob >> 4) & 15) - 8], 1)
+        got = {(int(a), int(b), int(c)) for a, (b, c) in zip(nb, o)}
+        assert got <= want[v] and (cnt < deg[v] or got == want[v])
+        # starts at the smallest (id, offset) of the whole ring, turns clockwise
+        if cnt == deg[v]:
+            assert (nb[0], ob[0]) == min(zip(nb, ob))
+        q = p64[nb] + o * L - p64[v]
+        ang = np.arctan2(q[:, 1], q[:, 0])
+        turn = np.mod(ang[1:] - ang[:-1], 2 * np.pi)
+        assert (turn > np.pi).all()  # each step turns clockwise by less than pi
+        # closest among the ring, by the float formula, smallest id among equals
+        dx = (pos[v, 0] - (pos[nb, 0] + (o[:, 0] * L).astype(np.float32))).astype(np.float32)
+        dy = (pos[v, 1] - (pos[nb, 1] + (o[:, 1] * L).astype(np.float32))).astype(np.float32)
+        dd = (dx * dx + dy * dy).astype(np.float32)
+        best = nb[np.lexsort((nb, dd))[0]]
+        assert closest[v] == best

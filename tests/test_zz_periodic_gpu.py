@@ -104,3 +104,46 @@ def test_a_face_turned_over_is_reported(M):
     with pytest.raises(M.McleapError) as err:
         pt.step(cuda(d))
     assert err.value.code == 6 and pt.last_stats["inverted_faces"] > 0
+
+
+def test_ring_and_closest_after_steps(M):
+    """One-ring (clockwise from the smallest neighbour) and closest neighbour on
+    the torus, after steps with wraps, against the oracle's edges and brute force."""
+    import torch
+
+    n = 5000
+    xy = torus_points(n, 8)
+    pt = M.PeriodicTriangulation(xy, L)
+    h = L / np.sqrt(n)
+    pos = xy
+    for shift in [(0.6, 0.1), (-0.2, -0.7)]:
+        _, ev, _, eo = pt.download()
+        drift = (np.array(shift) * h).astype(np.float32)
+        d = (np.random.default_rng(3).normal(0, 0.05 * h, (n, 2)) + drift).astype(np.float32)
+        d = torus_settle(pos, d, ev, eo, drift)
+        pt.step(cuda(d))
+        pos = torus_wrap(pos + d)
+    R = 32
+    ring = torch.full((R * n,), -1, dtype=torch.int32, device="cuda")
+    offs = torch.zeros((R * n,), dtype=torch.uint8, device="cuda")
+    assert pt.oneRing(R, ring, offs) == 0
+    closest = torch.full((n,), -2, dtype=torch.int32, device="cuda")
+    pt.closestNeighbors(R, ring, offs, closest)
+    ring = ring.cpu().numpy().reshape(R, n)
+    offs = offs.cpu().numpy().reshape(R, n).astype(np.int64)
+    closest = closest.cpu().numpy()
+    want = {}
+    for u, v, ox, oy in P.periodic_edges(pos, L):
+        want.setdefault(u, set()).add((v, ox, oy))
+        want.setdefault(v, set()).add((u, -ox, -oy))
+    for v in range(n):
+        cnt = ring[0, v]
+        nb, ob = ring[1:cnt + 1, v], offs[1:cnt + 1, v]
+        o = np.stack([(ob & 15) - 8, ((ob >> 4) & 15) - 8], 1)
+        assert {(int(a), int(b), int(c)) for a, (b, c) in zip(nb, o)} == want[v] and cnt == len(want[v])
+        assert (nb[0], ob[0]) == min(zip(nb, ob))
+        # the nearest point on the torus is a Delaunay neighbour
+        dx = (pos[v, 0] - (pos[nb, 0] + (o[:, 0] * L).astype(np.float32))).astype(np.float32)
+        dy = (pos[v, 1] - (pos[nb, 1] + (o[:, 1] * L).astype(np.float32))).astype(np.float32)
+        dd = (dx * dx + dy * dy).astype(np.float32)
+        assert closest[v] == nb[np.lexsort((nb, dd))[0]]
