@@ -427,11 +427,14 @@ int mcl_periodic_positions(mcl_periodic* m, mcl_float2** pos_dev);
 
 /* One kinetic step on the torus: every point moves by d_dev[i] (device,
  * float2[n]; shorter than a period) and wraps into the domain, then parallel
- * Lawson flip rounds restore the periodic Delaunay triangulation.  Restoring
- * is by flips only: a move that turns a face over returns
- * MCL_ERR_DEGENERATE_INPUT with the positions moved.  stats (may be NULL):
- * inverted_faces, lawson_flips, lawson_rounds, the predicate counters, status;
- * wrapped (may be NULL): points that crossed a side. */
+ * Lawson flip rounds restore the periodic Delaunay triangulation.  Moves that
+ * would turn faces over are refused vertex by vertex: the moved vertices of
+ * every turned face go back to where they were (repeatedly, since sending one
+ * back can turn another face) before any flip, so the result is always the
+ * valid periodic Delaunay triangulation of where the points ended.  stats
+ * (may be NULL): inverted_faces (turned by the move), reverted_vertices (sent
+ * back), lawson_flips, lawson_rounds, the predicate counters, status; wrapped
+ * (may be NULL): points whose move crossed a side. */
 int mcl_periodic_step(mcl_periodic* m, const mcl_float2* d_dev, void* stream, mcl_step_stats* stats,
                       int64_t* wrapped);
 

@@ -15,7 +15,10 @@
 //           edge words (one launch over edges), then rounds of classify +
 //           claim / flip winners (one launch each) until no edge is
 //           non-Delaunay; the host reads the round's counters between
-//           launches.  Flips only: a move that turns a face over is reported.
+//           launches.  A classification that finds faces turned over sends
+//           their moved vertices back (one launch over vertices, then the
+//           fold again) and classifies again; flips start from a mesh whose
+//           faces are all positive.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -41,6 +44,9 @@ struct mcl_periodic {
   PI4* en;
   unsigned* eo;
   unsigned char* wv;
+  unsigned char* wt;
+  unsigned char* mark;
+  PF2* pos_old;
   unsigned* cand;
   unsigned long long* claim;
   int* vhe;          // one outgoing half-edge per vertex (queries)
@@ -53,6 +59,7 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kMaxRounds = 4096;
+constexpr int kMaxRevertPasses = 256;
 constexpr int kCenter = 4;  // copy index of the untranslated copy
 
 #define PCK(call)                                       \
@@ -64,6 +71,10 @@ constexpr int kCenter = 4;  // copy index of the untranslated copy
 __global__ void k_pmove(PView V, const PF2* d) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < V.n) mcl::p_body_move(V, d, i);
+}
+__global__ void k_prevert(PView V) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < V.n) mcl::p_body_revert(V, i);
 }
 __global__ void k_pwrap(PView V) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -93,7 +104,8 @@ __global__ void k_pclosest(PView V, bool column, int max_ring, const int* ring, 
 unsigned blocks(int64_t k) { return (unsigned)((k + kThreads - 1) / kThreads); }
 
 PView view(mcl_periodic* m) {
-  return PView{(int)m->n, (int)m->E, m->L, 2.0f * m->L, m->pos, m->ev, m->en, m->eo, m->wv, m->cand, m->claim, m->cnt};
+  return PView{(int)m->n, (int)m->E, m->L,    2.0f * m->L,  m->pos,  m->ev,    m->en,    m->eo,
+               m->wv,      m->wt,      m->mark, m->pos_old,   m->cand, m->claim, m->cnt};
 }
 
 void free_periodic(mcl_periodic* m) {
@@ -103,6 +115,9 @@ void free_periodic(mcl_periodic* m) {
   cudaFree(m->en);
   cudaFree(m->eo);
   cudaFree(m->wv);
+  cudaFree(m->wt);
+  cudaFree(m->mark);
+  cudaFree(m->pos_old);
   cudaFree(m->cand);
   cudaFree(m->claim);
   cudaFree(m->vhe);
@@ -291,6 +306,9 @@ int alloc_upload(const mcl_float2* pos, int64_t n, float L, const int32_t* ev, c
   A((void**)&m->en, 16 * (size_t)E);
   A((void**)&m->eo, 4 * (size_t)E);
   A((void**)&m->wv, (size_t)n);
+  A((void**)&m->wt, (size_t)n);
+  A((void**)&m->mark, (size_t)n);
+  A((void**)&m->pos_old, 8 * (size_t)n);
   A((void**)&m->cand, 4 * (size_t)E);
   A((void**)&m->claim, 16 * (size_t)E);
   A((void**)&m->vhe, 4 * (size_t)n);
@@ -301,6 +319,9 @@ int alloc_upload(const mcl_float2* pos, int64_t n, float L, const int32_t* ev, c
   if (e == cudaSuccess) e = cudaMemcpy(m->en, en, 16 * (size_t)E, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(m->eo, eo, 4 * (size_t)E, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemset(m->wv, 0x88, (size_t)n);
+  if (e == cudaSuccess) e = cudaMemset(m->wt, 0x88, (size_t)n);
+  if (e == cudaSuccess) e = cudaMemset(m->mark, 0, (size_t)n);
+  if (e == cudaSuccess) e = cudaMemcpy(m->pos_old, pos, 8 * (size_t)n, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemset(m->cand, 0, 4 * (size_t)E);
   if (e == cudaSuccess) e = cudaMemset(m->claim, 0, 16 * (size_t)E);
   if (e == cudaSuccess) e = cudaMemset(m->cnt, 0, sizeof(PCount));
@@ -450,7 +471,8 @@ int mcl_periodic_step(mcl_periodic* m, const mcl_float2* d_dev, void* stream, mc
   int rc = MCL_OK;
   std::string msg;
   unsigned long long inverted = 0;
-  int rounds = 0;
+  int rounds = 0, revert_passes = 0;
+  bool flipped = false;
   int64_t incircle_tests = 0;  // every edge of a round without a face turned over
   PCount c{};
   for (int r = 0; r < kMaxRounds; ++r) {
@@ -474,9 +496,23 @@ int mcl_periodic_step(mcl_periodic* m, const mcl_float2* d_dev, void* stream, mc
     }
     if (r == 0) inverted = c.inverted;
     if (c.inverted) {
-      rc = MCL_ERR_DEGENERATE_INPUT;
-      msg = "mcl_periodic_step: the move turned faces over; periodic meshes restore Delaunay by flips only";
-      break;
+      // send the moved vertices of the turned faces back, fold their unwraps,
+      // classify again (flips only start from a mesh with every face positive)
+      if (flipped) {
+        rc = MCL_ERR_DEGENERATE_INPUT;
+        msg = "mcl_periodic_step: a face turned over after flips (the mesh was not valid)";
+        break;
+      }
+      if (revert_passes == kMaxRevertPasses) {
+        rc = MCL_ERR_NO_CONVERGENCE;
+        msg = "mcl_periodic_step: sending vertices back did not end";
+        break;
+      }
+      k_prevert<<<blocks(m->n), kThreads, 0, s>>>(V);
+      k_pwrap<<<blocks(m->E), kThreads, 0, s>>>(V);
+      PCK(cudaGetLastError());
+      ++revert_passes;
+      continue;
     }
     incircle_tests += m->E;
     if (!c.nondelaunay) break;
@@ -487,10 +523,12 @@ int mcl_periodic_step(mcl_periodic* m, const mcl_float2* d_dev, void* stream, mc
     }
     k_pflip<<<blocks(m->E), kThreads, 0, s>>>(V, stamp);
     PCK(cudaGetLastError());
+    flipped = true;
   }
   if (stats) {
     std::memset(stats, 0, sizeof(*stats));
     stats->inverted_faces = (int64_t)((inverted + 2) / 3);  // each face is seen from its three edges
+    stats->reverted_vertices = (int64_t)c.reverted;
     stats->lawson_flips = (int64_t)c.flips;
     stats->lawson_rounds = rounds;
     stats->incircle_tests = incircle_tests;

@@ -165,7 +165,7 @@ struct alignas(16) PI4 {
 // step counters, reset by the host before each step (nondelaunay before each round)
 struct PCount {
   unsigned long long wrapped, inverted, nondelaunay, flips, incircle_fp64, incircle_exact, orient_fp64, orient_exact,
-      sos, overflow, error, error_site, truncated;
+      sos, overflow, error, error_site, truncated, reverted;
 };
 
 struct PView {
@@ -176,7 +176,10 @@ struct PView {
   PI4* ev;        // (a, b, c, d)
   PI4* en;        // (next h0, prev h0, next h1, prev h1)
   unsigned* eo;   // offsets (B, C, X1)
-  unsigned char* wv;          // this step's wrap of each vertex (an offset byte)
+  unsigned char* wv;          // wraps still to fold into the edge words (an offset byte per vertex)
+  unsigned char* wt;          // this step's net wrap of each vertex
+  unsigned char* mark;        // vertices of faces the move turned over
+  PF2* pos_old;               // positions before the step's move
   unsigned* cand;             // round stamp of the non-Delaunay edges
   unsigned long long* claim;  // face claims, by the smallest half-edge id of the face
   PCount* cnt;
@@ -246,6 +249,9 @@ MCL_HD void p_flush(const PView& V, const PLocal& lc) {
 // vertex v: move by d[v], wrap into the domain, record the wrap
 MCL_HD void p_body_move(const PView& V, const PF2* d, int v) {
   PF2 p = V.pos[v];
+  V.pos_old[v] = p;
+  V.mark[v] = 0;
+  V.wt[v] = (unsigned char)off_byte(Off{0, 0});
   const PF2 dv = d[v];
   p.x = fadd(p.x, dv.x);
   p.y = fadd(p.y, dv.y);
@@ -257,7 +263,26 @@ MCL_HD void p_body_move(const PView& V, const PF2* d, int v) {
   }
   V.pos[v] = p;
   V.wv[v] = (unsigned char)off_byte(w);
+  V.wt[v] = (unsigned char)off_byte(w);
   if (!off_zero(w)) p_add(&V.cnt->wrapped, 1);
+}
+
+// vertex v, after a classification that found faces turned over: a marked
+// vertex that moved goes back to its old position, and its wrap is undone in
+// the next fold; every other vertex folds nothing.  Repeated until no face is
+// turned over, this ends (at worst every moved vertex of a turned face is back
+// where the valid mesh had it).
+MCL_HD void p_body_revert(const PView& V, int v) {
+  const Off none{0, 0};
+  V.wv[v] = (unsigned char)off_byte(none);
+  if (!V.mark[v]) return;
+  V.mark[v] = 0;
+  const PF2 p = V.pos[v], q = V.pos_old[v];
+  if (p.x == q.x && p.y == q.y) return;
+  V.pos[v] = q;
+  V.wv[v] = (unsigned char)off_byte(off_neg(off_from_byte(V.wt[v])));
+  V.wt[v] = (unsigned char)off_byte(none);
+  p_add(&V.cnt->reverted, 1);
 }
 
 // edge e: the wraps of its quad's vertices into its offset word
@@ -297,6 +322,10 @@ MCL_HD void p_body_classify(const PView& V, int e, unsigned stamp) {
   const int sb = orient2d(qb.x, qb.y, pa.x, pa.y, qd.x, qd.y, &lc, &lc.overflow);
   if (sa <= 0 || sb <= 0) {
     p_add(&V.cnt->inverted, (unsigned long long)((sa <= 0) + (sb <= 0)));
+    V.mark[q.x] = 1;
+    V.mark[q.y] = 1;
+    if (sa <= 0) V.mark[q.z] = 1;
+    if (sb <= 0) V.mark[q.w] = 1;
     p_flush(V, lc);
     return;
   }

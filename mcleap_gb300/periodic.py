@@ -75,7 +75,9 @@ class PeriodicTriangulation:
             pass
 
     def step(self, d, stream=None):
-        """Move by d (device float2[n]), wrap, flip back to Delaunay."""
+        """Move by d (device float2[n]), wrap, flip back to Delaunay.  Moves
+        that would turn faces over are refused for the vertices involved
+        (counted in ``reverted_vertices``)."""
         st = L.StepStats()
         wrapped = C.c_int64()
         rc = L.lib().mcl_periodic_step(self.handle, L.ptr(d), _stream_ptr(stream), C.byref(st), C.byref(wrapped))

@@ -1,7 +1,8 @@
 // Serial run, on the CPU, of the periodic step's kernel bodies
 // (mcleap_gb300/csrc/periodic.cuh) in the order the GPU launches them: move +
 // wrap every vertex, fold the wraps into every edge word, then rounds of
-// classify-all / flip-winners until no edge is non-Delaunay.  A serial run of
+// classify-all and either (faces turned over) send their moved vertices back
+// and fold again, or flip the winners, until no edge is non-Delaunay.  A serial run of
 // one launch gives the GPU's result (claims are max-reductions, one round's
 // flips write disjoint fields), so this checks the device code's logic and
 // indexing without a GPU.
@@ -10,7 +11,8 @@
 //   IN : int32 n, int32 E, float L, float pos[n][2], float d[n][2],
 //        int32 ev[E][4], int32 en[E][4], uint32 eo[E]
 //   OUT: int32 status, int32 flips, int32 wrapped, int32 inverted, int32 rounds,
-//        int32 nonpositive_after, int32 truncated, float pos[n][2], int32 ev[E][4],
+//        int32 nonpositive_after, int32 truncated, int32 reverted, int32 revert_passes,
+//        float pos[n][2], int32 ev[E][4],
 //        int32 en[E][4], uint32 eo[E], then the queries on the final mesh:
 //        int32 ring[kRing][n] and uint8 offs[kRing][n] (column layout), int32 closest[n]
 // status: an MCL_* code from the bodies (0 ok), 100 + an I/O failure.
@@ -31,6 +33,7 @@ template <typename T>
 void wr(FILE* f, const T* p, size_t k) { fwrite(p, sizeof(T), k, f); }
 
 constexpr int kRing = 8;  // small enough that some rings are truncated
+constexpr int kMaxRevertPasses = 256;
 
 struct NoCount {
   int incircle_fp64, incircle_exact, orient_fp64, orient_exact, sos;
@@ -58,7 +61,8 @@ int main(int argc, char** argv) {
   std::vector<PF2> pos(n), d(n);
   std::vector<PI4> ev(E), en(E);
   std::vector<uint32_t> eo(E), cand(E, 0);
-  std::vector<unsigned char> wv(n, 0);
+  std::vector<unsigned char> wv(n, 0x88), wt(n, 0x88), mark(n, 0);
+  std::vector<PF2> pos_old(n);
   std::vector<unsigned long long> claim(2 * (size_t)E, 0);
   if (!rd(in, pos.data(), n) || !rd(in, d.data(), n) || !rd(in, ev.data(), E) || !rd(in, en.data(), E) ||
       !rd(in, eo.data(), E))
@@ -66,9 +70,10 @@ int main(int argc, char** argv) {
   fclose(in);
 
   mcl::PCount cnt{};
-  mcl::PView V{n, E, L, 2.0f * L, pos.data(), ev.data(), en.data(), eo.data(), wv.data(), cand.data(),
-               claim.data(), &cnt};
-  int rounds = 0;
+  mcl::PView V{n,         E,           L,           2.0f * L,       pos.data(),  ev.data(),    en.data(), eo.data(),
+               wv.data(),  wt.data(),   mark.data(), pos_old.data(), cand.data(), claim.data(), &cnt};
+  int rounds = 0, revert_passes = 0;
+  bool flipped = false;
   unsigned long long inverted = 0;
   for (int v = 0; v < n; ++v) mcl::p_body_move(V, d.data(), v);
   if (!cnt.error)
@@ -80,8 +85,19 @@ int main(int argc, char** argv) {
     ++rounds;
     if (cnt.error) break;
     if (stamp == 1) inverted = cnt.inverted;
-    if (cnt.inverted || !cnt.nondelaunay) break;
+    if (cnt.inverted) {
+      if (flipped || revert_passes == kMaxRevertPasses) {
+        cnt.error = flipped ? MCL_ERR_DEGENERATE_INPUT : MCL_ERR_NO_CONVERGENCE;
+        break;
+      }
+      for (int v = 0; v < n; ++v) mcl::p_body_revert(V, v);
+      for (int e = 0; e < E; ++e) mcl::p_body_wrap(V, e);
+      ++revert_passes;
+      continue;
+    }
+    if (!cnt.nondelaunay) break;
     for (int e = 0; e < E; ++e) mcl::p_body_flip(V, e, stamp);
+    flipped = true;
   }
   int after = 0;
   if (!cnt.error)
@@ -99,9 +115,10 @@ int main(int argc, char** argv) {
 
   FILE* out = fopen(argv[2], "wb");
   if (!out) return 4;
-  const int32_t head[7] = {(int32_t)cnt.error, (int32_t)cnt.flips, (int32_t)cnt.wrapped, (int32_t)inverted, rounds,
-                           after, (int32_t)cnt.truncated};
-  wr(out, head, 7);
+  const int32_t head[9] = {(int32_t)cnt.error, (int32_t)cnt.flips,     (int32_t)cnt.wrapped,
+                           (int32_t)inverted,  rounds,                  after,
+                           (int32_t)cnt.truncated, (int32_t)cnt.reverted, revert_passes};
+  wr(out, head, 9);
   wr(out, pos.data(), n);
   wr(out, ev.data(), E);
   wr(out, en.data(), E);

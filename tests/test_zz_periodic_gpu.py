@@ -91,19 +91,36 @@ def test_mesh_from_arrays_steps_like_the_built_one(M):
     assert all(np.array_equal(x, y) for x, y in zip(a.download(), b.download()))
 
 
-def test_a_face_turned_over_is_reported(M):
-    """Flips only on the torus: a move that turns a face over is an error, with
-    the count of faces turned."""
+def test_a_face_turned_over_sends_its_vertex_back(M):
+    """A move that would turn faces over is refused for the vertex involved."""
     xy = torus_points(2000, 12)
     pt = M.PeriodicTriangulation(xy, L)
-    _, ev, _, eo = pt.download()
+    before = pt.download()
+    _, ev, _, eo = before
     a, b = ev[0, 0], ev[0, 1]
     B = M.periodic.eo_offsets(eo[:1])[0][0].astype(np.float32)
     d = np.zeros_like(xy)
     d[a] = 2.0 * (xy[b] + B * np.float32(L) - xy[a])
-    with pytest.raises(M.McleapError) as err:
-        pt.step(cuda(d))
-    assert err.value.code == 6 and pt.last_stats["inverted_faces"] > 0
+    st = pt.step(cuda(d))
+    assert st["status"] == 0 and st["inverted_faces"] > 0 and st["reverted_vertices"] == 1
+    assert all(np.array_equal(x, y) for x, y in zip(before, pt.download()))
+
+
+@pytest.mark.parametrize("sigma,shift,seed", [(0.1, (0.0, 0.0), 51), (0.2, (0.4, -0.3), 52)])
+def test_tangling_moves_are_refused_vertex_by_vertex(M, sigma, shift, seed):
+    n = 4000
+    xy = torus_points(n, seed)
+    pt = M.PeriodicTriangulation(xy, L)
+    h = L / np.sqrt(n)
+    d = (np.random.default_rng(seed).normal(0, sigma * h, (n, 2)) + np.array(shift) * h).astype(np.float32)
+    st = pt.step(cuda(d))
+    assert st["status"] == 0 and st["inverted_faces"] > 0 and st["reverted_vertices"] > 0, st
+    pos, ev, en, eo = pt.download()
+    moved = torus_wrap(xy + d)
+    back = (pos == xy).all(1) & ~(moved == xy).all(1)
+    assert ((pos == moved).all(1) | back).all() and back.sum() == st["reverted_vertices"]
+    assert torus_faces_consistent(ev, en, eo)
+    assert np.array_equal(M.periodic.canonical_edges(ev, eo), P.periodic_edges(pos, L))
 
 
 def test_ring_and_closest_after_steps(M):
