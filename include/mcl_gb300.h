@@ -430,11 +430,15 @@ int mcl_periodic_positions(mcl_periodic* m, mcl_float2** pos_dev);
  * Lawson flip rounds restore the periodic Delaunay triangulation.  Moves that
  * would turn faces over are refused vertex by vertex: the moved vertices of
  * every turned face go back to where they were (repeatedly, since sending one
- * back can turn another face) before any flip, so the result is always the
- * valid periodic Delaunay triangulation of where the points ended.  stats
- * (may be NULL): inverted_faces (turned by the move), reverted_vertices (sent
- * back), lawson_flips, lawson_rounds, the predicate counters, status; wrapped
- * (may be NULL): points whose move crossed a side. */
+ * back can turn another face) before any flip; then up to five sub-steps move
+ * the vertices still owing part of their displacement by half of it (the last
+ * by all of it, landing exactly on the target), each with the same refusal
+ * and flips.  The result is always the valid periodic Delaunay triangulation
+ * of where the points ended.  stats (may be NULL): inverted_faces (turned by
+ * the move), reverted_vertices (not at their target at the end),
+ * substep_vertices (sent back, then brought to their target by sub-steps),
+ * lawson_flips, lawson_rounds, the predicate counters, status; wrapped (may be
+ * NULL): wraps across a side (a vertex may wrap in more than one sub-step). */
 int mcl_periodic_step(mcl_periodic* m, const mcl_float2* d_dev, void* stream, mcl_step_stats* stats,
                       int64_t* wrapped);
 

@@ -47,6 +47,8 @@ struct mcl_periodic {
   unsigned char* wt;
   unsigned char* mark;
   PF2* pos_old;
+  PF2* target;
+  PF2* dsub;         // sub-step displacements
   unsigned* cand;
   unsigned long long* claim;
   int* vhe;          // one outgoing half-edge per vertex (queries)
@@ -60,6 +62,7 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kMaxRounds = 4096;
 constexpr int kMaxRevertPasses = 256;
+constexpr int kSubLevels = 5;  // sub-steps for vertices sent back
 constexpr int kCenter = 4;  // copy index of the untranslated copy
 
 #define PCK(call)                                       \
@@ -71,6 +74,14 @@ constexpr int kCenter = 4;  // copy index of the untranslated copy
 __global__ void k_pmove(PView V, const PF2* d) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < V.n) mcl::p_body_move(V, d, i);
+}
+__global__ void k_ptarget(PView V, const PF2* d) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < V.n) mcl::p_body_target(V, d, i);
+}
+__global__ void k_presume(PView V, PF2* d, bool last) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < V.n) mcl::p_body_resume(V, d, i, last);
 }
 __global__ void k_prevert(PView V) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -104,8 +115,8 @@ __global__ void k_pclosest(PView V, bool column, int max_ring, const int* ring, 
 unsigned blocks(int64_t k) { return (unsigned)((k + kThreads - 1) / kThreads); }
 
 PView view(mcl_periodic* m) {
-  return PView{(int)m->n, (int)m->E, m->L,    2.0f * m->L,  m->pos,  m->ev,    m->en,    m->eo,
-               m->wv,      m->wt,      m->mark, m->pos_old,   m->cand, m->claim, m->cnt};
+  return PView{(int)m->n, (int)m->E, m->L,       2.0f * m->L, m->pos,  m->ev,    m->en,   m->eo,
+               m->wv,      m->wt,      m->mark,    m->pos_old,  m->target, m->cand, m->claim, m->cnt};
 }
 
 void free_periodic(mcl_periodic* m) {
@@ -118,6 +129,8 @@ void free_periodic(mcl_periodic* m) {
   cudaFree(m->wt);
   cudaFree(m->mark);
   cudaFree(m->pos_old);
+  cudaFree(m->target);
+  cudaFree(m->dsub);
   cudaFree(m->cand);
   cudaFree(m->claim);
   cudaFree(m->vhe);
@@ -309,6 +322,8 @@ int alloc_upload(const mcl_float2* pos, int64_t n, float L, const int32_t* ev, c
   A((void**)&m->wt, (size_t)n);
   A((void**)&m->mark, (size_t)n);
   A((void**)&m->pos_old, 8 * (size_t)n);
+  A((void**)&m->target, 8 * (size_t)n);
+  A((void**)&m->dsub, 8 * (size_t)n);
   A((void**)&m->cand, 4 * (size_t)E);
   A((void**)&m->claim, 16 * (size_t)E);
   A((void**)&m->vhe, 4 * (size_t)n);
@@ -322,6 +337,7 @@ int alloc_upload(const mcl_float2* pos, int64_t n, float L, const int32_t* ev, c
   if (e == cudaSuccess) e = cudaMemset(m->wt, 0x88, (size_t)n);
   if (e == cudaSuccess) e = cudaMemset(m->mark, 0, (size_t)n);
   if (e == cudaSuccess) e = cudaMemcpy(m->pos_old, pos, 8 * (size_t)n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(m->target, pos, 8 * (size_t)n, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemset(m->cand, 0, 4 * (size_t)E);
   if (e == cudaSuccess) e = cudaMemset(m->claim, 0, 16 * (size_t)E);
   if (e == cudaSuccess) e = cudaMemset(m->cnt, 0, sizeof(PCount));
@@ -332,6 +348,72 @@ int alloc_upload(const mcl_float2* pos, int64_t n, float L, const int32_t* ev, c
   }
   *out = m;
   return MCL_OK;
+}
+
+// Rounds of classification after a move: faces turned over send their moved
+// vertices back (then the fold again), otherwise the winners of the
+// non-Delaunay edges flip, until no edge is non-Delaunay.  Counters
+// accumulate in z across calls.
+struct Settle {
+  PCount c{};
+  unsigned long long inverted_first = 0;
+  bool classified = false;
+  int rounds = 0;
+  int64_t incircle_tests = 0;  // every edge of a round without a face turned over
+  std::string msg;
+};
+
+int settle(mcl_periodic* m, cudaStream_t s, const PView& V, Settle& z) {
+  int revert_passes = 0;
+  bool flipped = false;
+  for (int r = 0; r < kMaxRounds; ++r) {
+    if (m->stamp == 0xFFFFFFFFu) {  // stamps wrapped: forget every old claim
+      PCK(cudaMemsetAsync(m->claim, 0, 16 * (size_t)m->E, s));
+      PCK(cudaMemsetAsync(m->cand, 0, 4 * (size_t)m->E, s));
+      m->stamp = 0;
+    }
+    const unsigned stamp = ++m->stamp;
+    PCK(cudaMemsetAsync(&m->cnt->inverted, 0, 2 * sizeof(unsigned long long), s));  // inverted, nondelaunay
+    k_pclassify<<<blocks(m->E), kThreads, 0, s>>>(V, stamp);
+    PCK(cudaGetLastError());
+    PCK(cudaMemcpyAsync(m->cnt_host, m->cnt, sizeof(PCount), cudaMemcpyDeviceToHost, s));
+    PCK(cudaStreamSynchronize(s));
+    z.c = *m->cnt_host;
+    ++z.rounds;
+    if (z.c.error) {
+      const int rc = (int)z.c.error;
+      z.msg = "mcl_periodic_step: " + std::string(mcl_status_string(rc)) + " (site " + std::to_string(z.c.error_site) +
+              ")";
+      return rc;
+    }
+    if (!z.classified) {
+      z.inverted_first = z.c.inverted;
+      z.classified = true;
+    }
+    if (z.c.inverted) {
+      // flips only start from a mesh whose faces are all positive
+      if (flipped) {
+        z.msg = "mcl_periodic_step: a face turned over after flips (the mesh was not valid)";
+        return MCL_ERR_DEGENERATE_INPUT;
+      }
+      if (revert_passes == kMaxRevertPasses) {
+        z.msg = "mcl_periodic_step: sending vertices back did not end";
+        return MCL_ERR_NO_CONVERGENCE;
+      }
+      k_prevert<<<blocks(m->n), kThreads, 0, s>>>(V);
+      k_pwrap<<<blocks(m->E), kThreads, 0, s>>>(V);
+      PCK(cudaGetLastError());
+      ++revert_passes;
+      continue;
+    }
+    z.incircle_tests += m->E;
+    if (!z.c.nondelaunay) return MCL_OK;
+    k_pflip<<<blocks(m->E), kThreads, 0, s>>>(V, stamp);
+    PCK(cudaGetLastError());
+    flipped = true;
+  }
+  z.msg = "mcl_periodic_step: flip rounds did not converge";
+  return MCL_ERR_NO_CONVERGENCE;
 }
 
 }  // namespace
@@ -464,74 +546,40 @@ int mcl_periodic_step(mcl_periodic* m, const mcl_float2* d_dev, void* stream, mc
   if (!m || !d_dev) return mcl::fail(MCL_ERR_INVALID_ARGUMENT, "null argument");
   cudaStream_t s = (cudaStream_t)stream;
   const PView V = view(m);
+  Settle z;
   PCK(cudaMemsetAsync(m->cnt, 0, sizeof(PCount), s));
+  k_ptarget<<<blocks(m->n), kThreads, 0, s>>>(V, reinterpret_cast<const PF2*>(d_dev));
   k_pmove<<<blocks(m->n), kThreads, 0, s>>>(V, reinterpret_cast<const PF2*>(d_dev));
   k_pwrap<<<blocks(m->E), kThreads, 0, s>>>(V);
   PCK(cudaGetLastError());
-  int rc = MCL_OK;
-  std::string msg;
-  unsigned long long inverted = 0;
-  int rounds = 0, revert_passes = 0;
-  bool flipped = false;
-  int64_t incircle_tests = 0;  // every edge of a round without a face turned over
-  PCount c{};
-  for (int r = 0; r < kMaxRounds; ++r) {
-    if (m->stamp == 0xFFFFFFFFu) {  // stamps wrapped: forget every old claim
-      PCK(cudaMemsetAsync(m->claim, 0, 16 * (size_t)m->E, s));
-      PCK(cudaMemsetAsync(m->cand, 0, 4 * (size_t)m->E, s));
-      m->stamp = 0;
-    }
-    const unsigned stamp = ++m->stamp;
-    PCK(cudaMemsetAsync(&m->cnt->inverted, 0, 2 * sizeof(unsigned long long), s));  // inverted, nondelaunay
-    k_pclassify<<<blocks(m->E), kThreads, 0, s>>>(V, stamp);
+  int rc = settle(m, s, V, z);
+  // sub-steps: vertices sent back move again by half of what they still owe,
+  // the last level by all of it (landing exactly on the target)
+  int64_t behind_first = -1, behind = 0;
+  for (int level = 1; rc == MCL_OK; ++level) {
+    const bool last = level >= kSubLevels;
+    PCK(cudaMemsetAsync(&m->cnt->behind, 0, sizeof(unsigned long long), s));
+    k_presume<<<blocks(m->n), kThreads, 0, s>>>(V, m->dsub, last);
     PCK(cudaGetLastError());
     PCK(cudaMemcpyAsync(m->cnt_host, m->cnt, sizeof(PCount), cudaMemcpyDeviceToHost, s));
     PCK(cudaStreamSynchronize(s));
-    c = *m->cnt_host;
-    ++rounds;
-    if (c.error) {
-      rc = (int)c.error;
-      msg = "mcl_periodic_step: " + std::string(mcl_status_string(rc)) + " (site " + std::to_string(c.error_site) + ")";
-      break;
-    }
-    if (r == 0) inverted = c.inverted;
-    if (c.inverted) {
-      // send the moved vertices of the turned faces back, fold their unwraps,
-      // classify again (flips only start from a mesh with every face positive)
-      if (flipped) {
-        rc = MCL_ERR_DEGENERATE_INPUT;
-        msg = "mcl_periodic_step: a face turned over after flips (the mesh was not valid)";
-        break;
-      }
-      if (revert_passes == kMaxRevertPasses) {
-        rc = MCL_ERR_NO_CONVERGENCE;
-        msg = "mcl_periodic_step: sending vertices back did not end";
-        break;
-      }
-      k_prevert<<<blocks(m->n), kThreads, 0, s>>>(V);
-      k_pwrap<<<blocks(m->E), kThreads, 0, s>>>(V);
-      PCK(cudaGetLastError());
-      ++revert_passes;
-      continue;
-    }
-    incircle_tests += m->E;
-    if (!c.nondelaunay) break;
-    if (r == kMaxRounds - 1) {
-      rc = MCL_ERR_NO_CONVERGENCE;
-      msg = "mcl_periodic_step: flip rounds did not converge";
-      break;
-    }
-    k_pflip<<<blocks(m->E), kThreads, 0, s>>>(V, stamp);
+    behind = (int64_t)m->cnt_host->behind;
+    if (behind_first < 0) behind_first = behind;
+    if (behind == 0 || level > kSubLevels) break;
+    k_pmove<<<blocks(m->n), kThreads, 0, s>>>(V, m->dsub);
+    k_pwrap<<<blocks(m->E), kThreads, 0, s>>>(V);
     PCK(cudaGetLastError());
-    flipped = true;
+    rc = settle(m, s, V, z);
   }
+  const PCount& c = z.c;
   if (stats) {
     std::memset(stats, 0, sizeof(*stats));
-    stats->inverted_faces = (int64_t)((inverted + 2) / 3);  // each face is seen from its three edges
-    stats->reverted_vertices = (int64_t)c.reverted;
+    stats->inverted_faces = (int64_t)((z.inverted_first + 2) / 3);  // each face is seen from its three edges
+    stats->reverted_vertices = behind;
+    stats->substep_vertices = behind_first > behind ? behind_first - behind : 0;
     stats->lawson_flips = (int64_t)c.flips;
-    stats->lawson_rounds = rounds;
-    stats->incircle_tests = incircle_tests;
+    stats->lawson_rounds = z.rounds;
+    stats->incircle_tests = z.incircle_tests;
     stats->incircle_fp64 = (int64_t)c.incircle_fp64;
     stats->incircle_exact = (int64_t)c.incircle_exact;
     stats->orient_fp64 = (int64_t)c.orient_fp64;
@@ -543,9 +591,9 @@ int mcl_periodic_step(mcl_periodic* m, const mcl_float2* d_dev, void* stream, mc
   if (wrapped) *wrapped = (int64_t)c.wrapped;
   if (rc == MCL_OK && c.overflow) {
     rc = MCL_ERR_PREDICATE;
-    msg = "mcl_periodic_step: exact predicate capacity exceeded";
+    z.msg = "mcl_periodic_step: exact predicate capacity exceeded";
   }
-  return rc == MCL_OK ? MCL_OK : mcl::fail(rc, msg);
+  return rc == MCL_OK ? MCL_OK : mcl::fail(rc, z.msg);
 }
 
 int mcl_periodic_one_ring(mcl_periodic* m, int max_ring, int layout, int32_t* ring_dev, uint8_t* offs_dev,

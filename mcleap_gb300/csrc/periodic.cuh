@@ -165,7 +165,7 @@ struct alignas(16) PI4 {
 // step counters, reset by the host before each step (nondelaunay before each round)
 struct PCount {
   unsigned long long wrapped, inverted, nondelaunay, flips, incircle_fp64, incircle_exact, orient_fp64, orient_exact,
-      sos, overflow, error, error_site, truncated, reverted;
+      sos, overflow, error, error_site, truncated, reverted, behind;
 };
 
 struct PView {
@@ -179,7 +179,8 @@ struct PView {
   unsigned char* wv;          // wraps still to fold into the edge words (an offset byte per vertex)
   unsigned char* wt;          // this step's net wrap of each vertex
   unsigned char* mark;        // vertices of faces the move turned over
-  PF2* pos_old;               // positions before the step's move
+  PF2* pos_old;               // positions before the current move
+  PF2* target;                // where the step's move puts each vertex (wrapped)
   unsigned* cand;             // round stamp of the non-Delaunay edges
   unsigned long long* claim;  // face claims, by the smallest half-edge id of the face
   PCount* cnt;
@@ -265,6 +266,45 @@ MCL_HD void p_body_move(const PView& V, const PF2* d, int v) {
   V.wv[v] = (unsigned char)off_byte(w);
   V.wt[v] = (unsigned char)off_byte(w);
   if (!off_zero(w)) p_add(&V.cnt->wrapped, 1);
+}
+
+// vertex v before the step: its target, the wrapped old position + d[v]
+// (the same arithmetic as p_body_move)
+MCL_HD void p_body_target(const PView& V, const PF2* d, int v) {
+  PF2 p = V.pos[v];
+  const PF2 dv = d[v];
+  p.x = fadd(p.x, dv.x);
+  p.y = fadd(p.y, dv.y);
+  wrap_position(p, V.lo, V.L);
+  V.target[v] = p;
+}
+
+// the exact difference to the copy of t nearest to p along one axis (both in
+// [lo, lo + L); t - p, t - L - p and t + L - p are exact by Sterbenz's lemma)
+MCL_HD float p_toward(float t, float p, float L) {
+  const float r = fsub(t, p);
+  if (r > 0.5f * L) return fsub(fsub(t, L), p);
+  if (r < -0.5f * L) return fsub(fadd(t, L), p);
+  return r;
+}
+
+// vertex v, between sub-steps: the displacement still owed to a vertex that
+// is not at its target: half of it, or (last) all of it, which lands the
+// vertex exactly on its target; zero for the others.  Counts the vertices
+// still behind.
+MCL_HD void p_body_resume(const PView& V, PF2* d, int v, bool last) {
+  const PF2 p = V.pos[v], t = V.target[v];
+  PF2 r{0.f, 0.f};
+  if (p.x != t.x || p.y != t.y) {
+    r.x = p_toward(t.x, p.x, V.L);
+    r.y = p_toward(t.y, p.y, V.L);
+    if (!last) {
+      r.x = fmul(r.x, 0.5f);
+      r.y = fmul(r.y, 0.5f);
+    }
+    p_add(&V.cnt->behind, 1);
+  }
+  d[v] = r;
 }
 
 // vertex v, after a classification that found faces turned over: a marked

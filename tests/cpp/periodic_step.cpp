@@ -12,6 +12,7 @@
 //        int32 ev[E][4], int32 en[E][4], uint32 eo[E]
 //   OUT: int32 status, int32 flips, int32 wrapped, int32 inverted, int32 rounds,
 //        int32 nonpositive_after, int32 truncated, int32 reverted, int32 revert_passes,
+//        int32 behind (not at the target at the end), int32 substep_arrivals,
 //        float pos[n][2], int32 ev[E][4],
 //        int32 en[E][4], uint32 eo[E], then the queries on the final mesh:
 //        int32 ring[kRing][n] and uint8 offs[kRing][n] (column layout), int32 closest[n]
@@ -34,6 +35,7 @@ void wr(FILE* f, const T* p, size_t k) { fwrite(p, sizeof(T), k, f); }
 
 constexpr int kRing = 8;  // small enough that some rings are truncated
 constexpr int kMaxRevertPasses = 256;
+constexpr int kSubLevels = 5;
 
 struct NoCount {
   int incircle_fp64, incircle_exact, orient_fp64, orient_exact, sos;
@@ -70,34 +72,57 @@ int main(int argc, char** argv) {
   fclose(in);
 
   mcl::PCount cnt{};
-  mcl::PView V{n,         E,           L,           2.0f * L,       pos.data(),  ev.data(),    en.data(), eo.data(),
-               wv.data(),  wt.data(),   mark.data(), pos_old.data(), cand.data(), claim.data(), &cnt};
+  std::vector<PF2> target(n), dsub(n);
+  mcl::PView V{n,         E,           L,           2.0f * L,       pos.data(),    ev.data(),   en.data(),    eo.data(),
+               wv.data(),  wt.data(),   mark.data(), pos_old.data(), target.data(), cand.data(), claim.data(), &cnt};
   int rounds = 0, revert_passes = 0;
-  bool flipped = false;
-  unsigned long long inverted = 0;
+  unsigned stamp = 0;
+  long long inverted = -1;
+  // the host loop of mcl_periodic_step, launch by launch
+  auto settle = [&]() {
+    bool flipped = false;
+    int passes = 0;
+    for (int r = 0; r < 4096; ++r) {
+      ++stamp;
+      cnt.nondelaunay = 0;
+      cnt.inverted = 0;
+      for (int e = 0; e < E; ++e) mcl::p_body_classify(V, e, stamp);
+      ++rounds;
+      if (cnt.error) return;
+      if (inverted < 0) inverted = (long long)cnt.inverted;
+      if (cnt.inverted) {
+        if (flipped || passes == kMaxRevertPasses) {
+          cnt.error = flipped ? MCL_ERR_DEGENERATE_INPUT : MCL_ERR_NO_CONVERGENCE;
+          return;
+        }
+        for (int v = 0; v < n; ++v) mcl::p_body_revert(V, v);
+        for (int e = 0; e < E; ++e) mcl::p_body_wrap(V, e);
+        ++passes;
+        ++revert_passes;
+        continue;
+      }
+      if (!cnt.nondelaunay) return;
+      for (int e = 0; e < E; ++e) mcl::p_body_flip(V, e, stamp);
+      flipped = true;
+    }
+    cnt.error = MCL_ERR_NO_CONVERGENCE;
+  };
+  for (int v = 0; v < n; ++v) mcl::p_body_target(V, d.data(), v);
   for (int v = 0; v < n; ++v) mcl::p_body_move(V, d.data(), v);
   if (!cnt.error)
     for (int e = 0; e < E; ++e) mcl::p_body_wrap(V, e);
-  for (unsigned stamp = 1; !cnt.error && stamp <= 4096; ++stamp) {
-    cnt.nondelaunay = 0;
-    cnt.inverted = 0;
-    for (int e = 0; e < E; ++e) mcl::p_body_classify(V, e, stamp);
-    ++rounds;
-    if (cnt.error) break;
-    if (stamp == 1) inverted = cnt.inverted;
-    if (cnt.inverted) {
-      if (flipped || revert_passes == kMaxRevertPasses) {
-        cnt.error = flipped ? MCL_ERR_DEGENERATE_INPUT : MCL_ERR_NO_CONVERGENCE;
-        break;
-      }
-      for (int v = 0; v < n; ++v) mcl::p_body_revert(V, v);
-      for (int e = 0; e < E; ++e) mcl::p_body_wrap(V, e);
-      ++revert_passes;
-      continue;
-    }
-    if (!cnt.nondelaunay) break;
-    for (int e = 0; e < E; ++e) mcl::p_body_flip(V, e, stamp);
-    flipped = true;
+  if (!cnt.error) settle();
+  long long behind_first = -1, behind = 0;
+  for (int level = 1; !cnt.error; ++level) {
+    const bool last = level >= kSubLevels;
+    cnt.behind = 0;
+    for (int v = 0; v < n; ++v) mcl::p_body_resume(V, dsub.data(), v, last);
+    behind = (long long)cnt.behind;
+    if (behind_first < 0) behind_first = behind;
+    if (behind == 0 || level > kSubLevels) break;
+    for (int v = 0; v < n; ++v) mcl::p_body_move(V, dsub.data(), v);
+    for (int e = 0; e < E; ++e) mcl::p_body_wrap(V, e);
+    settle();
   }
   int after = 0;
   if (!cnt.error)
@@ -115,10 +140,11 @@ int main(int argc, char** argv) {
 
   FILE* out = fopen(argv[2], "wb");
   if (!out) return 4;
-  const int32_t head[9] = {(int32_t)cnt.error, (int32_t)cnt.flips,     (int32_t)cnt.wrapped,
-                           (int32_t)inverted,  rounds,                  after,
-                           (int32_t)cnt.truncated, (int32_t)cnt.reverted, revert_passes};
-  wr(out, head, 9);
+  const int32_t head[11] = {(int32_t)cnt.error,     (int32_t)cnt.flips,    (int32_t)cnt.wrapped,
+                            (int32_t)inverted,      rounds,                after,
+                            (int32_t)cnt.truncated, (int32_t)cnt.reverted, revert_passes,
+                            (int32_t)behind,        (int32_t)(behind_first > behind ? behind_first - behind : 0)};
+  wr(out, head, 11);
   wr(out, pos.data(), n);
   wr(out, ev.data(), E);
   wr(out, en.data(), E);

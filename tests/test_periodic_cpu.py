@@ -36,8 +36,8 @@ def run(harness, tmp_path, pos, d, ev, en, eo):
             f.write(np.ascontiguousarray(a).tobytes())
     subprocess.run([harness, src, dst], check=True)
     raw = open(dst, "rb").read()
-    head = [int(x) for x in np.frombuffer(raw[:36], np.int32)]
-    o = 36
+    head = [int(x) for x in np.frombuffer(raw[:44], np.int32)]
+    o = 44
     pos2 = np.frombuffer(raw[o:o + 8 * n], np.float32).reshape(n, 2)
     o += 8 * n
     ev2 = np.frombuffer(raw[o:o + 16 * E], np.int32).reshape(E, 4)
@@ -53,7 +53,7 @@ def run(harness, tmp_path, pos, d, ev, en, eo):
     closest = np.frombuffer(raw[o:o + 4 * n], np.int32)
     run.queries = (ring, offs, closest)
     st = dict(zip(["status", "flips", "wrapped", "inverted", "rounds", "nonpositive_after", "truncated", "reverted",
-                   "revert_passes"], head))
+                   "revert_passes", "behind", "substep_arrivals"], head))
     return st, pos2, ev2, en2, eo2
 
 
@@ -80,7 +80,7 @@ def test_step_with_wraps_matches_oracle(harness, tmp_path, n, sigma, shift, seed
     assert (d != drift).any(1).mean() > 0.7
     st, pos, ev2, en2, eo2 = run(harness, tmp_path, xy, d, ev, en, eo)
     assert st["status"] == 0 and st["inverted"] == 0 and st["nonpositive_after"] == 0, st
-    assert st["reverted"] == 0 and st["revert_passes"] == 0
+    assert st["reverted"] == 0 and st["revert_passes"] == 0 and st["behind"] == 0
     assert np.array_equal(pos, torus_wrap(xy + d))
     assert st["wrapped"] > 0 and st["flips"] > 0 and st["rounds"] >= 2
     assert torus_faces_consistent(ev2, en2, eo2)
@@ -108,38 +108,46 @@ def test_whole_period_move_is_a_relabelling(harness, tmp_path):
     assert np.array_equal(pos, xy) and np.array_equal(eo2, eo)
 
 
-def test_a_face_turned_over_sends_its_vertex_back(harness, tmp_path):
-    """A move that would turn faces over is refused for the vertices involved:
-    they stay where they were, the rest of the step goes through."""
+def check_step(st, xy, d, pos, ev, en, eo):
+    """Every point at its target or counted behind; the mesh valid and the
+    periodic Delaunay triangulation of where the points are."""
+    assert st["status"] == 0 and st["nonpositive_after"] == 0, st
+    at = (pos == torus_wrap(xy + d)).all(1)
+    assert (~at).sum() == st["behind"]
+    assert torus_faces_consistent(ev, en, eo)
+    assert np.array_equal(P.mesh_edges(ev, eo), P.periodic_edges(pos, L))
+
+
+def test_a_face_turned_over_is_refused_then_resumed(harness, tmp_path):
+    """A vertex jumping across its neighbour is sent back, then sub-steps
+    (half of what it still owes, the last one all of it) take it on."""
     xy = torus_points(2000, 12)
     ev, en, eo = P.periodic_mesh(xy, L)
     a, b = ev[0, 0], ev[0, 1]
     d = np.zeros_like(xy)
     d[a] = 2.0 * (xy[b] - xy[a] + eo_b_vec(eo[0]) * L)   # a jumps across b
     st, pos, ev2, en2, eo2 = run(harness, tmp_path, xy, d, ev, en, eo)
-    assert st["status"] == 0 and st["inverted"] > 0 and st["reverted"] == 1 and st["revert_passes"] == 1, st
-    assert np.array_equal(pos, xy) and st["nonpositive_after"] == 0
-    assert np.array_equal(eo2, eo) and np.array_equal(ev2, ev)
+    assert st["inverted"] > 0 and st["reverted"] >= 1, st
+    check_step(st, xy, d, pos, ev2, en2, eo2)
+    moved = ~(pos == xy).all(1)
+    assert moved.sum() <= 1 and st["behind"] + st["substep_arrivals"] == 1
 
 
-@pytest.mark.parametrize("sigma,shift,seed", [(0.1, (0.0, 0.0), 51), (0.2, (0.4, -0.3), 52)])
-def test_tangling_moves_are_refused_vertex_by_vertex(harness, tmp_path, sigma, shift, seed):
+@pytest.mark.parametrize("sigma,shift,seed", [(0.1, (0.0, 0.0), 51), (0.2, (0.4, -0.3), 52), (0.3, (0.0, 0.0), 53)])
+def test_tangling_moves_are_resumed_by_sub_steps(harness, tmp_path, sigma, shift, seed):
     """Unsettled random moves: vertices of turned faces go back (repeatedly,
-    as reverting one can turn another face), everything else moves, and the
-    result is the periodic Delaunay triangulation of where the points ended."""
+    as sending one back can turn another face), then sub-steps bring most of
+    them to their targets; the result is always the periodic Delaunay
+    triangulation of where the points ended."""
     n = 4000
     xy = torus_points(n, seed)
     ev, en, eo = P.periodic_mesh(xy, L)
     h = L / np.sqrt(n)
     d = (np.random.default_rng(seed).normal(0, sigma * h, (n, 2)) + np.array(shift) * h).astype(np.float32)
     st, pos, ev2, en2, eo2 = run(harness, tmp_path, xy, d, ev, en, eo)
-    assert st["status"] == 0 and st["inverted"] > 0 and st["reverted"] > 0 and st["nonpositive_after"] == 0, st
-    moved = torus_wrap(xy + d)
-    back = (pos == xy).all(1) & ~(moved == xy).all(1)
-    assert ((pos == moved).all(1) | back).all()
-    assert back.sum() == st["reverted"] and st["reverted"] < n // 2 and st["revert_passes"] >= 2
-    assert torus_faces_consistent(ev2, en2, eo2)
-    assert np.array_equal(P.mesh_edges(ev2, eo2), P.periodic_edges(pos, L))
+    assert st["inverted"] > 0 and st["reverted"] > 0 and st["revert_passes"] >= 2, st
+    check_step(st, xy, d, pos, ev2, en2, eo2)
+    assert st["substep_arrivals"] > 0 and st["behind"] < n // 3
 
 
 def eo_b_vec(w):
