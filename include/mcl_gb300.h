@@ -428,9 +428,9 @@ int mcl_periodic_positions(mcl_periodic* m, mcl_float2** pos_dev);
 /* One kinetic step on the torus: every point moves by d_dev[i] (device,
  * float2[n]; shorter than a period) and wraps into the domain, then parallel
  * Lawson flip rounds restore the periodic Delaunay triangulation.  Moves that
- * would turn faces over are refused vertex by vertex: the moved vertices of
- * every turned face go back to where they were (repeatedly, since sending one
- * back can turn another face) before any flip; then up to five sub-steps move
+ * would turn faces over are refused vertex by vertex: the farthest-moved
+ * vertex of every turned face goes back to where it was (repeatedly, until no
+ * face is turned) before any flip; then up to five sub-steps move
  * the vertices still owing part of their displacement by half of it (the last
  * by all of it, landing exactly on the target), each with the same refusal
  * and flips.  The result is always the valid periodic Delaunay triangulation

@@ -308,10 +308,11 @@ MCL_HD void p_body_resume(const PView& V, PF2* d, int v, bool last) {
 }
 
 // vertex v, after a classification that found faces turned over: a marked
-// vertex that moved goes back to its old position, and its wrap is undone in
-// the next fold; every other vertex folds nothing.  Repeated until no face is
-// turned over, this ends (at worst every moved vertex of a turned face is back
-// where the valid mesh had it).
+// vertex (the farthest-moved of a turned face) goes back to its old position,
+// and its wrap is undone in the next fold; every other vertex folds nothing.
+// Repeated until no face is turned over, this ends: a turned face always has a
+// moved vertex, and at worst every moved vertex is back where the valid mesh
+// had it.
 MCL_HD void p_body_revert(const PView& V, int v) {
   const Off none{0, 0};
   V.wv[v] = (unsigned char)off_byte(none);
@@ -341,6 +342,25 @@ MCL_HD void p_body_wrap(const PView& V, int e) {
   if (delta) V.eo[e] = V.eo[e] + (unsigned)delta;
 }
 
+// the length, squared, of vertex v's current move on the torus (exact
+// differences; float squares)
+MCL_HD float p_moved2(const PView& V, int v) {
+  const PF2 p = V.pos[v], q = V.pos_old[v];
+  const float dx = p_toward(p.x, q.x, V.L), dy = p_toward(p.y, q.y, V.L);
+  return fadd(fmul(dx, dx), fmul(dy, dy));
+}
+// the vertex of a turned face that goes back: the one that moved farthest
+// (the smallest id among equals); sending it back ends the turn in most
+// cases, and a face still turned marks another vertex in the next pass
+MCL_HD int p_culprit(const PView& V, int a, int b, int c) {
+  const float ma = p_moved2(V, a), mb = p_moved2(V, b), mc = p_moved2(V, c);
+  int best = a;
+  float bm = ma;
+  if (mb > bm || (mb == bm && b < best)) { best = b; bm = mb; }
+  if (mc > bm || (mc == bm && c < best)) { best = c; bm = mc; }
+  return best;
+}
+
 // edge e: orientation of its two faces and, when both are positive, the
 // incircle test; a non-Delaunay edge claims both faces for this round
 MCL_HD void p_body_classify(const PView& V, int e, unsigned stamp) {
@@ -362,10 +382,8 @@ MCL_HD void p_body_classify(const PView& V, int e, unsigned stamp) {
   const int sb = orient2d(qb.x, qb.y, pa.x, pa.y, qd.x, qd.y, &lc, &lc.overflow);
   if (sa <= 0 || sb <= 0) {
     p_add(&V.cnt->inverted, (unsigned long long)((sa <= 0) + (sb <= 0)));
-    V.mark[q.x] = 1;
-    V.mark[q.y] = 1;
-    if (sa <= 0) V.mark[q.z] = 1;
-    if (sb <= 0) V.mark[q.w] = 1;
+    if (sa <= 0) V.mark[p_culprit(V, q.x, q.y, q.z)] = 1;
+    if (sb <= 0) V.mark[p_culprit(V, q.y, q.x, q.w)] = 1;
     p_flush(V, lc);
     return;
   }

@@ -135,9 +135,9 @@ def test_a_face_turned_over_is_refused_then_resumed(harness, tmp_path):
 
 @pytest.mark.parametrize("sigma,shift,seed", [(0.1, (0.0, 0.0), 51), (0.2, (0.4, -0.3), 52), (0.3, (0.0, 0.0), 53)])
 def test_tangling_moves_are_resumed_by_sub_steps(harness, tmp_path, sigma, shift, seed):
-    """Unsettled random moves: vertices of turned faces go back (repeatedly,
-    as sending one back can turn another face), then sub-steps bring most of
-    them to their targets; the result is always the periodic Delaunay
+    """Unsettled random moves: the farthest-moved vertex of each turned face
+    goes back (repeatedly, until no face is turned), then sub-steps bring most
+    of them to their targets; the result is always the periodic Delaunay
     triangulation of where the points ended."""
     n = 4000
     xy = torus_points(n, seed)
