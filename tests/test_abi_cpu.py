@@ -150,3 +150,35 @@ def test_single_point_moves_refuse_the_bounding_corners():
     for f in (ht.moveFlipflop, ht.moveFlipflopDelaunay, ht.moveUntangling, ht.moveUntanglingDelaunay):
         assert f(0, (1.0, 1.0)) is False and f(3, (1.0, 1.0)) is False and f(4, (1.0, 1.0)) is False
     assert np.array_equal(ht.m_pos, before)
+
+
+def test_malformed_aos_meshes_are_refused_on_the_host(L):
+    """mcl_mesh_create_from_aos validates the reference-layout arrays before any
+    device work: each corruption of a valid mesh is refused with its reason."""
+    import ctypes as C
+
+    pts = np.random.default_rng(2).random((50, 2)).astype(np.float32) * 1000
+    pos, v, he, t = (np.ascontiguousarray(a) for a in O.Mesh.build(pts, exact=True).aos())
+
+    def create(pos, v, he, t):
+        keep = [np.ascontiguousarray(a) for a in (pos, v, he, t)]
+        view = L.AosView(*(L.ptr(a) for a in keep), len(keep[0]), len(keep[2]), len(keep[3]))
+        h = C.c_void_p()
+        rc = L.lib().mcl_mesh_create_from_aos(C.byref(view), C.byref(h))
+        return rc, L.lib().mcl_last_error().decode()
+
+    cases = []
+    bad = he.copy(); bad[7, 0] = len(he) + 3
+    cases.append((bad, v, "half-edge index out of range"))
+    bad = he.copy(); bad[7, 0] = he[8, 0]
+    cases.append((bad, v, "two half-edges share a next"))
+    bad = he.copy(); bad[12, 1] = (he[12, 1] + 1) % len(pos)
+    cases.append((bad, v, "inconsistent"))
+    badv = v.copy(); badv[10, 1] = int(np.nonzero(he[:, 1] != 10)[0][0])
+    cases.append((he, badv, "vertex he is not outgoing"))
+    for h_, v_, why in cases:
+        rc, msg = create(pos, v_, h_, t)
+        assert rc == L.MCL_ERR_INVALID_ARGUMENT and why in msg, (rc, msg, why)
+    odd = he[:-1]
+    rc, msg = create(pos, v, odd, t)
+    assert rc == L.MCL_ERR_INVALID_ARGUMENT and "bad sizes" in msg
