@@ -458,6 +458,14 @@ int mcl_periodic_one_ring(mcl_periodic* m, int max_ring, int layout, int32_t* ri
 int mcl_periodic_closest(mcl_periodic* m, int max_ring, int layout, const int32_t* ring_dev,
                          const uint8_t* offs_dev, int32_t* closest_dev, void* stream);
 
+/* getFRNN<M,F> (include/Device_Triangulation.h:530-538) on a periodic mesh:
+ * for each vertex, every other vertex with a copy within r (r < L/2), found by
+ * a search over the mesh; ascending ids, slot 0 the count, at most
+ * max_frnn - 1 (layouts as for the ring).  offs_dev (may be NULL) receives
+ * each one's copy offset byte.  truncated (may be NULL): vertices with more. */
+int mcl_periodic_frnn(mcl_periodic* m, float r, int max_frnn, int layout, int32_t* out_dev, uint8_t* offs_dev,
+                      void* stream, int64_t* truncated);
+
 /* Host conversion behind mcl_periodic_build, for meshes built elsewhere: the
  * periodic mesh that a planar triangulation of a cover of the torus stands
  * for.  vertex_point[v] / vertex_copy[v] give, for each vertex of the planar

@@ -107,6 +107,10 @@ __global__ void k_pring(PView V, const int* vhe, bool column, int max_ring, int*
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < V.n) mcl::p_body_ring(V, vhe, i, column, max_ring, ring, offs);
 }
+__global__ void k_pfrnn(PView V, const int* vhe, float r2, bool column, int max_frnn, int* out, unsigned char* offs) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < V.n) mcl::p_body_frnn(V, vhe, i, r2, column, max_frnn, out, offs);
+}
 __global__ void k_pclosest(PView V, bool column, int max_ring, const int* ring, const unsigned char* offs, int* out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < V.n) mcl::p_body_closest(V, i, column, max_ring, ring, offs, out);
@@ -611,6 +615,26 @@ int mcl_periodic_one_ring(mcl_periodic* m, int max_ring, int layout, int32_t* ri
   if (m->cnt_host->error)
     return mcl::fail((int)m->cnt_host->error,
                      "mcl_periodic_one_ring: malformed mesh (site " + std::to_string(m->cnt_host->error_site) + ")");
+  if (truncated) *truncated = (int64_t)m->cnt_host->truncated;
+  return MCL_OK;
+}
+
+int mcl_periodic_frnn(mcl_periodic* m, float r, int max_frnn, int layout, int32_t* out_dev, uint8_t* offs_dev,
+                      void* stream, int64_t* truncated) {
+  if (!m || !out_dev || max_frnn < 1 || !(r >= 0.0f) || !(r < 0.5f * m->L) ||
+      (layout != MCL_LAYOUT_COLUMN && layout != MCL_LAYOUT_ROW))
+    return mcl::fail(MCL_ERR_INVALID_ARGUMENT, "mcl_periodic_frnn: bad arguments (0 <= r < L/2)");
+  cudaStream_t s = (cudaStream_t)stream;
+  const PView V = view(m);
+  PCK(cudaMemsetAsync(m->cnt, 0, sizeof(PCount), s));
+  k_pvhe<<<blocks(2 * m->E), kThreads, 0, s>>>(V, m->vhe);
+  k_pfrnn<<<blocks(m->n), kThreads, 0, s>>>(V, m->vhe, r * r, layout == MCL_LAYOUT_COLUMN, max_frnn, out_dev, offs_dev);
+  PCK(cudaGetLastError());
+  PCK(cudaMemcpyAsync(m->cnt_host, m->cnt, sizeof(PCount), cudaMemcpyDeviceToHost, s));
+  PCK(cudaStreamSynchronize(s));
+  if (m->cnt_host->error)
+    return mcl::fail((int)m->cnt_host->error,
+                     "mcl_periodic_frnn: malformed mesh (site " + std::to_string(m->cnt_host->error_site) + ")");
   if (truncated) *truncated = (int64_t)m->cnt_host->truncated;
   return MCL_OK;
 }

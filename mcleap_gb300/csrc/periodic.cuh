@@ -545,4 +545,88 @@ MCL_HD void p_body_closest(const PView& V, int v, bool column, int max_ring, con
   out[v] = best;
 }
 
+constexpr int kPeriodicFrnnLocal = 256;
+
+// vertex i: every other vertex with a copy within r of i (r < L / 2, so at
+// most one copy of each), found by a search over the mesh from i through the
+// vertices already found (the reference's getFRNN, include/kernels.cuh:169-219,
+// on the torus); written by ascending id, slot 0 the count, at most
+// max_frnn - 1 of them; offs (may be null) gets each one's copy offset byte.
+MCL_HD void p_body_frnn(const PView& V, const int* vhe, int i, float r2, bool column, int max_frnn, int* out,
+                        unsigned char* offs) {
+  int fid[kPeriodicFrnnLocal];
+  unsigned char foff[kPeriodicFrnnLocal];
+  int nf = 0, top = 0;
+  bool over = false;
+  const unsigned H = 2u * (unsigned)V.E;
+  const PF2 pi = V.pos[i];
+  int cur = i;
+  Off ocur{0, 0};
+  for (int guard = 0; guard < (1 << 20); ++guard) {
+    const int h0 = vhe[cur];
+    if ((unsigned)h0 < H) {
+      int h = h0, deg = 0;
+      do {
+        const int w = p_origin(V, h ^ 1);
+        const Off ow = off_add(ocur, eo_target(V.eo[h >> 1], h & 1));
+        if (w != i && (unsigned)w < (unsigned)V.n && off_small(ow)) {
+          bool seen = false;
+          for (int k = 0; k < nf; ++k)
+            if (fid[k] == w) {
+              seen = true;
+              break;
+            }
+          if (!seen) {
+            const PF2 q = off_translate(V.pos[w], ow, V.L);
+            const float dx = fsub(pi.x, q.x), dy = fsub(pi.y, q.y);
+            if (fadd(fmul(dx, dx), fmul(dy, dy)) <= r2) {
+              if (nf < kPeriodicFrnnLocal) {
+                fid[nf] = w;
+                foff[nf] = (unsigned char)off_byte(ow);
+                ++nf;
+              } else {
+                over = true;
+              }
+            }
+          }
+        }
+        h = p_rot(V, h);
+        ++deg;
+        if ((unsigned)h >= H) {
+          p_error(V, MCL_ERR_DEGENERATE_INPUT, 10);
+          return;
+        }
+      } while (h != h0 && deg < kPeriodicMaxDeg);
+    }
+    if (top >= nf) break;
+    cur = fid[top];
+    ocur = off_from_byte(foff[top]);
+    ++top;
+  }
+  for (int a = 1; a < nf; ++a) {  // insertion sort by id
+    const int x = fid[a];
+    const unsigned char xo = foff[a];
+    int b = a - 1;
+    while (b >= 0 && fid[b] > x) {
+      fid[b + 1] = fid[b];
+      foff[b + 1] = foff[b];
+      --b;
+    }
+    fid[b + 1] = x;
+    foff[b + 1] = xo;
+  }
+  const int cap = max_frnn - 1;
+  const int cnt = nf < cap ? nf : cap;
+  const size_t stride = column ? (size_t)V.n : 1;
+  int* row = column ? out + i : out + (size_t)i * max_frnn;
+  unsigned char* orow = offs ? (column ? offs + i : offs + (size_t)i * max_frnn) : nullptr;
+  for (int k = 0; k < cnt; ++k) {
+    row[(size_t)(k + 1) * stride] = fid[k];
+    if (orow) orow[(size_t)(k + 1) * stride] = foff[k];
+  }
+  row[0] = cnt;
+  if (orow) orow[0] = 0;
+  if (over || nf > cap) p_add(&V.cnt->truncated, 1);
+}
+
 }  // namespace mcl

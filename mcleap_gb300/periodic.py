@@ -112,6 +112,15 @@ class PeriodicTriangulation:
                                               _stream_ptr(stream), C.byref(trunc)))
         return trunc.value
 
+    def getFRNN(self, maxFRNNSize, r, neighbors, offsets=None, stream=None, layout=L.LAYOUT_COLUMN):
+        """Every other point with a copy within r (< L/2), ascending ids, slot 0
+        the count; offsets (optional uint8 device tensor): copy offset bytes.
+        Returns the number of truncated lists."""
+        trunc = C.c_int64()
+        L.check(L.lib().mcl_periodic_frnn(self.handle, float(r), maxFRNNSize, layout, L.ptr(neighbors),
+                                          L.ptr(offsets), _stream_ptr(stream), C.byref(trunc)))
+        return trunc.value
+
     def closestNeighbors(self, maxRingSize, ring_neighbors, offsets, closest_neighbors, stream=None,
                          layout=L.LAYOUT_COLUMN):
         L.check(L.lib().mcl_periodic_closest(self.handle, maxRingSize, layout, L.ptr(ring_neighbors), L.ptr(offsets),

@@ -8,14 +8,15 @@
 // indexing without a GPU.
 //
 //   periodic_step IN OUT
-//   IN : int32 n, int32 E, float L, float pos[n][2], float d[n][2],
+//   IN : int32 n, int32 E, float L, float r (FRNN radius), float pos[n][2], float d[n][2],
 //        int32 ev[E][4], int32 en[E][4], uint32 eo[E]
 //   OUT: int32 status, int32 flips, int32 wrapped, int32 inverted, int32 rounds,
 //        int32 nonpositive_after, int32 truncated, int32 reverted, int32 revert_passes,
 //        int32 behind (not at the target at the end), int32 substep_arrivals,
 //        float pos[n][2], int32 ev[E][4],
 //        int32 en[E][4], uint32 eo[E], then the queries on the final mesh:
-//        int32 ring[kRing][n] and uint8 offs[kRing][n] (column layout), int32 closest[n]
+//        int32 ring[kRing][n] and uint8 offs[kRing][n] (column layout), int32 closest[n],
+//        int32 frnn[kFrnn][n] and uint8 frnn_offs[kFrnn][n], int32 frnn_truncated
 // status: an MCL_* code from the bodies (0 ok), 100 + an I/O failure.
 #include <cstdint>
 #include <cstdio>
@@ -34,6 +35,7 @@ template <typename T>
 void wr(FILE* f, const T* p, size_t k) { fwrite(p, sizeof(T), k, f); }
 
 constexpr int kRing = 8;  // small enough that some rings are truncated
+constexpr int kFrnn = 64;
 constexpr int kMaxRevertPasses = 256;
 constexpr int kSubLevels = 5;
 
@@ -57,9 +59,9 @@ int face_sign(const mcl::PView& V, int h) {
 int main(int argc, char** argv) {
   if (argc != 3) return 1;
   int n = 0, E = 0;
-  float L = 0;
+  float L = 0, r = 0;
   FILE* in = fopen(argv[1], "rb");
-  if (!in || !rd(in, &n, 1) || !rd(in, &E, 1) || !rd(in, &L, 1)) return 2;
+  if (!in || !rd(in, &n, 1) || !rd(in, &E, 1) || !rd(in, &L, 1) || !rd(in, &r, 1)) return 2;
   std::vector<PF2> pos(n), d(n);
   std::vector<PI4> ev(E), en(E);
   std::vector<uint32_t> eo(E), cand(E, 0);
@@ -137,12 +139,19 @@ int main(int argc, char** argv) {
     for (int v = 0; v < n && !cnt.error; ++v)
       mcl::p_body_closest(V, v, true, kRing, ring.data(), offs.data(), closest.data());
   }
+  std::vector<int> frnn((size_t)kFrnn * n, -1);
+  std::vector<unsigned char> foffs((size_t)kFrnn * n, 0);
+  const unsigned long long trunc_rings = cnt.truncated;
+  if (!cnt.error)
+    for (int v = 0; v < n && !cnt.error; ++v)
+      mcl::p_body_frnn(V, vhe.data(), v, r * r, true, kFrnn, frnn.data(), foffs.data());
+  const int32_t frnn_truncated = (int32_t)(cnt.truncated - trunc_rings);
 
   FILE* out = fopen(argv[2], "wb");
   if (!out) return 4;
   const int32_t head[11] = {(int32_t)cnt.error,     (int32_t)cnt.flips,    (int32_t)cnt.wrapped,
                             (int32_t)inverted,      rounds,                after,
-                            (int32_t)cnt.truncated, (int32_t)cnt.reverted, revert_passes,
+                            (int32_t)trunc_rings,   (int32_t)cnt.reverted, revert_passes,
                             (int32_t)behind,        (int32_t)(behind_first > behind ? behind_first - behind : 0)};
   wr(out, head, 11);
   wr(out, pos.data(), n);
@@ -152,6 +161,9 @@ int main(int argc, char** argv) {
   wr(out, ring.data(), ring.size());
   wr(out, offs.data(), offs.size());
   wr(out, closest.data(), closest.size());
+  wr(out, frnn.data(), frnn.size());
+  wr(out, foffs.data(), foffs.size());
+  wr(out, &frnn_truncated, 1);
   fclose(out);
   return 0;
 }

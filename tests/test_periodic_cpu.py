@@ -16,6 +16,7 @@ from oracle import periodic as P
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 RING = 8  # ring slots of the harness (kRing)
+FRNN = 64  # FRNN slots of the harness (kFrnn)
 
 
 @pytest.fixture(scope="module")
@@ -26,11 +27,12 @@ def harness(tmp_path_factory):
     return exe
 
 
-def run(harness, tmp_path, pos, d, ev, en, eo):
+def run(harness, tmp_path, pos, d, ev, en, eo, r=None):
     n, E = len(pos), len(ev)
+    r = 2.5 * L / np.sqrt(n) if r is None else r
     src, dst = str(tmp_path / "in.bin"), str(tmp_path / "out.bin")
     with open(src, "wb") as f:
-        f.write(np.array([n, E], np.int32).tobytes() + np.float32(L).tobytes())
+        f.write(np.array([n, E], np.int32).tobytes() + np.float32(L).tobytes() + np.float32(r).tobytes())
         for a in (pos.astype(np.float32), d.astype(np.float32), ev.astype(np.int32), en.astype(np.int32),
                   eo.astype(np.uint32)):
             f.write(np.ascontiguousarray(a).tobytes())
@@ -51,7 +53,14 @@ def run(harness, tmp_path, pos, d, ev, en, eo):
     offs = np.frombuffer(raw[o:o + RING * n], np.uint8).reshape(RING, n)
     o += RING * n
     closest = np.frombuffer(raw[o:o + 4 * n], np.int32)
+    o += 4 * n
+    frnn = np.frombuffer(raw[o:o + 4 * FRNN * n], np.int32).reshape(FRNN, n)
+    o += 4 * FRNN * n
+    foffs = np.frombuffer(raw[o:o + FRNN * n], np.uint8).reshape(FRNN, n)
+    o += FRNN * n
+    frnn_truncated = int(np.frombuffer(raw[o:o + 4], np.int32)[0])
     run.queries = (ring, offs, closest)
+    run.frnn = (frnn, foffs, frnn_truncated, np.float32(r))
     st = dict(zip(["status", "flips", "wrapped", "inverted", "rounds", "nonpositive_after", "truncated", "reverted",
                    "revert_passes", "behind", "substep_arrivals"], head))
     return st, pos2, ev2, en2, eo2
@@ -227,6 +236,7 @@ def test_periodic_arguments_are_checked_before_device_work(lib):
     assert L_.mcl_periodic_step(None, None, None, C.byref(st), None) == lib.MCL_ERR_INVALID_ARGUMENT
     assert L_.mcl_periodic_one_ring(None, 8, 0, None, None, None, None) == lib.MCL_ERR_INVALID_ARGUMENT
     assert L_.mcl_periodic_closest(None, 8, 0, None, None, None, None) == lib.MCL_ERR_INVALID_ARGUMENT
+    assert L_.mcl_periodic_frnn(None, 1.0, 8, 0, None, None, None, None) == lib.MCL_ERR_INVALID_ARGUMENT
 
 
 def band_cover(xy, band):
@@ -315,3 +325,47 @@ def test_ring_and_closest_on_a_stepped_mesh(harness, tmp_path):
         dd = (dx * dx + dy * dy).astype(np.float32)
         best = nb[np.lexsort((nb, dd))[0]]
         assert closest[v] == best
+
+
+def frnn_brute(pos, r):
+    """(neighbour, ox, oy) sets within r on the torus by the reference's float
+    squared distance, over the nine copies of every point."""
+    n = len(pos)
+    r2 = np.float32(r) * np.float32(r)
+    out = [set() for _ in range(n)]
+    for oy in (-1, 0, 1):
+        for ox in (-1, 0, 1):
+            q = (pos + np.float32([ox * L, oy * L])).astype(np.float32)
+            for a in range(0, n, 500):
+                dx = (pos[a:a + 500, None, 0] - q[None, :, 0]).astype(np.float32)
+                dy = (pos[a:a + 500, None, 1] - q[None, :, 1]).astype(np.float32)
+                d2 = (dx * dx + dy * dy).astype(np.float32)
+                ii, jj = np.nonzero(d2 <= r2)
+                for i, j in zip(ii + a, jj):
+                    if i != j:
+                        out[i].add((int(j), ox, oy))
+    return out
+
+
+@pytest.mark.parametrize("rf", [1.5, 3.0])
+def test_frnn_on_a_stepped_mesh(harness, tmp_path, rf):
+    """getFRNN on the torus by the query body: every other point with a copy
+    within r, ascending ids, with the copy offsets; equal to brute force."""
+    n = 3000
+    xy = torus_points(n, 61)
+    ev, en, eo = P.periodic_mesh(xy, L)
+    h = L / np.sqrt(n)
+    drift = np.float32([-0.3 * h, 0.55 * h])
+    d = (np.random.default_rng(6).normal(0, 0.05 * h, (n, 2)) + drift).astype(np.float32)
+    st, pos, *_ = run(harness, tmp_path, xy, d, ev, en, eo, r=rf * h)
+    assert st["status"] == 0 and st["wrapped"] > 0
+    frnn, foffs, trunc, r = run.frnn
+    assert trunc == 0
+    want = frnn_brute(pos, r)
+    for i in range(n):
+        cnt = frnn[0, i]
+        ids = frnn[1:cnt + 1, i]
+        ob = foffs[1:cnt + 1, i].astype(np.int64)
+        assert (np.diff(ids) > 0).all()
+        got = {(int(a), int((b & 15) - 8), int(((b >> 4) & 15) - 8)) for a, b in zip(ids, ob)}
+        assert got == want[i], i

@@ -169,3 +169,40 @@ def test_ring_and_closest_after_steps(M):
         dy = (pos[v, 1] - (pos[nb, 1] + (o[:, 1] * L).astype(np.float32))).astype(np.float32)
         dd = (dx * dx + dy * dy).astype(np.float32)
         assert closest[v] == nb[np.lexsort((nb, dd))[0]]
+
+
+def test_frnn_after_steps(M):
+    """getFRNN on the torus: every other point with a copy within r, by the
+    reference's float distance, ascending ids, against brute force."""
+    import torch
+
+    n = 4000
+    xy = torus_points(n, 9)
+    pt = M.PeriodicTriangulation(xy, L)
+    h = L / np.sqrt(n)
+    _, ev, _, eo = pt.download()
+    drift = np.float32([0.5 * h, 0.5 * h])
+    d = (np.random.default_rng(5).normal(0, 0.05 * h, (n, 2)) + drift).astype(np.float32)
+    d = torus_settle(xy, d, ev, eo, drift)
+    pt.step(cuda(d))
+    pos = pt.download()[0]
+    F, r = 64, np.float32(2.5 * h)
+    out = torch.full((F * n,), -1, dtype=torch.int32, device="cuda")
+    offs = torch.zeros((F * n,), dtype=torch.uint8, device="cuda")
+    assert pt.getFRNN(F, float(r), out, offs) == 0
+    out = out.cpu().numpy().reshape(F, n)
+    offs = offs.cpu().numpy().reshape(F, n).astype(np.int64)
+    r2 = r * r
+    for i in range(0, n, 7):
+        cnt = out[0, i]
+        got = {(int(a), int((b & 15) - 8), int(((b >> 4) & 15) - 8)) for a, b in zip(out[1:cnt + 1, i], offs[1:cnt + 1, i])}
+        want = set()
+        for oy in (-1, 0, 1):
+            for ox in (-1, 0, 1):
+                q = (pos + np.float32([ox * L, oy * L])).astype(np.float32)
+                dx = (pos[i, 0] - q[:, 0]).astype(np.float32)
+                dy = (pos[i, 1] - q[:, 1]).astype(np.float32)
+                for j in np.nonzero((dx * dx + dy * dy).astype(np.float32) <= r2)[0]:
+                    if j != i:
+                        want.add((int(j), ox, oy))
+        assert got == want and (np.diff(out[1:cnt + 1, i]) > 0).all(), i
