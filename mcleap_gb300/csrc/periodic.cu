@@ -18,7 +18,10 @@
 //           launches.  A classification that finds faces turned over sends
 //           their moved vertices back (one launch over vertices, then the
 //           fold again) and classifies again; flips start from a mesh whose
-//           faces are all positive.
+//           faces are all positive.  Vertices sent back then follow in up to
+//           kSubLevels sub-steps (half of what they still owe, the last all).
+//   queries one-ring with copy offsets, closest neighbour, mesh FRNN (one
+//           launch for the outgoing half-edges, one per query).
 #include <cuda_runtime.h>
 
 #include <algorithm>
