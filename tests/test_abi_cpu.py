@@ -182,3 +182,42 @@ def test_malformed_aos_meshes_are_refused_on_the_host(L):
     odd = he[:-1]
     rc, msg = create(pos, v, odd, t)
     assert rc == L.MCL_ERR_INVALID_ARGUMENT and "bad sizes" in msg
+
+
+PERIODIC_PROGRAM = r"""
+#include <cstdio>
+#include <vector>
+#include "mcleap/Periodic_Triangulation.h"
+int main() {
+  std::vector<glm::vec2> pts;
+  for (int i = 0; i < 1000; ++i) pts.push_back(glm::vec2(16384.f + (i * 37 % 1000) * 8.f, 16384.f + i * 8.f));
+  PeriodicTriangulation pt(pts, 8192.f);
+  glm::vec2* d = nullptr;
+  int *ring = nullptr, *nb = nullptr, *cl = nullptr;
+  uint8_t* offs = nullptr;
+  pt.step(d);
+  pt.oneRing<32>(ring, offs);
+  pt.oneRing2<32>(ring, offs);
+  pt.closestNeighbors<32>(ring, offs, cl);
+  pt.getFRNN<32, 64>(20.f, ring, nb);
+  std::vector<glm::vec2> pos;
+  std::vector<int32_t> ev, en;
+  std::vector<uint32_t> eo;
+  pt.transferToHost(pos, ev, en, eo);
+  std::printf("%p %lld\n", (void*)pt.positions(), (long long)pt.E);
+  return 0;
+}
+"""
+
+
+def test_periodic_cpp_header_compiles_and_links(L, tmp_path):
+    from mcleap_gb300 import build as B
+
+    src = tmp_path / "periodic_dropin.cu"
+    src.write_text(PERIODIC_PROGRAM)
+    exe = str(tmp_path / "periodic_dropin")
+    cmd = [B.nvcc(), "-std=c++17", "-O0", "-gencode", "arch=compute_103a,code=sm_103a",
+           "-I", os.path.join(ROOT, "include"), str(src),
+           "-L", os.path.dirname(L.LIB_PATH), "-lmcl_gb300", "-o", exe]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
