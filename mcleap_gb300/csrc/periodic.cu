@@ -52,6 +52,9 @@ struct mcl_periodic {
   PF2* pos_old;
   PF2* target;
   PF2* dsub;         // sub-step displacements
+  int* clist;        // a round's non-Delaunay edges
+  int* wl[2];        // edge work-lists between rounds
+  unsigned* qstamp;
   unsigned* cand;
   unsigned long long* claim;
   int* vhe;          // one outgoing half-edge per vertex (queries)
@@ -94,13 +97,25 @@ __global__ void k_pwrap(PView V) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < V.E) mcl::p_body_wrap(V, i);
 }
-__global__ void k_pclassify(PView V, unsigned stamp) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < V.E) mcl::p_body_classify(V, i, stamp);
+// every edge (list < 0) or the entries of work-list `list`, grid-stride (the
+// list's length is read on the device)
+__global__ void k_pclassify(PView V, unsigned stamp, int list) {
+  const long long items = list < 0 ? (long long)V.E : (long long)V.cnt->lcount[list];
+  const int* wl = list == 1 ? V.wl1 : V.wl0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < items;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int e = list < 0 ? (int)i : wl[i];
+    if ((unsigned)e < (unsigned)V.E) mcl::p_body_classify(V, e, stamp);
+  }
 }
-__global__ void k_pflip(PView V, unsigned stamp) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < V.E) mcl::p_body_flip(V, i, stamp);
+// the round's non-Delaunay edges; winners flip and queue their wings on `next`
+__global__ void k_pflip(PView V, unsigned stamp, int next) {
+  const long long items = (long long)V.cnt->nondelaunay;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < items;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int e = V.clist[i];
+    if ((unsigned)e < (unsigned)V.E) mcl::p_body_flip(V, e, stamp, next);
+  }
 }
 __global__ void k_pvhe(PView V, int* vhe) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -120,10 +135,13 @@ __global__ void k_pclosest(PView V, bool column, int max_ring, const int* ring, 
 }
 
 unsigned blocks(int64_t k) { return (unsigned)((k + kThreads - 1) / kThreads); }
+// grid of the grid-stride list kernels: 16 blocks of 256 per SM of a GB300 at most
+unsigned list_blocks(int64_t k) { return std::min<unsigned>(blocks(k), 152u * 16u); }
 
 PView view(mcl_periodic* m) {
-  return PView{(int)m->n, (int)m->E, m->L,       2.0f * m->L, m->pos,  m->ev,    m->en,   m->eo,
-               m->wv,      m->wt,      m->mark,    m->pos_old,  m->target, m->cand, m->claim, m->cnt};
+  return PView{(int)m->n, (int)m->E,  m->L,       2.0f * m->L, m->pos,    m->ev,   m->en,    m->eo,
+               m->wv,      m->wt,      m->mark,    m->pos_old,  m->target, m->cand, m->claim, m->cnt,
+               m->clist,   m->wl[0],   m->wl[1],   m->qstamp};
 }
 
 void free_periodic(mcl_periodic* m) {
@@ -138,6 +156,10 @@ void free_periodic(mcl_periodic* m) {
   cudaFree(m->pos_old);
   cudaFree(m->target);
   cudaFree(m->dsub);
+  cudaFree(m->clist);
+  cudaFree(m->wl[0]);
+  cudaFree(m->wl[1]);
+  cudaFree(m->qstamp);
   cudaFree(m->cand);
   cudaFree(m->claim);
   cudaFree(m->vhe);
@@ -331,6 +353,10 @@ int alloc_upload(const mcl_float2* pos, int64_t n, float L, const int32_t* ev, c
   A((void**)&m->pos_old, 8 * (size_t)n);
   A((void**)&m->target, 8 * (size_t)n);
   A((void**)&m->dsub, 8 * (size_t)n);
+  A((void**)&m->clist, 4 * (size_t)E);
+  A((void**)&m->wl[0], 4 * (size_t)E);
+  A((void**)&m->wl[1], 4 * (size_t)E);
+  A((void**)&m->qstamp, 4 * (size_t)E);
   A((void**)&m->cand, 4 * (size_t)E);
   A((void**)&m->claim, 16 * (size_t)E);
   A((void**)&m->vhe, 4 * (size_t)n);
@@ -347,6 +373,7 @@ int alloc_upload(const mcl_float2* pos, int64_t n, float L, const int32_t* ev, c
   if (e == cudaSuccess) e = cudaMemcpy(m->target, pos, 8 * (size_t)n, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemset(m->cand, 0, 4 * (size_t)E);
   if (e == cudaSuccess) e = cudaMemset(m->claim, 0, 16 * (size_t)E);
+  if (e == cudaSuccess) e = cudaMemset(m->qstamp, 0, 4 * (size_t)E);
   if (e == cudaSuccess) e = cudaMemset(m->cnt, 0, sizeof(PCount));
   if (e == cudaSuccess) e = cudaDeviceSynchronize();
   if (e != cudaSuccess) {
@@ -366,27 +393,29 @@ struct Settle {
   unsigned long long inverted_first = 0;
   bool classified = false;
   int rounds = 0;
-  int64_t incircle_tests = 0;  // every edge of a round without a face turned over
+  int64_t incircle_tests = 0;  // the edges classified in rounds without a face turned over
   std::string msg;
 };
 
 int settle(mcl_periodic* m, cudaStream_t s, const PView& V, Settle& z) {
-  int revert_passes = 0;
+  int revert_passes = 0, cur = -1;  // the work-list to classify (-1: every edge)
   bool flipped = false;
   for (int r = 0; r < kMaxRounds; ++r) {
-    if (m->stamp == 0xFFFFFFFFu) {  // stamps wrapped: forget every old claim
+    if (m->stamp >= 0xFFFFFFFEu) {  // stamps about to wrap: forget every old claim and queue mark
       PCK(cudaMemsetAsync(m->claim, 0, 16 * (size_t)m->E, s));
       PCK(cudaMemsetAsync(m->cand, 0, 4 * (size_t)m->E, s));
+      PCK(cudaMemsetAsync(m->qstamp, 0, 4 * (size_t)m->E, s));
       m->stamp = 0;
     }
     const unsigned stamp = ++m->stamp;
     PCK(cudaMemsetAsync(&m->cnt->inverted, 0, 2 * sizeof(unsigned long long), s));  // inverted, nondelaunay
-    k_pclassify<<<blocks(m->E), kThreads, 0, s>>>(V, stamp);
+    k_pclassify<<<list_blocks(m->E), kThreads, 0, s>>>(V, stamp, cur);
     PCK(cudaGetLastError());
     PCK(cudaMemcpyAsync(m->cnt_host, m->cnt, sizeof(PCount), cudaMemcpyDeviceToHost, s));
     PCK(cudaStreamSynchronize(s));
     z.c = *m->cnt_host;
     ++z.rounds;
+    const int64_t classified = cur < 0 ? m->E : (int64_t)z.c.lcount[cur];
     if (z.c.error) {
       const int rc = (int)z.c.error;
       z.msg = "mcl_periodic_step: " + std::string(mcl_status_string(rc)) + " (site " + std::to_string(z.c.error_site) +
@@ -411,12 +440,16 @@ int settle(mcl_periodic* m, cudaStream_t s, const PView& V, Settle& z) {
       k_pwrap<<<blocks(m->E), kThreads, 0, s>>>(V);
       PCK(cudaGetLastError());
       ++revert_passes;
+      cur = -1;
       continue;
     }
-    z.incircle_tests += m->E;
+    z.incircle_tests += classified;
     if (!z.c.nondelaunay) return MCL_OK;
-    k_pflip<<<blocks(m->E), kThreads, 0, s>>>(V, stamp);
+    const int next = cur == 0 ? 1 : 0;
+    PCK(cudaMemsetAsync(&m->cnt->lcount[next], 0, sizeof(unsigned long long), s));
+    k_pflip<<<list_blocks((int64_t)z.c.nondelaunay), kThreads, 0, s>>>(V, stamp, next);
     PCK(cudaGetLastError());
+    cur = next;
     flipped = true;
   }
   z.msg = "mcl_periodic_step: flip rounds did not converge";

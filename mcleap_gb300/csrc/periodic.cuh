@@ -166,6 +166,7 @@ struct alignas(16) PI4 {
 struct PCount {
   unsigned long long wrapped, inverted, nondelaunay, flips, incircle_fp64, incircle_exact, orient_fp64, orient_exact,
       sos, overflow, error, error_site, truncated, reverted, behind;
+  unsigned long long lcount[2];  // entries of the two edge work-lists
 };
 
 struct PView {
@@ -184,6 +185,10 @@ struct PView {
   unsigned* cand;             // round stamp of the non-Delaunay edges
   unsigned long long* claim;  // face claims, by the smallest half-edge id of the face
   PCount* cnt;
+  int* clist;                 // this round's non-Delaunay edges (cnt->nondelaunay of them)
+  int* wl0;                   // edge work-lists: the edges whose quads a round's flips changed
+  int* wl1;
+  unsigned* qstamp;           // the round an edge was last queued for
 };
 
 MCL_HD void p_add(unsigned long long* p, unsigned long long v) {
@@ -191,6 +196,22 @@ MCL_HD void p_add(unsigned long long* p, unsigned long long v) {
   atomicAdd(p, v);
 #else
   *p += v;
+#endif
+}
+MCL_HD unsigned long long p_inc(unsigned long long* p) {
+#if defined(__CUDA_ARCH__)
+  return atomicAdd(p, 1ull);
+#else
+  return (*p)++;
+#endif
+}
+MCL_HD unsigned p_exch(unsigned* p, unsigned v) {
+#if defined(__CUDA_ARCH__)
+  return atomicExch(p, v);
+#else
+  const unsigned old = *p;
+  *p = v;
+  return old;
 #endif
 }
 MCL_HD void p_max(unsigned long long* p, unsigned long long v) {
@@ -362,7 +383,8 @@ MCL_HD int p_culprit(const PView& V, int a, int b, int c) {
 }
 
 // edge e: orientation of its two faces and, when both are positive, the
-// incircle test; a non-Delaunay edge claims both faces for this round
+// incircle test; a non-Delaunay edge claims both faces for this round and
+// joins the round's list
 MCL_HD void p_body_classify(const PView& V, int e, unsigned stamp) {
   const PI4 q = V.ev[e];
   const PI4 w = V.en[e];
@@ -391,11 +413,18 @@ MCL_HD void p_body_classify(const PView& V, int e, unsigned stamp) {
       incircle_sos(pa.x, pa.y, qb.x, qb.y, qc.x, qc.y, qd.x, qd.y, q.x, q.y, q.z, q.w, &lc, &lc.overflow) > 0;
   p_flush(V, lc);
   if (!nd) return;
-  p_add(&V.cnt->nondelaunay, 1);
   const unsigned long long key = p_key(e, stamp);
   p_max(V.claim + p_face_a(e, w), key);
   p_max(V.claim + p_face_b(e, w), key);
   V.cand[e] = stamp;
+  V.clist[p_inc(&V.cnt->nondelaunay)] = e;
+}
+
+// edge e onto work-list k for the round with stamp `next`, once
+MCL_HD void p_queue(const PView& V, int e, unsigned next, int k) {
+  if (p_exch(V.qstamp + e, next) == next) return;
+  int* wl = k ? V.wl1 : V.wl0;
+  wl[p_inc(&V.cnt->lcount[k])] = e;
 }
 
 // one side of a wing half-edge h: its apex, next and prev, and its apex offset byte
@@ -418,8 +447,10 @@ MCL_HD void p_set_face(const PView& V, int h, int apex, int next, int prev, unsi
 }
 
 // edge e: flip when it holds the claims of both its faces (the planar
-// engine's flip, plus the offsets)
-MCL_HD void p_body_flip(const PView& V, int e, unsigned stamp) {
+// engine's flip, plus the offsets); the four wing edges, whose quads changed,
+// go onto work-list `next` for the next round, and so does a candidate that
+// lost a claim
+MCL_HD void p_body_flip(const PView& V, int e, unsigned stamp, int next) {
   if (V.cand[e] != stamp) return;
   const PI4 q = V.ev[e];
   const PI4 w = V.en[e];
@@ -428,7 +459,11 @@ MCL_HD void p_body_flip(const PView& V, int e, unsigned stamp) {
     return;
   }
   const unsigned long long key = p_key(e, stamp);
-  if (V.claim[p_face_a(e, w)] != key || V.claim[p_face_b(e, w)] != key) return;
+  if (V.claim[p_face_a(e, w)] != key || V.claim[p_face_b(e, w)] != key) {
+    // lost a face (possibly to another loser, so no flip may touch it): retry
+    p_queue(V, e, stamp + 1, next);
+    return;
+  }
   const FlipOffsets f = flip_offsets(V.eo[e]);
   const int a = q.x, b = q.y, c = q.z, d = q.w;
   const int n0 = w.x, p0 = w.y, n1 = w.z, p1 = w.w;
@@ -441,6 +476,10 @@ MCL_HD void p_body_flip(const PView& V, int e, unsigned stamp) {
   p_set_face(V, p1, c, n0, h1, f.p1);
   p_set_face(V, n0, d, h1, p1, f.n0);
   p_add(&V.cnt->flips, 1);
+  p_queue(V, p0 >> 1, stamp + 1, next);
+  p_queue(V, n1 >> 1, stamp + 1, next);
+  p_queue(V, p1 >> 1, stamp + 1, next);
+  p_queue(V, n0 >> 1, stamp + 1, next);
 }
 
 // ---------------------------------------------------------------------------

@@ -13,6 +13,7 @@
 //   OUT: int32 status, int32 flips, int32 wrapped, int32 inverted, int32 rounds,
 //        int32 nonpositive_after, int32 truncated, int32 reverted, int32 revert_passes,
 //        int32 behind (not at the target at the end), int32 substep_arrivals,
+//        int32 classified (edge classifications over all rounds),
 //        float pos[n][2], int32 ev[E][4],
 //        int32 en[E][4], uint32 eo[E], then the queries on the final mesh:
 //        int32 ring[kRing][n] and uint8 offs[kRing][n] (column layout), int32 closest[n],
@@ -75,20 +76,27 @@ int main(int argc, char** argv) {
 
   mcl::PCount cnt{};
   std::vector<PF2> target(n), dsub(n);
-  mcl::PView V{n,         E,           L,           2.0f * L,       pos.data(),    ev.data(),   en.data(),    eo.data(),
-               wv.data(),  wt.data(),   mark.data(), pos_old.data(), target.data(), cand.data(), claim.data(), &cnt};
+  std::vector<int> clist(E), wl0(E), wl1(E);
+  std::vector<unsigned> qstamp(E, 0);
+  mcl::PView V{n,           E,           L,           2.0f * L,       pos.data(),    ev.data(),   en.data(),
+               eo.data(),   wv.data(),   wt.data(),   mark.data(),    pos_old.data(), target.data(), cand.data(),
+               claim.data(), &cnt,       clist.data(), wl0.data(),    wl1.data(),    qstamp.data()};
+  long long classified = 0;
   int rounds = 0, revert_passes = 0;
   unsigned stamp = 0;
   long long inverted = -1;
   // the host loop of mcl_periodic_step, launch by launch
   auto settle = [&]() {
     bool flipped = false;
-    int passes = 0;
+    int passes = 0, cur = -1;  // the work-list to classify (-1: every edge)
     for (int r = 0; r < 4096; ++r) {
       ++stamp;
       cnt.nondelaunay = 0;
       cnt.inverted = 0;
-      for (int e = 0; e < E; ++e) mcl::p_body_classify(V, e, stamp);
+      const long long items = cur < 0 ? E : (long long)cnt.lcount[cur];
+      const int* wl = cur == 1 ? wl1.data() : wl0.data();
+      for (long long i = 0; i < items; ++i) mcl::p_body_classify(V, cur < 0 ? (int)i : wl[i], stamp);
+      classified += items;
       ++rounds;
       if (cnt.error) return;
       if (inverted < 0) inverted = (long long)cnt.inverted;
@@ -101,10 +109,14 @@ int main(int argc, char** argv) {
         for (int e = 0; e < E; ++e) mcl::p_body_wrap(V, e);
         ++passes;
         ++revert_passes;
+        cur = -1;
         continue;
       }
       if (!cnt.nondelaunay) return;
-      for (int e = 0; e < E; ++e) mcl::p_body_flip(V, e, stamp);
+      const int next = cur == 0 ? 1 : 0;
+      cnt.lcount[next] = 0;
+      for (unsigned long long i = 0; i < cnt.nondelaunay; ++i) mcl::p_body_flip(V, clist[i], stamp, next);
+      cur = next;
       flipped = true;
     }
     cnt.error = MCL_ERR_NO_CONVERGENCE;
@@ -149,11 +161,12 @@ int main(int argc, char** argv) {
 
   FILE* out = fopen(argv[2], "wb");
   if (!out) return 4;
-  const int32_t head[11] = {(int32_t)cnt.error,     (int32_t)cnt.flips,    (int32_t)cnt.wrapped,
+  const int32_t head[12] = {(int32_t)cnt.error,     (int32_t)cnt.flips,    (int32_t)cnt.wrapped,
                             (int32_t)inverted,      rounds,                after,
                             (int32_t)trunc_rings,   (int32_t)cnt.reverted, revert_passes,
-                            (int32_t)behind,        (int32_t)(behind_first > behind ? behind_first - behind : 0)};
-  wr(out, head, 11);
+                            (int32_t)behind,        (int32_t)(behind_first > behind ? behind_first - behind : 0),
+                            (int32_t)classified};
+  wr(out, head, 12);
   wr(out, pos.data(), n);
   wr(out, ev.data(), E);
   wr(out, en.data(), E);

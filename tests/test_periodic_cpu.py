@@ -38,8 +38,8 @@ def run(harness, tmp_path, pos, d, ev, en, eo, r=None):
             f.write(np.ascontiguousarray(a).tobytes())
     subprocess.run([harness, src, dst], check=True)
     raw = open(dst, "rb").read()
-    head = [int(x) for x in np.frombuffer(raw[:44], np.int32)]
-    o = 44
+    head = [int(x) for x in np.frombuffer(raw[:48], np.int32)]
+    o = 48
     pos2 = np.frombuffer(raw[o:o + 8 * n], np.float32).reshape(n, 2)
     o += 8 * n
     ev2 = np.frombuffer(raw[o:o + 16 * E], np.int32).reshape(E, 4)
@@ -62,7 +62,7 @@ def run(harness, tmp_path, pos, d, ev, en, eo, r=None):
     run.queries = (ring, offs, closest)
     run.frnn = (frnn, foffs, frnn_truncated, np.float32(r))
     st = dict(zip(["status", "flips", "wrapped", "inverted", "rounds", "nonpositive_after", "truncated", "reverted",
-                   "revert_passes", "behind", "substep_arrivals"], head))
+                   "revert_passes", "behind", "substep_arrivals", "classified"], head))
     return st, pos2, ev2, en2, eo2
 
 
@@ -92,6 +92,8 @@ def test_step_with_wraps_matches_oracle(harness, tmp_path, n, sigma, shift, seed
     assert st["reverted"] == 0 and st["revert_passes"] == 0 and st["behind"] == 0
     assert np.array_equal(pos, torus_wrap(xy + d))
     assert st["wrapped"] > 0 and st["flips"] > 0 and st["rounds"] >= 2
+    # rounds after the first classify only the edges around the last flips
+    assert st["classified"] < len(ev) + 5 * st["flips"]
     assert torus_faces_consistent(ev2, en2, eo2)
     assert np.array_equal(P.mesh_edges(ev2, eo2), P.periodic_edges(pos, L))
 
