@@ -433,12 +433,16 @@ int mcl_periodic_positions(mcl_periodic* m, mcl_float2** pos_dev);
  * face is turned) before any flip; then up to five sub-steps move
  * the vertices still owing part of their displacement by half of it (the last
  * by all of it, landing exactly on the target), each with the same refusal
- * and flips.  The result is always the valid periodic Delaunay triangulation
- * of where the points ended.  stats (may be NULL): inverted_faces (turned by
- * the move), reverted_vertices (not at their target at the end),
+ * and flips; the vertices still away after that are removed and reinserted
+ * at their targets one by one (one GPU thread; at most 65,536 a step), with
+ * flips around each.  The result is the periodic Delaunay triangulation of
+ * the moved points (a point whose target is taken by another stays where it
+ * was).  stats (may be NULL): inverted_faces (turned by the move),
  * substep_vertices (sent back, then brought to their target by sub-steps),
- * lawson_flips, lawson_rounds, the predicate counters, status; wrapped (may be
- * NULL): wraps across a side (a vertex may wrap in more than one sub-step). */
+ * removed_vertices (removed and reinserted), reverted_vertices (not at their
+ * target at the end), lawson_flips, lawson_rounds, the predicate counters,
+ * status; wrapped (may be NULL): wraps across a side (a vertex may wrap in
+ * more than one sub-step). */
 int mcl_periodic_step(mcl_periodic* m, const mcl_float2* d_dev, void* stream, mcl_step_stats* stats,
                       int64_t* wrapped);
 

@@ -19,7 +19,9 @@
 //           their moved vertices back (one launch over vertices, then the
 //           fold again) and classifies again; flips start from a mesh whose
 //           faces are all positive.  Vertices sent back then follow in up to
-//           kSubLevels sub-steps (half of what they still owe, the last all).
+//           kSubLevels sub-steps (half of what they still owe, the last all);
+//           the few still away are removed and reinserted at their targets
+//           by one thread (k_preinsert).
 //   queries one-ring with copy offsets, closest neighbour, mesh FRNN (one
 //           launch for the outgoing half-edges, one per query).
 #include <cuda_runtime.h>
@@ -69,6 +71,9 @@ constexpr int kThreads = 256;
 constexpr int kMaxRounds = 4096;
 constexpr int kMaxRevertPasses = 256;
 constexpr int kSubLevels = 5;  // sub-steps for vertices sent back
+// vertices one thread removes and reinserts per step at most (the rest stay
+// behind, counted): the single-thread kernel's time stays bounded
+constexpr int kMaxReinsert = 1 << 16;
 constexpr int kCenter = 4;  // copy index of the untranslated copy
 
 #define PCK(call)                                       \
@@ -88,6 +93,17 @@ __global__ void k_ptarget(PView V, const PF2* d) {
 __global__ void k_presume(PView V, PF2* d, bool last) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < V.n) mcl::p_body_resume(V, d, i, last);
+}
+__global__ void k_pbehind(PView V, int* list) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < V.n) mcl::p_body_behind(V, list, i);
+}
+// one thread: the sequential removal and reinsertion
+__global__ void k_preinsert(PView V, int* vhe, const int* list) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    const unsigned long long k = V.cnt->behind;
+    mcl::p_body_reinsert(V, vhe, list, (int)(k < (unsigned long long)kMaxReinsert ? k : kMaxReinsert));
+  }
 }
 __global__ void k_prevert(PView V) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -611,12 +627,38 @@ int mcl_periodic_step(mcl_periodic* m, const mcl_float2* d_dev, void* stream, mc
     PCK(cudaGetLastError());
     rc = settle(m, s, V, z);
   }
+  const int64_t substep_arrivals = behind_first > behind ? behind_first - behind : 0;
+  // the rest: removed and reinserted at their targets, one by one
+  int64_t reinserted = 0;
+  if (rc == MCL_OK && behind > 0) {
+    PCK(cudaMemsetAsync(&m->cnt->behind, 0, sizeof(unsigned long long), s));
+    PCK(cudaMemsetAsync(&m->cnt->reinserted, 0, sizeof(unsigned long long), s));
+    k_pvhe<<<blocks(2 * m->E), kThreads, 0, s>>>(V, m->vhe);
+    k_pbehind<<<blocks(m->n), kThreads, 0, s>>>(V, m->clist);
+    k_preinsert<<<1, 32, 0, s>>>(V, m->vhe, m->clist);
+    PCK(cudaGetLastError());
+    PCK(cudaMemsetAsync(&m->cnt->behind, 0, sizeof(unsigned long long), s));
+    k_presume<<<blocks(m->n), kThreads, 0, s>>>(V, m->dsub, true);  // counts who is still behind
+    PCK(cudaGetLastError());
+    PCK(cudaMemcpyAsync(m->cnt_host, m->cnt, sizeof(PCount), cudaMemcpyDeviceToHost, s));
+    PCK(cudaStreamSynchronize(s));
+    const PCount& r = *m->cnt_host;
+    if (r.error) {
+      rc = (int)r.error;
+      z.msg = "mcl_periodic_step: removal and reinsertion failed (site " + std::to_string(r.error_site) + ")";
+    }
+    reinserted = (int64_t)r.reinserted;
+    behind = (int64_t)r.behind;
+    z.c.flips = r.flips;
+    z.c.error_site = r.error_site;
+  }
   const PCount& c = z.c;
   if (stats) {
     std::memset(stats, 0, sizeof(*stats));
     stats->inverted_faces = (int64_t)((z.inverted_first + 2) / 3);  // each face is seen from its three edges
     stats->reverted_vertices = behind;
-    stats->substep_vertices = behind_first > behind ? behind_first - behind : 0;
+    stats->removed_vertices = reinserted;
+    stats->substep_vertices = substep_arrivals;
     stats->lawson_flips = (int64_t)c.flips;
     stats->lawson_rounds = z.rounds;
     stats->incircle_tests = z.incircle_tests;

@@ -167,6 +167,7 @@ struct PCount {
   unsigned long long wrapped, inverted, nondelaunay, flips, incircle_fp64, incircle_exact, orient_fp64, orient_exact,
       sos, overflow, error, error_site, truncated, reverted, behind;
   unsigned long long lcount[2];  // entries of the two edge work-lists
+  unsigned long long reinserted;  // vertices removed and reinserted at their targets
 };
 
 struct PView {
@@ -328,6 +329,13 @@ MCL_HD void p_body_resume(const PView& V, PF2* d, int v, bool last) {
   d[v] = r;
 }
 
+// vertex v after the sub-steps: onto the list of vertices still away from
+// their targets (cnt->behind of them)
+MCL_HD void p_body_behind(const PView& V, int* list, int v) {
+  const PF2 p = V.pos[v], t = V.target[v];
+  if (p.x != t.x || p.y != t.y) list[p_inc(&V.cnt->behind)] = v;
+}
+
 // vertex v, after a classification that found faces turned over: a marked
 // vertex (the farthest-moved of a turned face) goes back to its old position,
 // and its wrap is undone in the next fold; every other vertex folds nothing.
@@ -482,6 +490,372 @@ MCL_HD void p_body_flip(const PView& V, int e, unsigned stamp, int next) {
   p_queue(V, n0 >> 1, stamp + 1, next);
 }
 
+constexpr int kPeriodicMaxDeg = 4096;
+
+MCL_HD int p_origin(const PView& V, int h) {
+  const PI4 q = V.ev[h >> 1];
+  return (h & 1) ? q.y : q.x;
+}
+// next outgoing half-edge clockwise around the origin: next(twin(h))
+MCL_HD int p_rot(const PView& V, int h) {
+  const PI4 w = V.en[(h ^ 1) >> 1];
+  return ((h ^ 1) & 1) ? w.z : w.x;
+}
+
+// ---------------------------------------------------------------------------
+// Removal and reinsertion of a vertex, one at a time (a single thread runs
+// these for the few vertices that neither the step nor its sub-steps brought
+// to their targets).  Faces are rewritten whole: p_make_face sets the three
+// half-edges of a face from its vertices and their offsets in its first
+// vertex's frame; vhe holds one outgoing half-edge per vertex and is kept up
+// to date.
+
+MCL_HD int p_next(const PView& V, int h) {
+  const PI4 w = V.en[h >> 1];
+  return (h & 1) ? w.z : w.x;
+}
+MCL_HD int p_prev(const PView& V, int h) {
+  const PI4 w = V.en[h >> 1];
+  return (h & 1) ? w.w : w.y;
+}
+MCL_HD int p_apex(const PView& V, int h) {
+  const PI4 q = V.ev[h >> 1];
+  return (h & 1) ? q.w : q.z;
+}
+MCL_HD Off p_tof(const PView& V, int h) { return eo_target(V.eo[h >> 1], h & 1); }
+MCL_HD Off p_xof(const PView& V, int h) { return eo_apex(V.eo[h >> 1], h & 1); }
+
+// one half-edge's whole record: origin, apex, next, prev, target offset t and
+// apex offset x (both relative to the origin)
+MCL_HD void p_set_half(const PView& V, int h, int origin, int apex, int next, int prev, Off t, Off x) {
+  const int e = h >> 1;
+  PI4 q = V.ev[e], w = V.en[e];
+  unsigned o = V.eo[e];
+  if (h & 1) {
+    q.y = origin;
+    q.w = apex;
+    w.z = next;
+    w.w = prev;
+    o = (o & 0xFF00FF00u) | off_byte(off_neg(t)) | (off_byte(x) << 16);
+  } else {
+    q.x = origin;
+    q.z = apex;
+    w.x = next;
+    w.y = prev;
+    o = (o & 0xFFFF0000u) | off_byte(t) | (off_byte(x) << 8);
+  }
+  V.ev[e] = q;
+  V.en[e] = w;
+  V.eo[e] = o;
+}
+
+// face v0 -> v1 -> v2 of half-edges h0 (v0 -> v1), h1, h2, with v1 at O1 and
+// v2 at O2 in v0's frame
+MCL_HD void p_make_face(const PView& V, int h0, int h1, int h2, int v0, int v1, int v2, Off O1, Off O2) {
+  p_set_half(V, h0, v0, v2, h1, h2, O1, O2);
+  p_set_half(V, h1, v1, v0, h2, h0, off_sub(O2, O1), off_neg(O1));
+  p_set_half(V, h2, v2, v1, h0, h1, off_neg(O2), off_sub(O1, O2));
+}
+
+MCL_HD int p_orient_at(const PView& V, PF2 a, PF2 b, PF2 c) {
+  PLocal lc;
+  const int s = orient2d(a.x, a.y, b.x, b.y, c.x, c.y, &lc, &lc.overflow);
+  p_flush(V, lc);
+  return s;
+}
+
+// flip of edge e done by one thread (the same rewrite as p_body_flip), with
+// vhe kept; false when the flip would not leave both new faces positive
+// (only checked when `check`)
+MCL_HD bool p_flip_seq(const PView& V, int* vhe, int e, bool check) {
+  const PI4 q = V.ev[e];
+  const PI4 w = V.en[e];
+  if (!p_vertices_ok(V, q) || !p_halfedges_ok(V, w)) {
+    p_error(V, MCL_ERR_DEGENERATE_INPUT, 11);
+    return false;
+  }
+  const unsigned o = V.eo[e];
+  const Off B = eo_b(o), C = eo_c(o), D = off_add(B, eo_x1(o));
+  if (!off_small(B) || !off_small(C) || !off_small(D)) {
+    p_error(V, MCL_ERR_DEGENERATE_INPUT, 12);
+    return false;
+  }
+  const int a = q.x, b = q.y, c = q.z, d = q.w;
+  if (check) {
+    const PF2 pa = V.pos[a], pb = off_translate(V.pos[b], B, V.L), pc = off_translate(V.pos[c], C, V.L),
+              pd = off_translate(V.pos[d], D, V.L);
+    if (p_orient_at(V, pd, pc, pa) <= 0 || p_orient_at(V, pc, pd, pb) <= 0) return false;
+  }
+  const int n0 = w.x, p0 = w.y, n1 = w.z, p1 = w.w, h0 = 2 * e, h1 = 2 * e + 1;
+  p_make_face(V, h0, p0, n1, d, c, a, off_sub(C, D), off_neg(D));
+  p_make_face(V, h1, p1, n0, c, d, b, off_sub(D, C), off_sub(B, C));
+  if (vhe[a] == h0) vhe[a] = n1;
+  if (vhe[b] == h1) vhe[b] = n0;
+  p_add(&V.cnt->flips, 1);
+  return true;
+}
+
+constexpr int kSeqStar = 64;  // largest star the one-thread removal takes apart
+
+// Removes vertex v from the mesh (vhe[v] must be one of its outgoing
+// half-edges): spoke flips down to degree 3, then its three faces merge into
+// one.  The three freed edges go to freed[0..2], a half-edge of the merged
+// face to *near, and every edge of the hole's new triangulation (and of its
+// boundary) to hole[0..*nhole) for the flips that follow.  False (the mesh
+// still valid) when the star is not one this can take apart.
+MCL_HD bool p_remove_seq(const PView& V, int* vhe, int v, int* freed, int* near, int* hole, int* nhole) {
+  const unsigned H = 2u * (unsigned)V.E;
+  *nhole = 0;
+  {
+    // the hole's boundary: the link edges of v's star
+    const int h0 = vhe[v];
+    if ((unsigned)h0 >= H || p_origin(V, h0) != v) {
+      p_error(V, MCL_ERR_DEGENERATE_INPUT, 13);
+      return false;
+    }
+    int h = h0, deg = 0;
+    do {
+      if (deg == kSeqStar) return false;
+      const int l = p_next(V, h);
+      if ((unsigned)l >= H) {
+        p_error(V, MCL_ERR_DEGENERATE_INPUT, 21);
+        return false;
+      }
+      hole[(*nhole)++] = l >> 1;
+      h = p_rot(V, h);
+      ++deg;
+    } while (h != h0 && (unsigned)h < H);
+    if (h != h0) {
+      p_error(V, MCL_ERR_DEGENERATE_INPUT, 14);
+      return false;
+    }
+  }
+  for (int guard = 0; guard < kSeqStar; ++guard) {
+    const int h0 = vhe[v];
+    if ((unsigned)h0 >= H || p_origin(V, h0) != v) {
+      p_error(V, MCL_ERR_DEGENERATE_INPUT, 13);
+      return false;
+    }
+    int deg = 0, h = h0;
+    do {
+      h = p_rot(V, h);
+      ++deg;
+    } while (h != h0 && deg < kPeriodicMaxDeg && (unsigned)h < H);
+    if (h != h0) {
+      p_error(V, MCL_ERR_DEGENERATE_INPUT, 14);
+      return false;
+    }
+    if (deg == 3) break;
+    if (deg < 3) return false;
+    // a spoke whose flip keeps both new faces positive (one exists while the
+    // star is a valid star of degree > 3)
+    bool flipped = false;
+    h = h0;
+    for (int k = 0; k < deg && !flipped; ++k) {
+      const int nh = p_rot(V, h);
+      if (vhe[v] == h) vhe[v] = nh;  // h stops being v's after the flip
+      if (p_flip_seq(V, vhe, h >> 1, true)) {
+        flipped = true;
+        hole[(*nhole)++] = h >> 1;  // now a diagonal of the hole
+      } else {
+        vhe[v] = h0;
+        h = nh;
+      }
+    }
+    if (!flipped) return false;
+  }
+  // degree 3: spokes s0, s1, s2; the link half-edges next(s_i) run between
+  // the link vertices and become the merged face
+  const int s0 = vhe[v], s1 = p_rot(V, s0), s2 = p_rot(V, s1);
+  const int l[3] = {p_next(V, s0), p_next(V, s1), p_next(V, s2)};
+  int lo[3], lt[3];
+  Off lt_off[3];
+  for (int k = 0; k < 3; ++k) {
+    if ((unsigned)l[k] >= H) return false;
+    lo[k] = p_origin(V, l[k]);
+    lt[k] = p_origin(V, l[k] ^ 1);
+    lt_off[k] = p_tof(V, l[k]);
+  }
+  if (lo[0] == lo[1] || lo[1] == lo[2] || lo[0] == lo[2]) return false;
+  // order the link half-edges into a cycle: after l[i] comes the one leaving its target
+  int ord[3] = {0, -1, -1};
+  for (int k = 1; k < 3; ++k)
+    for (int j = 0; j < 3; ++j)
+      if (lo[j] == lt[ord[k - 1]]) ord[k] = j;
+  if (ord[1] < 0 || ord[2] < 0 || lt[ord[2]] != lo[ord[0]]) return false;
+  const int A = lo[ord[0]], Bv = lo[ord[1]], Cv = lo[ord[2]];
+  const Off OB = lt_off[ord[0]], OC = off_add(OB, lt_off[ord[1]]);
+  if (!off_small(OB) || !off_small(OC)) return false;
+  freed[0] = s0 >> 1;
+  freed[1] = s1 >> 1;
+  freed[2] = s2 >> 1;
+  p_make_face(V, l[ord[0]], l[ord[1]], l[ord[2]], A, Bv, Cv, OB, OC);
+  vhe[A] = l[ord[0]];
+  vhe[Bv] = l[ord[1]];
+  vhe[Cv] = l[ord[2]];
+  vhe[v] = -1;
+  *near = l[ord[0]];
+  return true;
+}
+
+// the copy of t nearest to p, and its offset in periods (exact: see p_toward)
+MCL_HD PF2 p_nearest_copy(PF2 t, PF2 p, float L, Off& k) {
+  PF2 q;
+  q.x = fadd(p.x, p_toward(t.x, p.x, L));
+  q.y = fadd(p.y, p_toward(t.y, p.y, L));
+  k.x = q.x > t.x ? (fsub(q.x, t.x) > 0.5f * L ? 1 : 0) : (fsub(t.x, q.x) > 0.5f * L ? -1 : 0);
+  k.y = q.y > t.y ? (fsub(q.y, t.y) > 0.5f * L ? 1 : 0) : (fsub(t.y, q.y) > 0.5f * L ? -1 : 0);
+  return q;
+}
+
+// Inserts vertex v (not in the mesh) at canonical position t, using the
+// three free edges, starting the point location walk at half-edge `near`.
+// 1 -> 3 split inside a face, 2 -> 4 split on an edge; false when t is an
+// existing vertex or the walk does not end.  Returns the half-edges of the
+// new star's link in link[0..3] (count in *nlink) for the flips that follow.
+MCL_HD bool p_insert_seq(const PView& V, int* vhe, int v, PF2 t, const int* f, int near, int* link, int* nlink) {
+  const unsigned H = 2u * (unsigned)V.E;
+  int h = near;
+  for (int guard = 0; guard < (1 << 20); ++guard) {
+    if ((unsigned)h >= H) {
+      p_error(V, MCL_ERR_DEGENERATE_INPUT, 15);
+      return false;
+    }
+    // stochastic walk: the first edge tested turns with the step, so the walk
+    // ends in any triangulation, Delaunay or not
+    const int a = p_origin(V, h), b = p_origin(V, h ^ 1), c = p_apex(V, h);
+    if ((unsigned)a >= (unsigned)V.n || (unsigned)b >= (unsigned)V.n || (unsigned)c >= (unsigned)V.n) {
+      p_error(V, MCL_ERR_DEGENERATE_INPUT, 16);
+      return false;
+    }
+    const Off Ob = p_tof(V, h), Oc = p_xof(V, h);
+    const PF2 pa = V.pos[a], pb = off_translate(V.pos[b], Ob, V.L), pc = off_translate(V.pos[c], Oc, V.L);
+    Off K;
+    const PF2 pt = p_nearest_copy(t, pa, V.L, K);
+    const int o1 = p_orient_at(V, pa, pb, pt), o2 = p_orient_at(V, pb, pc, pt), o3 = p_orient_at(V, pc, pa, pt);
+    const int cross[3] = {o1 < 0 ? h : -1, o2 < 0 ? p_next(V, h) : -1, o3 < 0 ? p_prev(V, h) : -1};
+    int go = -1;
+    for (int k = 0; k < 3 && go < 0; ++k) go = cross[(guard + k) % 3];
+    if (go >= 0) {
+      h = go ^ 1;
+      continue;
+    }
+    const int zeros = (o1 == 0) + (o2 == 0) + (o3 == 0);
+    if (zeros >= 2) return false;  // t is a vertex
+    const Off Ov = K;              // v's copy in a's frame
+    if (zeros == 0) {
+      const int n = p_next(V, h), p = p_prev(V, h);
+      p_make_face(V, h, 2 * f[1], 2 * f[0] + 1, a, b, v, Ob, Ov);
+      p_make_face(V, n, 2 * f[2], 2 * f[1] + 1, b, c, v, off_sub(Oc, Ob), off_sub(Ov, Ob));
+      p_make_face(V, p, 2 * f[0], 2 * f[2] + 1, c, a, v, off_neg(Oc), off_sub(Ov, Oc));
+      vhe[v] = 2 * f[0] + 1;
+      link[0] = h;
+      link[1] = n;
+      link[2] = p;
+      *nlink = 3;
+      return true;
+    }
+    // on one edge: make it g (a -> b) with v on the segment a b
+    int g = h;
+    if (o2 == 0) g = p_next(V, h);
+    if (o3 == 0) g = p_prev(V, h);
+    const int ga = p_origin(V, g), gb = p_origin(V, g ^ 1), gc = p_apex(V, g), gd = p_apex(V, g ^ 1);
+    if ((unsigned)gd >= (unsigned)V.n) return false;
+    // offsets in ga's frame
+    const Off Gb = p_tof(V, g), Gc = p_xof(V, g), Gd = off_add(Gb, p_xof(V, g ^ 1));
+    Off Ka;
+    p_nearest_copy(t, off_translate(V.pos[ga], Off{0, 0}, V.L), V.L, Ka);
+    const int ng = p_next(V, g), pg = p_prev(V, g), g1 = g ^ 1, ng1 = p_next(V, g1), pg1 = p_prev(V, g1);
+    p_make_face(V, g, 2 * f[1] + 1, pg, ga, v, gc, Ka, Gc);
+    p_make_face(V, 2 * f[0], ng, 2 * f[1], v, gb, gc, off_sub(Gb, Ka), off_sub(Gc, Ka));
+    p_make_face(V, 2 * f[0] + 1, 2 * f[2] + 1, pg1, gb, v, gd, off_sub(Ka, Gb), off_sub(Gd, Gb));
+    p_make_face(V, g1, ng1, 2 * f[2], v, ga, gd, off_neg(Ka), off_sub(Gd, Ka));
+    vhe[v] = 2 * f[0];
+    if (vhe[gb] == g1) vhe[gb] = 2 * f[0] + 1;
+    link[0] = ng;
+    link[1] = pg;
+    link[2] = ng1;
+    link[3] = pg1;
+    *nlink = 4;
+    return true;
+  }
+  p_error(V, MCL_ERR_NO_CONVERGENCE, 17);
+  return false;
+}
+
+constexpr int kSeqStack = 512;
+
+// Lawson flips around a freshly inserted vertex, one thread: a stack of edges
+// starting from the link of its star
+MCL_HD bool p_lawson_seq(const PView& V, int* vhe, const int* link, int nlink) {
+  int stack[kSeqStack];
+  int top = 0;
+  for (int k = 0; k < nlink; ++k) stack[top++] = link[k] >> 1;
+  for (int guard = 0; top > 0 && guard < (1 << 20); ++guard) {
+    const int e = stack[--top];
+    const PI4 q = V.ev[e];
+    PF2 qb, qc, qd;
+    if (!p_vertices_ok(V, q) || !quad_frame(V.eo[e], V.pos[q.y], V.pos[q.z], V.pos[q.w], V.L, qb, qc, qd)) {
+      p_error(V, MCL_ERR_DEGENERATE_INPUT, 18);
+      return false;
+    }
+    const PF2 pa = V.pos[q.x];
+    PLocal lc;
+    const bool nd = orient2d(pa.x, pa.y, qb.x, qb.y, qc.x, qc.y, &lc, &lc.overflow) > 0 &&
+                    orient2d(qb.x, qb.y, pa.x, pa.y, qd.x, qd.y, &lc, &lc.overflow) > 0 &&
+                    incircle_sos(pa.x, pa.y, qb.x, qb.y, qc.x, qc.y, qd.x, qd.y, q.x, q.y, q.z, q.w, &lc,
+                                 &lc.overflow) > 0;
+    p_flush(V, lc);
+    if (!nd) continue;
+    const PI4 w = V.en[e];
+    if (!p_flip_seq(V, vhe, e, false)) return false;
+    if (top + 4 > kSeqStack) {
+      p_error(V, MCL_ERR_CAPACITY, 19);
+      return false;
+    }
+    stack[top++] = w.x >> 1;
+    stack[top++] = w.y >> 1;
+    stack[top++] = w.z >> 1;
+    stack[top++] = w.w >> 1;
+  }
+  return top == 0;
+}
+
+// One thread: every listed vertex that is not at its target is removed and
+// reinserted there (or, if its target is taken by another vertex, where it
+// was), then the flips around it restore Delaunay.
+MCL_HD void p_body_reinsert(const PView& V, int* vhe, const int* list, int count) {
+  for (int i = 0; i < count && !V.cnt->error; ++i) {
+    const int v = list[i];
+    if ((unsigned)v >= (unsigned)V.n) continue;
+    const PF2 here = V.pos[v], t = V.target[v];
+    if (here.x == t.x && here.y == t.y) continue;
+    int freed[3], near = -1, link[4], nlink = 0, hole[2 * kSeqStar], nhole = 0;
+    if (!p_remove_seq(V, vhe, v, freed, &near, hole, &nhole)) continue;
+    // the hole was filled by arbitrary flips: make it Delaunay again (its
+    // edges that died with v are skipped: they are free now)
+    int live[2 * kSeqStar], nlive = 0;
+    for (int k = 0; k < nhole; ++k)
+      if (hole[k] != freed[0] && hole[k] != freed[1] && hole[k] != freed[2]) live[nlive++] = 2 * hole[k];
+    if (!p_lawson_seq(V, vhe, live, nlive)) return;
+    // the merged face may have been flipped away: start the walk from a
+    // half-edge still leaving a link vertex
+    near = vhe[p_origin(V, near)];
+    bool ok = p_insert_seq(V, vhe, v, t, freed, near, link, &nlink);
+    if (ok) {
+      V.pos[v] = t;
+      p_add(&V.cnt->reinserted, 1);
+    } else {
+      ok = p_insert_seq(V, vhe, v, here, freed, near, link, &nlink);
+      if (!ok) {
+        p_error(V, MCL_ERR_DEGENERATE_INPUT, 20);  // v could not go back either
+        return;
+      }
+    }
+    if (!p_lawson_seq(V, vhe, link, nlink)) return;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Queries on a periodic mesh.
 
@@ -497,19 +871,8 @@ MCL_HD void p_body_vhe(const PView& V, int* vhe, int h) {
   vhe[o] = h;
 }
 
-MCL_HD int p_origin(const PView& V, int h) {
-  const PI4 q = V.ev[h >> 1];
-  return (h & 1) ? q.y : q.x;
-}
-// next outgoing half-edge clockwise around the origin: next(twin(h))
-MCL_HD int p_rot(const PView& V, int h) {
-  const PI4 w = V.en[(h ^ 1) >> 1];
-  return ((h ^ 1) & 1) ? w.z : w.x;
-}
 // neighbour key for the ring's start: smallest id, then smallest offset byte
 MCL_HD long long p_ring_key(int id, unsigned off) { return ((long long)id << 8) | off; }
-
-constexpr int kPeriodicMaxDeg = 4096;
 
 // vertex v: its neighbours clockwise, starting at the smallest (id, offset),
 // at most max_ring - 1 of them; slot 0 holds the count (the reference's ring

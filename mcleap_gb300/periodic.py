@@ -76,8 +76,10 @@ class PeriodicTriangulation:
 
     def step(self, d, stream=None):
         """Move by d (device float2[n]), wrap, flip back to Delaunay.  Moves
-        that would turn faces over are refused for the vertices involved
-        (counted in ``reverted_vertices``)."""
+        that would turn faces over are refused, then resumed by sub-steps
+        (``substep_vertices``) and, for the rest, removal and reinsertion
+        (``removed_vertices``); ``reverted_vertices`` counts points that end
+        the step away from their targets."""
         st = L.StepStats()
         wrapped = C.c_int64()
         rc = L.lib().mcl_periodic_step(self.handle, L.ptr(d), _stream_ptr(stream), C.byref(st), C.byref(wrapped))

@@ -13,7 +13,7 @@
 //   OUT: int32 status, int32 flips, int32 wrapped, int32 inverted, int32 rounds,
 //        int32 nonpositive_after, int32 truncated, int32 reverted, int32 revert_passes,
 //        int32 behind (not at the target at the end), int32 substep_arrivals,
-//        int32 classified (edge classifications over all rounds),
+//        int32 classified (edge classifications over all rounds), int32 reinserted,
 //        float pos[n][2], int32 ev[E][4],
 //        int32 en[E][4], uint32 eo[E], then the queries on the final mesh:
 //        int32 ring[kRing][n] and uint8 offs[kRing][n] (column layout), int32 closest[n],
@@ -138,6 +138,17 @@ int main(int argc, char** argv) {
     for (int e = 0; e < E; ++e) mcl::p_body_wrap(V, e);
     settle();
   }
+  // the rest: removed and reinserted one by one
+  long long substep_arrivals = behind_first > behind ? behind_first - behind : 0;
+  if (!cnt.error && behind > 0) {
+    std::vector<int> vh(n, -1), list;
+    for (int h = 0; h < 2 * E; ++h) mcl::p_body_vhe(V, vh.data(), h);
+    for (int v = 0; v < n; ++v)
+      if (pos[v].x != target[v].x || pos[v].y != target[v].y) list.push_back(v);
+    mcl::p_body_reinsert(V, vh.data(), list.data(), (int)list.size());
+    behind = 0;
+    for (int v = 0; v < n; ++v) behind += pos[v].x != target[v].x || pos[v].y != target[v].y;
+  }
   int after = 0;
   if (!cnt.error)
     for (int h = 0; h < 2 * E; ++h) after += face_sign(V, h) <= 0;
@@ -161,12 +172,12 @@ int main(int argc, char** argv) {
 
   FILE* out = fopen(argv[2], "wb");
   if (!out) return 4;
-  const int32_t head[12] = {(int32_t)cnt.error,     (int32_t)cnt.flips,    (int32_t)cnt.wrapped,
+  const int32_t head[13] = {(int32_t)cnt.error,     (int32_t)cnt.flips,    (int32_t)cnt.wrapped,
                             (int32_t)inverted,      rounds,                after,
                             (int32_t)trunc_rings,   (int32_t)cnt.reverted, revert_passes,
-                            (int32_t)behind,        (int32_t)(behind_first > behind ? behind_first - behind : 0),
-                            (int32_t)classified};
-  wr(out, head, 12);
+                            (int32_t)behind,        (int32_t)substep_arrivals,
+                            (int32_t)classified,    (int32_t)cnt.reinserted};
+  wr(out, head, 13);
   wr(out, pos.data(), n);
   wr(out, ev.data(), E);
   wr(out, en.data(), E);

@@ -102,8 +102,8 @@ def check_step(M, st, xy, d, pos, ev, en, eo):
 
 
 def test_a_face_turned_over_is_refused_then_resumed(M):
-    """A vertex jumping across its neighbour is sent back, then taken on by
-    sub-steps (or left behind and counted)."""
+    """A vertex jumping across its neighbour is sent back, then taken to its
+    target by sub-steps or by removal and reinsertion."""
     xy = torus_points(2000, 12)
     pt = M.PeriodicTriangulation(xy, L)
     _, ev, _, eo = pt.download()
@@ -112,19 +112,21 @@ def test_a_face_turned_over_is_refused_then_resumed(M):
     d = np.zeros_like(xy)
     d[a] = 2.0 * (xy[b] + B * np.float32(L) - xy[a])
     st = pt.step(cuda(d))
-    assert st["inverted_faces"] > 0 and st["reverted_vertices"] + st["substep_vertices"] == 1, st
+    assert st["inverted_faces"] > 0 and st["reverted_vertices"] == 0, st
+    assert st["substep_vertices"] + st["removed_vertices"] == 1
     check_step(M, st, xy, d, *pt.download())
 
 
-@pytest.mark.parametrize("sigma,shift,seed", [(0.1, (0.0, 0.0), 51), (0.2, (0.4, -0.3), 52)])
-def test_tangling_moves_are_resumed_by_sub_steps(M, sigma, shift, seed):
+@pytest.mark.parametrize("sigma,shift,seed", [(0.1, (0.0, 0.0), 51), (0.2, (0.4, -0.3), 52), (1.0, (0.3, 0.3), 55)])
+def test_tangling_moves_all_arrive(M, sigma, shift, seed):
     n = 4000
     xy = torus_points(n, seed)
     pt = M.PeriodicTriangulation(xy, L)
     h = L / np.sqrt(n)
     d = (np.random.default_rng(seed).normal(0, sigma * h, (n, 2)) + np.array(shift) * h).astype(np.float32)
     st = pt.step(cuda(d))
-    assert st["inverted_faces"] > 0 and st["substep_vertices"] > 0 and st["reverted_vertices"] < n // 3, st
+    assert st["inverted_faces"] > 0 and st["substep_vertices"] > 0 and st["removed_vertices"] > 0, st
+    assert st["reverted_vertices"] == 0
     check_step(M, st, xy, d, *pt.download())
 
 
