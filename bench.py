@@ -870,7 +870,8 @@ def run_periodic(args, rank, world, dist):
     stream.synchronize()
     cp, cf = clocks_start()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
-    tot = {"lawson_flips": 0, "lawson_rounds": 0, "wrapped": 0, "reverted_vertices": 0}
+    tot = {"lawson_flips": 0, "lawson_rounds": 0, "wrapped": 0, "inverted_faces": 0, "substep_vertices": 0,
+           "removed_vertices": 0, "reverted_vertices": 0}
     for k in range(K):
         ev[k][0].record(stream)
         st = pt.step(disp[Wm + k], stream=stream)
