@@ -372,3 +372,28 @@ def test_frnn_on_a_stepped_mesh(harness, tmp_path, rf):
         assert (np.diff(ids) > 0).all()
         got = {(int(a), int((b & 15) - 8), int(((b >> 4) & 15) - 8)) for a, b in zip(ids, ob)}
         assert got == want[i], i
+
+
+def test_many_steps_of_advection_with_drift(harness, tmp_path):
+    """Twenty steps of Taylor-Green advection plus a drift on the torus (the
+    periodic benchmark's motion): points cross the sides every step, and after
+    every step the mesh is the oracle's periodic triangulation of the moved points."""
+    n = 3000
+    pos = torus_points(n, 71)
+    ev, en, eo = P.periodic_mesh(pos, L)
+    h = L / np.sqrt(n)
+    wrapped = 0
+    for k in range(20):
+        q = (pos.astype(np.float64) - 2 * L) / L
+        u = np.sin(2 * np.pi * q[:, 0]) * np.cos(2 * np.pi * q[:, 1]) + 0.3
+        v = -np.cos(2 * np.pi * q[:, 0]) * np.sin(2 * np.pi * q[:, 1]) + 0.2
+        d = (np.stack([u, v], 1) * 0.5 * h).astype(np.float32)
+        st, pos2, ev, en, eo = run(harness, tmp_path, pos, d, ev, en, eo)
+        assert st["status"] == 0 and st["behind"] == 0 and st["nonpositive_after"] == 0, (k, st)
+        assert np.array_equal(pos2, torus_wrap(pos + d))
+        wrapped += st["wrapped"]
+        pos = pos2.copy()
+        ev, en, eo = ev.copy(), en.copy(), eo.copy()
+    assert wrapped > 20 * 10
+    assert torus_faces_consistent(ev, en, eo)
+    assert np.array_equal(P.mesh_edges(ev, eo), P.periodic_edges(pos, L))
