@@ -391,6 +391,7 @@ def test_many_steps_of_advection_with_drift(harness, tmp_path):
         st, pos2, ev, en, eo = run(harness, tmp_path, pos, d, ev, en, eo)
         assert st["status"] == 0 and st["behind"] == 0 and st["nonpositive_after"] == 0, (k, st)
         assert np.array_equal(pos2, torus_wrap(pos + d))
+        assert np.array_equal(P.mesh_edges(ev, eo), P.periodic_edges(pos2, L)), k
         wrapped += st["wrapped"]
         pos = pos2.copy()
         ev, en, eo = ev.copy(), en.copy(), eo.copy()
