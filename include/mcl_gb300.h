@@ -445,6 +445,9 @@ int mcl_periodic_positions(mcl_periodic* m, mcl_float2** pos_dev);
  * more than one sub-step). */
 int mcl_periodic_step(mcl_periodic* m, const mcl_float2* d_dev, void* stream, mcl_step_stats* stats,
                       int64_t* wrapped);
+/* The same step with the displacements in host memory (copied in on `stream`). */
+int mcl_periodic_step_host(mcl_periodic* m, const mcl_float2* d_host, void* stream, mcl_step_stats* stats,
+                           int64_t* wrapped);
 
 /* oneRing<M> / oneRing2<M> (include/Device_Triangulation.h:500-517) on a
  * periodic mesh: each vertex's neighbours clockwise, starting at the smallest

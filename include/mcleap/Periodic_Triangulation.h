@@ -35,11 +35,19 @@ struct PeriodicTriangulation {
   PeriodicTriangulation& operator=(const PeriodicTriangulation&) = delete;
 
   // movePoints + untangle + delonize on the torus (d: device array of n
-  // glm::vec2): moves that would turn faces over are refused vertex by vertex
-  // and resumed by sub-steps; false (message in mcl_last_error()) on failure
+  // glm::vec2): moves that would turn faces over are refused vertex by vertex,
+  // resumed by sub-steps, the rest removed and reinserted at their targets;
+  // false (message in mcl_last_error()) on failure
   bool step(const glm::vec2* d, void* stream = nullptr) {
     return mcl_periodic_step(mesh, reinterpret_cast<const mcl_float2*>(d), stream, &last_stats, &last_wrapped) ==
            MCL_OK;
+  }
+
+  // step with the displacements in host memory
+  bool step_host(const std::vector<glm::vec2>& d, void* stream = nullptr) {
+    if ((int64_t)d.size() != n) return false;
+    return mcl_periodic_step_host(mesh, reinterpret_cast<const mcl_float2*>(d.data()), stream, &last_stats,
+                                  &last_wrapped) == MCL_OK;
   }
 
   // oneRing<M> / oneRing2<M>: clockwise from the smallest (id, offset); offs

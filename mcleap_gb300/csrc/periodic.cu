@@ -54,6 +54,7 @@ struct mcl_periodic {
   PF2* pos_old;
   PF2* target;
   PF2* dsub;         // sub-step displacements
+  PF2* dstage;       // host displacements copied in
   int* clist;        // a round's non-Delaunay edges
   int* wl[2];        // edge work-lists between rounds
   unsigned* qstamp;
@@ -172,6 +173,7 @@ void free_periodic(mcl_periodic* m) {
   cudaFree(m->pos_old);
   cudaFree(m->target);
   cudaFree(m->dsub);
+  cudaFree(m->dstage);
   cudaFree(m->clist);
   cudaFree(m->wl[0]);
   cudaFree(m->wl[1]);
@@ -369,6 +371,7 @@ int alloc_upload(const mcl_float2* pos, int64_t n, float L, const int32_t* ev, c
   A((void**)&m->pos_old, 8 * (size_t)n);
   A((void**)&m->target, 8 * (size_t)n);
   A((void**)&m->dsub, 8 * (size_t)n);
+  A((void**)&m->dstage, 8 * (size_t)n);
   A((void**)&m->clist, 4 * (size_t)E);
   A((void**)&m->wl[0], 4 * (size_t)E);
   A((void**)&m->wl[1], 4 * (size_t)E);
@@ -676,6 +679,13 @@ int mcl_periodic_step(mcl_periodic* m, const mcl_float2* d_dev, void* stream, mc
     z.msg = "mcl_periodic_step: exact predicate capacity exceeded";
   }
   return rc == MCL_OK ? MCL_OK : mcl::fail(rc, z.msg);
+}
+
+int mcl_periodic_step_host(mcl_periodic* m, const mcl_float2* d_host, void* stream, mcl_step_stats* stats,
+                           int64_t* wrapped) {
+  if (!m || !d_host) return mcl::fail(MCL_ERR_INVALID_ARGUMENT, "null argument");
+  PCK(cudaMemcpyAsync(m->dstage, d_host, 8 * (size_t)m->n, cudaMemcpyHostToDevice, (cudaStream_t)stream));
+  return mcl_periodic_step(m, reinterpret_cast<const mcl_float2*>(m->dstage), stream, stats, wrapped);
 }
 
 int mcl_periodic_one_ring(mcl_periodic* m, int max_ring, int layout, int32_t* ring_dev, uint8_t* offs_dev,

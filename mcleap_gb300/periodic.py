@@ -88,6 +88,18 @@ class PeriodicTriangulation:
         L.check(rc)
         return self.last_stats
 
+    def step_host(self, d_host, stream=None):
+        """step() with the displacements in host memory (float32 (n, 2))."""
+        d = np.ascontiguousarray(d_host, np.float32)
+        st = L.StepStats()
+        wrapped = C.c_int64()
+        rc = L.lib().mcl_periodic_step_host(self.handle, L.ptr(d), _stream_ptr(stream), C.byref(st),
+                                            C.byref(wrapped))
+        self.last_stats = st.as_dict()
+        self.last_stats["wrapped"] = wrapped.value
+        L.check(rc)
+        return self.last_stats
+
     def download(self):
         pos = np.zeros((self.n, 2), np.float32)
         ev = np.zeros((self.E, 4), np.int32)

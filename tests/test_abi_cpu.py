@@ -196,6 +196,7 @@ int main() {
   int *ring = nullptr, *nb = nullptr, *cl = nullptr;
   uint8_t* offs = nullptr;
   pt.step(d);
+  pt.step_host(std::vector<glm::vec2>(pts.size()));
   pt.oneRing<32>(ring, offs);
   pt.oneRing2<32>(ring, offs);
   pt.closestNeighbors<32>(ring, offs, cl);

@@ -87,7 +87,7 @@ def test_mesh_from_arrays_steps_like_the_built_one(M):
     d = (np.random.default_rng(2).normal(0, 0.05 * h, (n, 2)) + drift).astype(np.float32)
     d = torus_settle(xy, d, ev, eo, drift)
     a.step(cuda(d))
-    b.step(cuda(d))
+    b.step_host(d)
     assert all(np.array_equal(x, y) for x, y in zip(a.download(), b.download()))
 
 
