@@ -65,3 +65,18 @@ def test_domain_and_exactness_guards():
                   [x0 + 0.001953125, x0 + L / 3]], np.float32)
     c = P.cover(p, L).reshape(9, 2, 2).astype(np.float64)
     assert np.array_equal(c - P.OFFSETS[:, None, :] * L, np.broadcast_to(p.astype(np.float64), (9, 2, 2)))
+
+
+def test_point_order_is_a_relabelling():
+    """The periodic triangulation does not depend on the order of the points:
+    a permutation relabels the edges and nothing else."""
+    n = 2500
+    xy = torus_points(n, 13)
+    perm = np.random.default_rng(4).permutation(n)
+    e = P.periodic_edges(xy, L)
+    e2 = P.periodic_edges(xy[perm], L)
+    inv = np.empty(n, np.int64)
+    inv[perm] = np.arange(n)
+    back = np.column_stack([perm[e2[:, 0]], perm[e2[:, 1]], e2[:, 2:]])
+    assert np.array_equal(P.canonical(back), e)
+    assert inv[perm[7]] == 7
