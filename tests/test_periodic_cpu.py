@@ -398,3 +398,66 @@ def test_many_steps_of_advection_with_drift(harness, tmp_path):
     assert wrapped > 20 * 10
     assert torus_faces_consistent(ev, en, eo)
     assert np.array_equal(P.mesh_edges(ev, eo), P.periodic_edges(pos, L))
+
+
+@pytest.fixture(scope="module")
+def reinsert_harness(tmp_path_factory):
+    exe = str(tmp_path_factory.mktemp("reinsert") / "periodic_reinsert")
+    subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-I", os.path.join(ROOT, "mcleap_gb300", "csrc"),
+                    os.path.join(ROOT, "tests", "cpp", "periodic_reinsert.cpp"), "-o", exe], check=True)
+    return exe
+
+
+def run_reinsert(exe, tmp_path, pos, ev, en, eo, verts, targets):
+    n, E, k = len(pos), len(ev), len(verts)
+    src, dst = str(tmp_path / "rin.bin"), str(tmp_path / "rout.bin")
+    with open(src, "wb") as f:
+        f.write(np.array([n, E], np.int32).tobytes() + np.float32(L).tobytes() + np.int32(k).tobytes())
+        for a in (pos.astype(np.float32), ev.astype(np.int32), en.astype(np.int32), eo.astype(np.uint32),
+                  np.asarray(verts, np.int32), np.asarray(targets, np.float32)):
+            f.write(np.ascontiguousarray(a).tobytes())
+    subprocess.run([exe, src, dst], check=True)
+    raw = open(dst, "rb").read()
+    status, reinserted = (int(x) for x in np.frombuffer(raw[:8], np.int32))
+    o = 8
+    pos2 = np.frombuffer(raw[o:o + 8 * n], np.float32).reshape(n, 2)
+    o += 8 * n
+    ev2 = np.frombuffer(raw[o:o + 16 * E], np.int32).reshape(E, 4)
+    o += 16 * E
+    en2 = np.frombuffer(raw[o:o + 16 * E], np.int32).reshape(E, 4)
+    o += 16 * E
+    eo2 = np.frombuffer(raw[o:o + 4 * E], np.uint32)
+    return status, reinserted, pos2, ev2, en2, eo2
+
+
+def test_reinsertion_inside_a_face_on_an_edge_and_onto_a_taken_spot(reinsert_harness, tmp_path):
+    """The one-thread removal and reinsertion: a target inside a face (1 -> 3
+    split), a target exactly on an edge (2 -> 4 split, three collinear points
+    afterwards) and a target that another point occupies (the vertex goes
+    back where it was); the mesh is the oracle's triangulation after each."""
+    n = 2000
+    xy = torus_points(n, 81)
+    h = L / np.sqrt(n)
+    X = Y = np.float32(2.5 * L)
+    dl = np.float32(np.round(0.25 * h))
+    xy[0] = (X, Y)
+    xy[1] = (X + 2 * dl, Y)
+    ev, en, eo = P.periodic_mesh(xy, L)
+    edges = P.periodic_edges(xy, L)
+    assert ((edges[:, 0] == 0) & (edges[:, 1] == 1)).any()
+    mid = np.float32([X + dl, Y])
+    far = np.argsort(((xy - mid) ** 2).sum(1))[::-1]
+    v_edge, v_taken, v_face = int(far[0]), int(far[1]), int(far[2])
+    t_face = np.float32([2.25 * L + 0.123, 2.75 * L - 0.456])
+    targets = [mid, xy[5], t_face]
+    st, re, pos, ev2, en2, eo2 = run_reinsert(reinsert_harness, tmp_path, xy, ev, en, eo,
+                                              [v_edge, v_taken, v_face], targets)
+    assert st == 0 and re == 2
+    assert (pos[v_edge] == mid).all() and (pos[v_taken] == xy[v_taken]).all() and (pos[v_face] == t_face).all()
+    assert torus_faces_consistent(ev2, en2, eo2)
+    got = P.mesh_edges(ev2, eo2)
+    assert np.array_equal(got, P.periodic_edges(pos, L))
+    # the split edge: 0 - v - 1 on one line
+    assert not ((got[:, 0] == 0) & (got[:, 1] == 1)).any()
+    assert ((got[:, 0] == min(0, v_edge)) & (got[:, 1] == max(0, v_edge))).any()
+    assert ((got[:, 0] == min(1, v_edge)) & (got[:, 1] == max(1, v_edge))).any()
