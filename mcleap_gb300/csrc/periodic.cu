@@ -95,16 +95,9 @@ __global__ void k_presume(PView V, PF2* d, bool last) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < V.n) mcl::p_body_resume(V, d, i, last);
 }
-__global__ void k_pbehind(PView V, int* list) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < V.n) mcl::p_body_behind(V, list, i);
-}
-// one thread: the sequential removal and reinsertion
-__global__ void k_preinsert(PView V, int* vhe, const int* list) {
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    const unsigned long long k = V.cnt->behind;
-    mcl::p_body_reinsert(V, vhe, list, (int)(k < (unsigned long long)kMaxReinsert ? k : kMaxReinsert));
-  }
+// one thread: the sequential removal and reinsertion, vertices by ascending id
+__global__ void k_preinsert(PView V, int* vhe) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) mcl::p_body_reinsert(V, vhe, nullptr, V.n, kMaxReinsert);
 }
 __global__ void k_prevert(PView V) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -636,9 +629,9 @@ int mcl_periodic_step(mcl_periodic* m, const mcl_float2* d_dev, void* stream, mc
   if (rc == MCL_OK && behind > 0) {
     PCK(cudaMemsetAsync(&m->cnt->behind, 0, sizeof(unsigned long long), s));
     PCK(cudaMemsetAsync(&m->cnt->reinserted, 0, sizeof(unsigned long long), s));
+    PCK(cudaMemsetAsync(m->vhe, 0xFF, 4 * (size_t)m->n, s));  // vhe = -1: the largest candidate wins
     k_pvhe<<<blocks(2 * m->E), kThreads, 0, s>>>(V, m->vhe);
-    k_pbehind<<<blocks(m->n), kThreads, 0, s>>>(V, m->clist);
-    k_preinsert<<<1, 32, 0, s>>>(V, m->vhe, m->clist);
+    k_preinsert<<<1, 32, 0, s>>>(V, m->vhe);
     PCK(cudaGetLastError());
     PCK(cudaMemsetAsync(&m->cnt->behind, 0, sizeof(unsigned long long), s));
     k_presume<<<blocks(m->n), kThreads, 0, s>>>(V, m->dsub, true);  // counts who is still behind
@@ -695,6 +688,7 @@ int mcl_periodic_one_ring(mcl_periodic* m, int max_ring, int layout, int32_t* ri
   cudaStream_t s = (cudaStream_t)stream;
   const PView V = view(m);
   PCK(cudaMemsetAsync(m->cnt, 0, sizeof(PCount), s));
+  PCK(cudaMemsetAsync(m->vhe, 0xFF, 4 * (size_t)m->n, s));  // vhe = -1: the largest candidate wins
   k_pvhe<<<blocks(2 * m->E), kThreads, 0, s>>>(V, m->vhe);
   k_pring<<<blocks(m->n), kThreads, 0, s>>>(V, m->vhe, layout == MCL_LAYOUT_COLUMN, max_ring, ring_dev, offs_dev);
   PCK(cudaGetLastError());
@@ -715,6 +709,7 @@ int mcl_periodic_frnn(mcl_periodic* m, float r, int max_frnn, int layout, int32_
   cudaStream_t s = (cudaStream_t)stream;
   const PView V = view(m);
   PCK(cudaMemsetAsync(m->cnt, 0, sizeof(PCount), s));
+  PCK(cudaMemsetAsync(m->vhe, 0xFF, 4 * (size_t)m->n, s));  // vhe = -1: the largest candidate wins
   k_pvhe<<<blocks(2 * m->E), kThreads, 0, s>>>(V, m->vhe);
   k_pfrnn<<<blocks(m->n), kThreads, 0, s>>>(V, m->vhe, r * r, layout == MCL_LAYOUT_COLUMN, max_frnn, out_dev, offs_dev);
   PCK(cudaGetLastError());

@@ -329,13 +329,6 @@ MCL_HD void p_body_resume(const PView& V, PF2* d, int v, bool last) {
   d[v] = r;
 }
 
-// vertex v after the sub-steps: onto the list of vertices still away from
-// their targets (cnt->behind of them)
-MCL_HD void p_body_behind(const PView& V, int* list, int v) {
-  const PF2 p = V.pos[v], t = V.target[v];
-  if (p.x != t.x || p.y != t.y) list[p_inc(&V.cnt->behind)] = v;
-}
-
 // vertex v, after a classification that found faces turned over: a marked
 // vertex (the farthest-moved of a turned face) goes back to its old position,
 // and its wrap is undone in the next fold; every other vertex folds nothing.
@@ -821,15 +814,18 @@ MCL_HD bool p_lawson_seq(const PView& V, int* vhe, const int* link, int nlink) {
   return top == 0;
 }
 
-// One thread: every listed vertex that is not at its target is removed and
-// reinserted there (or, if its target is taken by another vertex, where it
-// was), then the flips around it restore Delaunay.
-MCL_HD void p_body_reinsert(const PView& V, int* vhe, const int* list, int count) {
-  for (int i = 0; i < count && !V.cnt->error; ++i) {
-    const int v = list[i];
+// One thread: every listed vertex (list == null: every vertex, by ascending
+// id) that is not at its target is removed and reinserted there (or, if its
+// target is taken by another vertex, where it was), then the flips around it
+// restore Delaunay; at most `limit` of them.
+MCL_HD void p_body_reinsert(const PView& V, int* vhe, const int* list, int count, int limit) {
+  int done = 0;
+  for (int i = 0; i < count && done < limit && !V.cnt->error; ++i) {
+    const int v = list ? list[i] : i;
     if ((unsigned)v >= (unsigned)V.n) continue;
     const PF2 here = V.pos[v], t = V.target[v];
     if (here.x == t.x && here.y == t.y) continue;
+    ++done;
     int freed[3], near = -1, link[4], nlink = 0, hole[2 * kSeqStar], nhole = 0;
     if (!p_remove_seq(V, vhe, v, freed, &near, hole, &nhole)) continue;
     // the hole was filled by arbitrary flips: make it Delaunay again (its
@@ -859,8 +855,8 @@ MCL_HD void p_body_reinsert(const PView& V, int* vhe, const int* list, int count
 // ---------------------------------------------------------------------------
 // Queries on a periodic mesh.
 
-// half-edge h: make it its origin's outgoing half-edge (any one will do; the
-// ring below starts at its smallest neighbour whatever the walk's start)
+// half-edge h: a candidate for its origin's outgoing half-edge; the largest
+// id wins (vhe starts at -1), so every run picks the same one
 MCL_HD void p_body_vhe(const PView& V, int* vhe, int h) {
   const PI4 q = V.ev[h >> 1];
   const int o = (h & 1) ? q.y : q.x;
@@ -868,7 +864,11 @@ MCL_HD void p_body_vhe(const PView& V, int* vhe, int h) {
     p_error(V, MCL_ERR_DEGENERATE_INPUT, 6);
     return;
   }
-  vhe[o] = h;
+#if defined(__CUDA_ARCH__)
+  atomicMax(vhe + o, h);
+#else
+  if (h > vhe[o]) vhe[o] = h;
+#endif
 }
 
 // neighbour key for the ring's start: smallest id, then smallest offset byte

@@ -45,7 +45,7 @@ int main(int argc, char** argv) {
                eo.data(),   wv.data(),   wt.data(),   mark.data(),    pos_old.data(), target.data(), cand.data(),
                claim.data(), &cnt,       clist.data(), wl0.data(),    wl1.data(),    qstamp.data()};
   for (int h = 0; h < 2 * E; ++h) mcl::p_body_vhe(V, vhe.data(), h);
-  mcl::p_body_reinsert(V, vhe.data(), vert.data(), k);
+  mcl::p_body_reinsert(V, vhe.data(), vert.data(), k, 1 << 16);
   FILE* out = fopen(argv[2], "wb");
   if (!out) return 4;
   const int32_t head[2] = {(int32_t)cnt.error, (int32_t)cnt.reinserted};

@@ -141,11 +141,9 @@ int main(int argc, char** argv) {
   // the rest: removed and reinserted one by one
   long long substep_arrivals = behind_first > behind ? behind_first - behind : 0;
   if (!cnt.error && behind > 0) {
-    std::vector<int> vh(n, -1), list;
+    std::vector<int> vh(n, -1);
     for (int h = 0; h < 2 * E; ++h) mcl::p_body_vhe(V, vh.data(), h);
-    for (int v = 0; v < n; ++v)
-      if (pos[v].x != target[v].x || pos[v].y != target[v].y) list.push_back(v);
-    mcl::p_body_reinsert(V, vh.data(), list.data(), (int)list.size());
+    mcl::p_body_reinsert(V, vh.data(), nullptr, n, 1 << 16);
     behind = 0;
     for (int v = 0; v < n; ++v) behind += pos[v].x != target[v].x || pos[v].y != target[v].y;
   }
