@@ -38,15 +38,17 @@ def parse():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=10)
-    ap.add_argument("--e2e-steps", type=int, default=200)
+    ap.add_argument("--e2e-steps", type=int, default=120, help="timed e2e steps (segments of 40)")
+    ap.add_argument("--repair-steps", type=int, default=10, help="timed steps of the 1M random-walk repair run")
     ap.add_argument("--n", type=int, default=1_000_000)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
-    ap.add_argument("--cpu-sample", type=int, default=20000)
+    ap.add_argument("--cpu-sample", type=int, default=0, help="points per CPU mesh (0: the workload's own size)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-queries", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--no-repair", action="store_true")
     ap.add_argument("--workload", default="taylor-green",
                     choices=["taylor-green", "batched", "serving", "precision", "periodic"])
     ap.add_argument("--rate", type=float, default=2000.0)
@@ -126,61 +128,105 @@ def peaks():
 
 
 # ---------------------------------------------------------------------------
-def cpu_reference(n, frac_n, seconds, seed, workers):
+def cpu_reference(n, seconds, seed, workers, max_steps=0):
     """The reference CPU kinetic path (oracle port: movePoint, untangle until
-    false, delonize restart-scan, FP64 predicates) on `workers` processes, each an
-    independent Taylor-Green mesh of `n` points with the displacement scale of
-    the `frac_n`-point workload; returns aggregate pts*steps/s."""
+    false, delonize restart-scan, FP64 predicates) on `workers` processes, each
+    stepping an independent n-point Taylor-Green mesh (seeds seed, seed+1, ...)
+    for about `seconds` (at least one step; at most `max_steps` when > 0).
+    Returns the aggregate pts*steps/s over the slowest worker's wall time and
+    the per-worker details."""
     import multiprocessing as mp
 
     ctx = mp.get_context("spawn")
     with ctx.Pool(workers) as pool:
-        res = pool.starmap(_cpu_worker, [(n, frac_n, seconds, seed + i) for i in range(workers)])
-    pts_steps = sum(r[0] for r in res)
-    wall = max(r[1] for r in res)
-    flips = sum(r[2] for r in res)
-    steps = sum(r[3] for r in res)
-    capped = sum(r[4] for r in res)
-    return pts_steps / wall, wall, flips, steps, capped
+        res = pool.starmap(_cpu_worker, [(n, seconds, seed + i, max_steps) for i in range(workers)])
+    wall = max(r["wall_s"] for r in res)
+    steps = sum(r["steps"] for r in res)
+    return {"value": n * steps / wall, "wall_s": wall, "steps": steps,
+            "flips": sum(r["flips"] for r in res), "capped": sum(r["capped"] for r in res),
+            "s_per_step": float(np.median([s for r in res for s in r["step_s"]])),
+            "build_s": float(np.median([r["build_s"] for r in res])),
+            "final_mesh": {k: int(sum(r["final"][k] for r in res)) for k in res[0]["final"]}}
 
 
-def _cpu_worker(n, frac_n, seconds, seed):
+def _cpu_worker(n, seconds, seed, max_steps):
     sys.path.insert(0, ROOT)
     from mcleap_gb300 import workloads as W
     from oracle import oracle as O
 
+    t0 = time.perf_counter()
     pts = O.morton_sort(W.uniform_points(n, seed))
     m = O.Mesh.build(pts, exact=False)  # the reference's own build (FP64)
+    build_s = time.perf_counter() - t0
     pos = m.positions()
-    # the same displacement per step relative to the local spacing as the GPU workload
-    frac = 0.5
     t0 = time.perf_counter()
     steps = flips = capped = 0
-    while time.perf_counter() - t0 < seconds or steps == 0:
-        d = W.taylor_green_displacements(pos, n, 1, frac=frac)[0]
+    step_s = []
+    while (time.perf_counter() - t0 < seconds or steps == 0) and (max_steps <= 0 or steps < max_steps):
+        # the GPU workload's displacement: Taylor-Green, dt = 0.5 x mean spacing
+        d = W.taylor_green_displacements(pos, n, 1, frac=0.5)[0]
         r = m.kinetic_step_ref(d)
+        step_s.append(float(r["seconds"]))
         flips += r["untangle_flips"] + r["delonize_flips"]
         capped += r["capped"]
         pos = m.positions()
         steps += 1
     wall = time.perf_counter() - t0
-    return n * steps, wall, flips, steps, capped
+    # what the reference's path left (exact predicates, untimed): its untangle
+    # covers only two cases and its restart scan stops where no tangled quad tests
+    # positive, so the mesh can stay inverted and non-Delaunay
+    chk = m.check(exact=True)
+    return {"steps": steps, "wall_s": wall, "flips": flips, "capped": capped,
+            "step_s": step_s, "build_s": build_s, "final": chk}
 
 
-def _cpu_rebuild_seconds(n, seed):
-    """One exact Delaunay rebuild (the oracle's insertion with exact
-    predicates) of an n-point Taylor-Green mesh after one step, in seconds."""
-    sys.path.insert(0, ROOT)
-    from mcleap_gb300 import workloads as W
+def oracle_parity(dt, ht, n_points):
+    """Checker, run outside every timed region: the GPU mesh after the timed
+    steps against the oracle's exact Delaunay triangulation of the same
+    positions (sorted edge sets, bit for bit), and the engine's predicate
+    ladder on every live quad and face against the oracle's exact signs.
+    Returns the parity record and the oracle rebuild time in seconds."""
+    import torch
+
+    from mcleap_gb300 import _lib as L
     from oracle import oracle as O
 
-    pts = O.morton_sort(W.uniform_points(n, seed))
-    m = O.Mesh.build(pts, exact=False)
-    d = W.taylor_green_displacements(m.positions(), n, 1, frac=0.5)[0]
-    pos = (m.positions() + d).astype(np.float32)
+    dt.transferToHost()
+    pos, he = ht.m_pos, ht.m_he
     t0 = time.perf_counter()
-    O.Mesh.build(pos[4:], exact=True)
-    return time.perf_counter() - t0
+    exact = O.Mesh.build(pos[4:], exact=True)
+    rebuild_s = time.perf_counter() - t0
+    got, want = ht.edges(), exact.edges()
+    edges_equal = bool(np.array_equal(got, want))
+    diff = 0
+    if not edges_equal:
+        diff = len(set(map(tuple, got.tolist())) ^ set(map(tuple, want.tolist())))
+    org, apex = he[:, 1], he[:, 3]
+    inner = np.nonzero((apex[0::2] >= 0) & (apex[1::2] >= 0))[0]
+    a, b, c, d = org[2 * inner], org[2 * inner + 1], apex[2 * inner], apex[2 * inner + 1]
+    pts8 = np.stack([pos[a], pos[b], pos[c], pos[d]], 1).reshape(-1, 8).astype(np.float32)
+    ids = np.stack([a, b, c, d], 1).astype(np.int32)
+    h = np.nonzero(apex >= 0)[0]
+    pts6 = np.stack([pos[org[h]], pos[org[h ^ 1]], pos[apex[h]]], 1).reshape(-1, 6).astype(np.float32)
+
+    def dev(kind, pts, idx=None):
+        dp = torch.from_numpy(np.ascontiguousarray(pts)).cuda()
+        di = torch.from_numpy(np.ascontiguousarray(idx)).cuda() if idx is not None else None
+        sg = torch.zeros(len(pts), dtype=torch.int32, device="cuda")
+        stg = torch.zeros(len(pts), dtype=torch.int32, device="cuda")
+        L.check(L.lib().mcl_debug_predicates_device(kind, dp.data_ptr(), di.data_ptr() if di is not None else None,
+                                                    len(pts), sg.data_ptr(), stg.data_ptr(), None))
+        return sg.cpu().numpy()
+
+    dis_in = int((dev(1, pts8) != O.incircle(pts8, mode=1)).sum())
+    dis_sos = int((dev(2, pts8, ids) != O.incircle(pts8, mode=2, ids=ids)).sum())
+    dis_or = int((dev(0, pts6) != O.orient2d(pts6, mode=1)).sum())
+    return {"edges_equal": edges_equal, "edges": int(len(got)), "edge_differences": diff,
+            "sign_disagreements": dis_in + dis_sos + dis_or,
+            "quads_sampled": int(len(pts8)), "faces_sampled": int(len(pts6)),
+            "what": f"final {n_points}-point mesh after the timed steps vs the oracle's exact Delaunay rebuild of "
+                    "the same positions; incircle (exact and with symbolic perturbation) on every interior edge's "
+                    "quad and orient2d on every face by the engine's predicate ladder vs the exact oracle"}, rebuild_s
 
 
 def run_reference(args, rank, world):
@@ -190,21 +236,26 @@ def run_reference(args, rank, world):
 
     O.build()
     workers = max(1, os.cpu_count() or 1)
-    sample = min(args.cpu_sample, args.n)
+    sample = args.cpu_sample or args.n
     secs = max(3.0, args.cpu_seconds)
     t_all = time.perf_counter()
-    value, wall, flips, steps, capped = cpu_reference(sample, args.n, secs, 1234, workers)
+    r = cpu_reference(sample, secs, 2026, workers)
+    value = r["value"]
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * r["s_per_step"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"taylor-green {args.n} pts", "parallelism": "cpu processes"},
+        "config": {"workload": f"taylor-green {args.n} pts, dt = 0.5 x mean spacing, periodic wrap",
+                   "points": sample, "same_config": sample == args.n, "parallelism": "cpu processes"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": workers, "kind": "port",
-                         "sample": f"{workers} independent Taylor-Green meshes of {sample} points, "
-                                   f"{secs:.0f} s each; reference kinetic step = movePoint + untangle "
-                                   f"until false + delonize (restart scan), FP64 predicates; {steps} steps, "
-                                   f"{capped} stopped at the Lawson cap of 64 flips per edge (tangled)"},
+                         "sample": f"{workers} independent Taylor-Green meshes of {sample} points (one per core), "
+                                   f"about {secs:.0f} s of steps each ({r['steps']} steps in all, median "
+                                   f"{r['s_per_step']:.2f} s per step, {r['capped']} stopped at the Lawson cap); "
+                                   "reference kinetic step = movePoint + untangle until false + delonize "
+                                   "(restart scan), FP64 predicates; mesh build untimed"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "flips_per_s": r["flips"] / r["wall_s"],
+        "final_mesh_exact_check": r["final_mesh"],
         "wall_s": time.perf_counter() - t_all,
     }
     print(json.dumps(line), flush=True)
@@ -235,8 +286,10 @@ def run_ours(args, rank, world, dist):
     E = dt.m_he_size // 2
     # displacements for warm-up + timed + e2e steps (Taylor-Green, generated on
     # the device; the e2e ones are staged in pinned host memory)
-    KE = 0 if args.no_e2e else min(args.e2e_steps, K)
-    KEW = min(25, KE)  # untimed warm-up steps of the host-displacement pipeline
+    # e2e: segments of 40 steps, at least 3, whatever --steps is
+    SEG = 40
+    KE = 0 if args.no_e2e else SEG * max(3, -(-args.e2e_steps // SEG))
+    KEW = min(20, KE)  # untimed warm-up steps of the host-displacement pipeline
     dev_disp = W.taylor_green_displacements_device(ht.m_pos, n, Wm + K + KEW + KE, device=f"cuda:{local}")
     host_e2e = [d.cpu().pin_memory() for d in dev_disp[Wm + K:]]
     dev_disp = dev_disp[:Wm + K]
@@ -365,7 +418,6 @@ def run_ours(args, rank, world, dist):
         # timed in segments of SEG steps (the pipeline drained after each); the
         # median segment is reported, so that one host-side stall of a few
         # milliseconds does not stand for the whole run
-        SEG = min(50, KE)
         seg_s = []
         # the first KEW steps warm the pipeline up (host threads, clocks) untimed
         for s0 in [0] + list(range(KEW, KEW + KE - SEG + 1, SEG)):
@@ -408,19 +460,28 @@ def run_ours(args, rank, world, dist):
                                                "submitted", "iterations")},
                   "capacity": info["capacity"]}
 
-    cpu = None
+    cpu = parity = None
     if rank == 0 and not args.no_cpu_baseline:
+        # the CPU leg: the oracle checks the timed mesh (edges and signs, outside
+        # every timed region) and the reference's CPU kinetic path is timed on
+        # one core on a mesh of the same workload
         from oracle import oracle as O
 
         O.build()
-        sample = min(args.cpu_sample, n)
-        v, w_s, fl, steps, capped = cpu_reference(sample, n, args.cpu_seconds, 99, 1)
-        rebuild_s = _cpu_rebuild_seconds(sample, 99)
-        cpu = {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
-               "oracle_rebuild_pts_per_s": sample / rebuild_s,
-               "sample": f"1 core, Taylor-Green mesh of {sample} points for {w_s:.1f} s ({steps} steps, {capped} "
-                         f"stopped at the Lawson cap); reference kinetic step = movePoint + untangle until false "
-                         f"+ delonize (restart scan)"}
+        parity, rebuild_s = oracle_parity(dt, ht, n)
+        sample = args.cpu_sample or n
+        r = cpu_reference(sample, args.cpu_seconds, 2026, 1)
+        cpu = {"value": r["value"], "unit": UNIT, "cores": 1, "kind": "port", "points": sample,
+               "same_config": sample == n, "s_per_step": r["s_per_step"],
+               "oracle_rebuild_pts_per_s": n / rebuild_s, "final_mesh_exact_check": r["final_mesh"],
+               "sample": f"1 core, Taylor-Green mesh of {sample} points (the workload's own size), {r['steps']} "
+                         f"steps in {r['wall_s']:.1f} s ({r['capped']} stopped at the Lawson cap); reference kinetic "
+                         "step = movePoint + untangle until false + delonize (restart scan), FP64 predicates; "
+                         f"mesh build ({r['build_s']:.1f} s) untimed"}
+
+    repair = None
+    if not args.no_repair:
+        repair = repair_measure(1_000_000, args.repair_steps, 3, 2026 + rank, local)
 
     if rank == 0:
         line = {
@@ -442,15 +503,93 @@ def run_ours(args, rank, world, dist):
                          "kernel": "k_step", "alg_bytes_per_launch": alg_bytes},
             "queries": qinfo,
             "served_vs_plain": served,
-            # every timed step ended with status OK: no expansion overflow, no
-            # undecided sign (sampled signs vs the exact oracle: the GPU tests)
-            "predicate_errors": 0 if st["status"] == 0 else st["status"],
+            # sign disagreements of the engine's predicate ladder with the exact
+            # oracle on every live quad and face of the final mesh (null
+            # without the CPU leg); the edge set against the exact rebuild
+            "predicate_errors": parity["sign_disagreements"] if parity else None,
+            "parity": parity, "repair": repair,
             "e2e": e2e, "cpu_baseline": cpu, "clocks": clocks,
             # k_step per step, plus k_one_ring + 7 grid-build kernels + k_grid_frnn per step
             "gpu_launches": K * (10 if do_q else 1),
             "wall_s": wall, "build_s": t_build,
         }
         print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+def repair_measure(n, K, Wm, seed, local):
+    """The repair path at the headline size: an n-point mesh under a Gaussian
+    random walk (sigma = 0.1 x mean spacing, clamped to the box, coincident
+    moves settled), which inverts faces every step, so every step runs the
+    untangle repair (send back, remove, Lawson, reinsert).  K timed steps of
+    k_step (CUDA events on its stream, L2 flushed before each), with the
+    phase split from the kernel's own %globaltimer marks."""
+    import ctypes as C
+
+    import torch
+
+    from mcleap_gb300 import _lib as L
+    from mcleap_gb300 import batch as MB
+    from mcleap_gb300 import workloads as W
+
+    dev = f"cuda:{local}"
+    mesh = MB.MeshBatch(MB.build_mesh(W.uniform_points(n, seed)))
+    V, E = mesh.V, mesh.E
+    sigma = torch.tensor([0.1 * W.mean_spacing(n)], dtype=torch.float32, device=dev)
+    counter = torch.zeros(1, dtype=torch.int64, device=dev)
+    d = torch.zeros((V, 2), dtype=torch.float32, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.Stream()
+    lib = L.lib()
+    keys = ("inverted_faces", "reverted_vertices", "removed_vertices", "lawson_flips", "removal_flips",
+            "insert_rounds", "lawson_rounds", "incircle_tests")
+    tot = {k: 0 for k in keys}
+    ms, phases = [], []
+    tl = np.zeros(48, np.int64)
+    for k in range(Wm + K):
+        mesh.walk(sigma, counter, d, seed=77, stream=stream)
+        mesh.settle(d, stream=stream)
+        with torch.cuda.stream(stream):
+            flush.fill_(k & 0xFF)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        st = L.StepStats()
+        a.record(stream)
+        L.check(lib.mcl_step(mesh.handle, d.data_ptr(), stream.cuda_stream, None))
+        b.record(stream)
+        stream.synchronize()
+        L.check(lib.mcl_mesh_last_status(mesh.handle, stream.cuda_stream, C.byref(st)))
+        sd = st.as_dict()
+        if sd["status"] != 0:
+            raise RuntimeError(f"repair step {k} failed: {sd}")
+        if k < Wm:
+            continue
+        ms.append(a.elapsed_time(b))
+        for key in keys:
+            tot[key] += sd[key]
+        L.check(lib.mcl_debug_timeline(mesh.handle, L.ptr(tl)))
+        t0 = tl[0]
+        # start -> classified -> reverted -> removed -> Lawson -> reinserted -> end
+        marks = [tl[1], tl[43], tl[44], tl[45], tl[46], tl[47]]
+        phases.append(np.diff(np.array([t0] + marks, np.float64)) / 1e3)
+    ms = np.array(ms)
+    ph = np.median(np.array(phases), 0)
+    flips = tot["lawson_flips"] + tot["removal_flips"]
+    wl_items = max(0, tot["incircle_tests"] - K * (E - 4))
+    alg = 24 * V + 16 * E + 8 * V + 20 * wl_items / K + 96 * flips / K
+    peak, peak_kind = peaks()
+    mesh.close()
+    return {"workload": f"{n} points uniform, Gaussian random walk sigma = 0.1 x mean spacing (clamped, coincident "
+                        "moves settled); every step inverts faces and runs the repair",
+            "steps": K, "ms_per_step": float(ms.mean()), "p50_ms": float(np.median(ms)),
+            "p99_ms": float(np.percentile(ms, 99)), "pts_steps_per_s": n * K / (ms.sum() / 1e3),
+            "flips_per_s": flips / (ms.sum() / 1e3),
+            "per_step": {k: tot[k] / K for k in keys},
+            "phase_us_median": {"classify": ph[0], "send_back": ph[1], "remove": ph[2], "lawson_after_removal": ph[3],
+                                "reinsert": ph[4], "tail": ph[5]},
+            "roofline": {"bound": "hbm", "achieved": alg / (ms.mean() / 1e3) / 1e9, "peak": peak,
+                         "frac": alg / (ms.mean() / 1e3) / 1e9 / peak, "peak_kind": peak_kind,
+                         "alg_bytes_per_launch": alg, "kernel": "k_step (repair)"},
+            "l2": "flushed (256 MB write) before every timed step"}
 
 
 # ---------------------------------------------------------------------------

@@ -1270,7 +1270,7 @@ extern "C" int mcl_batch_frnn_grid(mcl_mesh* m, const float* r_host, const float
 // tables and per-point work arrays) in one fixed array that lives in the
 // library's device image, so the call itself allocates nothing.  Limits:
 // at most kNoAllocMaxPoints points and kNoAllocMaxCells cell-table entries
-// (the Morton-padded cell count; see mcl_grid_create).  Every GPU that loads the
+// (cells_x * cells_y, row-major cells as mcl_grid_create).  Every GPU that loads the
 // library holds these 5.3 MB until the process exits.
 constexpr int64_t kNoAllocMaxPoints = 262144;
 constexpr int64_t kNoAllocMaxCells = 262144;
@@ -1304,11 +1304,8 @@ extern "C" int mcl_grid_frnn_noalloc(const mcl_float2* pos, int64_t n, float min
   if (!pos || !sorted_pos || !perm || !counts || !ids || n < 0 || cells_x < 1 || cells_y < 1 || max_nb < 1 ||
       !(cell_x > 0.f) || !(cell_y > 0.f) || !(r >= 0.f))
     return qfail(MCL_ERR_INVALID_ARGUMENT, "bad args");
-  int side = 1;
-  while (side < std::max(cells_x, cells_y)) side <<= 1;
-  const int64_t mcells = (int64_t)side * side;
   const int morton = 0;  // row-major cells, as mcl_grid_create
-  const int64_t ncells = morton ? mcells : (int64_t)cells_x * cells_y;
+  const int64_t ncells = (int64_t)cells_x * cells_y;
   if (n > kNoAllocMaxPoints)
     return qfail(MCL_ERR_CAPACITY, "mcl_grid_frnn_noalloc: more than 262144 points");
   if (ncells > kNoAllocMaxCells)
