@@ -50,7 +50,7 @@ def parse():
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-repair", action="store_true")
     ap.add_argument("--workload", default="taylor-green",
-                    choices=["taylor-green", "batched", "serving", "precision", "periodic"])
+                    choices=["taylor-green", "batched", "serving", "precision", "periodic", "repair"])
     ap.add_argument("--rate", type=float, default=2000.0)
     ap.add_argument("--duration", type=float, default=10.0)
     ap.add_argument("--drain-limit", type=float, default=60.0)
@@ -410,10 +410,15 @@ def run_ours(args, rank, world, dist):
         if dist:
             dist.barrier()
 
+        e2e_tot = {"lawson_flips": 0, "inverted_faces": 0, "removed_vertices": 0, "steps": 0}
+
         def check(j):
             done_ev[j].synchronize()
             if views[j].status != 0:
                 raise RuntimeError(f"e2e step failed: {views[j].as_dict()}")
+            for key in ("lawson_flips", "inverted_faces", "removed_vertices"):
+                e2e_tot[key] += getattr(views[j], key)
+            e2e_tot["steps"] += 1
 
         # timed in segments of SEG steps (the pipeline drained after each); the
         # median segment is reported, so that one host-side stall of a few
@@ -441,6 +446,7 @@ def run_ours(args, rank, world, dist):
         e2e = {"value": world * n * SEG / e_s, "unit": UNIT, "h2d_bytes_per_step": 8 * V,
                "d2h_bytes_per_step": nstat, "ms_per_step": 1e3 * e_s / SEG, "steps": SEG * len(seg_s),
                "segments_ms_per_step": [1e3 * x / SEG for x in seg_s],
+               "per_step": {k: v / max(1, e2e_tot["steps"]) for k, v in e2e_tot.items() if k != "steps"},
                "path": "mcl_step_host_async (pinned host displacements, copy overlapped with the previous step); "
                        f"{KEW} untimed warm-up steps, then the median of {len(seg_s)} segments of {SEG} steps; "
                        "steps back to back as an application runs them (no L2 flush in between, unlike the "
@@ -544,8 +550,12 @@ def repair_measure(n, K, Wm, seed, local):
     keys = ("inverted_faces", "reverted_vertices", "removed_vertices", "lawson_flips", "removal_flips",
             "insert_rounds", "lawson_rounds", "incircle_tests")
     tot = {k: 0 for k in keys}
-    ms, phases = [], []
+    ms, phases, rounds = [], [], []
     tl = np.zeros(48, np.int64)
+    cn = np.zeros(32, np.int64)
+    trm = np.zeros(64, np.int64)
+    tin = np.zeros(64, np.int64)
+    last_rounds = None
     for k in range(Wm + K):
         mesh.walk(sigma, counter, d, seed=77, stream=stream)
         mesh.settle(d, stream=stream)
@@ -568,9 +578,36 @@ def repair_measure(n, K, Wm, seed, local):
             tot[key] += sd[key]
         L.check(lib.mcl_debug_timeline(mesh.handle, L.ptr(tl)))
         t0 = tl[0]
-        # start -> classified -> reverted -> removed -> Lawson -> reinserted -> end
+        # start -> classified -> reverted -> removed -> reinserted -> Lawson -> end
         marks = [tl[1], tl[43], tl[44], tl[45], tl[46], tl[47]]
         phases.append(np.diff(np.array([t0] + marks, np.float64)) / 1e3)
+        if lib.mcl_debug_counters(mesh.handle, L.ptr(cn), len(cn)) < 16:  # returns how many counters exist
+            raise RuntimeError("mcl_debug_counters failed")
+        rounds.append((cn[14], cn[15], sd["insert_rounds"], sd["lawson_rounds"]))
+        # the last step's rounds: send-back passes, removal rounds (claim,
+        # verify, remove), insertion rounds (locate, win, split), in us
+        L.check(lib.mcl_debug_remove_timeline(mesh.handle, L.ptr(trm)))
+        L.check(lib.mcl_debug_insert_timeline(mesh.handle, L.ptr(tin)))
+        npass, nrem, nins = int(min(cn[14], 16)), int(min(cn[15], 16)), int(min(sd["insert_rounds"], 16))
+        prev = tl[1]
+        passes = []
+        for p_ in range(npass):
+            passes.append((trm[48 + p_] - prev) / 1e3)
+            prev = trm[48 + p_]
+        prev = tl[43]
+        rem = []
+        for r_ in range(nrem):
+            m3 = [trm[4 * r_], trm[4 * r_ + 1], trm[4 * r_ + 2]]
+            rem.append([round((m3[0] - prev) / 1e3, 1), round((m3[1] - m3[0]) / 1e3, 1), round((m3[2] - m3[1]) / 1e3, 1)])
+            prev = m3[2]
+        prev = tl[44]
+        ins = []
+        for r_ in range(nins):
+            m3 = [tin[4 * r_], tin[4 * r_ + 1], tin[4 * r_ + 2]]
+            ins.append([round((m3[0] - prev) / 1e3, 1), round((m3[1] - m3[0]) / 1e3, 1), round((m3[2] - m3[1]) / 1e3, 1)])
+            prev = tin[4 * r_ + 3]
+        last_rounds = {"send_back_pass_us": [round(x, 1) for x in passes], "removal_round_us": rem,
+                       "insertion_round_us": ins}
     ms = np.array(ms)
     ph = np.median(np.array(phases), 0)
     flips = tot["lawson_flips"] + tot["removal_flips"]
@@ -584,12 +621,37 @@ def repair_measure(n, K, Wm, seed, local):
             "p99_ms": float(np.percentile(ms, 99)), "pts_steps_per_s": n * K / (ms.sum() / 1e3),
             "flips_per_s": flips / (ms.sum() / 1e3),
             "per_step": {k: tot[k] / K for k in keys},
-            "phase_us_median": {"classify": ph[0], "send_back": ph[1], "remove": ph[2], "lawson_after_removal": ph[3],
-                                "reinsert": ph[4], "tail": ph[5]},
+            "phase_us_median": {"classify": ph[0], "send_back": ph[1], "remove": ph[2], "reinsert": ph[3],
+                                "lawson": ph[4], "tail": ph[5]},
+            "rounds_median": dict(zip(("fixpoint_passes", "removal", "insertion", "flip"),
+                                      np.median(np.array(rounds), 0).tolist())),
+            "last_step_rounds": last_rounds,
             "roofline": {"bound": "hbm", "achieved": alg / (ms.mean() / 1e3) / 1e9, "peak": peak,
                          "frac": alg / (ms.mean() / 1e3) / 1e9 / peak, "peak_kind": peak_kind,
                          "alg_bytes_per_launch": alg, "kernel": "k_step (repair)"},
             "l2": "flushed (256 MB write) before every timed step"}
+
+
+def run_repair(args, rank, world, dist):
+    """The repair-path run alone (1M random walk), as its own JSON line."""
+    import torch
+
+    from mcleap_gb300 import build as B
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    B.build()
+    cp, cf = clocks_start()
+    rep = repair_measure(args.n, args.steps, max(3, args.warmup), 2026 + rank, local)
+    clocks = clocks_stop(cp, cf, local)
+    line = {"metric": "repair-path kinetic pts*steps/s (Gaussian random walk, every step untangles)",
+            "value": world * rep["pts_steps_per_s"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": max(3, args.warmup), "ms_per_step": rep["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": rep["workload"], "points": args.n, "parallelism": f"replicas x{world}"},
+            "repair": rep, "clocks": clocks, "gpu_launches": args.steps * 4}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
 
 
 # ---------------------------------------------------------------------------
@@ -1062,6 +1124,8 @@ def main():
             run_precision(args, rank, world, dist)
         elif args.workload == "periodic":
             run_periodic(args, rank, world, dist)
+        elif args.workload == "repair":
+            run_repair(args, rank, world, dist)
         else:
             run_ours(args, rank, world, dist)
     finally:

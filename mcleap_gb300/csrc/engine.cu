@@ -88,6 +88,13 @@ __device__ __forceinline__ bool enqueue_once(const KParams& P, int e, unsigned s
   return atomicMax(P.qmark + e, stamp) < stamp;
 }
 
+// Mark edge e for a later work-list built by collect_marked (mk == 0: no-op).
+// Repair marks the edges its removals and splits touch instead of running
+// Lawson after each of its phases; one pass over the marks then queues them.
+__device__ __forceinline__ void mark_edge(const KParams& P, int e, unsigned mk) {
+  if (mk && e >= 0 && e < P.E) atomicMax(P.qmark + e, mk);
+}
+
 // Called by every thread of the block (it holds a block barrier).
 __device__ void flush_counters(const KParams& P, LocalCounters& lc) {
   // the common counter is reduced over the block (one atomic per block: one
@@ -301,6 +308,8 @@ __device__ void phase_classify(cg::grid_group& g, const KParams& P, unsigned qst
     int k = 0;
     int hard[U];
     int kh = 0;
+    int inv[U];
+    int ki = 0;
 #pragma unroll
     for (int j = 0; j < U; ++j) {
       const int4 r = q[j];
@@ -313,6 +322,7 @@ __device__ void phase_classify(cg::grid_group& g, const KParams& P, unsigned qst
         defer = true;
       } else if (sa <= 0 || sb <= 0) {
         bad += (sa <= 0) + (sb <= 0);
+        inv[ki++] = e[j];
       } else if (r.z >= 0 && r.w >= 0) {
         ++ninc;
         const int si = incircle_fp32(a.x, a.y, b.x, b.y, c.x, c.y, d.x, d.y);
@@ -331,6 +341,9 @@ __device__ void phase_classify(cg::grid_group& g, const KParams& P, unsigned qst
     }
     if (__any_sync(kFull, k > 0)) warp_push(mine, k, P.wl0, &P.st->wl_count[0], P.E, P.st);
     if (__any_sync(kFull, kh > 0)) warp_push(hard, kh, P.hard, &P.st->hard_count, P.E, P.st);
+    // edges with a non-positive face: the repair's first send-back pass
+    // starts from them (work-list 1 is free until the flip rounds)
+    if (__any_sync(kFull, ki > 0)) warp_push(inv, ki, P.wl1, &P.st->wl_count[1], P.E, P.st);
   }
   cp_async_wait<0>();  // nothing left in flight into the staging slots
   // the deferred edges, with the full predicate ladder (out of the loop, so
@@ -338,15 +351,21 @@ __device__ void phase_classify(cg::grid_group& g, const KParams& P, unsigned qst
   {
     int mine[2];
     int k = 0;
+    int inv[2];
+    int ki = 0;
     const int defs[2] = {def0, def1};
     for (int j = 0; j < 2; ++j) {
       const int e = defs[j];
-      if (e >= 0 && resolve_edge<kFixedPos>(P, e, lc, bad) && enqueue_once(P, e, qstamp)) {
+      if (e < 0) continue;
+      const int bad0 = bad;
+      if (resolve_edge<kFixedPos>(P, e, lc, bad) && enqueue_once(P, e, qstamp)) {
         claim_edge(P, e, sc);
         mine[k++] = e;
       }
+      if (bad != bad0) inv[ki++] = e;
     }
     if (__any_sync(kFull, k > 0)) warp_push(mine, k, P.wl0, &P.st->wl_count[0], P.E, P.st);
+    if (__any_sync(kFull, ki > 0)) warp_push(inv, ki, P.wl1, &P.st->wl_count[1], P.E, P.st);
   }
   lc.incircle += ninc;
   if (bad) atomicAdd(&P.st->inverted, bad);
@@ -367,17 +386,30 @@ __device__ void phase_classify_hard(cg::grid_group& g, const KParams& P, unsigne
     const int i = base + lane;
     int mine[1];
     int k = 0;
+    int inv[1];
+    int ki = 0;
     if (i < n) {
       const int e = ld_i(P.hard + i);
+      const int bad0 = bad;
       if (resolve_edge<kFixedPos>(P, e, lc, bad) && enqueue_once(P, e, qstamp)) {
         claim_edge(P, e, sc);
         mine[k++] = e;
       }
+      if (bad != bad0) inv[ki++] = e;
     }
     if (__any_sync(kFull, k > 0)) warp_push(mine, k, P.wl0, &P.st->wl_count[0], P.E, P.st);
+    if (__any_sync(kFull, ki > 0)) warp_push(inv, ki, P.wl1, &P.st->wl_count[1], P.E, P.st);
   }
   if (bad) atomicAdd(&P.st->inverted, bad);
   g.sync();
+}
+
+__device__ __forceinline__ void timeline_remove(const KParams& P, int slot) {
+  if (blockIdx.x == 0 && threadIdx.x == 0 && slot < 64) {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    P.st->ts_remove[slot] = t;
+  }
 }
 
 __device__ __forceinline__ void timeline_insert(const KParams& P, int round, int k) {
@@ -629,9 +661,11 @@ __device__ bool phase_fixpoint(cg::grid_group& g, const KParams& P, LocalCounter
     }
     int fresh = 0, bad = 0;
     if (pass == 0) {
-      // every face, once per edge side
-      for (int ei = gtid; ei < P.E_it; ei += stride) {
-        const int e = edge_at(P, ei);
+      // every face the classification found non-positive, once per edge
+      // side (its edges are on work-list 1)
+      const int nb = ld_i(&P.st->wl_count[1]);
+      for (int ii = spread_tid(); ii < nb; ii += stride) {
+        const int e = ld_i(P.wl1 + ii);
         const int4 q = ld_ev(P, e);
         if (q.x < 0) continue;
         if (bad_v(P, q.x) || bad_v(P, q.y) || q.z >= P.V || q.w >= P.V) {
@@ -669,6 +703,7 @@ __device__ bool phase_fixpoint(cg::grid_group& g, const KParams& P, LocalCounter
     if (fresh) atomicAdd(&P.st->fix_new[slot], fresh);
     if (bad) atomicAdd(&P.st->fix_bad[slot], bad);
     g.sync();
+    if (pass < 16) timeline_remove(P, 48 + pass);
     const int nfresh = ld_i(&P.st->fix_new[slot]);
     const int nbad = ld_i(&P.st->fix_bad[slot]);
     if (nfresh == 0) {
@@ -692,7 +727,7 @@ __device__ bool phase_fixpoint(cg::grid_group& g, const KParams& P, LocalCounter
 // The k spoke edges become k-3 diagonals plus the 3 free edges of v.
 constexpr int kEarMax = 128;
 
-__device__ int remove_vertex_ears(const KParams& P, int v, LocalCounters& lc) {
+__device__ int remove_vertex_ears(const KParams& P, int v, LocalCounters& lc, unsigned mk) {
   int sp[kEarMax], lk[kEarMax], w[kEarMax], nx[kEarMax], pv[kEarMax], bnd[kEarMax];
   float2 q[kEarMax];
   const int s0 = ld_i(P.vhe + v);
@@ -740,6 +775,7 @@ __device__ int remove_vertex_ears(const KParams& P, int v, LocalCounters& lc) {
     __stcg(P.en + g, make_int4(bnd[a], bnd[b], -1, -1));
     he_set_face(P, bnd[a], w[c], bnd[b], d0);
     he_set_face(P, bnd[b], w[a], d0, bnd[a]);
+    mark_edge(P, g, mk);
     bnd[a] = d1;
     nx[a] = c;
     pv[c] = a;
@@ -753,8 +789,10 @@ __device__ int remove_vertex_ears(const KParams& P, int v, LocalCounters& lc) {
     he_set_face(P, bnd[c], w[b], bnd[a], bnd[b]);
     __stcg(P.vhint + v, bnd[a]);
   }
-  for (int i = 0; i < k; ++i)
+  for (int i = 0; i < k; ++i) {
     if (ld_i(P.vhe + w[i]) == (sp[i] ^ 1)) __stcg(P.vhe + w[i], lk[i]);
+    mark_edge(P, lk[i] >> 1, mk);  // the hole's sides face new triangles
+  }
   for (int r = 0; r < 3; ++r) {
     const int e = sp[r] >> 1;
     __stcg(P.vfree + 3 * v + r, e);
@@ -786,13 +824,13 @@ __device__ int remove_vertex_ears(const KParams& P, int v, LocalCounters& lc) {
 // its star polygon, or, for stars above kEarMax spokes, flipping its spokes
 // until it has degree 3, then merging its three faces.  Runs in one thread;
 // the caller owns every face of the vertex's star.
-__device__ int remove_vertex(const KParams& P, int v, LocalCounters& lc, int& flips) {
+__device__ int remove_vertex(const KParams& P, int v, LocalCounters& lc, int& flips, unsigned mk) {
   {
     // Ear clipping first: one walk around the star, then local work on the
     // loaded polygon (the spoke flips below walk the star again after every
     // flip, a chain of dependent loads per flip).  Stars of more than
     // kEarMax spokes take the flips.
-    const int rc = remove_vertex_ears(P, v, lc);
+    const int rc = remove_vertex_ears(P, v, lc, mk);
     if ((rc & 0xff) != MCL_ERR_CAPACITY) {
       ++flips;  // counted as one repair operation
       return rc;
@@ -836,7 +874,7 @@ __device__ int remove_vertex(const KParams& P, int v, LocalCounters& lc, int& fl
     if (deg < 3) return MCL_ERR_DEGENERATE_INPUT | (__LINE__ << 8);
     if (flipped < 0) {
       // no spoke flip is valid (exactly collinear neighbours): clip ears
-      const int rc = remove_vertex_ears(P, v, lc);
+      const int rc = remove_vertex_ears(P, v, lc, mk);
       if (rc != MCL_OK && atomicCAS(&P.st->dbg[0], 0, v + 1) == 0) {
         P.st->dbg[1] = deg;
         int hh = s0;
@@ -849,6 +887,14 @@ __device__ int remove_vertex(const KParams& P, int v, LocalCounters& lc, int& fl
       return rc;
     }
     if (!flip_edge(P, flipped)) return MCL_ERR_DEGENERATE_INPUT | (__LINE__ << 8);
+    if (mk) {
+      const int4 wg = ld_en(P, flipped);  // the flipped edge's four wings
+      mark_edge(P, flipped, mk);
+      mark_edge(P, wg.x >> 1, mk);
+      mark_edge(P, wg.y >> 1, mk);
+      mark_edge(P, wg.z >> 1, mk);
+      mark_edge(P, wg.w >> 1, mk);
+    }
     ++flips;
   }
   // merge the three faces (v,x,y), (v,y,z), (v,z,x) into (x,y,z)
@@ -863,6 +909,9 @@ __device__ int remove_vertex(const KParams& P, int v, LocalCounters& lc, int& fl
   he_set_face(P, lxy, z, lyz, lzx);
   he_set_face(P, lyz, x, lzx, lxy);
   he_set_face(P, lzx, y, lxy, lyz);
+  mark_edge(P, lxy >> 1, mk);
+  mark_edge(P, lyz >> 1, mk);
+  mark_edge(P, lzx >> 1, mk);
   if (ld_i(P.vhe + x) == (s0 ^ 1)) __stcg(P.vhe + x, lxy);
   if (ld_i(P.vhe + y) == (s1 ^ 1)) __stcg(P.vhe + y, lyz);
   if (ld_i(P.vhe + z) == (s2 ^ 1)) __stcg(P.vhe + z, lzx);
@@ -881,7 +930,7 @@ __device__ int remove_vertex(const KParams& P, int v, LocalCounters& lc, int& fl
   return MCL_OK;
 }
 
-__device__ bool phase_remove(cg::grid_group& g, const KParams& P, unsigned& stamp, LocalCounters& lc) {
+__device__ bool phase_remove(cg::grid_group& g, const KParams& P, unsigned& stamp, LocalCounters& lc, unsigned mk) {
   const int stride = gridDim.x * blockDim.x;
   const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
   int src = 0;
@@ -907,6 +956,7 @@ __device__ bool phase_remove(cg::grid_group& g, const KParams& P, unsigned& stam
       for_spokes(P, v, [&](int h) { atomicMax(P.claim + face_min(P, h), key); });
     }
     g.sync();
+    if (round < 16) timeline_remove(P, 4 * round);
     for (int i = spread_tid(); i < n; i += stride) {
       const int v = ld_i(in + i);
       const unsigned long long key = ((unsigned long long)sk << 32) | (unsigned)(~mix32((unsigned)v ^ sk));
@@ -918,6 +968,7 @@ __device__ bool phase_remove(cg::grid_group& g, const KParams& P, unsigned& stam
       if (!ok) set_error(P, MCL_ERR_DEGENERATE_INPUT);
     }
     g.sync();
+    if (round < 16) timeline_remove(P, 4 * round + 1);
     int removed = 0, flips = 0;
     for (int base = spread_tid() - (int)(threadIdx.x & 31); base < n; base += stride) {
       const int i = base + (int)(threadIdx.x & 31);
@@ -926,7 +977,7 @@ __device__ bool phase_remove(cg::grid_group& g, const KParams& P, unsigned& stam
       if (i < n) {
         const int v = ld_i(in + i);
         if (__ldcg(P.vlocf + v) == 1) {
-          const int rc = remove_vertex(P, v, lc, flips);
+          const int rc = remove_vertex(P, v, lc, flips, mk);
           if (rc != MCL_OK) flag_error_at(P, rc & 0xff, 100000 + (rc >> 8));
           else ++removed;
         } else if (ld_i(&P.st->status) == MCL_OK) {
@@ -938,6 +989,7 @@ __device__ bool phase_remove(cg::grid_group& g, const KParams& P, unsigned& stam
     if (removed) atomicAdd(&P.st->c[C_REMOVED], (unsigned long long)removed);
     if (flips) atomicAdd(&P.st->c[C_REMOVAL_FLIPS], (unsigned long long)flips);
     g.sync();
+    if (round < 16) timeline_remove(P, 4 * round + 2);
     src = dst;
   }
 }
@@ -948,8 +1000,11 @@ __device__ bool phase_remove(cg::grid_group& g, const KParams& P, unsigned& stam
 // (or -1).  Errors are returned as negative MCL codes.  With max_steps > 0 the
 // walk stops after that many steps, returns -1 and leaves the face it reached
 // in *resume (a parallel round then waits for the longest walk only that long).
+// salt != 0: the edge tested first in each face is drawn from a hash of
+// (salt, step) (a stochastic walk, which terminates on any triangulation);
+// salt == 0: it rotates with the step (enough on a Delaunay triangulation).
 __device__ int locate(const KParams& P, float2 p, int h, int* on, LocalCounters& lc, int max_steps = 0,
-                      int* resume = nullptr) {
+                      int* resume = nullptr, unsigned salt = 0) {
   *on = -1;
   for (int it = 0; it < P.walk_cap; ++it) {
     if (max_steps > 0 && it == max_steps) {
@@ -967,7 +1022,7 @@ __device__ int locate(const KParams& P, float2 p, int h, int* on, LocalCounters&
     const float2 q[3] = {ldpos(P, o[0]), ldpos(P, o[1]), ldpos(P, o[2])};
     int s[3] = {1, 1, 1};
     int cross = -1;
-    const int start = it % 3;
+    const int start = salt ? (int)(mix32(salt + (unsigned)it * 0x9e3779b9u) % 3u) : it % 3;
     // Every edge with p on its far side is a valid step; an edge with a
     // bounding corner is taken only when no other is (stepping through a
     // corner's fan of long hull triangles can take hundreds of steps).
@@ -1102,8 +1157,13 @@ __device__ int insert_start(const KParams& P, int v, bool resume) {
 // the next round (which starts where it stopped).
 constexpr int kWalkSlice = 48;
 
+// With mk != 0 (repair) the rounds only split: the edges each split touches
+// are marked with mk for one Lawson pass after the last round (the walks of
+// later rounds run on a valid, not yet Delaunay, triangulation; their edge
+// order is randomised, so they cannot cycle).  With mk == 0 (the initial
+// build) every round ends with Lawson over the edges it touched.
 __device__ bool phase_insert(cg::grid_group& g, const KParams& P, unsigned& stamp,
-                             LocalCounters& lc) {
+                             LocalCounters& lc, unsigned mk = 0) {
   const int stride = gridDim.x * blockDim.x;
   const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
   int src = 0;
@@ -1133,7 +1193,8 @@ __device__ bool phase_insert(cg::grid_group& g, const KParams& P, unsigned& stam
       // other start is the closer of the hint (the face located last round,
       // which can reach far along the hull) and the anchor
       const bool paused = round > 0 && __ldcg(P.vlocf + v) == 4;
-      const int h = locate(P, ldpos(P, v), insert_start(P, v, paused), &on, lc, kWalkSlice, &resume);
+      const int h = locate(P, ldpos(P, v), insert_start(P, v, paused), &on, lc, kWalkSlice, &resume,
+                           mk ? mix32((unsigned)v ^ sk) | 1u : 0u);
       if (h == -1) {
         // not there yet: go on from here in the next round
         P.vloc[v] = resume;
@@ -1203,10 +1264,18 @@ __device__ bool phase_insert(cg::grid_group& g, const KParams& P, unsigned& stam
           ++inserted;
           for (int j = 0; j < nl; ++j)
             if (bad_h(P, link[j])) { link[j] = 0; flag_error(P, MCL_ERR_DEGENERATE_INPUT); }
-          for (int j = 0; j < nl; ++j)
-            if (enqueue_once(P, link[j] >> 1, sq)) mine[k++] = link[j] >> 1;
-          for (int j = 0; j < 3; ++j)
-            if (enqueue_once(P, f[j], sq)) mine[k++] = f[j];
+          if (mk) {
+            // on a triangulation that is not Delaunay the new spokes need not
+            // be legal either: the split edge (now v's spoke to a) and f0..f2
+            for (int j = 0; j < nl; ++j) mark_edge(P, link[j] >> 1, mk);
+            for (int j = 0; j < 3; ++j) mark_edge(P, f[j], mk);
+            if (fl & 2) mark_edge(P, __ldcg(P.vloc + v) >> 1, mk);
+          } else {
+            for (int j = 0; j < nl; ++j)
+              if (enqueue_once(P, link[j] >> 1, sq)) mine[k++] = link[j] >> 1;
+            for (int j = 0; j < 3; ++j)
+              if (enqueue_once(P, f[j], sq)) mine[k++] = f[j];
+          }
         } else if (fl >= 0) {
           __stcg(P.vhint + v, __ldcg(P.vloc + v));
           again[ka++] = v;
@@ -1218,8 +1287,10 @@ __device__ bool phase_insert(cg::grid_group& g, const KParams& P, unsigned& stam
     (void)inserted;
     g.sync();
     timeline_insert(P, round, 2);
-    phase_lawson<false>(g, P, 0, stamp, lc, 0);
-    g.sync();
+    if (!mk) {
+      phase_lawson<false>(g, P, 0, stamp, lc, 0);
+      g.sync();
+    }
     timeline_insert(P, round, 3);
     src = dst;
   }
@@ -1491,7 +1562,7 @@ __device__ void phase_substeps(cg::grid_group& g, const KParams& P, unsigned& st
 // Repair of a step whose classification found inverted faces: revert, remove,
 // Lawson, reinsert.  Out of line, so k_step's hot loops keep their registers;
 // keeps its own counters and returns the next free stamp.
-__device__ __noinline__ unsigned repair_step(cg::grid_group g, const KParams P, unsigned stamp) {
+__device__ __noinline__ unsigned repair_step(cg::grid_group g, const KParams P, unsigned stamp, unsigned q0) {
   LocalCounters lc = {0, 0, 0, 0, 0, 0, 0};
   const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
   KParams Q = P;
@@ -1499,6 +1570,13 @@ __device__ __noinline__ unsigned repair_step(cg::grid_group g, const KParams P, 
   const int inverted = ld_i(&P.st->inverted);
   if (gtid == 0) P.st->c[C_INVERTED] += (unsigned long long)inverted;
   const unsigned fs = stamp++;  // revert marks of this launch
+  // Edges to pass through Lawson at the end carry the mark mk: the
+  // classification's non-Delaunay edges (queued with q0), then every edge a
+  // removal or a split touches.  Any other edge is Delaunay: its quad keeps
+  // the positions it was classified with (every sent-back vertex is removed,
+  // and each edge whose quad held one is a spoke, gone, or a side of its
+  // hole, marked).
+  unsigned mk = q0;
   // (1) revert until valid
   bool ok = phase_fixpoint(g, Q, lc, fs);
   g.sync();
@@ -1529,59 +1607,65 @@ __device__ __noinline__ unsigned repair_step(cg::grid_group g, const KParams P, 
     if (gtid == 0) P.st->c[C_REVERTED] += (unsigned long long)nrev;
     if (nrev > 0 && P.substeps > 0) {
       // (1b) Delaunay over every edge with the sent-back vertices at their old
-      // positions, then sub-steps toward their targets
+      // positions, then sub-steps toward their targets; the mesh is then
+      // Delaunay, so only what removal and reinsertion touch is marked
       if (gtid == 0) { P.st->wl_count[0] = 0; P.st->wl_count[1] = 0; P.st->inverted = 0; P.st->hard_count = 0; }
       g.sync();
-      const unsigned q0 = stamp++;
+      const unsigned qa = stamp++;
       const unsigned sc0 = stamp++;
-      phase_classify<false>(g, Q, q0, sc0, lc);
+      phase_classify<false>(g, Q, qa, sc0, lc);
       g.sync();
-      phase_classify_hard<false>(g, Q, q0, sc0, lc);
+      phase_classify_hard<false>(g, Q, qa, sc0, lc);
       phase_lawson<false>(g, Q, 0, stamp, lc, sc0);
       g.sync();
       timeline_insert(P, 15, 0);
       phase_substeps(g, Q, stamp, lc);
       timeline_insert(P, 15, 1);
+      mk = stamp++;
     }
     const int nrem = ld_i(&P.st->vl_count[0]);
-    if (nrem == 0) {
+    if (nrem > 0) {
+      // (2) remove what is left, marking each hole's sides and diagonals
+      ok = phase_remove(g, Q, stamp, lc, mk);
+      g.sync();
       timeline(P, 44);
-      timeline(P, 45);
-      timeline(P, 46);
-      flush_counters(P, lc);
-      return stamp;
-    }
-    // (2) remove what is left
-    ok = phase_remove(g, Q, stamp, lc);
-    g.sync();
-    timeline(P, 44);
-    // (3) Lawson over every edge of the reduced mesh
-    if (gtid == 0) { P.st->wl_count[0] = 0; P.st->wl_count[1] = 0; P.st->inverted = 0; P.st->hard_count = 0; }
-    g.sync();
-    const unsigned q1 = stamp++;
-    const unsigned sc1 = stamp++;
-    phase_classify<false>(g, Q, q1, sc1, lc);
-    g.sync();
-    phase_classify_hard<false>(g, Q, q1, sc1, lc);
-    phase_lawson<false>(g, Q, 0, stamp, lc, sc1);
-    g.sync();
-    timeline(P, 45);
-    // (4) reinsert at the new positions
-    if (gtid == 0) { P.st->vl_count[0] = 0; P.st->vl_count[1] = 0; }
-    g.sync();
-    for (int base = blockIdx.x * blockDim.x; base < P.V_it; base += stride) {
-      const int vi = base + threadIdx.x;
-      const int v = vi < P.V_it ? vert_at(P, vi) : 0;
-      int mine[1];
-      int k = 0;
-      if (vi < P.V_it && ld_i(P.vhe + v) < 0 && marked(Q, v, fs)) {
-        __stcg(P.pos + v, __ldcg(P.target + v));
-        mine[k++] = v;
+      // (3) reinsert at the new positions: splits only, their edges marked
+      if (gtid == 0) { P.st->vl_count[0] = 0; P.st->vl_count[1] = 0; }
+      g.sync();
+      for (int base = blockIdx.x * blockDim.x; base < P.V_it; base += stride) {
+        const int vi = base + threadIdx.x;
+        const int v = vi < P.V_it ? vert_at(P, vi) : 0;
+        int mine[1];
+        int k = 0;
+        if (vi < P.V_it && ld_i(P.vhe + v) < 0 && marked(Q, v, fs)) {
+          __stcg(P.pos + v, __ldcg(P.target + v));
+          mine[k++] = v;
+        }
+        warp_push(mine, k, P.vl0, &P.st->vl_count[0], P.V, P.st);
       }
-      warp_push(mine, k, P.vl0, &P.st->vl_count[0], P.V, P.st);
+      g.sync();
+      if (ok) ok = phase_insert(g, Q, stamp, lc, mk);
+      g.sync();
+    } else {
+      timeline(P, 44);
     }
-    g.sync();
-    if (ok) phase_insert(g, Q, stamp, lc);
+    timeline(P, 45);
+    // (4) one Lawson pass from every marked edge
+    if (ok) {
+      if (gtid == 0) { P.st->wl_count[0] = 0; P.st->wl_count[1] = 0; }
+      g.sync();
+      for (int base = blockIdx.x * blockDim.x; base < P.E_it; base += stride) {
+        const int ei = base + threadIdx.x;
+        const int e = ei < P.E_it ? edge_at(P, ei) : -1;
+        int mine[1];
+        int k = 0;
+        if (e >= 0 && (unsigned)ld_i(reinterpret_cast<const int*>(P.qmark) + e) == mk) mine[k++] = e;
+        if (__any_sync(kFull, k > 0)) warp_push(mine, k, P.wl0, &P.st->wl_count[0], P.E, P.st);
+      }
+      g.sync();
+      phase_lawson<false>(g, Q, 0, stamp, lc, 0);
+      g.sync();
+    }
     timeline(P, 46);
   }
   flush_counters(P, lc);
@@ -1603,7 +1687,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_step(KParams P) {
   timeline(P, 1);
   const int inverted = ld_i(&P.st->inverted);
   if (inverted == 0) phase_lawson<true, true>(g, P, 0, stamp, lc, sc0);
-  else stamp = repair_step(g, P, stamp);
+  else stamp = repair_step(g, P, stamp, q0);
   flush_counters(P, lc);
   // No closing grid barrier: each block leaves when its own work is done and
   // the last one to leave publishes the launch.  The block barrier orders its
@@ -2156,6 +2240,14 @@ int mcl_debug_insert_timeline(mcl_mesh* m, int64_t* out64) {
   CK(cudaDeviceSynchronize());
   CK(cudaMemcpy(m->st_host, m->st, sizeof(DevState), cudaMemcpyDeviceToHost));
   for (int i = 0; i < 64; ++i) out64[i] = (int64_t)m->st_host->ts_insert[i];
+  return MCL_OK;
+}
+
+int mcl_debug_remove_timeline(mcl_mesh* m, int64_t* out64) {
+  if (!m || !out64) return fail(MCL_ERR_INVALID_ARGUMENT, "null argument");
+  CK(cudaDeviceSynchronize());
+  CK(cudaMemcpy(m->st_host, m->st, sizeof(DevState), cudaMemcpyDeviceToHost));
+  for (int i = 0; i < 64; ++i) out64[i] = (int64_t)m->st_host->ts_remove[i];
   return MCL_OK;
 }
 

@@ -82,6 +82,9 @@ struct DevState {
   unsigned long long ts[kTimeline];  // %globaltimer at phase boundaries of the last launch
   // insertion round r < 16: [4r] located, [4r+1] won, [4r+2] split, [4r+3] flips done
   unsigned long long ts_insert[64];
+  // removal round r < 16: [4r] claimed, [4r+1] winners known, [4r+2] removed;
+  // [48 + p]: end of send-back pass p < 16
+  unsigned long long ts_remove[64];
   // latest block at the move / classification marks of the running launch;
   // published to ts[43..46] by a step without repair (a repair step keeps its
   // own marks there)
