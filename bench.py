@@ -548,12 +548,13 @@ def repair_measure(n, K, Wm, seed, local):
     stream = torch.cuda.Stream()
     lib = L.lib()
     keys = ("inverted_faces", "reverted_vertices", "removed_vertices", "lawson_flips", "removal_flips",
-            "insert_rounds", "lawson_rounds", "incircle_tests")
+            "insert_rounds", "lawson_rounds", "incircle_tests", "incircle_fp64", "incircle_exact", "orient_fp64",
+            "orient_exact")
     tot = {k: 0 for k in keys}
     ms, phases, rounds = [], [], []
     tl = np.zeros(48, np.int64)
     cn = np.zeros(32, np.int64)
-    trm = np.zeros(64, np.int64)
+    trm = np.zeros(96, np.int64)
     tin = np.zeros(64, np.int64)
     last_rounds = None
     for k in range(Wm + K):
@@ -607,7 +608,10 @@ def repair_measure(n, K, Wm, seed, local):
             ins.append([round((m3[0] - prev) / 1e3, 1), round((m3[1] - m3[0]) / 1e3, 1), round((m3[2] - m3[1]) / 1e3, 1)])
             prev = tin[4 * r_ + 3]
         last_rounds = {"send_back_pass_us": [round(x, 1) for x in passes], "removal_round_us": rem,
-                       "insertion_round_us": ins}
+                       "insertion_round_us": ins,
+                       "slowest_removal_cycles_spokes": [[int(trm[64 + r_]) >> 16, int(trm[64 + r_]) & 0xffff]
+                                                         for r_ in range(nrem)],
+                       "uncached_removals": [int(trm[80 + r_]) for r_ in range(nrem)]}
     ms = np.array(ms)
     ph = np.median(np.array(phases), 0)
     flips = tot["lawson_flips"] + tot["removal_flips"]

@@ -382,8 +382,10 @@ int mcl_debug_counters(mcl_mesh* m, int64_t* out, int n);
 int mcl_debug_insert_timeline(mcl_mesh* m, int64_t* out64);
 /* %globaltimer marks of the repair's removal rounds r < 16 of the last launch:
  * [4r] stars claimed, [4r+1] winners known, [4r+2] removed; [48 + p] end of
- * send-back pass p < 16.  Diagnostics only (no reference counterpart). */
-int mcl_debug_remove_timeline(mcl_mesh* m, int64_t* out64);
+ * send-back pass p < 16; [64 + r] the slowest removal of round r since the
+ * last call, (SM cycles << 16) | spokes; [80 + r] removals of round r that
+ * walked their star again.  Diagnostics only (no reference counterpart). */
+int mcl_debug_remove_timeline(mcl_mesh* m, int64_t* out96);
 
 /* The device predicate ladder evaluated on the host CPU (same source as the
  * device code), for testing without a GPU.  kind 0 = orient2d on n records of

@@ -27,6 +27,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -727,48 +728,73 @@ __device__ bool phase_fixpoint(cg::grid_group& g, const KParams& P, LocalCounter
 // The k spoke edges become k-3 diagonals plus the 3 free edges of v.
 constexpr int kEarMax = 128;
 
-__device__ int remove_vertex_ears(const KParams& P, int v, LocalCounters& lc, unsigned mk) {
-  int sp[kEarMax], lk[kEarMax], w[kEarMax], nx[kEarMax], pv[kEarMax], bnd[kEarMax];
-  float2 q[kEarMax];
-  const int s0 = ld_i(P.vhe + v);
-  if (bad_h(P, s0)) return MCL_ERR_DEGENERATE_INPUT | (__LINE__ << 8);
-  int k = 0, h = s0;
-  do {
-    if (k >= kEarMax) return MCL_ERR_CAPACITY | (__LINE__ << 8);
-    sp[k] = h;
-    lk[k] = he_next(P, h);
-    if (bad_h(P, lk[k])) return MCL_ERR_DEGENERATE_INPUT | (__LINE__ << 8);
-    w[k] = he_origin(P, lk[k]);
-    if (bad_v(P, w[k])) return MCL_ERR_DEGENERATE_INPUT | (__LINE__ << 8);
-    q[k] = ldpos(P, w[k]);
-    ++k;
-    h = he_prev(P, h) ^ 1;
-    if (bad_h(P, h)) return MCL_ERR_DEGENERATE_INPUT | (__LINE__ << 8);
-  } while (h != s0);
+// The star polygon under ear clipping: cyclic links and corner positions.
+// Any star up to kEarMax corners: local arrays.
+struct LocalPoly {
+  int nx_[kEarMax], pv_[kEarMax];
+  float2 q_[kEarMax];
+  __device__ __forceinline__ int nx(int j) const { return nx_[j]; }
+  __device__ __forceinline__ int pv(int j) const { return pv_[j]; }
+  __device__ __forceinline__ void set_nx(int j, int x) { nx_[j] = x; }
+  __device__ __forceinline__ void set_pv(int j, int x) { pv_[j] = x; }
+  __device__ __forceinline__ float2 q(int j) const { return q_[j]; }
+  __device__ __forceinline__ void set_q(int j, float2 x) { q_[j] = x; }
+};
+
+// Stars of up to kSmallStar corners: links packed four bits each in
+// registers and positions in this thread's slots of the classification's
+// shared staging array (idle during repair), which the ear search reads
+// O(k^2) times.
+constexpr int kSmallStar = 16;
+struct SmallPoly {
+  unsigned long long nx_ = 0, pv_ = 0;
+  __device__ __forceinline__ static float2* slot(int j) {
+    return reinterpret_cast<float2*>(&s_ev[(j >> 3) & 1][(j >> 1) & 3][threadIdx.x]) + (j & 1);
+  }
+  __device__ __forceinline__ int nx(int j) const { return (int)((nx_ >> (4 * j)) & 15u); }
+  __device__ __forceinline__ int pv(int j) const { return (int)((pv_ >> (4 * j)) & 15u); }
+  __device__ __forceinline__ void set_nx(int j, int x) {
+    nx_ = (nx_ & ~(15ull << (4 * j))) | ((unsigned long long)x << (4 * j));
+  }
+  __device__ __forceinline__ void set_pv(int j, int x) {
+    pv_ = (pv_ & ~(15ull << (4 * j))) | ((unsigned long long)x << (4 * j));
+  }
+  __device__ __forceinline__ float2 q(int j) const { return *slot(j); }
+  __device__ __forceinline__ void set_q(int j, float2 x) { *slot(j) = x; }
+};
+
+// Clip the star polygon of v given its k spokes sp (counter-clockwise), the
+// link half-edges lk (lk[i] = next(sp[i]), the side of face i opposite v),
+// their origins w and, in poly, their positions; bnd is scratch of size k.
+template <typename Poly>
+__device__ int clip_star(const KParams& P, int v, LocalCounters& lc, unsigned mk, int k, const int* sp, const int* lk,
+                         const int* w, Poly& poly, int* bnd) {
   if (k < 3) return MCL_ERR_DEGENERATE_INPUT | (__LINE__ << 8);
   for (int j = 0; j < k; ++j) {
-    nx[j] = j + 1 == k ? 0 : j + 1;
-    pv[j] = j == 0 ? k - 1 : j - 1;
+    poly.set_nx(j, j + 1 == k ? 0 : j + 1);
+    poly.set_pv(j, j == 0 ? k - 1 : j - 1);
     bnd[j] = lk[j];
   }
   int remaining = k, j = 0, used = 3;
   while (remaining > 3) {
     bool found = false;
     for (int t = 0; t < remaining && !found; ++t) {
-      const int a = pv[j], b = j, c = nx[j];
-      if (orient_v(P, q[a], q[b], q[c], lc) > 0) {
+      const int a = poly.pv(j), b = j, c = poly.nx(j);
+      const float2 qa = poly.q(a), qb = poly.q(b), qc = poly.q(c);
+      if (orient_v(P, qa, qb, qc, lc) > 0) {
         bool empty = true;
-        for (int m = nx[c]; m != a && empty; m = nx[m]) {
-          if (orient_v(P, q[a], q[b], q[m], lc) >= 0 && orient_v(P, q[b], q[c], q[m], lc) >= 0 &&
-              orient_v(P, q[c], q[a], q[m], lc) >= 0)
+        for (int m = poly.nx(c); m != a && empty; m = poly.nx(m)) {
+          const float2 qm = poly.q(m);
+          if (orient_v(P, qa, qb, qm, lc) >= 0 && orient_v(P, qb, qc, qm, lc) >= 0 &&
+              orient_v(P, qc, qa, qm, lc) >= 0)
             empty = false;
         }
         found = empty;
       }
-      if (!found) j = nx[j];
+      if (!found) j = poly.nx(j);
     }
     if (!found) return MCL_ERR_NO_CONVERGENCE | (__LINE__ << 8);
-    const int a = pv[j], b = j, c = nx[j];
+    const int a = poly.pv(j), b = j, c = poly.nx(j);
     const int g = sp[used++] >> 1;
     const int d0 = 2 * g, d1 = 2 * g + 1;  // d0: w_c -> w_a inside the ear, d1: w_a -> w_c outside
     __stcg(P.ev + g, make_int4(w[c], w[a], w[b], -1));
@@ -777,13 +803,13 @@ __device__ int remove_vertex_ears(const KParams& P, int v, LocalCounters& lc, un
     he_set_face(P, bnd[b], w[a], d0, bnd[a]);
     mark_edge(P, g, mk);
     bnd[a] = d1;
-    nx[a] = c;
-    pv[c] = a;
+    poly.set_nx(a, c);
+    poly.set_pv(c, a);
     --remaining;
     j = c;
   }
   {
-    const int a = j, b = nx[a], c = nx[b];
+    const int a = j, b = poly.nx(a), c = poly.nx(b);
     he_set_face(P, bnd[a], w[c], bnd[b], bnd[c]);
     he_set_face(P, bnd[b], w[a], bnd[c], bnd[a]);
     he_set_face(P, bnd[c], w[b], bnd[a], bnd[b]);
@@ -804,12 +830,12 @@ __device__ int remove_vertex_ears(const KParams& P, int v, LocalCounters& lc, un
   // v; so do the edges between consecutive hull points)
   int anchor = w[0];
   {
-    const float2 pv = ldpos(P, v);
+    const float2 p0 = ldpos(P, v);
     float best = INFINITY;
     for (int i = 0; i < k; ++i) {
       if (P.vfix[w[i]]) continue;
-      const float2 q = ldpos(P, w[i]);
-      const float dx = __fsub_rn(q.x, pv.x), dy = __fsub_rn(q.y, pv.y);
+      const float2 qi = poly.q(i);
+      const float dx = __fsub_rn(qi.x, p0.x), dy = __fsub_rn(qi.y, p0.y);
       const float d2 = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
       if (d2 < best) { best = d2; anchor = w[i]; }
     }
@@ -817,6 +843,84 @@ __device__ int remove_vertex_ears(const KParams& P, int v, LocalCounters& lc, un
   __stcg(P.vaux + v, anchor);
   __stcg(P.vhe + v, -1);
   return MCL_OK;
+}
+
+__device__ int remove_vertex_ears(const KParams& P, int v, LocalCounters& lc, unsigned mk) {
+  int sp[kEarMax], lk[kEarMax], w[kEarMax], bnd[kEarMax];
+  LocalPoly poly;
+  const int s0 = ld_i(P.vhe + v);
+  if (bad_h(P, s0)) return MCL_ERR_DEGENERATE_INPUT | (__LINE__ << 8);
+  int k = 0, h = s0;
+  do {
+    if (k >= kEarMax) return MCL_ERR_CAPACITY | (__LINE__ << 8);
+    sp[k] = h;
+    lk[k] = he_next(P, h);
+    if (bad_h(P, lk[k])) return MCL_ERR_DEGENERATE_INPUT | (__LINE__ << 8);
+    w[k] = he_origin(P, lk[k]);
+    if (bad_v(P, w[k])) return MCL_ERR_DEGENERATE_INPUT | (__LINE__ << 8);
+    poly.set_q(k, ldpos(P, w[k]));
+    ++k;
+    h = he_prev(P, h) ^ 1;
+    if (bad_h(P, h)) return MCL_ERR_DEGENERATE_INPUT | (__LINE__ << 8);
+  } while (h != s0);
+  return clip_star(P, v, lc, mk, k, sp, lk, w, poly, bnd);
+}
+
+// A star walked once per removal round and kept by its thread across the
+// round's barriers (claim, verify, remove): the thread handling list entry i
+// handles the same entry in all three sub-phases, and a round's winners own
+// every face of their stars, so nothing else writes them meanwhile.
+constexpr int kStarCache = 32;
+struct StarCache {
+  int v;                 // cached vertex, -1: none
+  int k;                 // its spokes; 0 when more than kStarCache
+  int sp[kStarCache];    // spokes, counter-clockwise
+  int lk[kStarCache];    // next(sp[i])
+  int fm[kStarCache];    // smallest half-edge of face i (its claim slot)
+};
+
+// Walk v's star once (one record load per spoke), claiming each face with key.
+__device__ bool claim_star(const KParams& P, int v, unsigned long long key, StarCache& sc) {
+  sc.v = v;
+  sc.k = 0;
+  const int s0 = ld_i(P.vhe + v);
+  if (bad_h(P, s0)) return false;
+  int h = s0, k = 0;
+  do {
+    const int4 r = ld_en(P, h >> 1);
+    const int nxt = (h & 1) ? r.z : r.x, prv = (h & 1) ? r.w : r.y;
+    if (bad_h(P, nxt) || bad_h(P, prv)) return false;
+    const int f = min(h, min(nxt, prv));
+    atomicMax(P.claim + f, key);
+    if (k < kStarCache) {
+      sc.sp[k] = h;
+      sc.lk[k] = nxt;
+      sc.fm[k] = f;
+    }
+    ++k;
+    h = prv ^ 1;
+  } while (h != s0 && k < 1024);
+  if (h != s0) return false;
+  sc.k = k <= kStarCache ? k : 0;
+  return true;
+}
+
+// Removal of v from its cached star (sc.k spokes): origins and positions of
+// the link loaded together, then the ear clipping.
+__device__ int remove_cached(const KParams& P, int v, const StarCache& sc, LocalCounters& lc, unsigned mk) {
+  const int k = sc.k;
+  int w[kStarCache], bnd[kStarCache];
+  for (int i = 0; i < k; ++i) w[i] = he_origin(P, sc.lk[i]);
+  for (int i = 0; i < k; ++i)
+    if (bad_v(P, w[i])) return MCL_ERR_DEGENERATE_INPUT | (__LINE__ << 8);
+  if (k <= kSmallStar) {
+    SmallPoly poly;
+    for (int i = 0; i < k; ++i) poly.set_q(i, ldpos(P, w[i]));
+    return clip_star(P, v, lc, mk, k, sc.sp, sc.lk, w, poly, bnd);
+  }
+  LocalPoly poly;
+  for (int i = 0; i < k; ++i) poly.set_q(i, ldpos(P, w[i]));
+  return clip_star(P, v, lc, mk, k, sc.sp, sc.lk, w, poly, bnd);
 }
 
 // ---------------------------------------------------------------------------
@@ -933,7 +1037,9 @@ __device__ int remove_vertex(const KParams& P, int v, LocalCounters& lc, int& fl
 __device__ bool phase_remove(cg::grid_group& g, const KParams& P, unsigned& stamp, LocalCounters& lc, unsigned mk) {
   const int stride = gridDim.x * blockDim.x;
   const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31, nwarps = stride >> 5, wid = spread_tid() >> 5;
   int src = 0;
+  StarCache sc;
   for (int round = 0;; ++round) {
     const int n = ld_i(&P.st->vl_count[src]);
     if (n == 0) return true;
@@ -949,35 +1055,64 @@ __device__ bool phase_remove(cg::grid_group& g, const KParams& P, unsigned& stam
       P.st->vl_count[dst] = 0;
       P.st->c[C_REMOVE_ROUNDS] += 1;
     }
-    // claim every face of the star
-    for (int i = spread_tid(); i < n; i += stride) {
+    // A removal is a long divergent chain (star loads, ear search, writes):
+    // when the list fits, each warp takes one vertex (lane 0), so no warp runs
+    // several of them side by side; else the spread order.
+    const bool sparse = n <= nwarps;
+    const int i0 = sparse ? (lane == 0 ? wid : n) : spread_tid(), di = sparse ? n : stride;
+    // claim every face of the star (the thread keeps the last star it walked)
+    sc.v = -1;
+    for (int i = i0; i < n; i += di) {
       const int v = ld_i(in + i);
       const unsigned long long key = ((unsigned long long)sk << 32) | (unsigned)(~mix32((unsigned)v ^ sk));
-      for_spokes(P, v, [&](int h) { atomicMax(P.claim + face_min(P, h), key); });
+      if (!claim_star(P, v, key, sc)) {
+        sc.v = -1;
+        set_error(P, MCL_ERR_DEGENERATE_INPUT);
+      }
     }
     g.sync();
     if (round < 16) timeline_remove(P, 4 * round);
-    for (int i = spread_tid(); i < n; i += stride) {
+    for (int i = i0; i < n; i += di) {
       const int v = ld_i(in + i);
       const unsigned long long key = ((unsigned long long)sk << 32) | (unsigned)(~mix32((unsigned)v ^ sk));
-      bool win = true;
-      const bool ok = for_spokes(P, v, [&](int h) {
-        if (__ldcg(P.claim + face_min(P, h)) != key) win = false;
-      });
+      bool win = true, ok = true;
+      if (sc.v == v && sc.k > 0) {
+        unsigned long long c[kStarCache];
+        for (int j = 0; j < sc.k; ++j) c[j] = __ldcg(P.claim + sc.fm[j]);
+        for (int j = 0; j < sc.k; ++j) win = win && c[j] == key;
+      } else {
+        ok = for_spokes(P, v, [&](int h) {
+          if (__ldcg(P.claim + face_min(P, h)) != key) win = false;
+        });
+      }
       P.vlocf[v] = (ok && win) ? 1 : 0;
       if (!ok) set_error(P, MCL_ERR_DEGENERATE_INPUT);
     }
     g.sync();
     if (round < 16) timeline_remove(P, 4 * round + 1);
     int removed = 0, flips = 0;
-    for (int base = spread_tid() - (int)(threadIdx.x & 31); base < n; base += stride) {
-      const int i = base + (int)(threadIdx.x & 31);
+    for (int base = sparse ? wid : spread_tid() - lane; base < n; base += sparse ? nwarps : stride) {
+      const int i = sparse ? (lane == 0 ? base : n) : base + lane;
       int mine[1];
       int k = 0;
       if (i < n) {
         const int v = ld_i(in + i);
         if (__ldcg(P.vlocf + v) == 1) {
-          const int rc = remove_vertex(P, v, lc, flips, mk);
+          int rc;
+          const long long t0 = clock64();
+          int deg = sc.k;
+          if (sc.v == v && sc.k > 0) {
+            rc = remove_cached(P, v, sc, lc, mk);
+            ++flips;  // counted as one repair operation
+          } else {
+            rc = remove_vertex(P, v, lc, flips, mk);
+            deg = 0;
+            if (round < 16) atomicAdd(&P.st->rm_uncached[round], 1ull);
+          }
+          if (round < 16) {
+            const unsigned long long dt = (unsigned long long)(clock64() - t0);
+            atomicMax(&P.st->rm_slow[round], (dt << 16) | (unsigned long long)(deg & 0xffff));
+          }
           if (rc != MCL_OK) flag_error_at(P, rc & 0xff, 100000 + (rc >> 8));
           else ++removed;
         } else if (ld_i(&P.st->status) == MCL_OK) {
@@ -1012,11 +1147,15 @@ __device__ int locate(const KParams& P, float2 p, int h, int* on, LocalCounters&
       return -1;
     }
     if (h < 0 || h >= 2 * P.E) return -MCL_ERR_DEGENERATE_INPUT;
-    const int hs[3] = {h, he_next(P, h), he_prev(P, h)};
-    int o[3];
+    // the face's three corners and its other two half-edges from h's two
+    // records (loaded together): origin(next(h)) = origin(twin(h)) and
+    // origin(prev(h)) = apex(h)
+    const int4 r = ld_ev(P, h >> 1), nn = ld_en(P, h >> 1);
+    const bool odd = h & 1;
+    const int hs[3] = {h, odd ? nn.z : nn.x, odd ? nn.w : nn.y};
+    const int o[3] = {odd ? r.y : r.x, odd ? r.x : r.y, odd ? r.w : r.z};
     for (int k = 0; k < 3; ++k) {
       if (hs[k] < 0 || hs[k] >= 2 * P.E) return -MCL_ERR_DEGENERATE_INPUT;
-      o[k] = he_origin(P, hs[k]);
       if (o[k] < 0 || o[k] >= P.V) return -MCL_ERR_DEGENERATE_INPUT;
     }
     const float2 q[3] = {ldpos(P, o[0]), ldpos(P, o[1]), ldpos(P, o[2])};
@@ -2248,6 +2387,15 @@ int mcl_debug_remove_timeline(mcl_mesh* m, int64_t* out64) {
   CK(cudaDeviceSynchronize());
   CK(cudaMemcpy(m->st_host, m->st, sizeof(DevState), cudaMemcpyDeviceToHost));
   for (int i = 0; i < 64; ++i) out64[i] = (int64_t)m->st_host->ts_remove[i];
+  for (int i = 0; i < 16; ++i) {
+    out64[64 + i] = (int64_t)m->st_host->rm_slow[i];
+    out64[80 + i] = (int64_t)m->st_host->rm_uncached[i];
+  }
+  // the next launches accumulate from zero
+  static_assert(offsetof(DevState, rm_uncached) == offsetof(DevState, rm_slow) + 16 * 8, "layout");
+  unsigned long long zero[32] = {};
+  CK(cudaMemcpy(reinterpret_cast<char*>(m->st) + offsetof(DevState, rm_slow), zero, sizeof(zero),
+                cudaMemcpyHostToDevice));
   return MCL_OK;
 }
 

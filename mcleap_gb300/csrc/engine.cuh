@@ -85,6 +85,11 @@ struct DevState {
   // removal round r < 16: [4r] claimed, [4r+1] winners known, [4r+2] removed;
   // [48 + p]: end of send-back pass p < 16
   unsigned long long ts_remove[64];
+  // removal round r < 16: the slowest removal ((SM cycles << 16) | spokes)
+  // and how many removals walked their star again (not cached); cleared by
+  // mcl_debug_remove_timeline
+  unsigned long long rm_slow[16];
+  unsigned long long rm_uncached[16];
   // latest block at the move / classification marks of the running launch;
   // published to ts[43..46] by a step without repair (a repair step keeps its
   // own marks there)
