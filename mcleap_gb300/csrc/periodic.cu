@@ -20,8 +20,9 @@
 //           fold again) and classifies again; flips start from a mesh whose
 //           faces are all positive.  Vertices sent back then follow in up to
 //           kSubLevels sub-steps (half of what they still owe, the last all);
-//           the few still away are removed and reinserted at their targets
-//           by one thread (k_preinsert).
+//           the few still away (listed in parallel, by ascending id) are
+//           removed and reinserted at their targets by one thread
+//           (k_preinsert).
 //   queries one-ring with copy offsets, closest neighbour, mesh FRNN (one
 //           launch for the outgoing half-edges, one per query).
 #include <cuda_runtime.h>
@@ -95,9 +96,64 @@ __global__ void k_presume(PView V, PF2* d, bool last) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < V.n) mcl::p_body_resume(V, d, i, last);
 }
-// one thread: the sequential removal and reinsertion, vertices by ascending id
-__global__ void k_preinsert(PView V, int* vhe) {
-  if (blockIdx.x == 0 && threadIdx.x == 0) mcl::p_body_reinsert(V, vhe, nullptr, V.n, kMaxReinsert);
+// The vertices still away from their targets, listed by ascending id (the
+// order the reinsertion takes them in), built in parallel: a count per chunk
+// of kChunk vertices, one block scanning the counts (total appended), then
+// each chunk writing its vertices in order.
+constexpr int kChunk = 1024;
+__device__ __forceinline__ bool p_behind(const PView& V, int i) {
+  const PF2 here = V.pos[i], t = V.target[i];
+  return !(here.x == t.x && here.y == t.y);
+}
+__global__ void __launch_bounds__(kChunk) k_pbehind_count(PView V, int* chunk) {
+  const int i = blockIdx.x * kChunk + threadIdx.x;
+  const int c = __syncthreads_count(i < V.n && p_behind(V, i));
+  if (threadIdx.x == 0) chunk[blockIdx.x] = c;
+}
+// exclusive scan of chunk[0..nb) in place, the total in chunk[nb] (one block)
+__global__ void __launch_bounds__(kChunk) k_pbehind_scan(int* chunk, int nb) {
+  __shared__ int tot[kChunk];
+  const int per = (nb + kChunk - 1) / kChunk, lo = threadIdx.x * per, hi = min(nb, lo + per);
+  int run = 0;
+  for (int i = lo; i < hi; ++i) run += chunk[i];
+  tot[threadIdx.x] = run;
+  __syncthreads();
+  for (int o = 1; o < kChunk; o <<= 1) {
+    const int y = threadIdx.x >= (unsigned)o ? tot[threadIdx.x - o] : 0;
+    __syncthreads();
+    tot[threadIdx.x] += y;
+    __syncthreads();
+  }
+  int acc = threadIdx.x ? tot[threadIdx.x - 1] : 0;
+  for (int i = lo; i < hi; ++i) {
+    const int x = chunk[i];
+    chunk[i] = acc;
+    acc += x;
+  }
+  if (threadIdx.x == kChunk - 1) chunk[nb] = tot[kChunk - 1];
+}
+__global__ void __launch_bounds__(kChunk) k_pbehind_scatter(PView V, const int* chunk, int* list) {
+  __shared__ int wbase[kChunk / 32];
+  const int i = blockIdx.x * kChunk + threadIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const bool b = i < V.n && p_behind(V, i);
+  const unsigned bal = __ballot_sync(0xffffffffu, b);
+  if (lane == 0) wbase[warp] = __popc(bal);
+  __syncthreads();
+  if (warp == 0) {
+    const int x = wbase[lane];
+    int incl = x;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    wbase[lane] = incl - x;
+  }
+  __syncthreads();
+  if (b) list[chunk[blockIdx.x] + wbase[warp] + __popc(bal & ((1u << lane) - 1u))] = i;
+}
+// one thread: the sequential removal and reinsertion of the listed vertices
+__global__ void k_preinsert(PView V, int* vhe, const int* list, const int* count) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) mcl::p_body_reinsert(V, vhe, list, *count, kMaxReinsert);
 }
 __global__ void k_prevert(PView V) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -631,7 +687,12 @@ int mcl_periodic_step(mcl_periodic* m, const mcl_float2* d_dev, void* stream, mc
     PCK(cudaMemsetAsync(&m->cnt->reinserted, 0, sizeof(unsigned long long), s));
     PCK(cudaMemsetAsync(m->vhe, 0xFF, 4 * (size_t)m->n, s));  // vhe = -1: the largest candidate wins
     k_pvhe<<<blocks(2 * m->E), kThreads, 0, s>>>(V, m->vhe);
-    k_preinsert<<<1, 32, 0, s>>>(V, m->vhe);
+    // the flip rounds are over: clist holds the list, wl[1] the chunk counts
+    const int nb = (int)((m->n + kChunk - 1) / kChunk);
+    k_pbehind_count<<<nb, kChunk, 0, s>>>(V, m->wl[1]);
+    k_pbehind_scan<<<1, kChunk, 0, s>>>(m->wl[1], nb);
+    k_pbehind_scatter<<<nb, kChunk, 0, s>>>(V, m->wl[1], m->clist);
+    k_preinsert<<<1, 32, 0, s>>>(V, m->vhe, m->clist, m->wl[1] + nb);
     PCK(cudaGetLastError());
     PCK(cudaMemsetAsync(&m->cnt->behind, 0, sizeof(unsigned long long), s));
     k_presume<<<blocks(m->n), kThreads, 0, s>>>(V, m->dsub, true);  // counts who is still behind

@@ -811,6 +811,7 @@ MCL_HD bool p_lawson_seq(const PView& V, int* vhe, const int* link, int nlink) {
     stack[top++] = w.z >> 1;
     stack[top++] = w.w >> 1;
   }
+  if (top != 0) p_error(V, MCL_ERR_NO_CONVERGENCE, 22);  // the flip guard ran out
   return top == 0;
 }
 
@@ -827,7 +828,26 @@ MCL_HD void p_body_reinsert(const PView& V, int* vhe, const int* list, int count
     if (here.x == t.x && here.y == t.y) continue;
     ++done;
     int freed[3], near = -1, link[4], nlink = 0, hole[2 * kSeqStar], nhole = 0;
-    if (!p_remove_seq(V, vhe, v, freed, &near, hole, &nhole)) continue;
+    if (!p_remove_seq(V, vhe, v, freed, &near, hole, &nhole)) {
+      if (V.cnt->error) return;
+      // refused (v stays where it was, counted as behind); spoke flips it
+      // made first leave its star non-Delaunay: Lawson over the hole's sides,
+      // the flipped spokes and v's remaining spokes
+      if (nhole > 0) {
+        int live[3 * kSeqStar], nlive = 0;
+        for (int k = 0; k < nhole && nlive < 3 * kSeqStar; ++k) live[nlive++] = 2 * hole[k];
+        const int h0 = vhe[v];
+        if ((unsigned)h0 < 2u * (unsigned)V.E) {
+          int h = h0;
+          do {
+            if (nlive < 3 * kSeqStar) live[nlive++] = h;
+            h = p_rot(V, h);
+          } while (h != h0 && (unsigned)h < 2u * (unsigned)V.E && nlive < 3 * kSeqStar);
+        }
+        if (!p_lawson_seq(V, vhe, live, nlive)) return;
+      }
+      continue;
+    }
     // the hole was filled by arbitrary flips: make it Delaunay again (its
     // edges that died with v are skipped: they are free now)
     int live[2 * kSeqStar], nlive = 0;

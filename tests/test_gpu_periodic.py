@@ -64,7 +64,7 @@ def test_steps_with_wraps_match_the_oracle(M):
         d = (rng.normal(0, 0.08 * h, (n, 2)) + drift).astype(np.float32)
         d = torus_settle(pos, d, ev, eo, drift)
         st = pt.step(cuda(d))
-        assert st["status"] == 0 and st["inverted_faces"] == 0, st
+        assert st["status"] == 0 and st["inverted_faces"] == 0 and st["reverted_vertices"] == 0, st
         want = torus_wrap(pos + d)
         pos2, ev2, en2, eo2 = pt.download()
         assert np.array_equal(pos2, want)

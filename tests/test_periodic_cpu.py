@@ -461,3 +461,35 @@ def test_reinsertion_inside_a_face_on_an_edge_and_onto_a_taken_spot(reinsert_har
     assert not ((got[:, 0] == 0) & (got[:, 1] == 1)).any()
     assert ((got[:, 0] == min(0, v_edge)) & (got[:, 1] == max(0, v_edge))).any()
     assert ((got[:, 0] == min(1, v_edge)) & (got[:, 1] == max(1, v_edge))).any()
+
+
+def test_refused_removal_leaves_the_torus_delaunay(reinsert_harness, tmp_path):
+    """Tiny tori, where a vertex's star can hold two copies of one neighbour:
+    the one-thread removal then refuses (the vertex stays where it was), some
+    of them after spoke flips.  Whatever happens, a call that returns OK leaves
+    the oracle's triangulation of the final positions (a refusal is counted,
+    never a silently non-Delaunay mesh); a failure is reported."""
+    outcomes = {"reinserted": 0, "refused": 0, "error": 0}
+    for n in (3, 4, 5, 6, 8):
+        for seed in range(8):
+            xy = torus_points(n, 1000 + 37 * n + seed)
+            try:
+                ev, en, eo = P.periodic_mesh(xy, L)
+            except ValueError:
+                continue  # too few points for the period: no torus triangulation
+            rng = np.random.default_rng(seed)
+            for v in range(n):
+                t = (2 * L + rng.random(2) * L).astype(np.float32)
+                st, re, pos, ev2, en2, eo2 = run_reinsert(reinsert_harness, tmp_path, xy, ev, en, eo, [v], [t])
+                if st != 0:
+                    outcomes["error"] += 1
+                    continue
+                assert torus_faces_consistent(ev2, en2, eo2), (n, seed, v)
+                assert np.array_equal(P.mesh_edges(ev2, eo2), P.periodic_edges(pos, L)), (n, seed, v)
+                if re == 1:
+                    assert (pos[v] == t).all()
+                    outcomes["reinserted"] += 1
+                else:
+                    assert (pos[v] == xy[v]).all()
+                    outcomes["refused"] += 1
+    assert outcomes["refused"] > 0 and outcomes["reinserted"] > 0, outcomes
