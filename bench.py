@@ -49,6 +49,7 @@ def parse():
     ap.add_argument("--no-queries", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-repair", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--workload", default="taylor-green",
                     choices=["taylor-green", "batched", "serving", "precision", "periodic", "repair"])
     ap.add_argument("--rate", type=float, default=2000.0)
@@ -489,6 +490,16 @@ def run_ours(args, rank, world, dist):
     if not args.no_repair:
         repair = repair_measure(1_000_000, args.repair_steps, 3, 2026 + rank, local)
 
+    # the batched form, scaled down to 512 meshes to keep the default run short
+    batched = None
+    if not args.no_batched:
+        r = batched_measure(512, 10, 3, 2, 4 + rank, local)
+        batched = {k: r[k] for k in ("meshes", "points", "steps", "kinetic_pts_steps_per_s", "ms_per_step",
+                                     "flips_per_s", "pipeline_graph", "plain", "speedup_vs_plain",
+                                     "speedup_vs_plain_launch_gaps_included", "same_as_plain", "autotune")}
+        batched["workload"] = ("512 meshes, sizes log-uniform in [100, 1e5], Gaussian walk sigma = 0.1 x spacing, "
+                               "FRNN r = 2 x spacing (the batched configuration at an eighth of its mesh count)")
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": Wm,
@@ -513,7 +524,7 @@ def run_ours(args, rank, world, dist):
             # oracle on every live quad and face of the final mesh (null
             # without the CPU leg); the edge set against the exact rebuild
             "predicate_errors": parity["sign_disagreements"] if parity else None,
-            "parity": parity, "repair": repair,
+            "parity": parity, "repair": repair, "batched": batched,
             "e2e": e2e, "cpu_baseline": cpu, "clocks": clocks,
             # k_step per step, plus k_one_ring + 7 grid-build kernels + k_grid_frnn per step
             "gpu_launches": K * (10 if do_q else 1),
@@ -659,25 +670,21 @@ def run_repair(args, rank, world, dist):
 
 
 # ---------------------------------------------------------------------------
-def run_batched(args, rank, world, dist):
-    """Batched form: many independent meshes (sizes log-uniform in [100, 1e5]),
+def batched_measure(nm, K, Wm, KP, seed, local, dist=None, tune=True):
+    """Batched form: nm independent meshes (sizes log-uniform in [100, 1e5]),
     each with its own Gaussian walk (sigma = 0.1 x its spacing, clamped to its
-    box) and FRNN at r = 2 x its spacing, all stepped by one launch per step;
-    against the plain form, the same meshes stepped one launch per mesh."""
+    box) and FRNN at r = 2 x its spacing.  Kinetic steps of the whole batch in
+    one launch each (CUDA events around the step launch), the whole per-step
+    pipeline (walk, settle, step, FRNN) as the library's captured StepPipeline,
+    and the plain form: the same meshes stepped one launch per mesh."""
     import torch
 
     from mcleap_gb300 import _lib as L
-    from mcleap_gb300 import autotune as AT
     from mcleap_gb300 import batch as MB
-    from mcleap_gb300 import build as B
     from mcleap_gb300 import workloads as W
 
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
     dev = f"cuda:{local}"
-    B.build()
-    K, Wm, nm = args.steps, max(3, args.warmup), args.meshes
-    rng = np.random.default_rng(4 + rank)
+    rng = np.random.default_rng(seed)
     sizes = np.exp(rng.uniform(np.log(100), np.log(1e5), nm)).astype(np.int64)
     t0 = time.perf_counter()
     handles = [MB.build_mesh(W.uniform_points(int(n), 40000 + i)) for i, n in enumerate(sizes)]
@@ -701,6 +708,15 @@ def run_batched(args, rank, world, dist):
     lib = L.lib()
     SEED = 1234
 
+    # the library's captured pipeline (autotuned on clones first); its own
+    # walk counters, so the kinetic run below steps the same states
+    t0 = time.perf_counter()
+    pipe = MB.StepPipeline(batch.clone(), sigma, radius_host, radius, F, seed=SEED, steps_per_graph=1, stream=stream,
+                           tune=tune)
+    t_tune = time.perf_counter() - t0
+    tuned = pipe.batch.tuning()
+    batch.set_tuning(tuned["blocks_per_sm"], tuned["tail_items"], tuned["removal_tile"])
+
     def pipeline_step(m, ctr, dd, outp, s, with_events=None):
         m.walk(sigma, ctr, dd, seed=SEED, stream=s)
         m.settle(dd, stream=s, sync=False)
@@ -713,20 +729,6 @@ def run_batched(args, rank, world, dist):
         if with_events:
             with_events[2].record(s)
 
-    # autotune the launch shape on clones (walk + settle + step per candidate)
-    tune_ctr = torch.zeros(nm, dtype=torch.int64, device=dev)
-
-    def tune_step(m, k, s):
-        with torch.cuda.stream(s):
-            tune_ctr.fill_(10_000 + k)
-        m.walk(sigma, tune_ctr, d, seed=SEED, stream=s)
-        m.settle(d, stream=s, sync=False)
-        L.check(lib.mcl_step(m.handle, L.ptr(d), s.cuda_stream, None))
-
-    t0 = time.perf_counter()
-    best, trials = AT.autotune(batch, tune_step, stream=stream)
-    t_tune = time.perf_counter() - t0
-
     # warm-up, then K timed steps (inputs far larger than L2)
     for k in range(Wm):
         pipeline_step(batch, counter, d, out, stream)
@@ -736,7 +738,6 @@ def run_batched(args, rank, world, dist):
         raise RuntimeError(f"batched warm-up failed: {st}")
     tot0 = batch.totals()
     evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(K)]
-    cp, cf = clocks_start()
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
@@ -755,34 +756,25 @@ def run_batched(args, rank, world, dist):
     flips = tot1["lawson_flips"] - tot0["lawson_flips"] + tot1["removal_flips"] - tot0["removal_flips"]
     wl_items = (tot1["incircle_tests"] - tot0["incircle_tests"]) - K * (E - 4 * nm)
 
-    # the whole per-step pipeline (walk, settle, step, FRNN) as a CUDA graph of two steps
-    graph = None
-    try:
-        g = torch.cuda.CUDAGraph()
-        with torch.cuda.graph(g, stream=stream):
-            for _ in range(2):
-                pipeline_step(batch, counter, d, out, stream)
-        reps = max(1, K // 2)
-        ge = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
-        with torch.cuda.stream(stream):
-            for r in range(reps):
-                ge[r][0].record(stream)
-                g.replay()
-                ge[r][1].record(stream)
-        stream.synchronize()
-        if batch.totals()["failed_launches"] != tot1["failed_launches"]:
-            raise RuntimeError("a replayed step failed")
-        gms = np.array([a.elapsed_time(b) for a, b in ge]) / 2
-        graph = {"ms_per_step": float(gms.mean()), "p50": float(np.median(gms)), "p99": float(np.percentile(gms, 99)),
-                 "pts_steps_per_s": npts / (gms.mean() / 1e3), "steps": 2 * reps,
-                 "contents": "walk + settle + step + per-mesh FRNN, two steps per graph"}
-    except Exception as ex:  # noqa: BLE001 - reported, not fatal
-        graph = {"unavailable": str(ex)[:200]}
-    clocks = clocks_stop(cp, cf, local)
+    # the whole per-step pipeline, replayed from the captured graph
+    for _ in range(Wm):
+        pipe.replay()
+    ge = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    with torch.cuda.stream(stream):
+        for r in range(K):
+            ge[r][0].record(stream)
+            pipe.replay()
+            ge[r][1].record(stream)
+    pipe.check()
+    gms = np.array([a.elapsed_time(b) for a, b in ge])
+    graph = {"ms_per_step": float(gms.mean()), "p50": float(np.median(gms)), "p99": float(np.percentile(gms, 99)),
+             "pts_steps_per_s": npts / (gms.mean() / 1e3), "steps": K,
+             "contents": "mcleap_gb300.batch.StepPipeline: walk + settle + step + per-mesh grid FRNN, one CUDA "
+                         "graph replay per step"}
+    pipe.batch.close()
 
     # plain form: the same meshes, one launch per mesh (device time of the
     # steps only: host launch gaps are not counted against it)
-    KP = args.plain_steps
     ctrs = torch.zeros(nm, dtype=torch.int64, device=dev)
     pe = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(nm)]
           for _ in range(KP)]
@@ -818,17 +810,14 @@ def run_batched(args, rank, world, dist):
     check = sorted(set([0, nm - 1, int(np.argmax(sizes)), int(np.argmin(sizes))] +
                        rng.choice(nm, size=min(nm, 12), replace=False).tolist()))
     same = all(np.array_equal(verify.edges(i), singles[i].edges(0)) for i in check)
-
-    line = {
-        "metric": "batched kinetic pts*steps/s (move + untangle + Delaunay restore), one launch per step",
-        "value": world * npts * K / kin_s, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": Wm,
-        "ms_per_step": 1e3 * kin_s / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"batched: {nm} meshes, sizes log-uniform in [100, 1e5] (seed 4), Gaussian walk "
-                               "sigma = 0.1 x spacing clamped to each mesh's box, FRNN r = 2 x spacing",
-                   "meshes": nm, "points": npts, "vertices": V, "edges": E,
-                   "l2": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{world}"},
-        "flips_per_s": world * flips / kin_s,
+    for m in singles:
+        m.close()
+    verify.close()
+    batch.close()
+    return {
+        "meshes": nm, "points": npts, "vertices": V, "edges": E, "steps": K, "warmup": Wm,
+        "kinetic_pts_steps_per_s": npts * K / kin_s, "ms_per_step": 1e3 * kin_s / K, "kin_s": kin_s,
+        "flips_per_s": flips / kin_s,
         "step_ms": {"p50": float(np.median(step_ms)), "p99": float(np.percentile(step_ms, 99)),
                     "max": float(step_ms.max())},
         "per_step": {"flips": flips / K, "worklist_items": wl_items / K},
@@ -839,16 +828,44 @@ def run_batched(args, rank, world, dist):
                   "launch_gaps_included_pts_steps_per_s": npts * KP / plain_wall_s,
                   "ms_per_step": 1e3 * plain_step_s / KP, "failed_meshes": bad},
         "speedup_vs_plain": (npts * K / kin_s) / (npts * KP / plain_step_s),
+        "speedup_vs_plain_launch_gaps_included": (npts * K / kin_s) / (npts * KP / plain_wall_s),
         "same_as_plain": {"meshes_checked": len(check), "identical": same},
-        "autotune": {"best": best, "trials": len(trials), "seconds": t_tune},
+        "autotune": {"best": pipe.tuned, "seconds": t_tune},
         "predicates": {k: tot1[k] - tot0[k] for k in ("incircle_tests", "incircle_fp64", "incircle_exact",
                                                       "orient_fp64", "orient_exact", "sos_decisions")},
+        "setup_s": {"build_meshes": t_build, "batch": t_batch},
+    }
+
+
+def run_batched(args, rank, world, dist):
+    """The batched form at its full size (4096 meshes), one JSON line."""
+    import torch
+
+    from mcleap_gb300 import build as B
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    B.build()
+    cp, cf = clocks_start()
+    r = batched_measure(args.meshes, args.steps, max(3, args.warmup), args.plain_steps, 4 + rank, local, dist)
+    clocks = clocks_stop(cp, cf, local)
+    line = {
+        "metric": "batched kinetic pts*steps/s (move + untangle + Delaunay restore), one launch per step",
+        "value": world * r["kinetic_pts_steps_per_s"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": r["warmup"], "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"batched: {r['meshes']} meshes, sizes log-uniform in [100, 1e5] (seed 4), Gaussian "
+                               "walk sigma = 0.1 x spacing clamped to each mesh's box, FRNN r = 2 x spacing",
+                   "meshes": r["meshes"], "points": r["points"], "vertices": r["vertices"], "edges": r["edges"],
+                   "l2": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{world}"},
+        "clocks": clocks,
         # per step: k_walk + k_advance, k_settle, k_step, and the grid FRNN
         # (k_bgrid_hash, 3 scan kernels, k_bgrid_scatter, k_grid_sort_cells,
         # k_gather, k_bgrid_frnn)
-        "clocks": clocks, "gpu_launches": K * 12,
-        "setup_s": {"build_meshes": t_build, "batch": t_batch},
+        "gpu_launches": args.steps * 12,
     }
+    line.update({k: v for k, v in r.items() if k not in ("kin_s", "steps", "warmup", "meshes", "points", "vertices",
+                                                        "edges", "ms_per_step")})
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -898,12 +915,12 @@ def serving_measure(nm, rate, duration, drain, budget_gb, seed):
                                           "query_vertices_per_s", "requests_per_s")}
     cap["speedup_pts_steps"] = cap["served"]["pts_steps_per_s"] / max(cap["plain"]["pts_steps_per_s"], 1e-9)
     cap["speedup_requests"] = cap["served"]["requests_per_s"] / max(cap["plain"]["requests_per_s"], 1e-9)
-    frozen = float(server.frozen.float().mean().item())
+    frozen = server.frozen_fraction()
     info = {"meshes": server.n, "points": int(sizes.sum()), "admitted": len(server.admitted),
             "rejected": len(server.rejected), "budget_used_gb": server.admission.used / 1e9,
             "rate": rate, "duration_s": duration, "setup_s": t_setup, "launches": launches,
             "capacity": cap, "frozen_fraction_at_end": frozen}
-    server.batch.close()
+    server.close()
     return served, plain, info
 
 

@@ -112,6 +112,13 @@ int mcl_mesh_download_aos(mcl_mesh* m, mcl_float2* pos_host, int32_t* v_host, in
 /* transferToDevice (include/Device_Triangulation.h:255-263) with new host arrays of
  * the same sizes. */
 int mcl_mesh_upload_aos(mcl_mesh* m, const mcl_aos_view* aos_host);
+/* DeviceTriangulation's public device arrays m_v / m_he / m_t
+ * (include/Device_Triangulation.h:139-142): the reference's AoS records
+ * (Vertex {id, he}, HalfEdge {next, v, t, op}, Triangle {he}) written into
+ * caller-owned device buffers of V, 2E and T records, with the face numbering
+ * of mcl_mesh_download_aos.  Any pointer may be NULL.  Asynchronous on
+ * `stream`; the first call allocates the conversion scratch. */
+int mcl_mesh_export_aos(mcl_mesh* m, int32_t* v_dev, int32_t* he_dev, int32_t* t_dev, void* stream);
 
 /* m_pos: the device position array (float2[V]).  The pointer changes after every
  * call that moves points (positions are double-buffered); fetch it again. */
@@ -318,6 +325,13 @@ int mcl_mesh_clone(const mcl_mesh* src, mcl_mesh** out);
  * the work-list size at or below which one block finishes the flip rounds
  * (0 = 2048).  Results do not depend on either. */
 int mcl_mesh_set_tuning(mcl_mesh* m, int blocks_per_sm, int tail_items);
+/* Work-list tile of the repair's removal rounds: how many lanes of each warp
+ * take entries of the vertex list (1..32; 0 = automatic, as few as let one
+ * pass over the grid take the list).  A removal is a long divergent chain,
+ * so fewer lanes per warp run faster when the grid has warps to spare.
+ * Results do not depend on it.  No reference counterpart. */
+int mcl_mesh_set_removal_tile(mcl_mesh* m, int tile);
+int mcl_mesh_get_removal_tile(const mcl_mesh* m, int* tile);
 
 /* Repair sub-steps per kinetic step (default 0: every vertex sent back while
  * untangling is removed and reinserted at its target).  A sub-step moves the
@@ -342,6 +356,12 @@ int mcl_mesh_get_tuning(const mcl_mesh* m, int* blocks_per_sm, int* tail_items, 
  * captured CUDA graph replays new steps. */
 int mcl_walk(mcl_mesh* m, const float* sigma_dev, const uint8_t* frozen_dev, uint64_t seed, uint64_t* counter_dev,
              float lo, float hi, mcl_float2* d_dev, void* stream);
+/* mcl_walk with the generator key of mesh c taken from seeds_dev[c]
+ * (uint64[meshes]) instead of seed + c, so a mesh keeps its own draws when it
+ * moves to another batch or position in a batch (the serving layer regroups
+ * meshes as they arrive and leave).  No reference counterpart. */
+int mcl_walk_seeded(mcl_mesh* m, const float* sigma_dev, const uint8_t* frozen_dev, const uint64_t* seeds_dev,
+                    uint64_t* counter_dev, float lo, float hi, mcl_float2* d_dev, void* stream);
 /* Refuse moves that would put two vertices of one mesh at the same point: while
  * two vertices sit at one point, each of them that moves is sent back (its
  * displacement zeroed).  The result does not depend on thread order; vertices

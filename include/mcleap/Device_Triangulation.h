@@ -9,8 +9,15 @@
 //  - neighbour lists start at the smallest neighbour id (clockwise, as the
 //    reference walks) and FRNN lists are sorted ascending;
 //  - getFRNN ignores the ring table argument (the search walks the mesh);
-//  - calls return false (and keep the error in mcl_last_error()) on failure.
+//  - calls return false (and keep the error in mcl_last_error()) on failure;
+//  - m_v, m_he, m_t are device copies of the mesh in the reference's records,
+//    rewritten from the engine's own layout after every call that changes
+//    the topology (construction, transferToDevice, untangle, delonize, step,
+//    the single-point moves): read them, do not write them (a write is not
+//    seen by the engine; change the host arrays and call transferToDevice).
 #pragma once
+
+#include <cuda_runtime.h>
 
 #include "Host_Triangulation.h"
 
@@ -18,6 +25,9 @@ struct DeviceTriangulation {
   HostTriangulation* h_triangulation;
   int m_pos_size = 0, m_v_size = 0, m_he_size = 0, m_t_size = 0;
   glm::vec2* m_pos = nullptr;
+  Vertex* m_v = nullptr;
+  HalfEdge* m_he = nullptr;
+  Triangle* m_t = nullptr;
   mcl_mesh* mesh = nullptr;
   mcl_step_stats last_stats{};
 
@@ -37,13 +47,23 @@ struct DeviceTriangulation {
     m_pos_size = m_v_size = (int)V;
     m_he_size = (int)HE;
     m_t_size = (int)T;
+    const bool ok = cudaMalloc((void**)&m_v, sizeof(Vertex) * (size_t)V) == cudaSuccess &&
+                    cudaMalloc((void**)&m_he, sizeof(HalfEdge) * (size_t)HE) == cudaSuccess &&
+                    cudaMalloc((void**)&m_t, sizeof(Triangle) * (size_t)(T > 0 ? T : 1)) == cudaSuccess;
+    if (!ok) mcleap_detail::check(MCL_ERR_OUT_OF_MEMORY);
     refresh();
-    return true;
+    return export_aos();
   }
   bool freeMemory() {
     if (mesh) mcl_mesh_destroy(mesh);
     mesh = nullptr;
     m_pos = nullptr;
+    cudaFree(m_v);
+    cudaFree(m_he);
+    cudaFree(m_t);
+    m_v = nullptr;
+    m_he = nullptr;
+    m_t = nullptr;
     return true;
   }
   bool transferToHost() {
@@ -54,7 +74,7 @@ struct DeviceTriangulation {
     mcl_aos_view a = h_triangulation->view();
     const bool ok = mcl_mesh_upload_aos(mesh, &a) == MCL_OK;
     refresh();
-    return ok;
+    return ok && export_aos();
   }
 
   bool delonize() { return restore(); }
@@ -85,7 +105,7 @@ struct DeviceTriangulation {
   bool step(glm::vec2* d) {
     const bool ok = mcl_step(mesh, reinterpret_cast<const mcl_float2*>(d), nullptr, &last_stats) == MCL_OK;
     refresh();
-    return ok;
+    return ok && export_aos();
   }
 
   template <int maxRingSize>
@@ -124,7 +144,12 @@ struct DeviceTriangulation {
     const bool ok =
         mcl_step_host(mesh, reinterpret_cast<const mcl_float2*>(one_.data()), nullptr, &last_stats) == MCL_OK;
     refresh();
-    return ok;
+    return ok && export_aos();
+  }
+  // m_v / m_he / m_t from the engine's layout (default stream)
+  bool export_aos() {
+    return mcl_mesh_export_aos(mesh, reinterpret_cast<int32_t*>(m_v), reinterpret_cast<int32_t*>(m_he),
+                               reinterpret_cast<int32_t*>(m_t), nullptr) == MCL_OK;
   }
   void refresh() {
     mcl_float2* p = nullptr;
@@ -134,6 +159,6 @@ struct DeviceTriangulation {
   bool restore() {
     const bool ok = mcl_delaunay_restore(mesh, nullptr, &last_stats) == MCL_OK;
     refresh();
-    return ok;
+    return ok && export_aos();
   }
 };

@@ -38,7 +38,8 @@ EXPORTS = [
     "mcl_batch_frnn", "mcl_mesh_clone", "mcl_mesh_set_tuning", "mcl_mesh_get_tuning", "mcl_mesh_set_substeps", "mcl_walk",
     "mcl_settle_moves", "mcl_dla_freeze", "mcl_batch_frnn_list", "mcl_one_ring_list", "mcl_batch_set_active", "mcl_batch_frnn_grid",
     "mcl_grid_mean_occupancy", "mcl_debug_predicates_host", "mcl_debug_predicates_device", "mcl_mesh_validate", "mcl_debug_state", "mcl_debug_timeline", "mcl_grid_frnn_noalloc", "mcl_debug_counters",
-    "mcl_debug_insert_timeline", "mcl_debug_remove_timeline",
+    "mcl_debug_insert_timeline", "mcl_debug_remove_timeline", "mcl_mesh_export_aos", "mcl_walk_seeded",
+    "mcl_mesh_set_removal_tile", "mcl_mesh_get_removal_tile",
     "mcl_periodic_build", "mcl_periodic_create", "mcl_periodic_destroy", "mcl_periodic_sizes", "mcl_periodic_download",
     "mcl_periodic_positions", "mcl_periodic_step", "mcl_periodic_from_planar", "mcl_periodic_one_ring",
     "mcl_periodic_closest", "mcl_periodic_frnn", "mcl_periodic_step_host",
@@ -119,6 +120,10 @@ def lib():
             "mcl_debug_counters": ([vp, vp, i32], i32),
             "mcl_debug_insert_timeline": ([vp, vp], i32),
             "mcl_debug_remove_timeline": ([vp, vp], i32),
+            "mcl_mesh_export_aos": ([vp, vp, vp, vp, vp], i32),
+            "mcl_walk_seeded": ([vp, vp, vp, vp, vp, f32, f32, vp, vp], i32),
+            "mcl_mesh_set_removal_tile": ([vp, i32], i32),
+            "mcl_mesh_get_removal_tile": ([vp, C.POINTER(i32)], i32),
             "mcl_grid_frnn_noalloc": ([vp, i64, f32, f32, f32, f32, i32, i32, i32, f32, i32, vp, vp, vp, vp, vp,
                                        C.POINTER(i64)], i32),
             "mcl_debug_predicates_device": ([i32, vp, vp, i64, vp, vp, vp], i32),

@@ -104,17 +104,20 @@ class MeshBatch:
         L.check(L.lib().mcl_mesh_clone(self.handle, C.byref(out)))
         return MeshBatch(out)
 
-    def set_tuning(self, blocks_per_sm=0, tail_items=0):
+    def set_tuning(self, blocks_per_sm=0, tail_items=0, removal_tile=None):
         L.check(L.lib().mcl_mesh_set_tuning(self.handle, int(blocks_per_sm), int(tail_items)))
+        if removal_tile is not None:
+            L.check(L.lib().mcl_mesh_set_removal_tile(self.handle, int(removal_tile)))
 
     def set_substeps(self, substeps):
         """Repair sub-steps per step (0: straight to removal and reinsertion)."""
         L.check(L.lib().mcl_mesh_set_substeps(self.handle, int(substeps)))
 
     def tuning(self):
-        a, b, c = C.c_int(), C.c_int(), C.c_int()
+        a, b, c, t = C.c_int(), C.c_int(), C.c_int(), C.c_int()
         L.check(L.lib().mcl_mesh_get_tuning(self.handle, C.byref(a), C.byref(b), C.byref(c)))
-        return dict(blocks_per_sm=a.value, tail_items=b.value, max_blocks_per_sm=c.value)
+        L.check(L.lib().mcl_mesh_get_removal_tile(self.handle, C.byref(t)))
+        return dict(blocks_per_sm=a.value, tail_items=b.value, max_blocks_per_sm=c.value, removal_tile=t.value)
 
     # -- stepping and motion -------------------------------------------------------
     def step(self, d, stream=None, stats=True):
@@ -144,9 +147,14 @@ class MeshBatch:
         return out
 
     def walk(self, sigma, counter, d, seed=0, frozen=None, lo=0.0, hi=float(np.nextafter(np.float32(8192), 0)),
-             stream=None):
+             stream=None, seeds=None):
         """Gaussian random-walk displacements into ``d`` (sigma and step counter
-        per mesh, device arrays)."""
+        per mesh, device arrays); ``seeds`` (uint64 device array, one key per
+        mesh) replaces the keys seed + mesh index."""
+        if seeds is not None:
+            L.check(L.lib().mcl_walk_seeded(self.handle, L.ptr(sigma), L.ptr(frozen), L.ptr(seeds), L.ptr(counter),
+                                            float(lo), float(hi), L.ptr(d), _stream_ptr(stream)))
+            return
         L.check(L.lib().mcl_walk(self.handle, L.ptr(sigma), L.ptr(frozen), int(seed), L.ptr(counter), float(lo),
                                  float(hi), L.ptr(d), _stream_ptr(stream)))
 
@@ -208,3 +216,71 @@ class MeshBatch:
         L.check(L.lib().mcl_one_ring(self.handle, layout, int(max_ring), L.ptr(out), _stream_ptr(stream),
                                      C.byref(tr) if sync else None))
         return tr.value if sync else None
+
+
+class StepPipeline:
+    """The per-step pipeline of a batch of random-walk meshes: Gaussian walk
+    (sigma per mesh, clamped to each mesh's box), coincident moves settled, the
+    kinetic step, and per-mesh grid FRNN (radius per mesh) into ``out`` (ROW
+    layout, ``max_frnn`` slots per vertex) -- captured once in a CUDA graph of
+    ``steps_per_graph`` steps and replayed.  Walk counters advance on the
+    device, so every replay draws new steps.  With ``tune`` the launch shape
+    (blocks per SM, single-block flip-round threshold, removal tile) is
+    autotuned on clones first.  The reference steps one DeviceTriangulation
+    per call (include/Device_Triangulation.h:324-351, :461-495)."""
+
+    def __init__(self, batch, sigma, radius_host, radius, max_frnn, seed=0, steps_per_graph=1, stream=None,
+                 tune=False, frnn=True):
+        import torch
+
+        self.torch = torch
+        self.batch = batch
+        self.sigma, self.radius, self.radius_host = sigma, radius, np.ascontiguousarray(radius_host, np.float32)
+        self.max_frnn, self.seed, self.frnn = int(max_frnn), int(seed), frnn
+        self.stream = stream or torch.cuda.Stream()
+        dev = sigma.device
+        self.counter = torch.zeros(batch.count, dtype=torch.int64, device=dev)
+        self.d = torch.zeros((batch.V, 2), dtype=torch.float32, device=dev)
+        self.out = torch.empty(batch.V * self.max_frnn, dtype=torch.int32, device=dev)
+        self.tuned = None
+        if tune:
+            from .autotune import autotune
+
+            tune_ctr = torch.zeros(batch.count, dtype=torch.int64, device=dev)
+
+            def one(m, k, s):
+                with torch.cuda.stream(s):
+                    tune_ctr.fill_(1 << 40 | k)
+                m.walk(self.sigma, tune_ctr, self.d, seed=self.seed, stream=s)
+                m.settle(self.d, stream=s, sync=False)
+                L.check(L.lib().mcl_step(m.handle, L.ptr(self.d), s.cuda_stream, None))
+
+            self.tuned, _ = autotune(batch, one, stream=self.stream)
+        # first calls allocate their scratch: run one step outside the capture
+        self._launch()
+        self.stream.synchronize()
+        self.failed0 = batch.totals()["failed_launches"]
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph, stream=self.stream):
+            for _ in range(steps_per_graph):
+                self._launch()
+        self.steps_per_graph = steps_per_graph
+
+    def _launch(self):
+        b, s = self.batch, self.stream
+        b.walk(self.sigma, self.counter, self.d, seed=self.seed, stream=s)
+        b.settle(self.d, stream=s, sync=False)
+        L.check(L.lib().mcl_step(b.handle, L.ptr(self.d), s.cuda_stream, None))
+        if self.frnn:
+            b.frnn_grid(self.radius_host, self.radius, self.max_frnn, self.out, stream=s, sync=False)
+
+    def replay(self):
+        """Launch ``steps_per_graph`` steps (asynchronous on the pipeline's stream)."""
+        self.graph.replay()
+
+    def check(self):
+        """Wait for the replays and raise if any captured step failed."""
+        self.stream.synchronize()
+        st = self.batch.status(self.stream)
+        if st["status"] != 0 or self.batch.totals()["failed_launches"] != self.failed0:
+            raise RuntimeError(f"a replayed step failed: {st}")

@@ -95,6 +95,7 @@ __device__ __forceinline__ float2 normal2(unsigned long long seed, unsigned long
 __global__ void k_walk(ActV A, const float2* __restrict__ pos, const unsigned char* __restrict__ vfix,
                        const int* __restrict__ vcomp, const int* __restrict__ cbase, const float* __restrict__ sigma,
                        const unsigned char* __restrict__ frozen, unsigned long long seed,
+                       const unsigned long long* __restrict__ seeds,
                        const unsigned long long* __restrict__ counter, float lo, float hi, float2* __restrict__ d) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= A.V_it) return;
@@ -103,7 +104,7 @@ __global__ void k_walk(ActV A, const float2* __restrict__ pos, const unsigned ch
   if (!vfix[v] && !(frozen && frozen[v])) {
     const int c = vcomp ? vcomp[v] : 0;
     const float sg = sigma[c];
-    const float2 z = normal2(seed + (unsigned long long)c, counter[c], cbase ? v - cbase[c] : v);
+    const float2 z = normal2(seeds ? seeds[c] : seed + (unsigned long long)c, counter[c], cbase ? v - cbase[c] : v);
     const float2 p = pos[v];
     const float tx = fminf(fmaxf(__fadd_rn(p.x, __fmul_rn(sg, z.x)), lo), hi);
     const float ty = fminf(fmaxf(__fadd_rn(p.y, __fmul_rn(sg, z.y)), lo), hi);
@@ -358,6 +359,7 @@ int mcl_mesh_clone(const mcl_mesh* src, mcl_mesh** out) {
     std::memcpy(m->comp_host, src->comp_host, sizeof(int64_t) * 4 * src->ncomp);
   }
   m->tail_items = src->tail_items;
+  m->rm_tile = src->rm_tile;
   m->coop_blocks = src->coop_blocks;
   if (src->substeps > 0 && (rc = mcl_mesh_set_substeps(m, src->substeps)) != MCL_OK) {
     free_mesh(m);
@@ -429,6 +431,18 @@ int mcl_mesh_set_tuning(mcl_mesh* m, int blocks_per_sm, int tail_items) {
   return MCL_OK;
 }
 
+int mcl_mesh_set_removal_tile(mcl_mesh* m, int tile) {
+  if (!m || tile < 0 || tile > 32) return fail(MCL_ERR_INVALID_ARGUMENT, "removal tile must be in [0, 32]");
+  m->rm_tile = tile;
+  return MCL_OK;
+}
+
+int mcl_mesh_get_removal_tile(const mcl_mesh* m, int* tile) {
+  if (!m || !tile) return fail(MCL_ERR_INVALID_ARGUMENT, "null argument");
+  *tile = m->rm_tile;
+  return MCL_OK;
+}
+
 int mcl_mesh_set_substeps(mcl_mesh* m, int substeps) {
   if (!m || substeps < 0 || substeps > 64) return fail(MCL_ERR_INVALID_ARGUMENT, "substeps must be in [0, 64]");
   if (substeps > 0 && !m->vl2) {
@@ -453,8 +467,9 @@ int mcl_mesh_get_tuning(const mcl_mesh* m, int* blocks_per_sm, int* tail_items, 
   return MCL_OK;
 }
 
-int mcl_walk(mcl_mesh* m, const float* sigma_dev, const uint8_t* frozen_dev, uint64_t seed,
-             uint64_t* counter_dev, float lo, float hi, mcl_float2* d_dev, void* stream) {
+static int walk(mcl_mesh* m, const float* sigma_dev, const uint8_t* frozen_dev, uint64_t seed,
+                const uint64_t* seeds_dev, uint64_t* counter_dev, float lo, float hi, mcl_float2* d_dev,
+                void* stream) {
   if (!m || !sigma_dev || !counter_dev || !d_dev || !(lo <= hi)) return fail(MCL_ERR_INVALID_ARGUMENT, "bad args");
   cudaStream_t s = (cudaStream_t)stream;
   const int V = (int)m->V;
@@ -462,7 +477,8 @@ int mcl_walk(mcl_mesh* m, const float* sigma_dev, const uint8_t* frozen_dev, uin
   (void)V;
   if (A.V_it > 0)
     k_walk<<<(A.V_it + 255) / 256, 256, 0, s>>>(A, m->pos[m->cur], m->vfix, m->vcomp, m->cbase, sigma_dev, frozen_dev,
-                                                seed, reinterpret_cast<const unsigned long long*>(counter_dev), lo, hi,
+                                                seed, reinterpret_cast<const unsigned long long*>(seeds_dev),
+                                                reinterpret_cast<const unsigned long long*>(counter_dev), lo, hi,
                                                 reinterpret_cast<float2*>(d_dev));
   const int na = m->nact ? m->nact : (int)m->ncomp;
   k_advance<<<(na + 255) / 256, 256, 0, s>>>(reinterpret_cast<unsigned long long*>(counter_dev), m->nact,
@@ -470,6 +486,17 @@ int mcl_walk(mcl_mesh* m, const float* sigma_dev, const uint8_t* frozen_dev, uin
                                              (int)m->ncomp);
   BCK(cudaGetLastError());
   return MCL_OK;
+}
+
+int mcl_walk(mcl_mesh* m, const float* sigma_dev, const uint8_t* frozen_dev, uint64_t seed,
+             uint64_t* counter_dev, float lo, float hi, mcl_float2* d_dev, void* stream) {
+  return walk(m, sigma_dev, frozen_dev, seed, nullptr, counter_dev, lo, hi, d_dev, stream);
+}
+
+int mcl_walk_seeded(mcl_mesh* m, const float* sigma_dev, const uint8_t* frozen_dev, const uint64_t* seeds_dev,
+                    uint64_t* counter_dev, float lo, float hi, mcl_float2* d_dev, void* stream) {
+  if (!seeds_dev) return fail(MCL_ERR_INVALID_ARGUMENT, "mcl_walk_seeded: null seed table");
+  return walk(m, sigma_dev, frozen_dev, 0, seeds_dev, counter_dev, lo, hi, d_dev, stream);
 }
 
 int mcl_settle_moves(mcl_mesh* m, mcl_float2* d_dev, void* stream, int64_t* sent_back_host) {

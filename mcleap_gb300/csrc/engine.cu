@@ -1055,11 +1055,12 @@ __device__ bool phase_remove(cg::grid_group& g, const KParams& P, unsigned& stam
       P.st->vl_count[dst] = 0;
       P.st->c[C_REMOVE_ROUNDS] += 1;
     }
-    // A removal is a long divergent chain (star loads, ear search, writes):
-    // when the list fits, each warp takes one vertex (lane 0), so no warp runs
-    // several of them side by side; else the spread order.
-    const bool sparse = n <= nwarps;
-    const int i0 = sparse ? (lane == 0 ? wid : n) : spread_tid(), di = sparse ? n : stride;
+    // A removal is a long divergent chain (star loads, ear search, writes), so
+    // a warp runs its lanes' removals largely one after another: entries are
+    // dealt in tiles of T lanes per warp (entry i: warp (i / T) mod warps,
+    // lane i mod T), by default as few lanes as let one pass take the list.
+    const int T = P.rm_tile > 0 ? min(P.rm_tile, 32) : max(1, min(32, (n + nwarps - 1) / nwarps));
+    const int i0 = lane < T ? wid * T + lane : n, di = nwarps * T;
     // claim every face of the star (the thread keeps the last star it walked)
     sc.v = -1;
     for (int i = i0; i < n; i += di) {
@@ -1091,8 +1092,8 @@ __device__ bool phase_remove(cg::grid_group& g, const KParams& P, unsigned& stam
     g.sync();
     if (round < 16) timeline_remove(P, 4 * round + 1);
     int removed = 0, flips = 0;
-    for (int base = sparse ? wid : spread_tid() - lane; base < n; base += sparse ? nwarps : stride) {
-      const int i = sparse ? (lane == 0 ? base : n) : base + lane;
+    for (int base = wid * T; base < n; base += di) {
+      const int i = lane < T ? base + lane : n;
       int mine[1];
       int k = 0;
       if (i < n) {
@@ -1893,7 +1894,7 @@ void free_mesh(mcl_mesh* m) {
                   m->vaux, m->vloc, m->vlocf, m->target, m->vprev, m->vl2, m->dstage, m->scratch, m->st,
                   m->vcomp, m->vroot, m->cbase, m->table, m->smark, m->fnew, m->act_dev,
                   m->bg_cell, m->bg_src, m->bg_perm, m->bg_pos, m->bg_count, m->bg_start, m->bg_cursor,
-                  m->bg_tmp, m->bg_par};
+                  m->bg_tmp, m->bg_par, m->aos_tmp};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (m->dstage2) cudaFree(m->dstage2);
@@ -2174,6 +2175,7 @@ static KParams make_params(mcl_mesh* m, int mode) {
   P.max_rounds = 1 << 16;
   P.walk_cap = 1 << 18;
   P.tail_items = m->tail_items;
+  P.rm_tile = m->rm_tile;
   P.substeps = m->vl2 ? m->substeps : 0;  // no scratch, no sub-steps
   P.vroot = m->vroot;
   P.nact = m->nact;

@@ -140,6 +140,7 @@ struct KParams {
   int max_rounds;
   int walk_cap;
   int tail_items;          // flip rounds with at most this many queued edges run in one block
+  int rm_tile;             // lanes of a warp that take removal-list entries (0: as few as fit one pass)
   int substeps;            // repair sub-steps before removal
   mcl_step_stats* stats_out;  // device-visible host record the launch fills at its end (or NULL)
   const int* vroot;        // per vertex: a never-freed half-edge of its mesh (batches); NULL = half-edge 0
@@ -360,6 +361,7 @@ struct mcl_mesh {
   int nsm;                 // SMs of the device
   int max_blocks_per_sm;   // k_step occupancy limit
   int tail_items;          // single-block flip-round threshold
+  int rm_tile;             // removal tile (mcl_mesh_set_removal_tile; 0 = automatic)
   int substeps;            // repair sub-steps before removal (mcl_mesh_set_substeps)
   // batches: a mesh made of independent components (mcl_batch_create)
   int64_t ncomp;           // 1 for a plain mesh
@@ -393,6 +395,9 @@ struct mcl_mesh {
   int* act_host;           // pinned staging of the same
   int* act_list;           // host: the active mesh ids
   unsigned char* dirty;    // host, per mesh: its two position buffers differ
+  // mcl_mesh_export_aos: per half-edge face-owner flags and their prefix sums
+  int* aos_tmp;
+  int64_t aos_cap;         // ints aos_tmp holds
 };
 
 // Host-side helpers shared by the translation units of the library.

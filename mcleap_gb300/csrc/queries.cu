@@ -1345,3 +1345,78 @@ extern "C" int mcl_grid_frnn_noalloc(const mcl_float2* pos, int64_t n, float min
   }
   return MCL_OK;
 }
+
+// ---------------------------------------------------------------------------
+// The reference's AoS mesh arrays written on the device (DeviceTriangulation's
+// public m_v / m_he / m_t, include/Device_Triangulation.h:139-142), in the
+// layout and face numbering of mcl_mesh_download_aos: faces numbered in the
+// order of their smallest half-edge.
+namespace {
+
+__device__ __forceinline__ bool aos_owner(const int4* ev, const int4* en, int64_t h, int* nxt, int* prv) {
+  const int4 q = ev[h >> 1], w = en[h >> 1];
+  const bool odd = h & 1;
+  const int org = odd ? q.y : q.x, apex = odd ? q.w : q.z;
+  *nxt = odd ? w.z : w.x;
+  *prv = odd ? w.w : w.y;
+  return apex >= 0 && org >= 0;
+}
+
+__global__ void k_aos_flags(const int4* ev, const int4* en, int64_t HE, int* flag) {
+  const int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (h >= HE) return;
+  int n, p;
+  const bool inner = aos_owner(ev, en, h, &n, &p);
+  flag[h] = inner && h < n && h < p ? 1 : 0;
+}
+
+__global__ void k_aos_write(const int4* ev, const int4* en, const int* vhe, int64_t V, int64_t HE, const int* fid,
+                            int* v, int* he, int* t) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < HE) {
+    int n, p;
+    const bool inner = aos_owner(ev, en, i, &n, &p);
+    const int4 q = ev[i >> 1];
+    const bool odd = i & 1;
+    const int org = odd ? q.y : q.x, apex = odd ? q.w : q.z;
+    int face = -1;
+    if (inner) {
+      const int64_t f = min(i, (int64_t)min(n, p));
+      if (f >= 0 && f < HE) face = fid[f];
+      if (t && i < n && i < p) t[fid[i]] = (int)i;
+    }
+    if (he) *reinterpret_cast<int4*>(he + 4 * i) = make_int4(n, org, face, apex >= 0 ? apex : -1);
+  }
+  if (v && i < V) *reinterpret_cast<int2*>(v + 2 * i) = make_int2((int)i, vhe[i]);
+}
+
+}  // namespace
+
+extern "C" int mcl_mesh_export_aos(mcl_mesh* m, int32_t* v_dev, int32_t* he_dev, int32_t* t_dev, void* stream) {
+  if (!m) return qfail(MCL_ERR_INVALID_ARGUMENT, "mcl_mesh_export_aos: null mesh");
+  if (((uintptr_t)v_dev & 7) || ((uintptr_t)he_dev & 15))
+    return qfail(MCL_ERR_INVALID_ARGUMENT, "mcl_mesh_export_aos: m_v must be 8-byte and m_he 16-byte aligned");
+  cudaStream_t s = (cudaStream_t)stream;
+  const int64_t HE = 2 * m->E, nb = (HE + 1023) / 1024;
+  const int64_t need = 2 * HE + 2 * (nb + 2);
+  if (m->aos_cap < need) {
+    if (m->aos_tmp) QCK(cudaFree(m->aos_tmp));
+    m->aos_tmp = nullptr;
+    m->aos_cap = 0;
+    if (cudaMalloc((void**)&m->aos_tmp, 4 * need) != cudaSuccess) {
+      (void)cudaGetLastError();
+      return qfail(MCL_ERR_OUT_OF_MEMORY, "mcl_mesh_export_aos: scratch");
+    }
+    m->aos_cap = need;
+  }
+  int* flag = m->aos_tmp;
+  int* fid = flag + HE;
+  int* tmp = fid + HE;
+  const unsigned gb = (unsigned)((std::max(HE, m->V) + 255) / 256);
+  k_aos_flags<<<(unsigned)((HE + 255) / 256), 256, 0, s>>>(m->ev, m->en, HE, flag);
+  const int rc = scan_exclusive(flag, fid, HE, tmp, tmp + nb + 1, s);
+  if (rc != MCL_OK) return rc;
+  k_aos_write<<<gb, 256, 0, s>>>(m->ev, m->en, m->vhe, m->V, HE, fid, v_dev, he_dev, t_dev);
+  QCK(cudaGetLastError());
+  return MCL_OK;
+}

@@ -152,6 +152,13 @@ class DeviceTriangulation:
         L.check(L.lib().mcl_mesh_positions(self.handle, C.byref(p)))
         return p.value
 
+    def export_aos(self, v=None, he=None, t=None, stream=None):
+        """The reference's public device arrays m_v / m_he / m_t
+        (include/Device_Triangulation.h:139-142) written into caller-owned
+        int32 CUDA tensors of shape (V, 2), (HE, 4), (T,) (any may be None),
+        with the face numbering of transferToHost."""
+        L.check(L.lib().mcl_mesh_export_aos(self.handle, L.ptr(v), L.ptr(he), L.ptr(t), _stream_ptr(stream)))
+
     def positions(self, out=None, stream=None):
         """Copy the current positions into ``out`` (torch CUDA tensor) or a numpy array."""
         if out is None:

@@ -190,6 +190,22 @@ static void test_kinetic() {
       if (!(o > 0)) ++inverted;
     }
     CHECK(inverted == 0, "kinetic step %d: %d faces not positive", step, inverted);
+    // the public device arrays hold the same records as the host download
+    {
+      std::vector<Vertex> dv(ht.m_v.size());
+      std::vector<HalfEdge> dh(ht.m_he.size());
+      std::vector<Triangle> dtr(ht.m_t.size());
+      cudaMemcpy(dv.data(), dt.m_v, sizeof(Vertex) * dv.size(), cudaMemcpyDeviceToHost);
+      cudaMemcpy(dh.data(), dt.m_he, sizeof(HalfEdge) * dh.size(), cudaMemcpyDeviceToHost);
+      cudaMemcpy(dtr.data(), dt.m_t, sizeof(Triangle) * dtr.size(), cudaMemcpyDeviceToHost);
+      int diff = 0;
+      for (size_t i = 0; i < dv.size(); ++i) diff += dv[i].pos_index != ht.m_v[i].pos_index || dv[i].he != ht.m_v[i].he;
+      for (size_t i = 0; i < dh.size(); ++i)
+        diff += dh[i].next != ht.m_he[i].next || dh[i].v != ht.m_he[i].v || dh[i].t != ht.m_he[i].t ||
+                dh[i].op != ht.m_he[i].op;
+      for (size_t i = 0; i < dtr.size(); ++i) diff += dtr[i].he != ht.m_t[i].he;
+      CHECK(diff == 0, "kinetic step %d: device m_v/m_he/m_t differ from the download in %d records", step, diff);
+    }
     std::printf("kinetic step %d removed=%lld flips=%lld inverted_after=%d\n", step,
                 (long long)dt.last_stats.removed_vertices, (long long)dt.last_stats.lawson_flips, inverted);
   }

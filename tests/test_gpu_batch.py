@@ -111,8 +111,8 @@ def test_clone_and_tuning_do_not_change_results(M):
     b = a.clone()
     t = b.tuning()
     assert t["max_blocks_per_sm"] >= 1
-    b.set_tuning(blocks_per_sm=1, tail_items=64)
-    assert b.tuning()["blocks_per_sm"] == 1 and b.tuning()["tail_items"] == 64
+    b.set_tuning(blocks_per_sm=1, tail_items=64, removal_tile=1)
+    assert b.tuning()["blocks_per_sm"] == 1 and b.tuning()["tail_items"] == 64 and b.tuning()["removal_tile"] == 1
     pos = [a.download(i)[0] for i in range(a.count)]
     for k in range(3):
         d = np.concatenate([gaussian_disp(len(pos[i]), 0.4 * spacing(SIZES[i]), 77 * k + i, clamp_pos=pos[i])
@@ -417,3 +417,47 @@ def test_batch_frnn_grid_equals_mesh_walk(M):
     ra, rb = a.view(batch.V, F).cpu().numpy(), b.view(batch.V, F).cpu().numpy()
     assert np.array_equal(ra[:, 0], rb[:, 0])
     assert all(np.array_equal(ra[v, 1:1 + ra[v, 0]], rb[v, 1:1 + ra[v, 0]]) for v in range(batch.V))
+
+
+def test_captured_step_pipeline_equals_direct_steps(M):
+    """StepPipeline (walk + settle + step + per-mesh grid FRNN captured in a
+    CUDA graph, replayed) leaves every mesh exactly as the same calls made
+    one by one, and every mesh the exact Delaunay triangulation; its FRNN rows
+    are the mesh-walk FRNN rows.  Autotuning changes the launch shape only."""
+    import torch
+
+    from mcleap_gb300 import batch as MB
+
+    pts = make_points()
+    a = M.MeshBatch.from_points([p.copy() for p in pts])
+    b = a.clone()
+    sizes = np.array([len(p) for p in pts])
+    h = (8192.0 / np.sqrt(np.maximum(sizes, 1))).astype(np.float32)
+    sigma = torch.tensor(0.3 * h, device="cuda")
+    r_host = (2.0 * h).astype(np.float32)
+    radius = torch.tensor(r_host, device="cuda")
+    F = 48
+    pipe = MB.StepPipeline(a, sigma, r_host, radius, F, seed=9, steps_per_graph=2, tune=True)
+    for _ in range(3):
+        pipe.replay()
+    pipe.check()
+    assert pipe.tuned is not None
+    # the same seven steps (one before the capture, two per replay) made directly
+    ctr = torch.zeros(b.count, dtype=torch.int64, device="cuda")
+    d = torch.zeros((b.V, 2), dtype=torch.float32, device="cuda")
+    for _ in range(7):
+        b.walk(sigma, ctr, d, seed=9)
+        b.settle(d)
+        assert b.step(d)["status"] == 0
+    out = torch.empty(b.V * F, dtype=torch.int32, device="cuda")
+    b.frnn(radius, F, out)
+    for i in range(a.count):
+        assert np.array_equal(a.download(i)[0], b.download(i)[0]), i
+        assert np.array_equal(a.edges(i), b.edges(i)), i
+        assert matches_oracle(a.edges(i), a.download(i)[0]), i
+    rows_a = pipe.out.view(a.V, F).cpu().numpy()
+    rows_b = out.view(b.V, F).cpu().numpy()
+    points_only = np.concatenate([np.arange(int(a.v0[i]) + 4, int(a.v0[i] + a.nv[i])) for i in range(a.count)])
+    for v in points_only:
+        c = rows_b[v, 0]
+        assert rows_a[v, 0] == c and np.array_equal(np.sort(rows_a[v, 1:1 + c]), np.sort(rows_b[v, 1:1 + c])), v

@@ -597,3 +597,29 @@ def test_step_host_async_matches_step(M):
     got = L.StepStats.from_buffer(page).as_dict()
     assert got["status"] == 0 and got["inverted_faces"] == want2["inverted_faces"]
     assert got["incircle_tests"] > 0
+
+
+def test_device_aos_arrays_equal_the_download(M):
+    """DeviceTriangulation's public device arrays m_v / m_he / m_t
+    (reference include/Device_Triangulation.h:139-142), written on the device
+    from the engine's layout, equal the records transferToHost produces, for a
+    built mesh and after repair steps."""
+    import torch
+
+    n = 30000
+    ht, _ = build_pair(M, uniform_points(n, 55))
+    dt = M.DeviceTriangulation(ht)
+    V, HE, T = dt.m_v_size, dt.m_he_size, dt.m_t_size
+    v = torch.empty((V, 2), dtype=torch.int32, device="cuda")
+    he = torch.empty((HE, 4), dtype=torch.int32, device="cuda")
+    t = torch.empty(T, dtype=torch.int32, device="cuda")
+    for k in range(3):
+        dt.export_aos(v, he, t)
+        torch.cuda.synchronize()
+        dt.transferToHost()
+        assert np.array_equal(v.cpu().numpy(), ht.m_v.reshape(V, 2)), k
+        assert np.array_equal(he.cpu().numpy(), ht.m_he.reshape(HE, 4)), k
+        assert np.array_equal(t.cpu().numpy(), ht.m_t.reshape(T)), k
+        d = gaussian_disp(n + 4, 0.3 * spacing(n), 77 + k, clamp_pos=ht.m_pos)
+        st = dt.step(cuda(d))
+        assert st["status"] == 0 and st["inverted_faces"] > 0, st
