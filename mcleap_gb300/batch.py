@@ -224,14 +224,20 @@ class StepPipeline:
     kinetic step, and per-mesh grid FRNN (radius per mesh) into ``out`` (ROW
     layout, ``max_frnn`` slots per vertex) -- captured once in a CUDA graph of
     ``steps_per_graph`` steps and replayed.  Walk counters advance on the
-    device, so every replay draws new steps.  With ``tune`` the launch shape
+    device, so every replay draws new steps.  A step reads the positions from
+    one of the mesh's two position buffers and writes the other, and a graph
+    replays the buffers it was captured with, so it must hold an even number
+    of steps (it then ends on the buffer it starts from).  With ``tune`` the launch shape
     (blocks per SM, single-block flip-round threshold, removal tile) is
     autotuned on clones first.  The reference steps one DeviceTriangulation
     per call (include/Device_Triangulation.h:324-351, :461-495)."""
 
-    def __init__(self, batch, sigma, radius_host, radius, max_frnn, seed=0, steps_per_graph=1, stream=None,
+    def __init__(self, batch, sigma, radius_host, radius, max_frnn, seed=0, steps_per_graph=2, stream=None,
                  tune=False, frnn=True):
         import torch
+
+        if steps_per_graph < 2 or steps_per_graph % 2:
+            raise ValueError("steps_per_graph must be even: a replay must end on the position buffer it starts from")
 
         self.torch = torch
         self.batch = batch
@@ -260,10 +266,13 @@ class StepPipeline:
         self._launch()
         self.stream.synchronize()
         self.failed0 = batch.totals()["failed_launches"]
+        before = batch.positions_ptr
         self.graph = torch.cuda.CUDAGraph()
         with torch.cuda.graph(self.graph, stream=self.stream):
             for _ in range(steps_per_graph):
                 self._launch()
+        if batch.positions_ptr != before:
+            raise RuntimeError("the captured steps do not end on the position buffer they start from")
         self.steps_per_graph = steps_per_graph
 
     def _launch(self):
