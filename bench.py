@@ -895,6 +895,7 @@ def serving_measure(nm, rate, duration, drain, budget_gb, seed):
     done = server.serve(reqs, batched=True, realtime=True, time_limit=duration + drain)
     served = S.latency_summary(done, server.wall, server.point_steps, len(reqs))
     served["iterations"] = server.iterations - it0
+    served["device_wait_s"] = server.wait_s
     launches = server.launches - l0
     server.point_steps = 0
     it1 = server.iterations
@@ -910,10 +911,13 @@ def serving_measure(nm, rate, duration, drain, budget_gb, seed):
         rq = S.poisson_requests(server.n, rate, duration, seed=seed + 72, mesh_sizes=sizes)
         for r in rq:
             r.t_arrival = 0.0
+        it_c = server.iterations
         dn = server.serve(rq, batched=batched, realtime=False, time_limit=drain + duration)
         summ = S.latency_summary(dn, server.wall, server.point_steps, len(rq))
+        summ["iterations"] = server.iterations - it_c
+        summ["device_wait_s"] = server.wait_s
         cap[mode] = {k: summ[k] for k in ("completed", "submitted", "wall_s", "pts_steps_per_s",
-                                          "query_vertices_per_s", "requests_per_s")}
+                                          "query_vertices_per_s", "requests_per_s", "iterations", "device_wait_s")}
     cap["speedup_pts_steps"] = cap["served"]["pts_steps_per_s"] / max(cap["plain"]["pts_steps_per_s"], 1e-9)
     cap["speedup_requests"] = cap["served"]["requests_per_s"] / max(cap["plain"]["requests_per_s"], 1e-9)
     frozen = server.frozen_fraction()

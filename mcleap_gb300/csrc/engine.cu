@@ -241,6 +241,67 @@ __device__ __forceinline__ void stage_edges(const KParams& P, int base, int st) 
   cp_async_commit();
 }
 
+// Iterate the outgoing half-edges of v counter-clockwise.
+template <typename F>
+__device__ bool for_spokes(const KParams& P, int v, F f) {
+  const int s0 = ld_i(P.vhe + v);
+  if (s0 < 0 || s0 >= 2 * P.E) return false;
+  int h = s0;
+  for (int k = 0; k < 1024; ++k) {
+    f(h);
+    h = he_prev(P, h) ^ 1;
+    if (h < 0 || h >= 2 * P.E) return false;
+    if (h == s0) return true;
+  }
+  return false;
+}
+
+// A step moves few vertices (an aggregation whose walkers froze, a single
+// point moved): classify only the edges of their stars and the sides opposite
+// them (the edges whose quads hold a moved vertex), each once per launch
+// (stamp qstamp in `win`), with the full predicate ladder; work-lists and
+// claims as the full pass makes them.  Worth it while the movers touch well
+// under all the edges.
+constexpr int kSparseEdgesPerMover = 32;
+
+__device__ __forceinline__ void push_one(const KParams& P, int* list, int* count, int e) {
+  const int at = atomicAdd(count, 1);
+  if (at < P.E) list[at] = e;
+  else flag_error(P, MCL_ERR_CAPACITY);
+}
+
+template <bool kFixedPos>
+__device__ void classify_one(const KParams& P, int e, unsigned qstamp, unsigned sc, LocalCounters& lc, int& bad) {
+  if (e < 0 || e >= P.E || atomicMax(P.win + e, qstamp) >= qstamp) return;
+  const int4 q = ld_ev(P, e);
+  if (q.x < 0) return;
+  if (bad_v(P, q.x) || bad_v(P, q.y) || q.z >= P.V || q.w >= P.V) {
+    flag_error(P, MCL_ERR_DEGENERATE_INPUT);
+    return;
+  }
+  const int bad0 = bad;
+  if (resolve_edge<kFixedPos>(P, e, lc, bad) && enqueue_once(P, e, qstamp)) {
+    claim_edge(P, e, sc);
+    push_one(P, P.wl0, &P.st->wl_count[0], e);
+  }
+  if (bad != bad0) push_one(P, P.wl1, &P.st->wl_count[1], e);
+}
+
+template <bool kFixedPos>
+__device__ void classify_movers(const KParams& P, int nm, unsigned qstamp, unsigned sc, LocalCounters& lc) {
+  const int stride = gridDim.x * blockDim.x;
+  int bad = 0;
+  for (int i = spread_tid(); i < nm; i += stride) {
+    const int v = ld_i(P.vl0 + i);
+    const bool ok = for_spokes(P, v, [&](int h) {
+      classify_one<kFixedPos>(P, h >> 1, qstamp, sc, lc, bad);
+      classify_one<kFixedPos>(P, he_next(P, h) >> 1, qstamp, sc, lc, bad);
+    });
+    if (!ok) flag_error(P, MCL_ERR_DEGENERATE_INPUT);
+  }
+  if (bad) atomicAdd(&P.st->inverted, bad);
+}
+
 template <bool kFixedPos>
 __device__ void phase_classify(cg::grid_group& g, const KParams& P, unsigned qstamp, unsigned sc,
                                LocalCounters& lc) {
@@ -251,6 +312,10 @@ __device__ void phase_classify(cg::grid_group& g, const KParams& P, unsigned qst
   if (P.move_mode != MOVE_NONE) {
     // kMoveUnroll vertices per thread and iteration, every load before any
     // store (the pass is a stream: its loads must overlap)
+    // The vertices that actually move are listed (work-list vl0, free until
+    // the repair): when they are few, only the edges whose quads hold one of
+    // them are classified (every other edge kept the positions of the last
+    // step, which left the mesh Delaunay).
     constexpr int UM = kMoveUnroll;
     for (int base = blockIdx.x * blockDim.x * UM; base < P.V_it; base += stride * UM) {
       int v[UM];
@@ -261,13 +326,28 @@ __device__ void phase_classify(cg::grid_group& g, const KParams& P, unsigned qst
         v[j] = i < P.V_it ? vert_at(P, i) : -1;
         if (v[j] >= 0) np[j] = moved_pos(P, v[j]);
       }
+      int mv[UM];
+      int km = 0;
 #pragma unroll
       for (int j = 0; j < UM; ++j)
-        if (v[j] >= 0) __stcg(P.pos + v[j], np[j]);
+        if (v[j] >= 0) {
+          __stcg(P.pos + v[j], np[j]);
+          const float2 po = __ldg(P.pos_old + v[j]);
+          if (__float_as_uint(np[j].x) != __float_as_uint(po.x) || __float_as_uint(np[j].y) != __float_as_uint(po.y))
+            mv[km++] = v[j];
+        }
+      if (__any_sync(kFull, km > 0)) warp_push(mv, km, P.vl0, &P.st->vl_count[0], P.V, P.st);
     }
     if (kFixedPos) timeline_max(P, 43);
     g.sync();
     if (kFixedPos) timeline_max(P, 44);
+    const int nm = ld_i(&P.st->vl_count[0]);
+    if (P.sparse_ok && (long long)nm * kSparseEdgesPerMover < (long long)P.E_it) {
+      cp_async_wait<0>();  // the prefetched records are not used
+      classify_movers<kFixedPos>(P, nm, qstamp, sc, lc);
+      if (kFixedPos) timeline_max(P, 45);
+      return;
+    }
   }
   int bad = 0;
   unsigned ninc = 0;
@@ -580,20 +660,6 @@ __device__ void phase_lawson(cg::grid_group& g, const KParams& P, int src, unsig
   if ((threadIdx.x & 31) == 0 && flips) atomicAdd(&P.st->c[C_LAWSON_FLIPS], (unsigned long long)flips);
 }
 
-// Iterate the outgoing half-edges of v counter-clockwise.
-template <typename F>
-__device__ bool for_spokes(const KParams& P, int v, F f) {
-  const int s0 = ld_i(P.vhe + v);
-  if (s0 < 0 || s0 >= 2 * P.E) return false;
-  int h = s0;
-  for (int k = 0; k < 1024; ++k) {
-    f(h);
-    h = he_prev(P, h) ^ 1;
-    if (h < 0 || h >= 2 * P.E) return false;
-    if (h == s0) return true;
-  }
-  return false;
-}
 
 // ---------------------------------------------------------------------------
 // Repair (1): revert vertices of non-positive faces until all faces are positive.
@@ -2274,9 +2340,11 @@ static int run_step(mcl_mesh* m, int move_mode, const float2* d, cudaStream_t s,
     P.pos = m->pos[m->cur];
     P.pos_old = m->valid_cur ? m->pos[m->cur] : m->pos[m->cur ^ 1];
   }
+  P.sparse_ok = m->delaunay ? 1 : 0;
   int rc = launch_engine(m, P, s);
   if (rc != MCL_OK) return rc;
   m->valid_cur = true;
+  m->delaunay = true;  // a step ends Delaunay (or with an error status)
   return finish(m, s, stats);
 }
 
@@ -2441,6 +2509,7 @@ int mcl_mesh_create_from_aos(const mcl_aos_view* a, mcl_mesh** out) {
   if (rc != MCL_OK) return rc;
   rc = upload_soa(m, a->pos, ev, en, vhe);
   if (rc != MCL_OK) { free_mesh(m); return rc; }
+  m->delaunay = false;  // a caller's mesh: the first step classifies every edge
   *out = m;
   return MCL_OK;
 }
@@ -2452,6 +2521,7 @@ int mcl_mesh_upload_aos(mcl_mesh* m, const mcl_aos_view* a) {
   std::vector<int> vhe;
   std::string why;
   if (!aos_to_soa(a, ev, en, vhe, why)) return fail(MCL_ERR_INVALID_ARGUMENT, "malformed mesh: " + why);
+  m->delaunay = false;
   return upload_soa(m, a->pos, ev, en, vhe);
 }
 

@@ -142,6 +142,7 @@ struct KParams {
   int tail_items;          // flip rounds with at most this many queued edges run in one block
   int rm_tile;             // lanes of a warp that take removal-list entries (0: as few as fit one pass)
   int substeps;            // repair sub-steps before removal
+  int sparse_ok;           // the mesh is Delaunay at pos_old: a step may classify only its movers' stars
   mcl_step_stats* stats_out;  // device-visible host record the launch fills at its end (or NULL)
   const int* vroot;        // per vertex: a never-freed half-edge of its mesh (batches); NULL = half-edge 0
   // active meshes of a batch (nact == 0: every edge and vertex): the full
@@ -363,6 +364,7 @@ struct mcl_mesh {
   int tail_items;          // single-block flip-round threshold
   int rm_tile;             // removal tile (mcl_mesh_set_removal_tile; 0 = automatic)
   int substeps;            // repair sub-steps before removal (mcl_mesh_set_substeps)
+  bool delaunay;           // the last launch left the mesh Delaunay (set when a step or build is launched)
   // batches: a mesh made of independent components (mcl_batch_create)
   int64_t ncomp;           // 1 for a plain mesh
   int64_t* comp_host;      // [4 * ncomp]: first vertex, vertices, first edge, edges

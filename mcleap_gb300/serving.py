@@ -181,11 +181,18 @@ class MeshServer:
         self.max_frnn, self.max_ring = max_frnn, max_ring
         self.max_query_rows = max_query_rows
         self.qout = torch.empty(max_query_rows * max(max_frnn, max_ring), dtype=torch.int32, device="cuda")
+        # query vertex lists of an iteration: written into pinned memory with
+        # their batch offsets, copied in one transfer on the serving stream
+        self.qstage = torch.empty(max_query_rows, dtype=torch.int32, pin_memory=True)
+        self.qstage_np = self.qstage.numpy()
+        self.qverts = torch.empty(max_query_rows, dtype=torch.int32, device="cuda")
         self.stream = stream or torch.cuda.Stream()
         self.point_steps = 0
         self.iterations = 0
         self.launches = 0
         self.admissions = 0        # admission events (groups built)
+        self.profile = None        # set to {} for device seconds per launch kind (CUDA events)
+        self._events = []
         self.compactions = 0
         for p in point_sets:
             self.submit_mesh(p)
@@ -317,41 +324,64 @@ class MeshServer:
         self.where = {}
 
     # -- per-iteration work ---------------------------------------------------------
+    def _mark(self, name):
+        """With profiling on, a CUDA event after the work launched so far."""
+        if self.profile is not None:
+            ev = self.torch.cuda.Event(enable_timing=True)
+            ev.record(self.stream)
+            self._events.append((name, ev))
+
     def _step(self, grp, locals_):
         b, s = grp.batch, self.stream
         b.set_active(locals_, stream=s)
+        self._mark(None)
         b.walk(grp.sigma, grp.counter, grp.d, frozen=grp.frozen, hi=BOX_HI, stream=s, seeds=grp.seeds)
+        self._mark("walk")
         b.settle(grp.d, stream=s, sync=False)
+        self._mark("settle")
         L.check(L.lib().mcl_step(b.handle, L.ptr(grp.d), s.cuda_stream, None))
+        self._mark("step")
         b.dla_freeze(grp.contact, grp.frozen, stream=s, sync=False)
+        self._mark("freeze")
         self.launches += 6  # walk + counter, settle, step, contact (2)
         for i in locals_:
             self.point_steps += int(grp.sizes[i])
 
-    def _queries(self, grp, reqs, keep_results):
+    def _queries(self, grp, reqs, keep_results, at):
+        """Launch this group's query requests; their vertex lists go to
+        self.qstage from row `at` on.  Returns the next free row."""
         torch, b, s = self.torch, grp.batch, self.stream
         for kind in ("frnn", "ring"):
             group = [r for r in reqs if r.kind == kind]
             if not group:
                 continue
-            verts = np.concatenate([r.verts.astype(np.int32) + np.int32(b.v0[grp.local[r.mesh]]) for r in group])
+            start = at
+            for r in group:
+                n = len(r.verts)
+                np.add(r.verts, np.int32(b.v0[grp.local[r.mesh]]), out=self.qstage_np[at:at + n], casting="unsafe")
+                at += n
+            count = at - start
             width = self.max_frnn if kind == "frnn" else self.max_ring
-            out = self.qout[:len(verts) * width]
+            W = max(self.max_frnn, self.max_ring)  # row stride of qout's regions: kinds never overlap
+            out = self.qout[start * W:start * W + count * width]
+            vd = self.qverts[start:at]
             with torch.cuda.stream(s):
-                vd = torch.from_numpy(verts).to("cuda")  # ordered on the serving stream
+                vd.copy_(self.qstage[start:at], non_blocking=True)  # ordered on the serving stream
                 if kind == "frnn":
                     b.frnn_list(grp.radius, vd, width, out, stream=s, sync=False)
                 else:
                     b.one_ring_list(vd, width, out, stream=s, sync=False)
             self.launches += 1
+            self._mark(kind)
             if keep_results:
                 s.synchronize()
-                rows = out.view(len(verts), width).cpu().numpy()
+                rows = out.view(count, width).cpu().numpy()
                 off = 0
                 for r in group:
                     n = len(r.verts)
                     r.result = rows[off:off + n].copy()
                     off += n
+        return at
 
     # -- serving loops ------------------------------------------------------------------
     def serve(self, requests, batched=True, realtime=True, time_limit=None, keep_results=False):
@@ -359,6 +389,7 @@ class MeshServer:
         An "open" request submits its points as mesh `r.mesh` (the next id); a
         "close" request ends its mesh after the mesh's earlier requests."""
         t0 = time.perf_counter()
+        self.wait_s = 0.0  # time spent waiting for the device at the end of iterations
         queues = collections.defaultdict(collections.deque)
         fifo = collections.deque()  # plain form: global arrival order
         nxt = 0
@@ -418,12 +449,22 @@ class MeshServer:
                     rows += len(r.verts)
             for grp, rs in stepping.values():
                 self._step(grp, [grp.local[r.mesh] for r in rs])
+            at = 0
+            if qs:
+                self._mark(None)
             for grp, rs in qs.values():
-                self._queries(grp, rs, keep_results)
+                at = self._queries(grp, rs, keep_results, at)
             ran = [r for _, rs in stepping.values() for r in rs] + [r for _, rs in qs.values() for r in rs]
             if ran:
+                tw = time.perf_counter()
                 self.stream.synchronize()
+                self.wait_s += time.perf_counter() - tw
                 self.iterations += 1
+                if self.profile is not None:
+                    for (_, a), (name, b) in zip(self._events, self._events[1:]):
+                        if name is not None:
+                            self.profile[name] = self.profile.get(name, 0.0) + a.elapsed_time(b) / 1e3
+                    self._events = []
             t_end = time.perf_counter() - t0
             for r in closing:
                 if r.kind == "close" and self.status[r.mesh] == "resident":

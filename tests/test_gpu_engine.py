@@ -623,3 +623,30 @@ def test_device_aos_arrays_equal_the_download(M):
         d = gaussian_disp(n + 4, 0.3 * spacing(n), 77 + k, clamp_pos=ht.m_pos)
         st = dt.step(cuda(d))
         assert st["status"] == 0 and st["inverted_faces"] > 0, st
+
+
+@pytest.mark.parametrize("frac,sigma", [(0.002, 0.3), (0.01, 2.0), (0.2, 0.5)])
+def test_steps_moving_few_points_match_exact_dt(M, frac, sigma):
+    """Steps that move a small fraction of the points classify only the edges
+    whose quads hold a moved point (the rest of the mesh is Delaunay from the
+    step before); the mesh is the exact Delaunay triangulation after every
+    step, with and without inverted faces to repair."""
+    n = 20000
+    ht, _ = build_pair(M, uniform_points(n, 91))
+    dt = M.DeviceTriangulation(ht)
+    rng = np.random.default_rng(int(frac * 1e4))
+    pos = ht.m_pos.copy()
+    inverted = 0
+    for k in range(6):
+        d = gaussian_disp(n + 4, sigma * spacing(n), 500 + k, clamp_pos=pos)
+        still = rng.random(n + 4) > frac
+        d[still] = 0
+        st = dt.step(cuda(d))
+        assert st["status"] == 0, st
+        inverted += st["inverted_faces"]
+        pos = (pos + d).astype(np.float32)
+        dt.transferToHost()
+        assert np.array_equal(ht.m_pos, pos)
+        assert np.array_equal(ht.edges(), O.Mesh.build(pos[4:], exact=True).edges()), (k, st)
+    if sigma >= 2.0:
+        assert inverted > 0
