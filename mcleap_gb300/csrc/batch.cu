@@ -134,7 +134,10 @@ __global__ void k_advance(unsigned long long* counter, int n, const int* act, in
 // Each pass inserts every vertex's candidate position into an open-addressing
 // table keyed by (mesh, x, y) (entries stamped with the pass, so the table is
 // never cleared); a vertex whose key is already present marks itself and the
-// holder.  Marked movers are sent back, and passes repeat until none is.
+// holder.  Marked movers are sent back, and passes repeat until none is.  A
+// first pass flags the meshes that have a mover: the others cannot hold a
+// coincident pair (their positions are distinct), so their vertices are not
+// inserted (with an aggregation most meshes have no walker left).
 __device__ __forceinline__ unsigned fbits(float x) { return x == 0.f ? 0u : __float_as_uint(x); }
 
 __device__ __forceinline__ float2 cand_pos(const float2* pos, const float2* d, const unsigned char* vfix, int v) {
@@ -153,6 +156,7 @@ struct SettleArgs {
   unsigned long long* table;
   unsigned long long mask;
   int* smark;
+  unsigned* smove;         // per mesh: stamp of the call that found a mover in it
   DevState* st;
   int max_passes;
 };
@@ -166,14 +170,26 @@ __global__ void k_settle(SettleArgs A) {
   const unsigned long long probe_cap = 2 * (A.mask + 1) + 1024;
   int pass = 0;
   bool lost = false;
+  // meshes with a mover (stamp `base`, unique to this call)
+  for (int vi = gtid; vi < A.A.V_it; vi += stride) {
+    const int v = A.A.at(vi);
+    if (A.vfix[v]) continue;
+    const float2 q = A.d[v];
+    if (q.x != 0.f || q.y != 0.f) {
+      const int comp = A.vcomp ? A.vcomp[v] : 0;
+      if (__ldcg(A.smove + comp) != base) atomicExch(A.smove + comp, base);
+    }
+  }
+  g.sync();
   for (; pass < A.max_passes; ++pass) {
     const unsigned stamp = base + 1 + (unsigned)pass;
     const int slot = 1 + pass % 3;
     if (gtid == 0) words[1 + (pass + 1) % 3] = 0;
     for (int vi = gtid; vi < A.A.V_it; vi += stride) {
       const int v = A.A.at(vi);
-      const float2 p = cand_pos(A.pos, A.d, A.vfix, v);
       const int comp = A.vcomp ? A.vcomp[v] : 0;
+      if (__ldcg(A.smove + comp) != base) continue;  // no mover in this mesh
+      const float2 p = cand_pos(A.pos, A.d, A.vfix, v);
       const unsigned long long key = ((unsigned long long)fbits(p.x) << 32) | fbits(p.y);
       unsigned long long h = mix64(key ^ ((unsigned long long)comp * 0x9E3779B97F4A7C15ull)) & A.mask;
       bool placed = false;
@@ -229,8 +245,10 @@ int ensure_settle_scratch(mcl_mesh* m) {
   while (size < 2 * m->V) size <<= 1;
   BCK(cudaMalloc((void**)&m->table, 8 * size));
   BCK(cudaMalloc((void**)&m->smark, 4 * m->V));
+  BCK(cudaMalloc((void**)&m->smove, 4 * std::max<int64_t>(1, m->ncomp)));
   BCK(cudaMemset(m->table, 0, 8 * size));
   BCK(cudaMemset(m->smark, 0, 4 * m->V));
+  BCK(cudaMemset(m->smove, 0xFF, 4 * std::max<int64_t>(1, m->ncomp)));
   m->table_size = size;
   int per_sm = 0;
   BCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_settle, 256, 0));
@@ -514,6 +532,7 @@ int mcl_settle_moves(mcl_mesh* m, mcl_float2* d_dev, void* stream, int64_t* sent
   A.table = m->table;
   A.mask = (unsigned long long)(m->table_size - 1);
   A.smark = m->smark;
+  A.smove = m->smove;
   A.st = m->st;
   A.max_passes = 64;
   void* args[] = {&A};

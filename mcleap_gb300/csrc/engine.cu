@@ -1958,7 +1958,7 @@ void free_mesh(mcl_mesh* m) {
   void* ptrs[] = {m->pos[0], m->pos[1], m->ev, m->en, m->vhe, m->vfix, m->cand, m->win, m->qmark, m->efa, m->hard,
                   m->wl[0], m->wl[1], m->vl[0], m->vl[1], m->vmark, m->claim, m->vfree, m->vhint,
                   m->vaux, m->vloc, m->vlocf, m->target, m->vprev, m->vl2, m->dstage, m->scratch, m->st,
-                  m->vcomp, m->vroot, m->cbase, m->table, m->smark, m->fnew, m->act_dev,
+                  m->vcomp, m->vroot, m->cbase, m->table, m->smark, m->smove, m->fnew, m->act_dev,
                   m->bg_cell, m->bg_src, m->bg_perm, m->bg_pos, m->bg_count, m->bg_start, m->bg_cursor,
                   m->bg_tmp, m->bg_par, m->aos_tmp};
   for (void* p : ptrs)
@@ -2320,11 +2320,20 @@ static int run_step(mcl_mesh* m, int move_mode, const float2* d, cudaStream_t s,
       if (m->nact) {
         std::vector<unsigned char> on((size_t)m->ncomp, 0);
         for (int i = 0; i < m->nact; ++i) on[(size_t)m->act_list[i]] = 1;
-        for (int64_t c = 0; c < m->ncomp; ++c) {
-          if (on[(size_t)c] || !m->dirty[c]) continue;
-          const int64_t v0 = m->comp_host[4 * c], nv = m->comp_host[4 * c + 1];
-          CK(cudaMemcpyAsync(m->pos[m->cur ^ 1] + v0, m->pos[m->cur] + v0, 8 * nv, cudaMemcpyDeviceToDevice, s));
-          m->dirty[c] = 0;
+        int64_t stale = 0;
+        for (int64_t c = 0; c < m->ncomp; ++c) stale += (!on[(size_t)c] && m->dirty[c]) ? 1 : 0;
+        if (stale > 16) {
+          // many small copies cost more than one copy of every position (the
+          // launch rewrites the active meshes' part anyway)
+          CK(cudaMemcpyAsync(m->pos[m->cur ^ 1], m->pos[m->cur], 8 * m->V, cudaMemcpyDeviceToDevice, s));
+          std::memset(m->dirty, 0, (size_t)m->ncomp);
+        } else {
+          for (int64_t c = 0; c < m->ncomp; ++c) {
+            if (on[(size_t)c] || !m->dirty[c]) continue;
+            const int64_t v0 = m->comp_host[4 * c], nv = m->comp_host[4 * c + 1];
+            CK(cudaMemcpyAsync(m->pos[m->cur ^ 1] + v0, m->pos[m->cur] + v0, 8 * nv, cudaMemcpyDeviceToDevice, s));
+            m->dirty[c] = 0;
+          }
         }
         for (int i = 0; i < m->nact; ++i) m->dirty[m->act_list[i]] = 1;
       } else {

@@ -375,6 +375,7 @@ struct mcl_mesh {
   unsigned long long* table;  // hash table of positions, stamped entries
   int64_t table_size;
   int* smark;              // per vertex: stamp of the settle pass that found it coincident
+  unsigned* smove;         // per mesh: stamp of the settle call that found a mover in it
   int settle_blocks;       // k_settle grid (cooperative)
   unsigned char* fnew;     // per vertex: newly frozen flags of mcl_dla_freeze
   // mcl_batch_frnn_grid: one uniform grid per mesh, cells of all meshes in one table
