@@ -89,11 +89,35 @@ __device__ __forceinline__ bool enqueue_once(const KParams& P, int e, unsigned s
   return atomicMax(P.qmark + e, stamp) < stamp;
 }
 
-// Mark edge e for a later work-list built by collect_marked (mk == 0: no-op).
-// Repair marks the edges its removals and splits touch instead of running
-// Lawson after each of its phases; one pass over the marks then queues them.
+// Append v to a global list from divergent code: the threads that reach the
+// call together share one atomicAdd (their coalesced group's leader).
+__device__ __forceinline__ void push_coalesced(const KParams& P, int* list, int* count, int cap, int v) {
+  cg::coalesced_group grp = cg::coalesced_threads();
+  int base = 0;
+  if (grp.thread_rank() == 0) base = atomicAdd(count, (int)grp.size());
+  base = grp.shfl(base, 0);
+  const int at = base + (int)grp.thread_rank();
+  if (at < cap) __stcg(list + at, v);
+  else flag_error(P, MCL_ERR_CAPACITY);
+}
+
+// The repair's final Lawson pass starts from every edge its removals and
+// splits touched: each is marked (stamp mk in qmark, no return value waited
+// for) and appended, with the others of its removal or split, to work-list 0
+// after the classification's non-Delaunay edges (one atomicAdd per removal or
+// split).  Appends may repeat an edge; before the pass the list is deduplicated
+// when it is short, and rebuilt from the marks by a pass over every edge when
+// it is long or did not fit (mark_ovf).  mk == 0 marks nothing.
 __device__ __forceinline__ void mark_edge(const KParams& P, int e, unsigned mk) {
   if (mk && e >= 0 && e < P.E) atomicMax(P.qmark + e, mk);
+}
+__device__ __forceinline__ int reserve_marks(const KParams& P, unsigned mk, int cnt) {
+  return (mk && P.append_marks) ? atomicAdd(&P.st->wl_count[0], cnt) : -1;
+}
+__device__ __forceinline__ void append_mark(const KParams& P, int base, int j, int cnt, int e) {
+  if (base < 0) return;
+  if (base + cnt <= P.E) __stcg(P.wl0 + base + j, e);
+  else if (j == 0) P.st->mark_ovf = 1;
 }
 
 // Called by every thread of the block (it holds a block barrier).
@@ -671,11 +695,20 @@ __device__ __forceinline__ float2 qpos(const KParams& P, int v, unsigned fs) {
   return marked(P, v, fs) ? P.pos_old[v] : ldpos(P, v);
 }
 
+// The list of the vertices the next fixpoint pass checks (their stars):
+// pass p writes list p & 1 (vl0 / vl1) with count fix_list[p % 3].
+__device__ __forceinline__ void list_for_next_pass(const KParams& P, int v, int pass) {
+  push_coalesced(P, (pass & 1) ? P.vl1 : P.vl0, &P.st->fix_list[pass % 3], P.V, v);
+}
+
 // A newly marked vertex records the pass that marked it in vloc (free until
-// the insertion rounds): the next pass checks only the faces of its star.
+// the insertion rounds), joins the list of every vertex sent back (`hard`,
+// free after the classification) and the next pass's list.
 __device__ void mark_vertex(const KParams& P, int v, int& fresh, unsigned fs, int pass) {
   if (!marked(P, v, fs) && (unsigned)atomicExch(P.vmark + v, (int)fs) != fs) {
     __stcg(P.vloc + v, pass);
+    push_coalesced(P, P.hard, &P.st->fix_all, P.E, v);
+    list_for_next_pass(P, v, pass);
     ++fresh;
   }
 }
@@ -710,7 +743,8 @@ __device__ void mark_face(const KParams& P, int a, int b, int c, int& fresh, uns
   if (pick >= 0) {
     mark_vertex(P, pick, fresh, fs, pass);
   } else if (any >= 0) {
-    __stcg(P.vloc + any, pass);
+    // vloc of a marked vertex holds a pass of this launch: list it once per pass
+    if (atomicExch(P.vloc + any, pass) != pass) list_for_next_pass(P, any, pass);
     ++fresh;
   }
 }
@@ -724,6 +758,7 @@ __device__ bool phase_fixpoint(cg::grid_group& g, const KParams& P, LocalCounter
     if (gtid == 0) {
       P.st->fix_new[(pass + 1) % 3] = 0;
       P.st->fix_bad[(pass + 1) % 3] = 0;
+      P.st->fix_list[(pass + 1) % 3] = 0;
       P.st->c[C_FIX_PASSES] += 1;
     }
     int fresh = 0, bad = 0;
@@ -750,11 +785,12 @@ __device__ bool phase_fixpoint(cg::grid_group& g, const KParams& P, LocalCounter
         }
       }
     } else {
-      // only a face with a vertex sent back in the last pass can have changed
-      // sign: the stars of those vertices
-      for (int vi = gtid; vi < P.V_it; vi += stride) {
-        const int v = vert_at(P, vi);
-        if (!marked(P, v, fs) || __ldcg(P.vloc + v) != pass - 1) continue;
+      // only a face with a vertex sent back (or listed again) in the last pass
+      // can have changed sign: the stars of the last pass's list
+      const int nl = ld_i(&P.st->fix_list[(pass - 1) % 3]);
+      const int* lst = ((pass - 1) & 1) ? P.vl1 : P.vl0;
+      for (int ii = spread_tid(); ii < nl; ii += stride) {
+        const int v = ld_i(lst + ii);
         const float2 pv = qpos(P, v, fs);
         const bool ok = for_spokes(P, v, [&](int h) {
           const int d = he_origin(P, h ^ 1), a = he_apex(P, h);
@@ -836,6 +872,7 @@ template <typename Poly>
 __device__ int clip_star(const KParams& P, int v, LocalCounters& lc, unsigned mk, int k, const int* sp, const int* lk,
                          const int* w, Poly& poly, int* bnd) {
   if (k < 3) return MCL_ERR_DEGENERATE_INPUT | (__LINE__ << 8);
+  const int mbase = reserve_marks(P, mk, 2 * k - 3);  // its latency overlaps the clipping
   for (int j = 0; j < k; ++j) {
     poly.set_nx(j, j + 1 == k ? 0 : j + 1);
     poly.set_pv(j, j == 0 ? k - 1 : j - 1);
@@ -884,6 +921,11 @@ __device__ int clip_star(const KParams& P, int v, LocalCounters& lc, unsigned mk
   for (int i = 0; i < k; ++i) {
     if (ld_i(P.vhe + w[i]) == (sp[i] ^ 1)) __stcg(P.vhe + w[i], lk[i]);
     mark_edge(P, lk[i] >> 1, mk);  // the hole's sides face new triangles
+  }
+  if (mbase >= 0) {
+    // the list entries: the sides and the diagonals (the spoke slots sp[3..k)
+    // were reused for them); the slots were reserved at the start
+    for (int t = 0; t < 2 * k - 3; ++t) append_mark(P, mbase, t, 2 * k - 3, t < k ? lk[t] >> 1 : sp[t - k + 3] >> 1);
   }
   for (int r = 0; r < 3; ++r) {
     const int e = sp[r] >> 1;
@@ -1058,6 +1100,7 @@ __device__ int remove_vertex(const KParams& P, int v, LocalCounters& lc, int& fl
     }
     if (!flip_edge(P, flipped)) return MCL_ERR_DEGENERATE_INPUT | (__LINE__ << 8);
     if (mk) {
+      P.st->mark_ovf = 1;  // spoke flips are marked, not appended: rebuild the list from the marks
       const int4 wg = ld_en(P, flipped);  // the flipped edge's four wings
       mark_edge(P, flipped, mk);
       mark_edge(P, wg.x >> 1, mk);
@@ -1082,6 +1125,7 @@ __device__ int remove_vertex(const KParams& P, int v, LocalCounters& lc, int& fl
   mark_edge(P, lxy >> 1, mk);
   mark_edge(P, lyz >> 1, mk);
   mark_edge(P, lzx >> 1, mk);
+  if (mk) P.st->mark_ovf = 1;
   if (ld_i(P.vhe + x) == (s0 ^ 1)) __stcg(P.vhe + x, lxy);
   if (ld_i(P.vhe + y) == (s1 ^ 1)) __stcg(P.vhe + y, lyz);
   if (ld_i(P.vhe + z) == (s2 ^ 1)) __stcg(P.vhe + z, lzx);
@@ -1387,7 +1431,7 @@ __device__ bool phase_insert(cg::grid_group& g, const KParams& P, unsigned& stam
     const unsigned sq = stamp++;
     if (gtid == 0) {
       P.st->vl_count[dst] = 0;
-      P.st->wl_count[0] = 0;
+      if (!mk) P.st->wl_count[0] = 0;  // with mk the list gathers the marks of every round
       P.st->c[C_INSERT_ROUNDS] += 1;
     }
     // locate and claim
@@ -1473,9 +1517,16 @@ __device__ bool phase_insert(cg::grid_group& g, const KParams& P, unsigned& stam
           if (mk) {
             // on a triangulation that is not Delaunay the new spokes need not
             // be legal either: the split edge (now v's spoke to a) and f0..f2
-            for (int j = 0; j < nl; ++j) mark_edge(P, link[j] >> 1, mk);
-            for (int j = 0; j < 3; ++j) mark_edge(P, f[j], mk);
-            if (fl & 2) mark_edge(P, __ldcg(P.vloc + v) >> 1, mk);
+            int edges[8];
+            int cnt = 0;
+            for (int j = 0; j < nl; ++j) edges[cnt++] = link[j] >> 1;
+            for (int j = 0; j < 3; ++j) edges[cnt++] = f[j];
+            if (fl & 2) edges[cnt++] = __ldcg(P.vloc + v) >> 1;
+            const int mbase = reserve_marks(P, mk, cnt);
+            for (int j = 0; j < cnt; ++j) {
+              mark_edge(P, edges[j], mk);
+              append_mark(P, mbase, j, cnt, edges[j]);
+            }
           } else {
             for (int j = 0; j < nl; ++j)
               if (enqueue_once(P, link[j] >> 1, sq)) mine[k++] = link[j] >> 1;
@@ -1554,7 +1605,9 @@ __device__ void finish_launch(const KParams& P, unsigned stamp) {
   st->vl_count[0] = st->vl_count[1] = 0;
   st->inverted = 0;
   st->hard_count = 0;
-  for (int i = 0; i < 3; ++i) st->fix_new[i] = st->fix_bad[i] = 0;
+  for (int i = 0; i < 3; ++i) st->fix_new[i] = st->fix_bad[i] = st->fix_list[i] = 0;
+  st->fix_all = 0;
+  st->mark_ovf = 0;
   st->epoch = stamp;
 }
 
@@ -1788,16 +1841,23 @@ __device__ __noinline__ unsigned repair_step(cg::grid_group g, const KParams P, 
   g.sync();
   timeline(P, 43);
   if (ok) {
-    // removal list: reverted vertices that actually moved
+    // removal list: reverted vertices that actually moved.  Few: from the
+    // list of every vertex sent back (on `hard`); many: by a pass over the
+    // vertices, whose id order keeps neighbouring removals in one warp
+    // (the mark order scatters them).
     const int stride = gridDim.x * blockDim.x;
+    const int nall = ld_i(&P.st->fix_all);
+    const bool few = (long long)nall * 64 < (long long)P.V_it;
     if (gtid == 0) { P.st->vl_count[0] = 0; P.st->vl_count[1] = 0; }
     g.sync();
-    for (int base = blockIdx.x * blockDim.x; base < P.V_it; base += stride) {
-      const int vi = base + threadIdx.x;
-      const int v = vi < P.V_it ? vert_at(P, vi) : 0;
+    const int nsb = few ? nall : P.V_it;
+    for (int base = (few ? spread_tid() - (int)(threadIdx.x & 31) : blockIdx.x * blockDim.x); base < nsb;
+         base += stride) {
+      const int vi = base + (few ? (int)(threadIdx.x & 31) : (int)threadIdx.x);
+      const int v = vi < nsb ? (few ? ld_i(P.hard + vi) : vert_at(P, vi)) : 0;
       int mine[1];
       int k = 0;
-      if (vi < P.V_it && marked(Q, v, fs) && !P.vfix[v]) {
+      if (vi < nsb && marked(Q, v, fs) && !P.vfix[v]) {
         const float2 pn = ldpos(Q, v), po = P.pos_old[v];
         if (__float_as_uint(pn.x) != __float_as_uint(po.x) || __float_as_uint(pn.y) != __float_as_uint(po.y)) {
           __stcg(P.target + v, pn);
@@ -1828,8 +1888,15 @@ __device__ __noinline__ unsigned repair_step(cg::grid_group g, const KParams P, 
       phase_substeps(g, Q, stamp, lc);
       timeline_insert(P, 15, 1);
       mk = stamp++;
+      // the mesh is Delaunay again: the final Lawson list starts empty
+      if (gtid == 0) { P.st->wl_count[0] = 0; P.st->wl_count[1] = 0; }
+      g.sync();
     }
     const int nrem = ld_i(&P.st->vl_count[0]);
+    // few removals: their marks are appended to a list (no pass over every
+    // edge afterwards); many: the list is rebuilt from the marks
+    Q.append_marks = (long long)nrem * 64 < (long long)P.E_it ? 1 : 0;
+    if (!Q.append_marks && gtid == 0) P.st->mark_ovf = 1;
     if (nrem > 0) {
       // (2) remove what is left, marking each hole's sides and diagonals
       ok = phase_remove(g, Q, stamp, lc, mk);
@@ -1838,12 +1905,18 @@ __device__ __noinline__ unsigned repair_step(cg::grid_group g, const KParams P, 
       // (3) reinsert at the new positions: splits only, their edges marked
       if (gtid == 0) { P.st->vl_count[0] = 0; P.st->vl_count[1] = 0; }
       g.sync();
-      for (int base = blockIdx.x * blockDim.x; base < P.V_it; base += stride) {
-        const int vi = base + threadIdx.x;
-        const int v = vi < P.V_it ? vert_at(P, vi) : 0;
+      // the removed vertices: from the list of every vertex sent back when
+      // few (and the sub-steps' classification did not reuse its buffer),
+      // else by a pass over the vertices
+      const bool from_list = few && !(nrev > 0 && P.substeps > 0);
+      const int nscan = from_list ? nall : P.V_it;
+      for (int base = (from_list ? spread_tid() - (int)(threadIdx.x & 31) : blockIdx.x * blockDim.x); base < nscan;
+           base += stride) {
+        const int vi = base + (from_list ? (int)(threadIdx.x & 31) : (int)threadIdx.x);
+        const int v = vi < nscan ? (from_list ? ld_i(P.hard + vi) : vert_at(P, vi)) : 0;
         int mine[1];
         int k = 0;
-        if (vi < P.V_it && ld_i(P.vhe + v) < 0 && marked(Q, v, fs)) {
+        if (vi < nscan && ld_i(P.vhe + v) < 0 && marked(Q, v, fs)) {
           __stcg(P.pos + v, __ldcg(P.target + v));
           mine[k++] = v;
         }
@@ -1856,20 +1929,45 @@ __device__ __noinline__ unsigned repair_step(cg::grid_group g, const KParams P, 
       timeline(P, 44);
     }
     timeline(P, 45);
-    // (4) one Lawson pass from every marked edge
+    // (4) one Lawson pass from every marked edge: work-list 0 holds the
+    // classification's non-Delaunay edges and the appended marks, repeats
+    // included; deduplicated into work-list 1 when short, else rebuilt from
+    // the marks over every edge
     if (ok) {
-      if (gtid == 0) { P.st->wl_count[0] = 0; P.st->wl_count[1] = 0; }
-      g.sync();
-      for (int base = blockIdx.x * blockDim.x; base < P.E_it; base += stride) {
-        const int ei = base + threadIdx.x;
-        const int e = ei < P.E_it ? edge_at(P, ei) : -1;
-        int mine[1];
-        int k = 0;
-        if (e >= 0 && (unsigned)ld_i(reinterpret_cast<const int*>(P.qmark) + e) == mk) mine[k++] = e;
-        if (__any_sync(kFull, k > 0)) warp_push(mine, k, P.wl0, &P.st->wl_count[0], P.E, P.st);
+      const int nw = ld_i(&P.st->wl_count[0]);
+      const bool rebuild = ld_i(&P.st->mark_ovf) || (long long)nw * 4 >= (long long)P.E_it;
+      g.sync();  // every thread has read the count and the flag
+      if (rebuild) {
+        if (gtid == 0) { P.st->wl_count[0] = 0; P.st->wl_count[1] = 0; }
+        g.sync();
+        for (int base = blockIdx.x * blockDim.x; base < P.E_it; base += stride) {
+          const int ei = base + threadIdx.x;
+          const int e = ei < P.E_it ? edge_at(P, ei) : -1;
+          int mine[1];
+          int k = 0;
+          if (e >= 0 && (unsigned)ld_i(reinterpret_cast<const int*>(P.qmark) + e) == mk) mine[k++] = e;
+          if (__any_sync(kFull, k > 0)) warp_push(mine, k, P.wl0, &P.st->wl_count[0], P.E, P.st);
+        }
+        g.sync();
+        phase_lawson<false>(g, Q, 0, stamp, lc, 0);
+      } else {
+        const unsigned du = stamp++;  // first sight of an edge in this pass (cand is free until the flip rounds)
+        if (gtid == 0) P.st->wl_count[1] = 0;
+        g.sync();
+        for (int base = spread_tid() - (int)(threadIdx.x & 31); base < nw; base += stride) {
+          const int i = base + (int)(threadIdx.x & 31);
+          int mine[1];
+          int k = 0;
+          if (i < nw) {
+            const int e = ld_i(P.wl0 + i);
+            if (e >= 0 && e < P.E && atomicMax(P.cand + e, du) < du) mine[k++] = e;
+          }
+          if (__any_sync(kFull, k > 0)) warp_push(mine, k, P.wl1, &P.st->wl_count[1], P.E, P.st);
+        }
+        if (gtid == 0) P.st->wl_count[0] = 0;
+        g.sync();
+        phase_lawson<false>(g, Q, 1, stamp, lc, 0);
       }
-      g.sync();
-      phase_lawson<false>(g, Q, 0, stamp, lc, 0);
       g.sync();
     }
     timeline(P, 46);

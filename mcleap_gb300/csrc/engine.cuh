@@ -64,6 +64,9 @@ struct DevState {
   int hard_count;          // edges the FP32 filters could not classify
   int fix_new[3];          // vertices newly reverted per fixpoint pass (triple-buffered)
   int fix_bad[3];          // non-positive faces seen per fixpoint pass
+  int fix_list[3];         // vertices listed for the next fixpoint pass (triple-buffered counts)
+  int fix_all;             // vertices sent back by this launch (listed once, on `hard`)
+  int mark_ovf;            // the repair's appended marks did not fit, or were not all appended
   int sub_count[3];        // repair sub-steps: mover lists (2), vertices left for removal
   int sub_rev[3];          // movers sent back per sub-step pass (triple-buffered)
   unsigned int epoch;      // next unused stamp
@@ -143,6 +146,7 @@ struct KParams {
   int rm_tile;             // lanes of a warp that take removal-list entries (0: as few as fit one pass)
   int substeps;            // repair sub-steps before removal
   int sparse_ok;           // the mesh is Delaunay at pos_old: a step may classify only its movers' stars
+  int append_marks;        // repair: append marked edges to work-list 0 (few removals), else rebuild from the marks
   mcl_step_stats* stats_out;  // device-visible host record the launch fills at its end (or NULL)
   const int* vroot;        // per vertex: a never-freed half-edge of its mesh (batches); NULL = half-edge 0
   // active meshes of a batch (nact == 0: every edge and vertex): the full
