@@ -1119,8 +1119,8 @@ def run_periodic(args, rank, world, dist):
                    "points": n, "parallelism": f"replicas x{world}"},
         "totals": tot, "positions_match_mirror": bool(np.array_equal(pos, mirror.cpu().numpy())),
         "step_ms": {"p50": float(np.median(ms)), "p99": float(np.percentile(ms, 99))},
-        # at least: target + move + fold per step, one classification per round
-        "clocks": clocks, "gpu_launches": 3 * K + tot["lawson_rounds"], "build_s": t_build,
+        # one cooperative launch per step (mcl_periodic_step)
+        "clocks": clocks, "gpu_launches": K, "build_s": t_build,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -461,7 +461,8 @@ int mcl_periodic_positions(mcl_periodic* m, mcl_float2** pos_dev);
  * by all of it, landing exactly on the target), each with the same refusal
  * and flips; the vertices still away after that are removed and reinserted
  * at their targets one by one (one GPU thread; at most 65,536 a step), with
- * flips around each.  The result is the periodic Delaunay triangulation of
+ * flips around each.  The whole step is one cooperative kernel launch; the
+ * call returns after reading its result record (it synchronizes `stream`).  The result is the periodic Delaunay triangulation of
  * the moved points (a point whose target is taken by another stays where it
  * was).  stats (may be NULL): inverted_faces (turned by the move),
  * substep_vertices (sent back, then brought to their target by sub-steps),
@@ -474,6 +475,10 @@ int mcl_periodic_step(mcl_periodic* m, const mcl_float2* d_dev, void* stream, mc
 /* The same step with the displacements in host memory (copied in on `stream`). */
 int mcl_periodic_step_host(mcl_periodic* m, const mcl_float2* d_host, void* stream, mcl_step_stats* stats,
                            int64_t* wrapped);
+/* Diagnostics of the last step: out32[0] = 0, out32[k] = ns from the launch's
+ * start to the grid barrier ending its k-th phase (-1 past the last; 31
+ * phases at most); phases (may be NULL) = grid barriers the launch passed. */
+int mcl_periodic_debug_timeline(const mcl_periodic* m, int64_t* out32, int64_t* phases);
 
 /* oneRing<M> / oneRing2<M> (include/Device_Triangulation.h:500-517) on a
  * periodic mesh: each vertex's neighbours clockwise, starting at the smallest

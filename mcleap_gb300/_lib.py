@@ -42,7 +42,7 @@ EXPORTS = [
     "mcl_mesh_set_removal_tile", "mcl_mesh_get_removal_tile",
     "mcl_periodic_build", "mcl_periodic_create", "mcl_periodic_destroy", "mcl_periodic_sizes", "mcl_periodic_download",
     "mcl_periodic_positions", "mcl_periodic_step", "mcl_periodic_from_planar", "mcl_periodic_one_ring",
-    "mcl_periodic_closest", "mcl_periodic_frnn", "mcl_periodic_step_host",
+    "mcl_periodic_closest", "mcl_periodic_frnn", "mcl_periodic_step_host", "mcl_periodic_debug_timeline",
 ]
 
 
@@ -156,6 +156,7 @@ def lib():
             "mcl_periodic_closest": ([vp, i32, i32, vp, vp, vp, vp], i32),
             "mcl_periodic_frnn": ([vp, f32, i32, i32, vp, vp, vp, C.POINTER(i64)], i32),
             "mcl_periodic_step_host": ([vp, vp, vp, C.POINTER(StepStats), C.POINTER(i64)], i32),
+            "mcl_periodic_debug_timeline": ([vp, vp, C.POINTER(i64)], i32),
         }
         for name, (args, res) in sig.items():
             fn = getattr(L, name)

@@ -11,23 +11,25 @@
 //           copies within a band around the domain, downloaded and restricted
 //           to the torus on the host (periodic_from_planar); a quarter period
 //           of band first, the whole 3 x 3 cover if that does not close up.
-//   step    move + wrap (one launch over vertices), the wraps folded into the
-//           edge words (one launch over edges), then rounds of classify +
-//           claim / flip winners (one launch each) until no edge is
-//           non-Delaunay; the host reads the round's counters between
-//           launches.  A classification that finds faces turned over sends
-//           their moved vertices back (one launch over vertices, then the
-//           fold again) and classifies again; flips start from a mesh whose
-//           faces are all positive.  Vertices sent back then follow in up to
-//           kSubLevels sub-steps (half of what they still owe, the last all);
-//           the few still away (listed in parallel, by ascending id) are
-//           removed and reinserted at their targets by one thread
-//           (k_preinsert).
+//   step    one cooperative launch (k_pstep): move + wrap every vertex, the
+//           wraps folded into the edge words, then rounds of classify +
+//           claim / flip winners over edge work-lists until no edge is
+//           non-Delaunay, grid barriers between the phases and every
+//           decision taken on the device.  A classification that finds faces
+//           turned over sends their moved vertices back (then the fold again)
+//           and classifies again; flips start from a mesh whose faces are all
+//           positive.  Vertices sent back then follow in up to kSubLevels
+//           sub-steps (half of what they still owe, the last all); the few
+//           still away (listed in parallel, by ascending id) are removed and
+//           reinserted at their targets by one thread of the launch.  The
+//           host reads one record at the end.
 //   queries one-ring with copy offsets, closest neighbour, mesh FRNN (one
 //           launch for the outgoing half-edges, one per query).
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstddef>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -41,6 +43,7 @@ using mcl::PCount;
 using mcl::PF2;
 using mcl::PI4;
 using mcl::PView;
+namespace cg = cooperative_groups;
 
 struct mcl_periodic {
   int64_t n, E;
@@ -65,6 +68,13 @@ struct mcl_periodic {
   PCount* cnt;
   PCount* cnt_host;  // pinned
   unsigned stamp;    // last round stamp used
+  // the step's cooperative launch (allocated on the first step)
+  PCount* slots;     // three rotating phase counters, clear between launches
+  void* out;         // PStepOut (device)
+  void* out_host;    // PStepOut (pinned, mapped)
+  void* out_map;     // out_host's device address (NULL: copied back instead)
+  int* chunk;        // per-block counts of the behind list (grid + 1)
+  int grid;          // blocks of the launch
 };
 
 namespace {
@@ -84,105 +94,443 @@ constexpr int kCenter = 4;  // copy index of the untranslated copy
     if (_e != cudaSuccess) return mcl::cuda_fail(_e, #call); \
   } while (0)
 
-__global__ void k_pmove(PView V, const PF2* d) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < V.n) mcl::p_body_move(V, d, i);
+// ---------------------------------------------------------------------------
+// The step as one cooperative launch: phases over vertices or edges
+// (grid-stride) separated by grid barriers, every decision taken on the
+// device from the counters of the phase just ended.
+//
+// Counters: each phase counts into its own PCount slot, three in rotation.
+// After the barrier that ends phase p every thread reads slot p % 3 (the same
+// values in every thread, so all take the same branch and meet at the same
+// barriers); phase p + 1 reads at most the list length of slot p; at the start
+// of phase p + 2, one thread adds slot p % 3 to the step's totals and clears
+// it (no thread reads it after the barrier ending phase p + 1).  The launch
+// ends with every slot cleared, so the next launch needs no reset.
+struct PStepOut {
+  PCount tot;  // counters of the whole step (error and error_site: the first)
+  unsigned long long rounds, inverted_first, incircle_tests, behind_first, behind_sub, behind, reinserted, stamps;
+  int reason;  // kReason*
+  int phases;  // grid barriers passed
+  // %globaltimer at the launch's start (ts[0]) and after the barrier ending
+  // each of its first kPhaseMarks - 1 phases (mcl_periodic_debug_timeline)
+  unsigned long long ts[32];
+};
+constexpr int kPhaseMarks = 32;
+__device__ __forceinline__ unsigned long long p_now() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
 }
-__global__ void k_ptarget(PView V, const PF2* d) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < V.n) mcl::p_body_target(V, d, i);
+enum : int {
+  kReasonNone = 0,
+  kReasonBody,              // a kernel body flagged an error (tot.error)
+  kReasonTurnedAfterFlips,  // a face turned over after flips
+  kReasonRevertEndless,     // sending vertices back did not end
+  kReasonNoConverge,        // flip rounds did not converge
+  kReasonReinsert,          // removal and reinsertion failed (tot.error)
+};
+
+__device__ void p_fold(PCount* tot, PCount* slot) {
+  constexpr int kWords = (int)(sizeof(PCount) / 8), kErr = (int)(offsetof(PCount, error) / 8),
+                kSite = (int)(offsetof(PCount, error_site) / 8);
+  unsigned long long* t = reinterpret_cast<unsigned long long*>(tot);
+  unsigned long long* x = reinterpret_cast<unsigned long long*>(slot);
+  const bool first = t[kErr] == 0 && __ldcg(x + kErr) != 0;
+  for (int i = 0; i < kWords; ++i) {
+    const unsigned long long v = __ldcg(x + i);
+    if (i == kErr || i == kSite) {
+      if (first) t[i] = v;
+    } else {
+      t[i] += v;
+    }
+    x[i] = 0;
+  }
 }
-__global__ void k_presume(PView V, PF2* d, bool last) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < V.n) mcl::p_body_resume(V, d, i, last);
+
+struct PCtl {
+  cg::grid_group g;
+  PView V0;
+  PCount* slots;
+  PCount* tot;
+  unsigned long long* ts;
+  int ph;
+  long long gt, gs;
+  // the thread's id dealt across blocks (thread t of block b: t * blocks + b),
+  // for short work-lists: their items spread over every SM instead of filling
+  // the first blocks
+  __device__ long long gl() const { return (long long)threadIdx.x * gridDim.x + blockIdx.x; }
+  // start of a phase: its view (counting into its slot); recycles the slot of
+  // the phase before the last
+  __device__ PView begin() {
+    if (gt == 0) p_fold(tot, slots + (ph + 1) % 3);
+    PView V = V0;
+    V.cnt = slots + ph % 3;
+    return V;
+  }
+  // end of a phase: the grid barrier, then the phase's counters
+  __device__ const PCount* end() {
+    g.sync();
+    if (gt == 0 && ph + 1 < kPhaseMarks) ts[ph + 1] = p_now();
+    return slots + (ph++ % 3);
+  }
+};
+__device__ __forceinline__ bool p_failed(const PCount* c) { return __ldcg(&c->error) != 0; }
+
+// Streaming passes, kU items per thread and iteration with every load of an
+// iteration issued before its first store (item j of the iteration at base is
+// base + j * (threads of the grid), so each load stays coalesced).
+constexpr int kU = 4;
+
+// every vertex: the move by d (and first, at the step's start, the target)
+__device__ void p_move_pass(const PCtl& C, const PView& V, const PF2* d, bool target) {
+  for (long long base = C.gt; base < V.n; base += C.gs * kU) {
+    PF2 p[kU], dv[kU];
+#pragma unroll
+    for (int j = 0; j < kU; ++j) {
+      const long long v = base + j * C.gs;
+      if (v < V.n) {
+        p[j] = V.pos[v];
+        dv[j] = d[v];
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < kU; ++j) {
+      const long long v = base + j * C.gs;
+      if (v < V.n) {
+        if (target) mcl::p_target_with(V, (int)v, p[j], dv[j]);
+        mcl::p_move_with(V, (int)v, p[j], dv[j]);
+      }
+    }
+  }
 }
-// The vertices still away from their targets, listed by ascending id (the
-// order the reinsertion takes them in), built in parallel: a count per chunk
-// of kChunk vertices, one block scanning the counts (total appended), then
-// each chunk writing its vertices in order.
-constexpr int kChunk = 1024;
+
+// every vertex: the displacement it still owes (counting those behind)
+__device__ void p_resume_pass(const PCtl& C, const PView& V, PF2* dsub, bool last) {
+  for (long long base = C.gt; base < V.n; base += C.gs * kU) {
+    PF2 p[kU], t[kU];
+#pragma unroll
+    for (int j = 0; j < kU; ++j) {
+      const long long v = base + j * C.gs;
+      if (v < V.n) {
+        p[j] = V.pos[v];
+        t[j] = V.target[v];
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < kU; ++j) {
+      const long long v = base + j * C.gs;
+      if (v < V.n) mcl::p_resume_with(V, dsub, (int)v, p[j], t[j], last);
+    }
+  }
+}
+
+// every edge (cur < 0), each first folding the wraps of its quad's vertices
+// into its offset word (the fold of a move or of vertices sent back, which
+// always precedes a classification of every edge), or the first `items`
+// entries of work-list cur.  The loop decides each edge with the float32
+// filters; an edge they leave open, or with a face turned over, is classified
+// after the loop with the full predicates (p_body_classify), two per thread,
+// any more listed on `hard` (counted in the slot's `hard`) for a second pass
+// after the barrier.  So the loop holds no call of the exact predicates.
+__device__ void p_classify_pass(const PCtl& C, const PView& V, int cur, long long items, unsigned stamp, int* hard) {
+  constexpr int kU = 2;
+  const int* wl = cur == 1 ? V.wl1 : V.wl0;
+  int def0 = -1, def1 = -1;
+  for (long long base = cur < 0 ? C.gt : C.gl(); base < items; base += C.gs * kU) {
+    int e[kU];
+#pragma unroll
+    for (int j = 0; j < kU; ++j) {
+      const long long i = base + j * C.gs;
+      e[j] = i < items ? (cur < 0 ? (int)i : __ldcg(wl + i)) : -1;
+      if ((unsigned)e[j] >= (unsigned)V.E) e[j] = -1;
+    }
+    PI4 q[kU];
+    unsigned o[kU];
+#pragma unroll
+    for (int j = 0; j < kU; ++j)
+      if (e[j] >= 0) {
+        q[j] = V.ev[e[j]];
+        o[j] = V.eo[e[j]];
+      }
+    PF2 pa[kU], pb[kU], pc[kU], pd[kU];
+    unsigned char w[kU][4];
+#pragma unroll
+    for (int j = 0; j < kU; ++j) {
+      if (e[j] < 0) continue;
+      if (!mcl::p_vertices_ok(V, q[j])) {
+        mcl::p_error(V, MCL_ERR_DEGENERATE_INPUT, cur < 0 ? 2 : 3);
+        e[j] = -1;
+        continue;
+      }
+      if (cur < 0) {
+        w[j][0] = V.wv[q[j].x];
+        w[j][1] = V.wv[q[j].y];
+        w[j][2] = V.wv[q[j].z];
+        w[j][3] = V.wv[q[j].w];
+      }
+      pa[j] = V.pos[q[j].x];
+      pb[j] = V.pos[q[j].y];
+      pc[j] = V.pos[q[j].z];
+      pd[j] = V.pos[q[j].w];
+    }
+#pragma unroll
+    for (int j = 0; j < kU; ++j) {
+      if (e[j] < 0) continue;
+      if (cur < 0) {
+        mcl::p_wrap_with(V, e[j], w[j][0], w[j][1], w[j][2], w[j][3]);
+        o[j] = V.eo[e[j]];
+      }
+      PF2 qb, qc, qd;
+      bool open = !mcl::quad_frame(o[j], pb[j], pc[j], pd[j], V.L, qb, qc, qd);
+      if (!open) {
+        const int sa = mcl::orient2d_fp32(pa[j].x, pa[j].y, qb.x, qb.y, qc.x, qc.y);
+        const int sb = mcl::orient2d_fp32(qb.x, qb.y, pa[j].x, pa[j].y, qd.x, qd.y);
+        if (sa == 1 && sb == 1) {
+          const int si = mcl::incircle_fp32(pa[j].x, pa[j].y, qb.x, qb.y, qc.x, qc.y, qd.x, qd.y);
+          if (si == 1) mcl::p_claim_nd(V, e[j], stamp);
+          else open = si != -1;
+        } else {
+          open = true;  // a face turned over (marks its culprit) or undecided
+        }
+      }
+      if (open) {
+        if (def0 < 0) def0 = e[j];
+        else if (def1 < 0) def1 = e[j];
+        else hard[mcl::p_inc(&V.cnt->hard)] = e[j];
+      }
+    }
+  }
+  if (def0 >= 0) mcl::p_body_classify(V, def0, stamp);
+  if (def1 >= 0) mcl::p_body_classify(V, def1, stamp);
+}
+
+// the control state every thread keeps (the same in all of them)
+struct PZ {
+  unsigned stamp;
+  unsigned long long rounds, inverted_first, incircle_tests, reverted;
+  bool classified;
+};
+
+// Rounds of classification after a move: faces turned over send their moved
+// vertices back (then the fold again), otherwise the winners of the
+// non-Delaunay edges flip, until no edge is non-Delaunay.
+__device__ int p_settle(PCtl& C, PZ& z) {
+  int revert_passes = 0, cur = -1;  // the work-list to classify (-1: every edge)
+  long long len = 0;                // its length
+  bool flipped = false;
+  for (int r = 0; r < kMaxRounds; ++r) {
+    const unsigned stamp = ++z.stamp;
+    const long long items = cur < 0 ? (long long)C.V0.E : len;
+    const int next = cur == 0 ? 1 : 0;  // the list the round's flips fill, free until then
+    int* hard = next ? C.V0.wl1 : C.V0.wl0;
+    p_classify_pass(C, C.begin(), cur, items, stamp, hard);
+    const PCount* c = C.end();
+    const long long nh = (long long)__ldcg(&c->hard);
+    if (nh) {
+      // the edges the classification left over, into the same counters
+      PView V = C.V0;
+      V.cnt = const_cast<PCount*>(c);
+      for (long long i = C.gl(); i < nh; i += C.gs) mcl::p_body_classify(V, __ldcg(hard + i), stamp);
+      C.g.sync();
+    }
+    ++z.rounds;
+    if (p_failed(c)) return kReasonBody;
+    const unsigned long long inverted = __ldcg(&c->inverted), nd = __ldcg(&c->nondelaunay);
+    if (!z.classified) {
+      z.inverted_first = inverted;
+      z.classified = true;
+    }
+    if (inverted) {
+      // flips only start from a mesh whose faces are all positive
+      if (flipped) return kReasonTurnedAfterFlips;
+      if (revert_passes == kMaxRevertPasses) return kReasonRevertEndless;
+      {
+        const PView V = C.begin();
+        for (long long v = C.gt; v < V.n; v += C.gs) mcl::p_body_revert(V, (int)v);
+      }
+      const PCount* cr = C.end();
+      if (p_failed(cr)) return kReasonBody;
+      z.reverted += __ldcg(&cr->reverted);
+      ++revert_passes;
+      cur = -1;
+      continue;
+    }
+    z.incircle_tests += (unsigned long long)items;
+    if (!nd) return kReasonNone;
+    {
+      const PView V = C.begin();  // a fresh slot: work-list `next` starts empty
+      for (long long i = C.gl(); i < (long long)nd; i += C.gs) {
+        const int e = __ldcg(V.clist + i);
+        if ((unsigned)e < (unsigned)V.E) mcl::p_body_flip(V, e, stamp, next);
+      }
+    }
+    c = C.end();
+    if (p_failed(c)) return kReasonBody;
+    len = (long long)__ldcg(&c->lcount[next]);
+    cur = next;
+    flipped = true;
+  }
+  return kReasonNoConverge;
+}
+
 __device__ __forceinline__ bool p_behind(const PView& V, int i) {
-  const PF2 here = V.pos[i], t = V.target[i];
+  const float2 here = __ldcg(reinterpret_cast<const float2*>(V.pos) + i);
+  const PF2 t = V.target[i];
   return !(here.x == t.x && here.y == t.y);
 }
-__global__ void __launch_bounds__(kChunk) k_pbehind_count(PView V, int* chunk) {
-  const int i = blockIdx.x * kChunk + threadIdx.x;
-  const int c = __syncthreads_count(i < V.n && p_behind(V, i));
-  if (threadIdx.x == 0) chunk[blockIdx.x] = c;
-}
-// exclusive scan of chunk[0..nb) in place, the total in chunk[nb] (one block)
-__global__ void __launch_bounds__(kChunk) k_pbehind_scan(int* chunk, int nb) {
-  __shared__ int tot[kChunk];
-  const int per = (nb + kChunk - 1) / kChunk, lo = threadIdx.x * per, hi = min(nb, lo + per);
-  int run = 0;
-  for (int i = lo; i < hi; ++i) run += chunk[i];
-  tot[threadIdx.x] = run;
-  __syncthreads();
-  for (int o = 1; o < kChunk; o <<= 1) {
-    const int y = threadIdx.x >= (unsigned)o ? tot[threadIdx.x - o] : 0;
-    __syncthreads();
-    tot[threadIdx.x] += y;
-    __syncthreads();
-  }
-  int acc = threadIdx.x ? tot[threadIdx.x - 1] : 0;
-  for (int i = lo; i < hi; ++i) {
-    const int x = chunk[i];
-    chunk[i] = acc;
-    acc += x;
-  }
-  if (threadIdx.x == kChunk - 1) chunk[nb] = tot[kChunk - 1];
-}
-__global__ void __launch_bounds__(kChunk) k_pbehind_scatter(PView V, const int* chunk, int* list) {
-  __shared__ int wbase[kChunk / 32];
-  const int i = blockIdx.x * kChunk + threadIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const bool b = i < V.n && p_behind(V, i);
-  const unsigned bal = __ballot_sync(0xffffffffu, b);
-  if (lane == 0) wbase[warp] = __popc(bal);
-  __syncthreads();
-  if (warp == 0) {
-    const int x = wbase[lane];
-    int incl = x;
-    for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += y;
+
+// The vertices still away from their targets, listed by ascending id (the
+// order the reinsertion takes them in) into V.clist, their number into
+// chunk[gridDim.x]: each block counts a contiguous range, block 0 scans the
+// counts, each block writes its range in order.  Three phases.
+__device__ void p_list_behind(PCtl& C, int* chunk) {
+  __shared__ int wsum[kThreads / 32];
+  __shared__ int run;
+  const long long n = C.V0.n, per = (n + gridDim.x - 1) / gridDim.x;
+  const long long lo = min(n, (long long)blockIdx.x * per), hi = min(n, lo + per);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  {
+    const PView V = C.begin();
+    int k = 0;
+    for (long long base = lo; base < hi; base += blockDim.x) {
+      const long long i = base + threadIdx.x;
+      k += __syncthreads_count(i < hi && p_behind(V, (int)i));
     }
-    wbase[lane] = incl - x;
+    if (threadIdx.x == 0) chunk[blockIdx.x] = k;
   }
-  __syncthreads();
-  if (b) list[chunk[blockIdx.x] + wbase[warp] + __popc(bal & ((1u << lane) - 1u))] = i;
+  C.end();
+  {
+    C.begin();
+    if (blockIdx.x == 0) {
+      // exclusive scan of chunk[0 .. gridDim.x), the total into chunk[gridDim.x]
+      __shared__ int tot[kThreads];
+      const int nb = gridDim.x, seg = (nb + kThreads - 1) / kThreads;
+      const int a = min(nb, (int)threadIdx.x * seg), b = min(nb, a + seg);
+      int x = 0;
+      for (int i = a; i < b; ++i) x += __ldcg(chunk + i);
+      tot[threadIdx.x] = x;
+      __syncthreads();
+      for (int o = 1; o < kThreads; o <<= 1) {
+        const int y = (int)threadIdx.x >= o ? tot[threadIdx.x - o] : 0;
+        __syncthreads();
+        tot[threadIdx.x] += y;
+        __syncthreads();
+      }
+      int acc = tot[threadIdx.x] - x;
+      for (int i = a; i < b; ++i) {
+        const int c = __ldcg(chunk + i);
+        chunk[i] = acc;
+        acc += c;
+      }
+      if (threadIdx.x == kThreads - 1) chunk[nb] = tot[kThreads - 1];
+    }
+  }
+  C.end();
+  {
+    const PView V = C.begin();
+    if (threadIdx.x == 0) run = __ldcg(chunk + blockIdx.x);
+    __syncthreads();
+    for (long long base = lo; base < hi; base += blockDim.x) {
+      const long long i = base + threadIdx.x;
+      const bool b = i < hi && p_behind(V, (int)i);
+      const unsigned bal = __ballot_sync(0xffffffffu, b);
+      if (lane == 0) wsum[warp] = __popc(bal);
+      __syncthreads();
+      int before = run, total = 0;
+      for (int w = 0; w < kThreads / 32; ++w) {
+        if (w == warp) before += total;
+        total += wsum[w];
+      }
+      if (b) V.clist[before + __popc(bal & ((1u << lane) - 1u))] = (int)i;
+      __syncthreads();
+      if (threadIdx.x == 0) run += total;
+      __syncthreads();
+    }
+  }
+  C.end();
 }
-// one thread: the sequential removal and reinsertion of the listed vertices
-__global__ void k_preinsert(PView V, int* vhe, const int* list, const int* count) {
-  if (blockIdx.x == 0 && threadIdx.x == 0) mcl::p_body_reinsert(V, vhe, list, *count, kMaxReinsert);
-}
-__global__ void k_prevert(PView V) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < V.n) mcl::p_body_revert(V, i);
-}
-__global__ void k_pwrap(PView V) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < V.E) mcl::p_body_wrap(V, i);
-}
-// every edge (list < 0) or the entries of work-list `list`, grid-stride (the
-// list's length is read on the device)
-__global__ void k_pclassify(PView V, unsigned stamp, int list) {
-  const long long items = list < 0 ? (long long)V.E : (long long)V.cnt->lcount[list];
-  const int* wl = list == 1 ? V.wl1 : V.wl0;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < items;
-       i += (long long)gridDim.x * blockDim.x) {
-    const int e = list < 0 ? (int)i : wl[i];
-    if ((unsigned)e < (unsigned)V.E) mcl::p_body_classify(V, e, stamp);
+
+// out: the step's record in device memory; host_out (may be NULL): a
+// host-mapped copy of it written at the end
+__global__ void __launch_bounds__(kThreads, 2) k_pstep(PView V0, const PF2* d, PF2* dsub, PCount* slots, PStepOut* out,
+                                                       PStepOut* host_out, int* chunk, int* vhe, unsigned stamp0) {
+  PCtl C{cg::this_grid(), V0, slots, &out->tot, out->ts, 0, (long long)blockIdx.x * blockDim.x + threadIdx.x,
+         (long long)gridDim.x * blockDim.x};
+  if (C.gt == 0) {
+    out->ts[0] = p_now();
+    unsigned long long* t = reinterpret_cast<unsigned long long*>(&out->tot);
+    for (int i = 0; i < (int)(sizeof(PCount) / 8); ++i) t[i] = 0;
+  }
+  PZ z{stamp0, 0, 0, 0, 0, false};
+  int reason = kReasonNone;
+  unsigned long long behind_first = 0, behind = 0, behind_sub = 0, reinserted = 0;
+  bool first = true;
+  // the step's targets, then the move and wrap of every vertex
+  p_move_pass(C, C.begin(), d, true);
+  if (p_failed(C.end())) reason = kReasonBody;
+  if (!reason) reason = p_settle(C, z);
+  // sub-steps: vertices sent back move again by half of what they still owe,
+  // the last level by all of it (landing exactly on the target)
+  for (int level = 1; !reason; ++level) {
+    const bool last = level >= kSubLevels;
+    if (first && z.reverted == 0) {
+      // nothing was sent back: every vertex stands on its target (computed
+      // with the move's own arithmetic), so no vertex is behind
+      behind = 0;
+    } else {
+      p_resume_pass(C, C.begin(), dsub, last);
+      behind = __ldcg(&C.end()->behind);
+    }
+    if (first) behind_first = behind;
+    first = false;
+    if (behind == 0 || level > kSubLevels) break;
+    p_move_pass(C, C.begin(), dsub, false);
+    if (p_failed(C.end())) reason = kReasonBody;
+    if (!reason) reason = p_settle(C, z);
+  }
+  behind_sub = behind;
+  // the rest: removed and reinserted at their targets, one by one
+  if (!reason && behind > 0) {
+    {
+      const PView V = C.begin();
+      for (long long v = C.gt; v < V.n; v += C.gs) vhe[v] = -1;  // the largest candidate wins
+    }
+    C.end();
+    {
+      const PView V = C.begin();
+      for (long long h = C.gt; h < 2 * (long long)V.E; h += C.gs) mcl::p_body_vhe(V, vhe, (int)h);
+    }
+    if (p_failed(C.end())) reason = kReasonReinsert;
+    if (!reason) {
+      p_list_behind(C, chunk);
+      {
+        const PView V = C.begin();
+        if (C.gt == 0) mcl::p_body_reinsert(V, vhe, V.clist, __ldcg(chunk + gridDim.x), kMaxReinsert);
+      }
+      const PCount* c = C.end();
+      if (p_failed(c)) reason = kReasonReinsert;
+      reinserted = __ldcg(&c->reinserted);
+      p_resume_pass(C, C.begin(), dsub, true);  // counts who is still behind
+      behind = __ldcg(&C.end()->behind);
+    }
+  }
+  C.g.sync();  // every thread has read the last phase's counters
+  if (C.gt == 0) {
+    for (int k = 0; k < 3; ++k) p_fold(&out->tot, slots + k);
+    out->rounds = z.rounds;
+    out->inverted_first = z.inverted_first;
+    out->incircle_tests = z.incircle_tests;
+    out->behind_first = behind_first;
+    out->behind_sub = behind_sub;
+    out->behind = behind;
+    out->reinserted = reinserted;
+    out->stamps = z.stamp - stamp0;
+    out->reason = reason;
+    out->phases = C.ph;
+    if (host_out) *host_out = *out;
   }
 }
-// the round's non-Delaunay edges; winners flip and queue their wings on `next`
-__global__ void k_pflip(PView V, unsigned stamp, int next) {
-  const long long items = (long long)V.cnt->nondelaunay;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < items;
-       i += (long long)gridDim.x * blockDim.x) {
-    const int e = V.clist[i];
-    if ((unsigned)e < (unsigned)V.E) mcl::p_body_flip(V, e, stamp, next);
-  }
-}
+
 __global__ void k_pvhe(PView V, int* vhe) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < 2 * V.E) mcl::p_body_vhe(V, vhe, i);
@@ -201,8 +549,6 @@ __global__ void k_pclosest(PView V, bool column, int max_ring, const int* ring, 
 }
 
 unsigned blocks(int64_t k) { return (unsigned)((k + kThreads - 1) / kThreads); }
-// grid of the grid-stride list kernels: 16 blocks of 256 per SM of a GB300 at most
-unsigned list_blocks(int64_t k) { return std::min<unsigned>(blocks(k), 152u * 16u); }
 
 PView view(mcl_periodic* m) {
   return PView{(int)m->n, (int)m->E,  m->L,       2.0f * m->L, m->pos,    m->ev,   m->en,    m->eo,
@@ -232,6 +578,10 @@ void free_periodic(mcl_periodic* m) {
   cudaFree(m->vhe);
   cudaFree(m->cnt);
   if (m->cnt_host) cudaFreeHost(m->cnt_host);
+  cudaFree(m->slots);
+  cudaFree(m->out);
+  cudaFree(m->chunk);
+  if (m->out_host) cudaFreeHost(m->out_host);
   delete m;
 }
 
@@ -452,76 +802,29 @@ int alloc_upload(const mcl_float2* pos, int64_t n, float L, const int32_t* ev, c
   return MCL_OK;
 }
 
-// Rounds of classification after a move: faces turned over send their moved
-// vertices back (then the fold again), otherwise the winners of the
-// non-Delaunay edges flip, until no edge is non-Delaunay.  Counters
-// accumulate in z across calls.
-struct Settle {
-  PCount c{};
-  unsigned long long inverted_first = 0;
-  bool classified = false;
-  int rounds = 0;
-  int64_t incircle_tests = 0;  // the edges classified in rounds without a face turned over
-  std::string msg;
-};
-
-int settle(mcl_periodic* m, cudaStream_t s, const PView& V, Settle& z) {
-  int revert_passes = 0, cur = -1;  // the work-list to classify (-1: every edge)
-  bool flipped = false;
-  for (int r = 0; r < kMaxRounds; ++r) {
-    if (m->stamp >= 0xFFFFFFFEu) {  // stamps about to wrap: forget every old claim and queue mark
-      PCK(cudaMemsetAsync(m->claim, 0, 16 * (size_t)m->E, s));
-      PCK(cudaMemsetAsync(m->cand, 0, 4 * (size_t)m->E, s));
-      PCK(cudaMemsetAsync(m->qstamp, 0, 4 * (size_t)m->E, s));
-      m->stamp = 0;
-    }
-    const unsigned stamp = ++m->stamp;
-    PCK(cudaMemsetAsync(&m->cnt->inverted, 0, 2 * sizeof(unsigned long long), s));  // inverted, nondelaunay
-    k_pclassify<<<list_blocks(m->E), kThreads, 0, s>>>(V, stamp, cur);
-    PCK(cudaGetLastError());
-    PCK(cudaMemcpyAsync(m->cnt_host, m->cnt, sizeof(PCount), cudaMemcpyDeviceToHost, s));
-    PCK(cudaStreamSynchronize(s));
-    z.c = *m->cnt_host;
-    ++z.rounds;
-    const int64_t classified = cur < 0 ? m->E : (int64_t)z.c.lcount[cur];
-    if (z.c.error) {
-      const int rc = (int)z.c.error;
-      z.msg = "mcl_periodic_step: " + std::string(mcl_status_string(rc)) + " (site " + std::to_string(z.c.error_site) +
-              ")";
-      return rc;
-    }
-    if (!z.classified) {
-      z.inverted_first = z.c.inverted;
-      z.classified = true;
-    }
-    if (z.c.inverted) {
-      // flips only start from a mesh whose faces are all positive
-      if (flipped) {
-        z.msg = "mcl_periodic_step: a face turned over after flips (the mesh was not valid)";
-        return MCL_ERR_DEGENERATE_INPUT;
-      }
-      if (revert_passes == kMaxRevertPasses) {
-        z.msg = "mcl_periodic_step: sending vertices back did not end";
-        return MCL_ERR_NO_CONVERGENCE;
-      }
-      k_prevert<<<blocks(m->n), kThreads, 0, s>>>(V);
-      k_pwrap<<<blocks(m->E), kThreads, 0, s>>>(V);
-      PCK(cudaGetLastError());
-      ++revert_passes;
-      cur = -1;
-      continue;
-    }
-    z.incircle_tests += classified;
-    if (!z.c.nondelaunay) return MCL_OK;
-    const int next = cur == 0 ? 1 : 0;
-    PCK(cudaMemsetAsync(&m->cnt->lcount[next], 0, sizeof(unsigned long long), s));
-    k_pflip<<<list_blocks((int64_t)z.c.nondelaunay), kThreads, 0, s>>>(V, stamp, next);
-    PCK(cudaGetLastError());
-    cur = next;
-    flipped = true;
+// the step's launch state, allocated on the first step: the grid is as many
+// blocks as fit on the device at once (a cooperative launch), at most one per
+// kThreads edges
+int ensure_step(mcl_periodic* m) {
+  if (m->slots) return MCL_OK;
+  int dev = 0, sms = 0, per_sm = 0;
+  PCK(cudaGetDevice(&dev));
+  PCK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  PCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pstep, kThreads, 0));
+  if (per_sm < 1) return mcl::fail(MCL_ERR_CUDA, "mcl_periodic_step: the step kernel does not fit on an SM");
+  const int64_t want = std::max<int64_t>(1, (m->E + kThreads - 1) / kThreads);
+  const int grid = (int)std::min<int64_t>((int64_t)per_sm * sms, want);
+  PCK(cudaMalloc((void**)&m->slots, 3 * sizeof(PCount)));
+  PCK(cudaMemset(m->slots, 0, 3 * sizeof(PCount)));
+  PCK(cudaMalloc(&m->out, sizeof(PStepOut)));
+  PCK(cudaHostAlloc(&m->out_host, sizeof(PStepOut), cudaHostAllocMapped));
+  if (cudaHostGetDevicePointer(&m->out_map, m->out_host, 0) != cudaSuccess) {
+    cudaGetLastError();
+    m->out_map = nullptr;
   }
-  z.msg = "mcl_periodic_step: flip rounds did not converge";
-  return MCL_ERR_NO_CONVERGENCE;
+  PCK(cudaMalloc((void**)&m->chunk, sizeof(int) * (size_t)(grid + 1)));
+  m->grid = grid;
+  return MCL_OK;
 }
 
 }  // namespace
@@ -653,72 +956,66 @@ int mcl_periodic_step(mcl_periodic* m, const mcl_float2* d_dev, void* stream, mc
                       int64_t* wrapped) {
   if (!m || !d_dev) return mcl::fail(MCL_ERR_INVALID_ARGUMENT, "null argument");
   cudaStream_t s = (cudaStream_t)stream;
-  const PView V = view(m);
-  Settle z;
-  PCK(cudaMemsetAsync(m->cnt, 0, sizeof(PCount), s));
-  k_ptarget<<<blocks(m->n), kThreads, 0, s>>>(V, reinterpret_cast<const PF2*>(d_dev));
-  k_pmove<<<blocks(m->n), kThreads, 0, s>>>(V, reinterpret_cast<const PF2*>(d_dev));
-  k_pwrap<<<blocks(m->E), kThreads, 0, s>>>(V);
-  PCK(cudaGetLastError());
-  int rc = settle(m, s, V, z);
-  // sub-steps: vertices sent back move again by half of what they still owe,
-  // the last level by all of it (landing exactly on the target)
-  int64_t behind_first = -1, behind = 0;
-  for (int level = 1; rc == MCL_OK; ++level) {
-    const bool last = level >= kSubLevels;
-    PCK(cudaMemsetAsync(&m->cnt->behind, 0, sizeof(unsigned long long), s));
-    k_presume<<<blocks(m->n), kThreads, 0, s>>>(V, m->dsub, last);
-    PCK(cudaGetLastError());
-    PCK(cudaMemcpyAsync(m->cnt_host, m->cnt, sizeof(PCount), cudaMemcpyDeviceToHost, s));
-    PCK(cudaStreamSynchronize(s));
-    behind = (int64_t)m->cnt_host->behind;
-    if (behind_first < 0) behind_first = behind;
-    if (behind == 0 || level > kSubLevels) break;
-    k_pmove<<<blocks(m->n), kThreads, 0, s>>>(V, m->dsub);
-    k_pwrap<<<blocks(m->E), kThreads, 0, s>>>(V);
-    PCK(cudaGetLastError());
-    rc = settle(m, s, V, z);
+  const int rc0 = ensure_step(m);
+  if (rc0 != MCL_OK) return rc0;
+  // a step uses at most (1 + kSubLevels) * kMaxRounds round stamps (+1 for
+  // the queue marks of the last): forget every old claim and queue mark
+  // before the stamps could wrap
+  static_assert((1 + kSubLevels) * kMaxRounds + 2 < (1 << 16), "stamp budget");
+  if (m->stamp > 0xFFFFFFFFu - (1u << 16)) {
+    PCK(cudaMemsetAsync(m->claim, 0, 16 * (size_t)m->E, s));
+    PCK(cudaMemsetAsync(m->cand, 0, 4 * (size_t)m->E, s));
+    PCK(cudaMemsetAsync(m->qstamp, 0, 4 * (size_t)m->E, s));
+    m->stamp = 0;
   }
-  const int64_t substep_arrivals = behind_first > behind ? behind_first - behind : 0;
-  // the rest: removed and reinserted at their targets, one by one
-  int64_t reinserted = 0;
-  if (rc == MCL_OK && behind > 0) {
-    PCK(cudaMemsetAsync(&m->cnt->behind, 0, sizeof(unsigned long long), s));
-    PCK(cudaMemsetAsync(&m->cnt->reinserted, 0, sizeof(unsigned long long), s));
-    PCK(cudaMemsetAsync(m->vhe, 0xFF, 4 * (size_t)m->n, s));  // vhe = -1: the largest candidate wins
-    k_pvhe<<<blocks(2 * m->E), kThreads, 0, s>>>(V, m->vhe);
-    // the flip rounds are over: clist holds the list, wl[1] the chunk counts
-    const int nb = (int)((m->n + kChunk - 1) / kChunk);
-    k_pbehind_count<<<nb, kChunk, 0, s>>>(V, m->wl[1]);
-    k_pbehind_scan<<<1, kChunk, 0, s>>>(m->wl[1], nb);
-    k_pbehind_scatter<<<nb, kChunk, 0, s>>>(V, m->wl[1], m->clist);
-    k_preinsert<<<1, 32, 0, s>>>(V, m->vhe, m->clist, m->wl[1] + nb);
-    PCK(cudaGetLastError());
-    PCK(cudaMemsetAsync(&m->cnt->behind, 0, sizeof(unsigned long long), s));
-    k_presume<<<blocks(m->n), kThreads, 0, s>>>(V, m->dsub, true);  // counts who is still behind
-    PCK(cudaGetLastError());
-    PCK(cudaMemcpyAsync(m->cnt_host, m->cnt, sizeof(PCount), cudaMemcpyDeviceToHost, s));
-    PCK(cudaStreamSynchronize(s));
-    const PCount& r = *m->cnt_host;
-    if (r.error) {
-      rc = (int)r.error;
-      z.msg = "mcl_periodic_step: removal and reinsertion failed (site " + std::to_string(r.error_site) + ")";
-    }
-    reinserted = (int64_t)r.reinserted;
-    behind = (int64_t)r.behind;
-    z.c.flips = r.flips;
-    z.c.error_site = r.error_site;
+  PView V = view(m);
+  const PF2* d = reinterpret_cast<const PF2*>(d_dev);
+  PStepOut* out = static_cast<PStepOut*>(m->out);
+  unsigned stamp0 = m->stamp;
+  PStepOut* host_out = static_cast<PStepOut*>(m->out_map);
+  void* args[] = {&V, (void*)&d, &m->dsub, &m->slots, &out, &host_out, &m->chunk, &m->vhe, &stamp0};
+  PCK(cudaLaunchCooperativeKernel((const void*)k_pstep, dim3((unsigned)m->grid), dim3(kThreads), args, 0, s));
+  if (!host_out) PCK(cudaMemcpyAsync(m->out_host, m->out, sizeof(PStepOut), cudaMemcpyDeviceToHost, s));
+  PCK(cudaStreamSynchronize(s));
+  const PStepOut& o = *static_cast<const PStepOut*>(m->out_host);
+  const PCount& c = o.tot;
+  m->stamp += (unsigned)o.stamps;
+  int rc = MCL_OK;
+  std::string msg;
+  const std::string site = " (site " + std::to_string(c.error_site) + ")";
+  switch (o.reason) {
+    case kReasonNone:
+      break;
+    case kReasonBody:
+      rc = c.error ? (int)c.error : MCL_ERR_CUDA;
+      msg = "mcl_periodic_step: " + std::string(mcl_status_string(rc)) + site;
+      break;
+    case kReasonTurnedAfterFlips:
+      rc = MCL_ERR_DEGENERATE_INPUT;
+      msg = "mcl_periodic_step: a face turned over after flips (the mesh was not valid)";
+      break;
+    case kReasonRevertEndless:
+      rc = MCL_ERR_NO_CONVERGENCE;
+      msg = "mcl_periodic_step: sending vertices back did not end";
+      break;
+    case kReasonNoConverge:
+      rc = MCL_ERR_NO_CONVERGENCE;
+      msg = "mcl_periodic_step: flip rounds did not converge";
+      break;
+    default:
+      rc = c.error ? (int)c.error : MCL_ERR_CUDA;
+      msg = "mcl_periodic_step: removal and reinsertion failed" + site;
+      break;
   }
-  const PCount& c = z.c;
   if (stats) {
     std::memset(stats, 0, sizeof(*stats));
-    stats->inverted_faces = (int64_t)((z.inverted_first + 2) / 3);  // each face is seen from its three edges
-    stats->reverted_vertices = behind;
-    stats->removed_vertices = reinserted;
-    stats->substep_vertices = substep_arrivals;
+    stats->inverted_faces = (int64_t)((o.inverted_first + 2) / 3);  // each face is seen from its three edges
+    stats->reverted_vertices = (int64_t)o.behind;
+    stats->removed_vertices = (int64_t)o.reinserted;
+    stats->substep_vertices = o.behind_first > o.behind_sub ? (int64_t)(o.behind_first - o.behind_sub) : 0;
     stats->lawson_flips = (int64_t)c.flips;
-    stats->lawson_rounds = z.rounds;
-    stats->incircle_tests = z.incircle_tests;
+    stats->lawson_rounds = (int64_t)o.rounds;
+    stats->incircle_tests = (int64_t)o.incircle_tests;
     stats->incircle_fp64 = (int64_t)c.incircle_fp64;
     stats->incircle_exact = (int64_t)c.incircle_exact;
     stats->orient_fp64 = (int64_t)c.orient_fp64;
@@ -730,9 +1027,9 @@ int mcl_periodic_step(mcl_periodic* m, const mcl_float2* d_dev, void* stream, mc
   if (wrapped) *wrapped = (int64_t)c.wrapped;
   if (rc == MCL_OK && c.overflow) {
     rc = MCL_ERR_PREDICATE;
-    z.msg = "mcl_periodic_step: exact predicate capacity exceeded";
+    msg = "mcl_periodic_step: exact predicate capacity exceeded";
   }
-  return rc == MCL_OK ? MCL_OK : mcl::fail(rc, z.msg);
+  return rc == MCL_OK ? MCL_OK : mcl::fail(rc, msg);
 }
 
 int mcl_periodic_step_host(mcl_periodic* m, const mcl_float2* d_host, void* stream, mcl_step_stats* stats,
@@ -740,6 +1037,15 @@ int mcl_periodic_step_host(mcl_periodic* m, const mcl_float2* d_host, void* stre
   if (!m || !d_host) return mcl::fail(MCL_ERR_INVALID_ARGUMENT, "null argument");
   PCK(cudaMemcpyAsync(m->dstage, d_host, 8 * (size_t)m->n, cudaMemcpyHostToDevice, (cudaStream_t)stream));
   return mcl_periodic_step(m, reinterpret_cast<const mcl_float2*>(m->dstage), stream, stats, wrapped);
+}
+
+int mcl_periodic_debug_timeline(const mcl_periodic* m, int64_t* out32, int64_t* phases) {
+  if (!m || !out32) return mcl::fail(MCL_ERR_INVALID_ARGUMENT, "null argument");
+  if (!m->out_host) return mcl::fail(MCL_ERR_INVALID_ARGUMENT, "mcl_periodic_debug_timeline: no step yet");
+  const PStepOut& o = *static_cast<const PStepOut*>(m->out_host);
+  for (int i = 0; i < kPhaseMarks; ++i) out32[i] = i < o.phases + 1 ? (int64_t)(o.ts[i] - o.ts[0]) : -1;
+  if (phases) *phases = o.phases;
+  return MCL_OK;
 }
 
 int mcl_periodic_one_ring(mcl_periodic* m, int max_ring, int layout, int32_t* ring_dev, uint8_t* offs_dev,

@@ -29,6 +29,10 @@
 
 #include "predicates.cuh"
 #include "../../include/mcl_gb300.h"
+#if defined(__CUDACC__)
+#include <cooperative_groups.h>
+#include <cooperative_groups/scan.h>
+#endif
 
 namespace mcl {
 
@@ -168,6 +172,7 @@ struct PCount {
       sos, overflow, error, error_site, truncated, reverted, behind;
   unsigned long long lcount[2];  // entries of the two edge work-lists
   unsigned long long reinserted;  // vertices removed and reinserted at their targets
+  unsigned long long hard;        // edges a classification left to the full predicates
 };
 
 struct PView {
@@ -199,9 +204,31 @@ MCL_HD void p_add(unsigned long long* p, unsigned long long v) {
   *p += v;
 #endif
 }
+// a slot of a list counted by *p; on the device the threads that reach the
+// call together (which all count on the same *p in every caller) share one
+// atomicAdd
+// k slots of a list counted by *p (the same sharing as p_inc)
+MCL_HD unsigned long long p_inc_n(unsigned long long* p, unsigned k) {
+#if defined(__CUDA_ARCH__)
+  cooperative_groups::coalesced_group grp = cooperative_groups::coalesced_threads();
+  const unsigned before = cooperative_groups::exclusive_scan(grp, k);
+  unsigned long long base = 0;
+  if (grp.thread_rank() == grp.size() - 1) base = atomicAdd(p, (unsigned long long)(before + k));
+  base = grp.shfl(base, grp.size() - 1);
+  return base + before;
+#else
+  const unsigned long long at = *p;
+  *p += k;
+  return at;
+#endif
+}
 MCL_HD unsigned long long p_inc(unsigned long long* p) {
 #if defined(__CUDA_ARCH__)
-  return atomicAdd(p, 1ull);
+  cooperative_groups::coalesced_group grp = cooperative_groups::coalesced_threads();
+  unsigned long long base = 0;
+  if (grp.thread_rank() == 0) base = atomicAdd(p, (unsigned long long)grp.size());
+  base = grp.shfl(base, 0);
+  return base + grp.thread_rank();
 #else
   return (*p)++;
 #endif
@@ -269,13 +296,11 @@ MCL_HD void p_flush(const PView& V, const PLocal& lc) {
   if (lc.overflow) p_add(&V.cnt->overflow, 1);
 }
 
-// vertex v: move by d[v], wrap into the domain, record the wrap
-MCL_HD void p_body_move(const PView& V, const PF2* d, int v) {
-  PF2 p = V.pos[v];
+// vertex v at p: move by dv, wrap into the domain, record the wrap
+MCL_HD void p_move_with(const PView& V, int v, PF2 p, PF2 dv) {
   V.pos_old[v] = p;
   V.mark[v] = 0;
   V.wt[v] = (unsigned char)off_byte(Off{0, 0});
-  const PF2 dv = d[v];
   p.x = fadd(p.x, dv.x);
   p.y = fadd(p.y, dv.y);
   const Off w = wrap_position(p, V.lo, V.L);
@@ -289,17 +314,18 @@ MCL_HD void p_body_move(const PView& V, const PF2* d, int v) {
   V.wt[v] = (unsigned char)off_byte(w);
   if (!off_zero(w)) p_add(&V.cnt->wrapped, 1);
 }
+// vertex v: move by d[v]
+MCL_HD void p_body_move(const PView& V, const PF2* d, int v) { p_move_with(V, v, V.pos[v], d[v]); }
 
-// vertex v before the step: its target, the wrapped old position + d[v]
-// (the same arithmetic as p_body_move)
-MCL_HD void p_body_target(const PView& V, const PF2* d, int v) {
-  PF2 p = V.pos[v];
-  const PF2 dv = d[v];
+// vertex v at p before the step: its target, the wrapped p + dv (the same
+// arithmetic as p_move_with)
+MCL_HD void p_target_with(const PView& V, int v, PF2 p, PF2 dv) {
   p.x = fadd(p.x, dv.x);
   p.y = fadd(p.y, dv.y);
   wrap_position(p, V.lo, V.L);
   V.target[v] = p;
 }
+MCL_HD void p_body_target(const PView& V, const PF2* d, int v) { p_target_with(V, v, V.pos[v], d[v]); }
 
 // the exact difference to the copy of t nearest to p along one axis (both in
 // [lo, lo + L); t - p, t - L - p and t + L - p are exact by Sterbenz's lemma)
@@ -314,8 +340,7 @@ MCL_HD float p_toward(float t, float p, float L) {
 // is not at its target: half of it, or (last) all of it, which lands the
 // vertex exactly on its target; zero for the others.  Counts the vertices
 // still behind.
-MCL_HD void p_body_resume(const PView& V, PF2* d, int v, bool last) {
-  const PF2 p = V.pos[v], t = V.target[v];
+MCL_HD void p_resume_with(const PView& V, PF2* d, int v, PF2 p, PF2 t, bool last) {
   PF2 r{0.f, 0.f};
   if (p.x != t.x || p.y != t.y) {
     r.x = p_toward(t.x, p.x, V.L);
@@ -327,6 +352,9 @@ MCL_HD void p_body_resume(const PView& V, PF2* d, int v, bool last) {
     p_add(&V.cnt->behind, 1);
   }
   d[v] = r;
+}
+MCL_HD void p_body_resume(const PView& V, PF2* d, int v, bool last) {
+  p_resume_with(V, d, v, V.pos[v], V.target[v], last);
 }
 
 // vertex v, after a classification that found faces turned over: a marked
@@ -348,6 +376,18 @@ MCL_HD void p_body_revert(const PView& V, int v) {
   p_add(&V.cnt->reverted, 1);
 }
 
+// edge e of quad q: the wraps of its vertices (offset bytes wa..wd) into its
+// offset word
+MCL_HD void p_wrap_with(const PView& V, int e, unsigned char wa, unsigned char wb, unsigned char wc,
+                        unsigned char wd) {
+  const unsigned char r[4] = {wa, wb, wc, wd};
+  int delta = 0;
+  for (int k = 0; k < 4; ++k) {
+    const Off w = off_from_byte(r[k]);
+    if (!off_zero(w)) delta += eo_wrap_delta(k, w);
+  }
+  if (delta) V.eo[e] = V.eo[e] + (unsigned)delta;
+}
 // edge e: the wraps of its quad's vertices into its offset word
 MCL_HD void p_body_wrap(const PView& V, int e) {
   const PI4 q = V.ev[e];
@@ -355,13 +395,7 @@ MCL_HD void p_body_wrap(const PView& V, int e) {
     p_error(V, MCL_ERR_DEGENERATE_INPUT, 2);
     return;
   }
-  const int r[4] = {q.x, q.y, q.z, q.w};
-  int delta = 0;
-  for (int k = 0; k < 4; ++k) {
-    const Off w = off_from_byte(V.wv[r[k]]);
-    if (!off_zero(w)) delta += eo_wrap_delta(k, w);
-  }
-  if (delta) V.eo[e] = V.eo[e] + (unsigned)delta;
+  p_wrap_with(V, e, V.wv[q.x], V.wv[q.y], V.wv[q.z], V.wv[q.w]);
 }
 
 // the length, squared, of vertex v's current move on the torus (exact
@@ -383,23 +417,33 @@ MCL_HD int p_culprit(const PView& V, int a, int b, int c) {
   return best;
 }
 
-// edge e: orientation of its two faces and, when both are positive, the
-// incircle test; a non-Delaunay edge claims both faces for this round and
-// joins the round's list
-MCL_HD void p_body_classify(const PView& V, int e, unsigned stamp) {
-  const PI4 q = V.ev[e];
+// non-Delaunay edge e: its wings (en), a claim on both its faces for this
+// round, and a place in the round's list
+MCL_HD void p_claim_nd(const PView& V, int e, unsigned stamp) {
   const PI4 w = V.en[e];
-  const unsigned o = V.eo[e];
-  if (!p_vertices_ok(V, q) || !p_halfedges_ok(V, w)) {
+  if (!p_halfedges_ok(V, w)) {
     p_error(V, MCL_ERR_DEGENERATE_INPUT, 3);
     return;
   }
+  const unsigned long long key = p_key(e, stamp);
+  p_max(V.claim + p_face_a(e, w), key);
+  p_max(V.claim + p_face_b(e, w), key);
+  V.cand[e] = stamp;
+  V.clist[p_inc(&V.cnt->nondelaunay)] = e;
+}
+
+// edge e (record q with its vertices in range, offset word o, its quad's
+// vertices at pa .. pd in their canonical positions): orientation of its two
+// faces and, when both are positive, the incircle test; a non-Delaunay edge
+// reads its wings (en) and claims both faces for this round and joins the
+// round's list
+MCL_HD void p_classify_with(const PView& V, int e, unsigned stamp, PI4 q, unsigned o, PF2 pa, PF2 pb, PF2 pc,
+                            PF2 pd) {
   PF2 qb, qc, qd;
-  if (!quad_frame(o, V.pos[q.y], V.pos[q.z], V.pos[q.w], V.L, qb, qc, qd)) {
+  if (!quad_frame(o, pb, pc, pd, V.L, qb, qc, qd)) {
     p_error(V, MCL_ERR_DEGENERATE_INPUT, 4);  // an offset outside -1..+1
     return;
   }
-  const PF2 pa = V.pos[q.x];
   PLocal lc;
   const int sa = orient2d(pa.x, pa.y, qb.x, qb.y, qc.x, qc.y, &lc, &lc.overflow);
   const int sb = orient2d(qb.x, qb.y, pa.x, pa.y, qd.x, qd.y, &lc, &lc.overflow);
@@ -413,12 +457,17 @@ MCL_HD void p_body_classify(const PView& V, int e, unsigned stamp) {
   const bool nd =
       incircle_sos(pa.x, pa.y, qb.x, qb.y, qc.x, qc.y, qd.x, qd.y, q.x, q.y, q.z, q.w, &lc, &lc.overflow) > 0;
   p_flush(V, lc);
-  if (!nd) return;
-  const unsigned long long key = p_key(e, stamp);
-  p_max(V.claim + p_face_a(e, w), key);
-  p_max(V.claim + p_face_b(e, w), key);
-  V.cand[e] = stamp;
-  V.clist[p_inc(&V.cnt->nondelaunay)] = e;
+  if (nd) p_claim_nd(V, e, stamp);
+}
+// edge e: its record and positions, then p_classify_with
+MCL_HD void p_body_classify(const PView& V, int e, unsigned stamp) {
+  const PI4 q = V.ev[e];
+  const unsigned o = V.eo[e];
+  if (!p_vertices_ok(V, q)) {
+    p_error(V, MCL_ERR_DEGENERATE_INPUT, 3);
+    return;
+  }
+  p_classify_with(V, e, stamp, q, o, V.pos[q.x], V.pos[q.y], V.pos[q.z], V.pos[q.w]);
 }
 
 // edge e onto work-list k for the round with stamp `next`, once
@@ -426,6 +475,24 @@ MCL_HD void p_queue(const PView& V, int e, unsigned next, int k) {
   if (p_exch(V.qstamp + e, next) == next) return;
   int* wl = k ? V.wl1 : V.wl0;
   wl[p_inc(&V.cnt->lcount[k])] = e;
+}
+
+// the four wing edges of a flip onto work-list k for the round with stamp
+// `next`, each once: the four marks first, then one reservation for those
+// newly marked
+MCL_HD void p_queue4(const PView& V, int e0, int e1, int e2, int e3, unsigned next, int k) {
+  const int es[4] = {e0, e1, e2, e3};
+  bool put[4];
+  unsigned cnt = 0;
+  for (int i = 0; i < 4; ++i) {
+    put[i] = p_exch(V.qstamp + es[i], next) != next;
+    cnt += put[i] ? 1u : 0u;
+  }
+  if (!cnt) return;
+  int* wl = k ? V.wl1 : V.wl0;
+  unsigned long long at = p_inc_n(&V.cnt->lcount[k], cnt);
+  for (int i = 0; i < 4; ++i)
+    if (put[i]) wl[at++] = es[i];
 }
 
 // one side of a wing half-edge h: its apex, next and prev, and its apex offset byte
@@ -477,10 +544,7 @@ MCL_HD void p_body_flip(const PView& V, int e, unsigned stamp, int next) {
   p_set_face(V, p1, c, n0, h1, f.p1);
   p_set_face(V, n0, d, h1, p1, f.n0);
   p_add(&V.cnt->flips, 1);
-  p_queue(V, p0 >> 1, stamp + 1, next);
-  p_queue(V, n1 >> 1, stamp + 1, next);
-  p_queue(V, p1 >> 1, stamp + 1, next);
-  p_queue(V, n0 >> 1, stamp + 1, next);
+  p_queue4(V, p0 >> 1, n1 >> 1, p1 >> 1, n0 >> 1, stamp + 1, next);
 }
 
 constexpr int kPeriodicMaxDeg = 4096;

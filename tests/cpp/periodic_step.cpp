@@ -1,11 +1,13 @@
 // Serial run, on the CPU, of the periodic step's kernel bodies
-// (mcleap_gb300/csrc/periodic.cuh) in the order the GPU launches them: move +
+// (mcleap_gb300/csrc/periodic.cuh) in the order of the GPU step's phases: move +
 // wrap every vertex, fold the wraps into every edge word, then rounds of
 // classify-all and either (faces turned over) send their moved vertices back
-// and fold again, or flip the winners, until no edge is non-Delaunay.  A serial run of
-// one launch gives the GPU's result (claims are max-reductions, one round's
-// flips write disjoint fields), so this checks the device code's logic and
-// indexing without a GPU.
+// and fold again, or flip the winners, until no edge is non-Delaunay.  (The GPU
+// folds each edge's wraps just before classifying it, in the same pass; an
+// edge's fold touches only its own word, so the order is equivalent.)  A serial
+// run of one phase gives the GPU's result (claims are max-reductions, one
+// round's flips write disjoint fields), so this checks the device code's logic
+// and indexing without a GPU.
 //
 //   periodic_step IN OUT
 //   IN : int32 n, int32 E, float L, float r (FRNN radius), float pos[n][2], float d[n][2],

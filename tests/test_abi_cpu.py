@@ -65,7 +65,7 @@ NULL_MESH_CALLS = {
     "mcl_move": 2, "mcl_integrate": 3, "mcl_untangle": 2, "mcl_delaunay_restore": 2, "mcl_step": 3,
     "mcl_step_host": 3, "mcl_step_host_async": 3, "mcl_mesh_last_status": 2,
     "mcl_mesh_set_removal_tile": 1, "mcl_mesh_get_removal_tile": 1, "mcl_mesh_export_aos": 4,
-    "mcl_walk_seeded": 8, "mcl_debug_remove_timeline": 1,
+    "mcl_walk_seeded": 8, "mcl_debug_remove_timeline": 1, "mcl_periodic_debug_timeline": 2,
 }
 
 
