@@ -360,7 +360,11 @@ __device__ void phase_classify(cg::grid_group& g, const KParams& P, unsigned qst
           if (__float_as_uint(np[j].x) != __float_as_uint(po.x) || __float_as_uint(np[j].y) != __float_as_uint(po.y))
             mv[km++] = v[j];
         }
-      if (__any_sync(kFull, km > 0)) warp_push(mv, km, P.vl0, &P.st->vl_count[0], P.V, P.st);
+      // once the list is past the sparse limit the full pass runs: stop listing
+      // (a step that moves every vertex would otherwise append them all)
+      if (__any_sync(kFull, km > 0) && P.sparse_ok &&
+          (long long)ld_i(&P.st->vl_count[0]) * kSparseEdgesPerMover < (long long)P.E_it)
+        warp_push(mv, km, P.vl0, &P.st->vl_count[0], P.V, P.st);
     }
     if (kFixedPos) timeline_max(P, 43);
     g.sync();
