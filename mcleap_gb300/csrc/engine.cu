@@ -74,6 +74,62 @@ __device__ __forceinline__ void warp_push(const int (&mine)[K], int k, int* gl, 
 
 #define set_error(P, code) flag_error_at(P, code, __LINE__)
 
+// A per-thread count added to a global counter with one atomic per warp (every
+// lane calls it): after a pass in which most threads count something, one
+// atomic per thread on a single address would queue for tens of microseconds.
+template <typename T>
+__device__ __forceinline__ void warp_add(T* p, long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(kFull, v, o);
+  if ((threadIdx.x & 31) == 0 && v) atomicAdd(p, (T)v);
+}
+
+// A warp's appends to a global list gathered in a shared-memory buffer of
+// kWarpBuf entries and written out with one atomicAdd per flush (when the next
+// append could overflow it, and at the end of the pass): a pass whose every
+// warp appends on most iterations (the classification of a step that moves
+// every vertex by a random walk) would otherwise queue thousands of atomics on
+// one counter.  `n` is the same in every lane; calls are warp-uniform.
+constexpr int kWarpBuf = 128;
+struct WarpBuf {
+  int* buf;  // this warp's kWarpBuf slots
+  int n;
+};
+__device__ __forceinline__ void wb_flush(WarpBuf& b, int* gl, int* gcount, int gcap, DevState* st) {
+  if (b.n == 0) return;
+  const int lane = threadIdx.x & 31;
+  int base = 0;
+  if (lane == 0) base = atomicAdd(gcount, b.n);
+  base = __shfl_sync(kFull, base, 0);
+  for (int i = lane; i < b.n; i += 32) {
+    if (base + i < gcap) __stcg(gl + base + i, b.buf[i]);
+    else if (atomicCAS(&st->status, MCL_OK, MCL_ERR_CAPACITY) == MCL_OK) st->site = __LINE__;
+  }
+  __syncwarp();  // every lane has read the buffer before it is refilled
+  b.n = 0;
+}
+template <int K>
+__device__ __forceinline__ void wb_push(WarpBuf& b, const int (&mine)[K], int k, int* gl, int* gcount, int gcap,
+                                        DevState* st) {
+  static_assert(32 * K <= kWarpBuf, "one append must fit an empty buffer");
+  const int lane = threadIdx.x & 31;
+  int x = k;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(kFull, x, o);
+    if (lane >= o) x += y;
+  }
+  const int total = __shfl_sync(kFull, x, 31);
+  if (total == 0) return;
+  if (b.n + total > kWarpBuf) wb_flush(b, gl, gcount, gcap, st);
+  const int off = b.n + x - k;
+#pragma unroll
+  for (int j = 0; j < K; ++j)
+    if (j < k) b.buf[off + j] = mine[j];
+  __syncwarp();  // the entries are visible to the lanes of a later flush
+  b.n += total;
+}
+
 // This thread's position in the spread order used by whole-grid loops over a
 // work-list: warp slot w of block b has spread index w * gridDim.x + b, so a
 // short list is dealt out one warp per block (across every SM) instead of
@@ -243,6 +299,9 @@ constexpr int kMoveUnroll = 4;
 // iteration's records are requested before the move pass, which hides them.
 constexpr int kEvStages = 2;
 __shared__ int4 s_ev[kEvStages][kClassifyUnroll][kThreads];
+// the classification's append buffers (non-Delaunay edges, edges of a face
+// turned over): kWarpBuf entries per warp each
+__shared__ int s_wbuf[2][kThreads / 32][kWarpBuf];
 
 __device__ __forceinline__ void cp_async16(int4* smem, const int4* gmem) {
   const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
@@ -323,7 +382,7 @@ __device__ void classify_movers(const KParams& P, int nm, unsigned qstamp, unsig
     });
     if (!ok) flag_error(P, MCL_ERR_DEGENERATE_INPUT);
   }
-  if (bad) atomicAdd(&P.st->inverted, bad);
+  warp_add(&P.st->inverted, bad);
 }
 
 template <bool kFixedPos>
@@ -380,6 +439,7 @@ __device__ void phase_classify(cg::grid_group& g, const KParams& P, unsigned qst
   int bad = 0;
   unsigned ninc = 0;
   int def0 = -1, def1 = -1;  // edges deferred to the full ladder after the loop
+  WarpBuf wnd{s_wbuf[0][threadIdx.x >> 5], 0}, winv{s_wbuf[1][threadIdx.x >> 5], 0};
   // kClassifyUnroll edges per thread and iteration, their records and
   // positions loaded before any is evaluated (memory-level parallelism: the
   // pass is latency-bound on the position gathers); edge j of the iteration
@@ -437,7 +497,10 @@ __device__ void phase_classify(cg::grid_group& g, const KParams& P, unsigned qst
         const int si = incircle_fp32(a.x, a.y, b.x, b.y, c.x, c.y, d.x, d.y);
         if (si == 2) {
           defer = true;
-        } else if (si > 0 && enqueue_once(P, e[j], qstamp)) {
+        } else if (si > 0) {
+          // each edge comes once in this pass and qstamp is the launch's
+          // first stamp: the queue mark is a plain store (no atomic waited for)
+          __stcg(P.qmark + e[j], qstamp);
           claim_edge(P, e[j], sc);
           mine[k++] = e[j];
         }
@@ -448,12 +511,14 @@ __device__ void phase_classify(cg::grid_group& g, const KParams& P, unsigned qst
         else hard[kh++] = e[j];
       }
     }
-    if (__any_sync(kFull, k > 0)) warp_push(mine, k, P.wl0, &P.st->wl_count[0], P.E, P.st);
+    if (__any_sync(kFull, k > 0)) wb_push(wnd, mine, k, P.wl0, &P.st->wl_count[0], P.E, P.st);
     if (__any_sync(kFull, kh > 0)) warp_push(hard, kh, P.hard, &P.st->hard_count, P.E, P.st);
     // edges with a non-positive face: the repair's first send-back pass
     // starts from them (work-list 1 is free until the flip rounds)
-    if (__any_sync(kFull, ki > 0)) warp_push(inv, ki, P.wl1, &P.st->wl_count[1], P.E, P.st);
+    if (__any_sync(kFull, ki > 0)) wb_push(winv, inv, ki, P.wl1, &P.st->wl_count[1], P.E, P.st);
   }
+  wb_flush(wnd, P.wl0, &P.st->wl_count[0], P.E, P.st);
+  wb_flush(winv, P.wl1, &P.st->wl_count[1], P.E, P.st);
   cp_async_wait<0>();  // nothing left in flight into the staging slots
   // the deferred edges, with the full predicate ladder (out of the loop, so
   // the out-of-line calls do not weigh on the loop above)
@@ -477,7 +542,7 @@ __device__ void phase_classify(cg::grid_group& g, const KParams& P, unsigned qst
     if (__any_sync(kFull, ki > 0)) warp_push(inv, ki, P.wl1, &P.st->wl_count[1], P.E, P.st);
   }
   lc.incircle += ninc;
-  if (bad) atomicAdd(&P.st->inverted, bad);
+  warp_add(&P.st->inverted, bad);
   if (kFixedPos) timeline_max(P, 45);
 }
 
@@ -555,6 +620,7 @@ __device__ __forceinline__ int lawson_round(const KParams& P, const int* in, int
   }
   int flips = 0;
   const int lane = threadIdx.x & 31;
+  WarpBuf wb{s_wbuf[0][threadIdx.x >> 5], 0};
   for (int base = t0 - lane; base < n; base += nt) {
     const int i = base + lane;
     int mine[4];
@@ -585,8 +651,9 @@ __device__ __forceinline__ int lawson_round(const KParams& P, const int* in, int
         }
       }
     }
-    if (__any_sync(kFull, k > 0)) warp_push(mine, k, out, out_count, P.E, P.st);
+    if (__any_sync(kFull, k > 0)) wb_push(wb, mine, k, out, out_count, P.E, P.st);
   }
+  wb_flush(wb, out, out_count, P.E, P.st);
   return flips;
 }
 
@@ -705,14 +772,34 @@ __device__ __forceinline__ void list_for_next_pass(const KParams& P, int v, int 
   push_coalesced(P, (pass & 1) ? P.vl1 : P.vl0, &P.st->fix_list[pass % 3], P.V, v);
 }
 
-// A newly marked vertex records the pass that marked it in vloc (free until
-// the insertion rounds), joins the list of every vertex sent back (`hard`,
-// free after the classification) and the next pass's list.
-__device__ void mark_vertex(const KParams& P, int v, int& fresh, unsigned fs, int pass) {
-  if (!marked(P, v, fs) && (unsigned)atomicExch(P.vmark + v, (int)fs) != fs) {
-    __stcg(P.vloc + v, pass);
+// Where a fixpoint pass's marks go: appended at once from divergent code
+// (MarkNow), or kept by the thread (at most two per work item) for one
+// warp-wide buffered append afterwards (MarkLater).  A fresh vertex joins the
+// list of every vertex sent back (`hard`) and the next pass's list; a vertex
+// listed again joins the next pass's list.
+struct MarkNow {
+  const KParams& P;
+  int pass;
+  __device__ void fresh_vertex(int v) const {
     push_coalesced(P, P.hard, &P.st->fix_all, P.E, v);
     list_for_next_pass(P, v, pass);
+  }
+  __device__ void relist(int v) const { list_for_next_pass(P, v, pass); }
+};
+struct MarkLater {
+  int nv[2], rl[2];
+  int kn = 0, kr = 0;
+  __device__ void fresh_vertex(int v) { nv[kn++ & 1] = v; }
+  __device__ void relist(int v) { rl[kr++ & 1] = v; }
+};
+
+// A newly marked vertex records the pass that marked it in vloc (free until
+// the insertion rounds) and goes to the sink.
+template <typename Sink>
+__device__ void mark_vertex(const KParams& P, int v, int& fresh, unsigned fs, int pass, Sink& sink) {
+  if (!marked(P, v, fs) && (unsigned)atomicExch(P.vmark + v, (int)fs) != fs) {
+    __stcg(P.vloc + v, pass);
+    sink.fresh_vertex(v);
     ++fresh;
   }
 }
@@ -727,7 +814,8 @@ __device__ void mark_vertex(const KParams& P, int v, int& fresh, unsigned fs, in
 // A bad face whose free vertices all turned out marked (by other faces of the
 // same pass, after its orientation was read) is checked again next pass
 // through the star of one of them.
-__device__ void mark_face(const KParams& P, int a, int b, int c, int& fresh, unsigned fs, int pass) {
+template <typename Sink>
+__device__ void mark_face(const KParams& P, int a, int b, int c, int& fresh, unsigned fs, int pass, Sink& sink) {
   const int t[3] = {a, b, c};
   int pick = -1, any = -1;
   float best = -1.f;
@@ -745,10 +833,10 @@ __device__ void mark_face(const KParams& P, int a, int b, int c, int& fresh, uns
     if (m2 > best || (m2 == best && v < pick)) { best = m2; pick = v; }
   }
   if (pick >= 0) {
-    mark_vertex(P, pick, fresh, fs, pass);
+    mark_vertex(P, pick, fresh, fs, pass, sink);
   } else if (any >= 0) {
     // vloc of a marked vertex holds a pass of this launch: list it once per pass
-    if (atomicExch(P.vloc + any, pass) != pass) list_for_next_pass(P, any, pass);
+    if (atomicExch(P.vloc + any, pass) != pass) sink.relist(any);
     ++fresh;
   }
 }
@@ -769,25 +857,41 @@ __device__ bool phase_fixpoint(cg::grid_group& g, const KParams& P, LocalCounter
     if (pass == 0) {
       // every face the classification found non-positive, once per edge
       // side (its edges are on work-list 1)
+      // (most warps mark on most iterations: the marks go through the
+      // warp's append buffers, idle after the classification)
       const int nb = ld_i(&P.st->wl_count[1]);
-      for (int ii = spread_tid(); ii < nb; ii += stride) {
-        const int e = ld_i(P.wl1 + ii);
-        const int4 q = ld_ev(P, e);
-        if (q.x < 0) continue;
-        if (bad_v(P, q.x) || bad_v(P, q.y) || q.z >= P.V || q.w >= P.V) {
-          flag_error(P, MCL_ERR_DEGENERATE_INPUT);
-          continue;
+      const int lane = threadIdx.x & 31;
+      WarpBuf whard{s_wbuf[0][threadIdx.x >> 5], 0}, wnext{s_wbuf[1][threadIdx.x >> 5], 0};
+      int* nlist = (pass & 1) ? P.vl1 : P.vl0;
+      int* ncount = &P.st->fix_list[pass % 3];
+      for (int base = spread_tid() - lane; base < nb; base += stride) {
+        const int ii = base + lane;
+        MarkLater ml;
+        if (ii < nb) {
+          const int e = ld_i(P.wl1 + ii);
+          const int4 q = ld_ev(P, e);
+          if (q.x >= 0 && (bad_v(P, q.x) || bad_v(P, q.y) || q.z >= P.V || q.w >= P.V)) {
+            flag_error(P, MCL_ERR_DEGENERATE_INPUT);
+          } else if (q.x >= 0) {
+            const float2 a = qpos(P, q.x, fs), b = qpos(P, q.y, fs);
+            if (q.z >= 0 && orient_v(P, a, b, qpos(P, q.z, fs), lc) <= 0) {
+              ++bad;
+              mark_face(P, q.x, q.y, q.z, fresh, fs, pass, ml);
+            }
+            if (q.w >= 0 && orient_v(P, b, a, qpos(P, q.w, fs), lc) <= 0) {
+              ++bad;
+              mark_face(P, q.y, q.x, q.w, fresh, fs, pass, ml);
+            }
+          }
         }
-        const float2 a = qpos(P, q.x, fs), b = qpos(P, q.y, fs);
-        if (q.z >= 0 && orient_v(P, a, b, qpos(P, q.z, fs), lc) <= 0) {
-          ++bad;
-          mark_face(P, q.x, q.y, q.z, fresh, fs, pass);
+        if (__any_sync(kFull, ml.kn > 0)) {
+          wb_push(whard, ml.nv, ml.kn, P.hard, &P.st->fix_all, P.E, P.st);
+          wb_push(wnext, ml.nv, ml.kn, nlist, ncount, P.V, P.st);
         }
-        if (q.w >= 0 && orient_v(P, b, a, qpos(P, q.w, fs), lc) <= 0) {
-          ++bad;
-          mark_face(P, q.y, q.x, q.w, fresh, fs, pass);
-        }
+        if (__any_sync(kFull, ml.kr > 0)) wb_push(wnext, ml.rl, ml.kr, nlist, ncount, P.V, P.st);
       }
+      wb_flush(whard, P.hard, &P.st->fix_all, P.E, P.st);
+      wb_flush(wnext, nlist, ncount, P.V, P.st);
     } else {
       // only a face with a vertex sent back (or listed again) in the last pass
       // can have changed sign: the stars of the last pass's list
@@ -801,14 +905,15 @@ __device__ bool phase_fixpoint(cg::grid_group& g, const KParams& P, LocalCounter
           if (bad_v(P, d) || a < 0 || bad_v(P, a)) return;  // hull side: no face
           if (orient_v(P, pv, qpos(P, d, fs), qpos(P, a, fs), lc) <= 0) {
             ++bad;
-            mark_face(P, v, d, a, fresh, fs, pass);
+            MarkNow now{P, pass};
+            mark_face(P, v, d, a, fresh, fs, pass, now);
           }
         });
         if (!ok) flag_error(P, MCL_ERR_DEGENERATE_INPUT);
       }
     }
-    if (fresh) atomicAdd(&P.st->fix_new[slot], fresh);
-    if (bad) atomicAdd(&P.st->fix_bad[slot], bad);
+    warp_add(&P.st->fix_new[slot], fresh);
+    warp_add(&P.st->fix_bad[slot], bad);
     g.sync();
     if (pass < 16) timeline_remove(P, 48 + pass);
     const int nfresh = ld_i(&P.st->fix_new[slot]);
@@ -871,10 +976,22 @@ struct SmallPoly {
 
 // Clip the star polygon of v given its k spokes sp (counter-clockwise), the
 // link half-edges lk (lk[i] = next(sp[i]), the side of face i opposite v),
-// their origins w and, in poly, their positions; bnd is scratch of size k.
+// their origins w and, in poly, their positions; pv is v's position, at which
+// its star is valid; bnd is scratch of size k.
+//
+// Ears by a constant-time test while v stays strictly inside the kernel of the
+// remaining polygon (checked at the start: every face of the star positive):
+// then the corners are in strictly increasing angle around v, and a convex
+// corner b between a and c whose diagonal a -> c has v strictly on its left
+// spans an angle below 180 degrees from v; the cone of that angle is convex,
+// holds the triangle abc and no other corner, so abc is an ear, and the new
+// side a -> c keeps v strictly inside the kernel.  Only when no corner passes
+// does the general test run (every other corner checked against the
+// triangle, O(k) per candidate); an ear it clips whose diagonal does not have
+// v strictly on its left ends the constant-time tests for this star.
 template <typename Poly>
-__device__ int clip_star(const KParams& P, int v, LocalCounters& lc, unsigned mk, int k, const int* sp, const int* lk,
-                         const int* w, Poly& poly, int* bnd) {
+__device__ int clip_star(const KParams& P, int v, float2 pv, LocalCounters& lc, unsigned mk, int k, const int* sp,
+                         const int* lk, const int* w, Poly& poly, int* bnd) {
   if (k < 3) return MCL_ERR_DEGENERATE_INPUT | (__LINE__ << 8);
   const int mbase = reserve_marks(P, mk, 2 * k - 3);  // its latency overlaps the clipping
   for (int j = 0; j < k; ++j) {
@@ -883,8 +1000,20 @@ __device__ int clip_star(const KParams& P, int v, LocalCounters& lc, unsigned mk
     bnd[j] = lk[j];
   }
   int remaining = k, j = 0, used = 3;
+  // v strictly inside the kernel of the remaining polygon (checked: every
+  // side w_i -> w_i+1 has v strictly on its left)
+  bool kernel = true;
+  for (int i = 0; i < k && kernel; ++i) kernel = orient_v(P, poly.q(i), poly.q(poly.nx(i)), pv, lc) > 0;
   while (remaining > 3) {
     bool found = false;
+    if (kernel) {
+      for (int t = 0; t < remaining && !found; ++t) {
+        const int a = poly.pv(j), b = j, c = poly.nx(j);
+        const float2 qa = poly.q(a), qb = poly.q(b), qc = poly.q(c);
+        found = orient_v(P, qa, qc, pv, lc) > 0 && orient_v(P, qa, qb, qc, lc) > 0;
+        if (!found) j = poly.nx(j);
+      }
+    }
     for (int t = 0; t < remaining && !found; ++t) {
       const int a = poly.pv(j), b = j, c = poly.nx(j);
       const float2 qa = poly.q(a), qb = poly.q(b), qc = poly.q(c);
@@ -897,6 +1026,7 @@ __device__ int clip_star(const KParams& P, int v, LocalCounters& lc, unsigned mk
             empty = false;
         }
         found = empty;
+        if (found && kernel && orient_v(P, qa, qc, pv, lc) <= 0) kernel = false;
       }
       if (!found) j = poly.nx(j);
     }
@@ -975,7 +1105,7 @@ __device__ int remove_vertex_ears(const KParams& P, int v, LocalCounters& lc, un
     h = he_prev(P, h) ^ 1;
     if (bad_h(P, h)) return MCL_ERR_DEGENERATE_INPUT | (__LINE__ << 8);
   } while (h != s0);
-  return clip_star(P, v, lc, mk, k, sp, lk, w, poly, bnd);
+  return clip_star(P, v, ldpos(P, v), lc, mk, k, sp, lk, w, poly, bnd);
 }
 
 // A star walked once per removal round and kept by its thread across the
@@ -1028,11 +1158,11 @@ __device__ int remove_cached(const KParams& P, int v, const StarCache& sc, Local
   if (k <= kSmallStar) {
     SmallPoly poly;
     for (int i = 0; i < k; ++i) poly.set_q(i, ldpos(P, w[i]));
-    return clip_star(P, v, lc, mk, k, sc.sp, sc.lk, w, poly, bnd);
+    return clip_star(P, v, ldpos(P, v), lc, mk, k, sc.sp, sc.lk, w, poly, bnd);
   }
   LocalPoly poly;
   for (int i = 0; i < k; ++i) poly.set_q(i, ldpos(P, w[i]));
-  return clip_star(P, v, lc, mk, k, sc.sp, sc.lk, w, poly, bnd);
+  return clip_star(P, v, ldpos(P, v), lc, mk, k, sc.sp, sc.lk, w, poly, bnd);
 }
 
 // ---------------------------------------------------------------------------
@@ -1206,6 +1336,7 @@ __device__ bool phase_remove(cg::grid_group& g, const KParams& P, unsigned& stam
     g.sync();
     if (round < 16) timeline_remove(P, 4 * round + 1);
     int removed = 0, flips = 0;
+    WarpBuf wb{s_wbuf[0][threadIdx.x >> 5], 0};
     for (int base = wid * T; base < n; base += di) {
       const int i = lane < T ? base + lane : n;
       int mine[1];
@@ -1234,10 +1365,11 @@ __device__ bool phase_remove(cg::grid_group& g, const KParams& P, unsigned& stam
           mine[k++] = v;
         }
       }
-      warp_push(mine, k, out, &P.st->vl_count[dst], P.V, P.st);
+      wb_push(wb, mine, k, out, &P.st->vl_count[dst], P.V, P.st);
     }
-    if (removed) atomicAdd(&P.st->c[C_REMOVED], (unsigned long long)removed);
-    if (flips) atomicAdd(&P.st->c[C_REMOVAL_FLIPS], (unsigned long long)flips);
+    wb_flush(wb, out, &P.st->vl_count[dst], P.V, P.st);
+    warp_add(&P.st->c[C_REMOVED], removed);
+    warp_add(&P.st->c[C_REMOVAL_FLIPS], flips);
     g.sync();
     if (round < 16) timeline_remove(P, 4 * round + 2);
     src = dst;
@@ -1485,6 +1617,7 @@ __device__ bool phase_insert(cg::grid_group& g, const KParams& P, unsigned& stam
     g.sync();
     timeline_insert(P, round, 1);
     int inserted = 0;
+    WarpBuf wagain{s_wbuf[1][threadIdx.x >> 5], 0};
     for (int base = spread_tid() - (int)(threadIdx.x & 31); base < n; base += stride) {
       const int i = base + (int)(threadIdx.x & 31);
       int mine[8];
@@ -1543,8 +1676,9 @@ __device__ bool phase_insert(cg::grid_group& g, const KParams& P, unsigned& stam
         }
       }
       warp_push(mine, k, P.wl0, &P.st->wl_count[0], P.E, P.st);
-      warp_push(again, ka, out, &P.st->vl_count[dst], P.V, P.st);
+      wb_push(wagain, again, ka, out, &P.st->vl_count[dst], P.V, P.st);
     }
+    wb_flush(wagain, out, &P.st->vl_count[dst], P.V, P.st);
     (void)inserted;
     g.sync();
     timeline_insert(P, round, 2);
@@ -1818,7 +1952,7 @@ __device__ void phase_substeps(cg::grid_group& g, const KParams& P, unsigned& st
       if (src || i >= np) __stcg(P.vl0 + i, ld_i(P.vl2 + i));
   }
   if (gtid == 0) P.st->vl_count[0] = np + nl;
-  if (done) atomicAdd(&P.st->c[C_SUBSTEP_DONE], (unsigned long long)done);
+  warp_add(&P.st->c[C_SUBSTEP_DONE], done);
   g.sync();
 }
 
@@ -1855,6 +1989,7 @@ __device__ __noinline__ unsigned repair_step(cg::grid_group g, const KParams P, 
     if (gtid == 0) { P.st->vl_count[0] = 0; P.st->vl_count[1] = 0; }
     g.sync();
     const int nsb = few ? nall : P.V_it;
+    WarpBuf wrev{s_wbuf[0][threadIdx.x >> 5], 0};
     for (int base = (few ? spread_tid() - (int)(threadIdx.x & 31) : blockIdx.x * blockDim.x); base < nsb;
          base += stride) {
       const int vi = base + (few ? (int)(threadIdx.x & 31) : (int)threadIdx.x);
@@ -1870,8 +2005,9 @@ __device__ __noinline__ unsigned repair_step(cg::grid_group g, const KParams P, 
           mine[k++] = v;
         }
       }
-      warp_push(mine, k, P.vl0, &P.st->vl_count[0], P.V, P.st);
+      wb_push(wrev, mine, k, P.vl0, &P.st->vl_count[0], P.V, P.st);
     }
+    wb_flush(wrev, P.vl0, &P.st->vl_count[0], P.V, P.st);
     g.sync();
     const int nrev = ld_i(&P.st->vl_count[0]);
     if (gtid == 0) P.st->c[C_REVERTED] += (unsigned long long)nrev;
@@ -1914,6 +2050,7 @@ __device__ __noinline__ unsigned repair_step(cg::grid_group g, const KParams P, 
       // else by a pass over the vertices
       const bool from_list = few && !(nrev > 0 && P.substeps > 0);
       const int nscan = from_list ? nall : P.V_it;
+      WarpBuf wins{s_wbuf[0][threadIdx.x >> 5], 0};
       for (int base = (from_list ? spread_tid() - (int)(threadIdx.x & 31) : blockIdx.x * blockDim.x); base < nscan;
            base += stride) {
         const int vi = base + (from_list ? (int)(threadIdx.x & 31) : (int)threadIdx.x);
@@ -1924,8 +2061,9 @@ __device__ __noinline__ unsigned repair_step(cg::grid_group g, const KParams P, 
           __stcg(P.pos + v, __ldcg(P.target + v));
           mine[k++] = v;
         }
-        warp_push(mine, k, P.vl0, &P.st->vl_count[0], P.V, P.st);
+        wb_push(wins, mine, k, P.vl0, &P.st->vl_count[0], P.V, P.st);
       }
+      wb_flush(wins, P.vl0, &P.st->vl_count[0], P.V, P.st);
       g.sync();
       if (ok) ok = phase_insert(g, Q, stamp, lc, mk);
       g.sync();
@@ -1944,20 +2082,23 @@ __device__ __noinline__ unsigned repair_step(cg::grid_group g, const KParams P, 
       if (rebuild) {
         if (gtid == 0) { P.st->wl_count[0] = 0; P.st->wl_count[1] = 0; }
         g.sync();
+        WarpBuf wb{s_wbuf[0][threadIdx.x >> 5], 0};
         for (int base = blockIdx.x * blockDim.x; base < P.E_it; base += stride) {
           const int ei = base + threadIdx.x;
           const int e = ei < P.E_it ? edge_at(P, ei) : -1;
           int mine[1];
           int k = 0;
           if (e >= 0 && (unsigned)ld_i(reinterpret_cast<const int*>(P.qmark) + e) == mk) mine[k++] = e;
-          if (__any_sync(kFull, k > 0)) warp_push(mine, k, P.wl0, &P.st->wl_count[0], P.E, P.st);
+          if (__any_sync(kFull, k > 0)) wb_push(wb, mine, k, P.wl0, &P.st->wl_count[0], P.E, P.st);
         }
+        wb_flush(wb, P.wl0, &P.st->wl_count[0], P.E, P.st);
         g.sync();
         phase_lawson<false>(g, Q, 0, stamp, lc, 0);
       } else {
         const unsigned du = stamp++;  // first sight of an edge in this pass (cand is free until the flip rounds)
         if (gtid == 0) P.st->wl_count[1] = 0;
         g.sync();
+        WarpBuf wb{s_wbuf[0][threadIdx.x >> 5], 0};
         for (int base = spread_tid() - (int)(threadIdx.x & 31); base < nw; base += stride) {
           const int i = base + (int)(threadIdx.x & 31);
           int mine[1];
@@ -1966,8 +2107,9 @@ __device__ __noinline__ unsigned repair_step(cg::grid_group g, const KParams P, 
             const int e = ld_i(P.wl0 + i);
             if (e >= 0 && e < P.E && atomicMax(P.cand + e, du) < du) mine[k++] = e;
           }
-          if (__any_sync(kFull, k > 0)) warp_push(mine, k, P.wl1, &P.st->wl_count[1], P.E, P.st);
+          if (__any_sync(kFull, k > 0)) wb_push(wb, mine, k, P.wl1, &P.st->wl_count[1], P.E, P.st);
         }
+        wb_flush(wb, P.wl1, &P.st->wl_count[1], P.E, P.st);
         if (gtid == 0) P.st->wl_count[0] = 0;
         g.sync();
         phase_lawson<false>(g, Q, 1, stamp, lc, 0);
