@@ -1336,6 +1336,7 @@ __device__ bool phase_remove(cg::grid_group& g, const KParams& P, unsigned& stam
     g.sync();
     if (round < 16) timeline_remove(P, 4 * round + 1);
     int removed = 0, flips = 0;
+    unsigned long long slow = 0;  // the slowest removal of this thread: cycles << 16 | spokes
     WarpBuf wb{s_wbuf[0][threadIdx.x >> 5], 0};
     for (int base = wid * T; base < n; base += di) {
       const int i = lane < T ? base + lane : n;
@@ -1355,10 +1356,8 @@ __device__ bool phase_remove(cg::grid_group& g, const KParams& P, unsigned& stam
             deg = 0;
             if (round < 16) atomicAdd(&P.st->rm_uncached[round], 1ull);
           }
-          if (round < 16) {
-            const unsigned long long dt = (unsigned long long)(clock64() - t0);
-            atomicMax(&P.st->rm_slow[round], (dt << 16) | (unsigned long long)(deg & 0xffff));
-          }
+          const unsigned long long dt = (unsigned long long)(clock64() - t0);
+          slow = max(slow, (dt << 16) | (unsigned long long)(deg & 0xffff));
           if (rc != MCL_OK) flag_error_at(P, rc & 0xff, 100000 + (rc >> 8));
           else ++removed;
         } else if (ld_i(&P.st->status) == MCL_OK) {
@@ -1368,6 +1367,9 @@ __device__ bool phase_remove(cg::grid_group& g, const KParams& P, unsigned& stam
       wb_push(wb, mine, k, out, &P.st->vl_count[dst], P.V, P.st);
     }
     wb_flush(wb, out, &P.st->vl_count[dst], P.V, P.st);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) slow = max(slow, __shfl_down_sync(kFull, slow, o));
+    if (round < 16 && lane == 0 && slow) atomicMax(&P.st->rm_slow[round], slow);
     warp_add(&P.st->c[C_REMOVED], removed);
     warp_add(&P.st->c[C_REMOVAL_FLIPS], flips);
     g.sync();
