@@ -938,6 +938,10 @@ __device__ bool phase_fixpoint(cg::grid_group& g, const KParams& P, LocalCounter
 // closed triangle holds no other polygon vertex, so this always completes.
 // The k spoke edges become k-3 diagonals plus the 3 free edges of v.
 constexpr int kEarMax = 128;
+// Loads per group issued before any of their values is stored: a loop that
+// stores each loaded value (to local or shared memory) before the next load
+// waits for every load in turn.
+constexpr int kGather = 8;
 
 // The star polygon under ear clipping: cyclic links and corner positions.
 // Any star up to kEarMax corners: local arrays.
@@ -1052,9 +1056,19 @@ __device__ int clip_star(const KParams& P, int v, float2 pv, LocalCounters& lc, 
     he_set_face(P, bnd[c], w[b], bnd[a], bnd[b]);
     __stcg(P.vhint + v, bnd[a]);
   }
-  for (int i = 0; i < k; ++i) {
-    if (ld_i(P.vhe + w[i]) == (sp[i] ^ 1)) __stcg(P.vhe + w[i], lk[i]);
-    mark_edge(P, lk[i] >> 1, mk);  // the hole's sides face new triangles
+  for (int i0 = 0; i0 < k; i0 += kGather) {
+    // the corners' anchors kGather at a time, loaded before any is rewritten
+    // (the corners are distinct, so no store of a group aliases its loads)
+    int vh[kGather];
+#pragma unroll
+    for (int u = 0; u < kGather; ++u) vh[u] = i0 + u < k ? ld_i(P.vhe + w[i0 + u]) : -1;
+#pragma unroll
+    for (int u = 0; u < kGather; ++u) {
+      const int i = i0 + u;
+      if (i >= k) continue;
+      if (vh[u] == (sp[i] ^ 1)) __stcg(P.vhe + w[i], lk[i]);
+      mark_edge(P, lk[i] >> 1, mk);  // the hole's sides face new triangles
+    }
   }
   if (mbase >= 0) {
     // the list entries: the sides and the diagonals (the spoke slots sp[3..k)
@@ -1072,14 +1086,21 @@ __device__ int clip_star(const KParams& P, int v, float2 pv, LocalCounters& lc, 
   // v; so do the edges between consecutive hull points)
   int anchor = w[0];
   {
-    const float2 p0 = ldpos(P, v);
+    const float2 p0 = pv;
     float best = INFINITY;
-    for (int i = 0; i < k; ++i) {
-      if (P.vfix[w[i]]) continue;
-      const float2 qi = poly.q(i);
-      const float dx = __fsub_rn(qi.x, p0.x), dy = __fsub_rn(qi.y, p0.y);
-      const float d2 = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
-      if (d2 < best) { best = d2; anchor = w[i]; }
+    for (int i0 = 0; i0 < k; i0 += kGather) {
+      unsigned char fx[kGather];
+#pragma unroll
+      for (int u = 0; u < kGather; ++u) fx[u] = i0 + u < k ? P.vfix[w[i0 + u]] : 1;
+#pragma unroll
+      for (int u = 0; u < kGather; ++u) {
+        if (fx[u]) continue;
+        const int i = i0 + u;
+        const float2 qi = poly.q(i);
+        const float dx = __fsub_rn(qi.x, p0.x), dy = __fsub_rn(qi.y, p0.y);
+        const float d2 = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
+        if (d2 < best) { best = d2; anchor = w[i]; }
+      }
     }
   }
   __stcg(P.vaux + v, anchor);
@@ -1147,22 +1168,46 @@ __device__ bool claim_star(const KParams& P, int v, unsigned long long key, Star
   return true;
 }
 
+// The positions of corners w[0..k) into poly, kGather loads in flight at a time.
+template <typename Poly>
+__device__ __forceinline__ void gather_corners(const KParams& P, int k, const int* w, Poly& poly) {
+  for (int i0 = 0; i0 < k; i0 += kGather) {
+    float2 t[kGather];
+#pragma unroll
+    for (int u = 0; u < kGather; ++u) t[u] = i0 + u < k ? ldpos(P, w[i0 + u]) : make_float2(0.f, 0.f);
+#pragma unroll
+    for (int u = 0; u < kGather; ++u)
+      if (i0 + u < k) poly.set_q(i0 + u, t[u]);
+  }
+}
+
 // Removal of v from its cached star (sc.k spokes): origins and positions of
 // the link loaded together, then the ear clipping.
 __device__ int remove_cached(const KParams& P, int v, const StarCache& sc, LocalCounters& lc, unsigned mk) {
   const int k = sc.k;
   int w[kStarCache], bnd[kStarCache];
-  for (int i = 0; i < k; ++i) w[i] = he_origin(P, sc.lk[i]);
+  // link origins, then their positions, kGather loads in flight at a time (a
+  // loop that stores each loaded value before the next load waits for every
+  // load in turn)
+  for (int i0 = 0; i0 < k; i0 += kGather) {
+    int t[kGather];
+#pragma unroll
+    for (int u = 0; u < kGather; ++u) t[u] = i0 + u < k ? he_origin(P, sc.lk[i0 + u]) : 0;
+#pragma unroll
+    for (int u = 0; u < kGather; ++u)
+      if (i0 + u < k) w[i0 + u] = t[u];
+  }
   for (int i = 0; i < k; ++i)
     if (bad_v(P, w[i])) return MCL_ERR_DEGENERATE_INPUT | (__LINE__ << 8);
+  const float2 pv = ldpos(P, v);
   if (k <= kSmallStar) {
     SmallPoly poly;
-    for (int i = 0; i < k; ++i) poly.set_q(i, ldpos(P, w[i]));
-    return clip_star(P, v, ldpos(P, v), lc, mk, k, sc.sp, sc.lk, w, poly, bnd);
+    gather_corners(P, k, w, poly);
+    return clip_star(P, v, pv, lc, mk, k, sc.sp, sc.lk, w, poly, bnd);
   }
   LocalPoly poly;
-  for (int i = 0; i < k; ++i) poly.set_q(i, ldpos(P, w[i]));
-  return clip_star(P, v, ldpos(P, v), lc, mk, k, sc.sp, sc.lk, w, poly, bnd);
+  gather_corners(P, k, w, poly);
+  return clip_star(P, v, pv, lc, mk, k, sc.sp, sc.lk, w, poly, bnd);
 }
 
 // ---------------------------------------------------------------------------
@@ -1322,9 +1367,14 @@ __device__ bool phase_remove(cg::grid_group& g, const KParams& P, unsigned& stam
       const unsigned long long key = ((unsigned long long)sk << 32) | (unsigned)(~mix32((unsigned)v ^ sk));
       bool win = true, ok = true;
       if (sc.v == v && sc.k > 0) {
-        unsigned long long c[kStarCache];
-        for (int j = 0; j < sc.k; ++j) c[j] = __ldcg(P.claim + sc.fm[j]);
-        for (int j = 0; j < sc.k; ++j) win = win && c[j] == key;
+        // the claims kGather at a time, all loads of a group in flight together
+        for (int j0 = 0; j0 < sc.k; j0 += kGather) {
+          unsigned long long c[kGather];
+#pragma unroll
+          for (int u = 0; u < kGather; ++u) c[u] = j0 + u < sc.k ? __ldcg(P.claim + sc.fm[j0 + u]) : key;
+#pragma unroll
+          for (int u = 0; u < kGather; ++u) win &= c[u] == key;
+        }
       } else {
         ok = for_spokes(P, v, [&](int h) {
           if (__ldcg(P.claim + face_min(P, h)) != key) win = false;
