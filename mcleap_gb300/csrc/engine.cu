@@ -643,9 +643,13 @@ __device__ __forceinline__ int lawson_round(const KParams& P, const int* in, int
         if (ka == key && kb == key) {
           if (flip_edge_with(P, e, q, w, vha, vhb)) ++flips;
           const int wing[4] = {w.x >> 1, w.y >> 1, w.z >> 1, w.w >> 1};
+          // the four queue marks issued together, their answers used after
+          unsigned was[4];
+#pragma unroll
+          for (int j = 0; j < 4; ++j) was[j] = atomicMax(P.qmark + wing[j], sq);
 #pragma unroll
           for (int j = 0; j < 4; ++j)
-            if (enqueue_once(P, wing[j], sq)) mine[k++] = wing[j];
+            if (was[j] < sq) mine[k++] = wing[j];
         } else if (enqueue_once(P, e, sq)) {
           mine[k++] = e;
         }
