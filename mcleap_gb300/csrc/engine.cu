@@ -396,10 +396,16 @@ __device__ void phase_classify(cg::grid_group& g, const KParams& P, unsigned qst
     // kMoveUnroll vertices per thread and iteration, every load before any
     // store (the pass is a stream: its loads must overlap)
     // The vertices that actually move are listed (work-list vl0, free until
-    // the repair): when they are few, only the edges whose quads hold one of
-    // them are classified (every other edge kept the positions of the last
-    // step, which left the mesh Delaunay).
+    // the repair) when the last launch moved few: when they are few, only the
+    // edges whose quads hold one of them are classified (every other edge
+    // kept the positions of the last step, which left the mesh Delaunay).
+    // A launch that moves most vertices after one that did lists nothing
+    // (listing them would wait on an append per warp and iteration); the
+    // movers are counted either way, for the next launch's choice.
     constexpr int UM = kMoveUnroll;
+    const bool listing =
+        P.sparse_ok && (long long)ld_i(&P.st->movers_last) * kSparseEdgesPerMover < (long long)P.E_it;
+    int moved = 0;
     for (int base = blockIdx.x * blockDim.x * UM; base < P.V_it; base += stride * UM) {
       int v[UM];
       float2 np[UM];
@@ -419,17 +425,15 @@ __device__ void phase_classify(cg::grid_group& g, const KParams& P, unsigned qst
           if (__float_as_uint(np[j].x) != __float_as_uint(po.x) || __float_as_uint(np[j].y) != __float_as_uint(po.y))
             mv[km++] = v[j];
         }
-      // once the list is past the sparse limit the full pass runs: stop listing
-      // (a step that moves every vertex would otherwise append them all)
-      if (__any_sync(kFull, km > 0) && P.sparse_ok &&
-          (long long)ld_i(&P.st->vl_count[0]) * kSparseEdgesPerMover < (long long)P.E_it)
-        warp_push(mv, km, P.vl0, &P.st->vl_count[0], P.V, P.st);
+      moved += km;
+      if (listing && __any_sync(kFull, km > 0)) warp_push(mv, km, P.vl0, &P.st->vl_count[0], P.V, P.st);
     }
+    warp_add(&P.st->movers_now, moved);
     if (kFixedPos) timeline_max(P, 43);
     g.sync();
     if (kFixedPos) timeline_max(P, 44);
     const int nm = ld_i(&P.st->vl_count[0]);
-    if (P.sparse_ok && (long long)nm * kSparseEdgesPerMover < (long long)P.E_it) {
+    if (listing && (long long)nm * kSparseEdgesPerMover < (long long)P.E_it) {
       cp_async_wait<0>();  // the prefetched records are not used
       classify_movers<kFixedPos>(P, nm, qstamp, sc, lc);
       if (kFixedPos) timeline_max(P, 45);
@@ -1802,6 +1806,8 @@ __device__ void finish_launch(const KParams& P, unsigned stamp) {
   for (int i = 0; i < 3; ++i) st->fix_new[i] = st->fix_bad[i] = st->fix_list[i] = 0;
   st->fix_all = 0;
   st->mark_ovf = 0;
+  st->movers_last = __ldcg(&st->movers_now);
+  st->movers_now = 0;
   st->epoch = stamp;
 }
 

@@ -67,6 +67,8 @@ struct DevState {
   int fix_list[3];         // vertices listed for the next fixpoint pass (triple-buffered counts)
   int fix_all;             // vertices sent back by this launch (listed once, on `hard`)
   int mark_ovf;            // the repair's appended marks did not fit, or were not all appended
+  int movers_now;          // vertices this launch's move pass moved
+  int movers_last;         // ... the last launch's (whether this move pass lists them)
   int sub_count[3];        // repair sub-steps: mover lists (2), vertices left for removal
   int sub_rev[3];          // movers sent back per sub-step pass (triple-buffered)
   unsigned int epoch;      // next unused stamp
