@@ -21,8 +21,10 @@
 //           positive.  Vertices sent back then follow in up to kSubLevels
 //           sub-steps (half of what they still owe, the last all); the few
 //           still away (listed in parallel, by ascending id) are removed and
-//           reinserted at their targets by one thread of the launch.  The
-//           host reads one record at the end.
+//           reinserted at their targets in claim-based rounds (removal
+//           rounds, then insertion rounds; periodic.cuh), and flip rounds
+//           from the edges those rewrote restore Delaunay.  The host reads
+//           one record at the end.
 //   queries one-ring with copy offsets, closest neighbour, mesh FRNN (one
 //           launch for the outgoing half-edges, one per query).
 #include <cooperative_groups.h>
@@ -74,6 +76,7 @@ struct mcl_periodic {
   void* out_host;    // PStepOut (pinned, mapped)
   void* out_map;     // out_host's device address (NULL: copied back instead)
   int* chunk;        // per-block counts of the behind list (grid + 1)
+  int* par;          // removal and reinsertion rounds: 8 ints per vertex (state 0 between steps)
   int grid;          // blocks of the launch
 };
 
@@ -83,9 +86,6 @@ constexpr int kThreads = 256;
 constexpr int kMaxRounds = 4096;
 constexpr int kMaxRevertPasses = 256;
 constexpr int kSubLevels = 5;  // sub-steps for vertices sent back
-// vertices one thread removes and reinserts per step at most (the rest stay
-// behind, counted): the single-thread kernel's time stays bounded
-constexpr int kMaxReinsert = 1 << 16;
 constexpr int kCenter = 4;  // copy index of the untranslated copy
 
 #define PCK(call)                                       \
@@ -109,6 +109,7 @@ constexpr int kCenter = 4;  // copy index of the untranslated copy
 struct PStepOut {
   PCount tot;  // counters of the whole step (error and error_site: the first)
   unsigned long long rounds, inverted_first, incircle_tests, behind_first, behind_sub, behind, reinserted, stamps;
+  unsigned long long lq;  // entries of the removal and reinsertion rounds' work-list (wl0)
   int reason;  // kReason*
   int phases;  // grid barriers passed
   // %globaltimer at the launch's start (ts[0]) and after the barrier ending
@@ -314,9 +315,11 @@ struct PZ {
 // Rounds of classification after a move: faces turned over send their moved
 // vertices back (then the fold again), otherwise the winners of the
 // non-Delaunay edges flip, until no edge is non-Delaunay.
-__device__ int p_settle(PCtl& C, PZ& z) {
-  int revert_passes = 0, cur = -1;  // the work-list to classify (-1: every edge)
-  long long len = 0;                // its length
+// Starts from every edge (cur0 < 0) or from the first len0 entries of
+// work-list cur0.
+__device__ int p_settle(PCtl& C, PZ& z, int cur0 = -1, long long len0 = 0) {
+  int revert_passes = 0, cur = cur0;  // the work-list to classify (-1: every edge)
+  long long len = len0;               // its length
   bool flipped = false;
   for (int r = 0; r < kMaxRounds; ++r) {
     const unsigned stamp = ++z.stamp;
@@ -452,12 +455,156 @@ __device__ void p_list_behind(PCtl& C, int* chunk) {
 
 // out: the step's record in device memory; host_out (may be NULL): a
 // host-mapped copy of it written at the end
+// The vertices still away after the sub-steps (nl of them listed in V.clist):
+// removal rounds, then insertion rounds (periodic.cuh), each round three
+// phases (claims; verification, nothing written; winners' rewrites, losers
+// listed for the next round), the rewritten edges queued on wl0 (*lq).
+__device__ int p_reinsert_rounds_(PCtl& C, PZ& z, int* vhe, int* par, long long nl, unsigned long long* lq,
+                                  unsigned long long& reinserted) {
+  const int n = C.V0.n;
+  int* pf = par;           // 3 n: free edges
+  int* pa = par + 3 * n;   // n: a neighbour that stays (walk start)
+  int* loc = par + 4 * n;  // n: face located this round (-1 none, -2 the goal is a corner)
+  int* ps = par + 5 * n;   // n: state
+  int* la = par + 6 * n;   // n, n: vertex lists
+  int* lb = par + 7 * n;
+  constexpr int kWon = 16;  // state bit: holds its claims this round
+  const unsigned sq = ++z.stamp;  // the queue mark of this work-list
+  {
+    const PView V = C.begin();
+    for (long long i = C.gl(); i < nl; i += C.gs) {
+      const int v = V.clist[i];
+      ps[v] = mcl::kParPending;
+      loc[v] = -1;
+      la[i] = v;
+    }
+  }
+  if (p_failed(C.end())) return kReasonReinsert;
+  long long na = nl;
+  // removal rounds; a vertex left over stays where it is
+  for (int r = 0; r < mcl::kParRounds && na > 0; ++r) {
+    const unsigned s = ++z.stamp;
+    {
+      const PView V = C.begin();
+      for (long long i = C.gl(); i < na; i += C.gs) mcl::p_body_claim_star(V, vhe, la[i], s);
+    }
+    if (p_failed(C.end())) return kReasonReinsert;
+    {
+      const PView V = C.begin();
+      for (long long i = C.gl(); i < na; i += C.gs)
+        if (mcl::p_body_holds_star(V, vhe, la[i], s)) ps[la[i]] = mcl::kParPending | kWon;
+    }
+    if (p_failed(C.end())) return kReasonReinsert;
+    {
+      const PView V = C.begin();
+      for (long long i = C.gl(); i < na; i += C.gs) {
+        const int v = la[i];
+        if (ps[v] == (mcl::kParPending | kWon)) mcl::p_body_remove_par(V, vhe, v, pf, pa, ps, lq, sq);
+        else lb[mcl::p_inc(&V.cnt->lcount[1])] = v;
+      }
+    }
+    const PCount* c = C.end();
+    if (p_failed(c)) return kReasonReinsert;
+    na = (long long)__ldcg(&c->lcount[1]);
+    int* t = la;
+    la = lb;
+    lb = t;
+  }
+  // insertion rounds over the removed vertices
+  {
+    const PView V = C.begin();
+    for (long long i = C.gl(); i < na; i += C.gs) ps[la[i]] = mcl::kParStays;  // removal rounds ran out
+    for (long long i = C.gl(); i < nl; i += C.gs) {
+      const int v = V.clist[i];
+      if (ps[v] == mcl::kParRemoved) lb[mcl::p_inc(&V.cnt->lcount[1])] = v;
+    }
+  }
+  {
+    const PCount* c = C.end();
+    if (p_failed(c)) return kReasonReinsert;
+    na = (long long)__ldcg(&c->lcount[1]);
+    int* t = la;
+    la = lb;
+    lb = t;
+  }
+  for (int r = 0; na > 0; ++r) {
+    if (r == mcl::kParRounds) {
+      {
+        const PView V = C.begin();
+        if (C.gt == 0) mcl::p_error(V, MCL_ERR_NO_CONVERGENCE, 26);  // vertices would stay out of the mesh
+      }
+      C.end();
+      return kReasonReinsert;
+    }
+    const unsigned s = ++z.stamp;
+    {
+      const PView V = C.begin();
+      for (long long i = C.gl(); i < na; i += C.gs) mcl::p_body_locate_par(V, vhe, la[i], pa, loc, ps, s);
+    }
+    if (p_failed(C.end())) return kReasonReinsert;
+    {
+      const PView V = C.begin();
+      for (long long i = C.gl(); i < na; i += C.gs) {
+        const int v = la[i];
+        if (mcl::p_body_holds_face(V, v, loc, ps, s)) ps[v] |= kWon;
+      }
+    }
+    if (p_failed(C.end())) return kReasonReinsert;
+    {
+      const PView V = C.begin();
+      for (long long i = C.gl(); i < na; i += C.gs) {
+        const int v = la[i];
+        if (ps[v] & kWon) {
+          ps[v] &= ~kWon;
+          mcl::p_body_split_par(V, vhe, v, pf, loc, ps, lq, sq);
+        } else if (loc[v] == -2) {
+          // the goal is taken: back where it was, or (already going back) an error
+          if (ps[v] == mcl::kParBack) {
+            mcl::p_error(V, MCL_ERR_DEGENERATE_INPUT, 20);
+          } else {
+            ps[v] = mcl::kParBack;
+            loc[v] = -1;
+            lb[mcl::p_inc(&V.cnt->lcount[1])] = v;
+          }
+        } else {
+          lb[mcl::p_inc(&V.cnt->lcount[1])] = v;
+        }
+      }
+    }
+    const PCount* c = C.end();
+    if (p_failed(c)) return kReasonReinsert;
+    reinserted += __ldcg(&c->reinserted);
+    na = (long long)__ldcg(&c->lcount[1]);
+    int* t = la;
+    la = lb;
+    lb = t;
+  }
+  return kReasonNone;
+}
+__device__ int p_reinsert_rounds(PCtl& C, PZ& z, int* vhe, int* par, long long nl, unsigned long long* lq,
+                                 unsigned long long& reinserted) {
+  const int reason = p_reinsert_rounds_(C, z, vhe, par, nl, lq, reinserted);
+  {
+    // every listed vertex back to state 0 for the next step (V.clist still
+    // holds the list: the rounds keep their lists in par)
+    const PView V = C.begin();
+    int* ps = par + 5 * C.V0.n;
+    for (long long i = C.gl(); i < nl; i += C.gs) ps[V.clist[i]] = 0;
+  }
+  C.end();
+  return reason;
+}
+
+// par: the removal and reinsertion rounds' per-vertex arrays (8 n ints: free
+// edges, walk start, state, location, two vertex lists); state 0 between steps
 __global__ void __launch_bounds__(kThreads, 2) k_pstep(PView V0, const PF2* d, PF2* dsub, PCount* slots, PStepOut* out,
-                                                       PStepOut* host_out, int* chunk, int* vhe, unsigned stamp0) {
+                                                       PStepOut* host_out, int* chunk, int* vhe, int* par,
+                                                       unsigned stamp0) {
   PCtl C{cg::this_grid(), V0, slots, &out->tot, out->ts, 0, (long long)blockIdx.x * blockDim.x + threadIdx.x,
          (long long)gridDim.x * blockDim.x};
   if (C.gt == 0) {
     out->ts[0] = p_now();
+    out->lq = 0;
     unsigned long long* t = reinterpret_cast<unsigned long long*>(&out->tot);
     for (int i = 0; i < (int)(sizeof(PCount) / 8); ++i) t[i] = 0;
   }
@@ -503,13 +650,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_pstep(PView V0, const PF2* d, P
     if (p_failed(C.end())) reason = kReasonReinsert;
     if (!reason) {
       p_list_behind(C, chunk);
-      {
-        const PView V = C.begin();
-        if (C.gt == 0) mcl::p_body_reinsert(V, vhe, V.clist, __ldcg(chunk + gridDim.x), kMaxReinsert);
-      }
-      const PCount* c = C.end();
-      if (p_failed(c)) reason = kReasonReinsert;
-      reinserted = __ldcg(&c->reinserted);
+      reason = p_reinsert_rounds(C, z, vhe, par, __ldcg(chunk + gridDim.x), &out->lq, reinserted);
+      if (!reason) reason = p_settle(C, z, 0, (long long)__ldcg(&out->lq));
       p_resume_pass(C, C.begin(), dsub, true);  // counts who is still behind
       behind = __ldcg(&C.end()->behind);
     }
@@ -581,6 +723,7 @@ void free_periodic(mcl_periodic* m) {
   cudaFree(m->slots);
   cudaFree(m->out);
   cudaFree(m->chunk);
+  cudaFree(m->par);
   if (m->out_host) cudaFreeHost(m->out_host);
   delete m;
 }
@@ -823,6 +966,8 @@ int ensure_step(mcl_periodic* m) {
     m->out_map = nullptr;
   }
   PCK(cudaMalloc((void**)&m->chunk, sizeof(int) * (size_t)(grid + 1)));
+  PCK(cudaMalloc((void**)&m->par, 8 * sizeof(int) * (size_t)m->n));
+  PCK(cudaMemset(m->par, 0, 8 * sizeof(int) * (size_t)m->n));
   m->grid = grid;
   return MCL_OK;
 }
@@ -973,7 +1118,7 @@ int mcl_periodic_step(mcl_periodic* m, const mcl_float2* d_dev, void* stream, mc
   PStepOut* out = static_cast<PStepOut*>(m->out);
   unsigned stamp0 = m->stamp;
   PStepOut* host_out = static_cast<PStepOut*>(m->out_map);
-  void* args[] = {&V, (void*)&d, &m->dsub, &m->slots, &out, &host_out, &m->chunk, &m->vhe, &stamp0};
+  void* args[] = {&V, (void*)&d, &m->dsub, &m->slots, &out, &host_out, &m->chunk, &m->vhe, &m->par, &stamp0};
   PCK(cudaLaunchCooperativeKernel((const void*)k_pstep, dim3((unsigned)m->grid), dim3(kThreads), args, 0, s));
   if (!host_out) PCK(cudaMemcpyAsync(m->out_host, m->out, sizeof(PStepOut), cudaMemcpyDeviceToHost, s));
   PCK(cudaStreamSynchronize(s));

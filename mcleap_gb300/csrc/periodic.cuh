@@ -585,25 +585,26 @@ MCL_HD Off p_xof(const PView& V, int h) { return eo_apex(V.eo[h >> 1], h & 1); }
 // one half-edge's whole record: origin, apex, next, prev, target offset t and
 // apex offset x (both relative to the origin)
 MCL_HD void p_set_half(const PView& V, int h, int origin, int apex, int next, int prev, Off t, Off x) {
+  // field by field: the other side of the edge may be rewritten at the same
+  // time by another thread (the parallel removal and reinsertion rounds);
+  // byte 0 (the edge's offset) is the same value from either side
   const int e = h >> 1;
-  PI4 q = V.ev[e], w = V.en[e];
-  unsigned o = V.eo[e];
+  unsigned char* ob = reinterpret_cast<unsigned char*>(V.eo + e);
   if (h & 1) {
-    q.y = origin;
-    q.w = apex;
-    w.z = next;
-    w.w = prev;
-    o = (o & 0xFF00FF00u) | off_byte(off_neg(t)) | (off_byte(x) << 16);
+    V.ev[e].y = origin;
+    V.ev[e].w = apex;
+    V.en[e].z = next;
+    V.en[e].w = prev;
+    ob[0] = (unsigned char)off_byte(off_neg(t));
+    ob[2] = (unsigned char)off_byte(x);
   } else {
-    q.x = origin;
-    q.z = apex;
-    w.x = next;
-    w.y = prev;
-    o = (o & 0xFFFF0000u) | off_byte(t) | (off_byte(x) << 8);
+    V.ev[e].x = origin;
+    V.ev[e].z = apex;
+    V.en[e].x = next;
+    V.en[e].y = prev;
+    ob[0] = (unsigned char)off_byte(t);
+    ob[1] = (unsigned char)off_byte(x);
   }
-  V.ev[e] = q;
-  V.en[e] = w;
-  V.eo[e] = o;
 }
 
 // face v0 -> v1 -> v2 of half-edges h0 (v0 -> v1), h1, h2, with v1 at O1 and
@@ -765,14 +766,11 @@ MCL_HD PF2 p_nearest_copy(PF2 t, PF2 p, float L, Off& k) {
   return q;
 }
 
-// Inserts vertex v (not in the mesh) at canonical position t, using the
-// three free edges, starting the point location walk at half-edge `near`.
-// 1 -> 3 split inside a face, 2 -> 4 split on an edge; false when t is an
-// existing vertex or the walk does not end.  Returns the half-edges of the
-// new star's link in link[0..3] (count in *nlink) for the flips that follow.
-MCL_HD bool p_insert_seq(const PView& V, int* vhe, int v, PF2 t, const int* f, int near, int* link, int* nlink) {
+// The face of canonical position t by the stochastic walk from half-edge h:
+// *face = a half-edge of it, *vertex = t is one of its corners.  False (an
+// error flagged) on a malformed mesh or a walk that does not end.
+MCL_HD bool p_locate_face(const PView& V, PF2 t, int h, int* face, bool* vertex) {
   const unsigned H = 2u * (unsigned)V.E;
-  int h = near;
   for (int guard = 0; guard < (1 << 20); ++guard) {
     if ((unsigned)h >= H) {
       p_error(V, MCL_ERR_DEGENERATE_INPUT, 15);
@@ -797,47 +795,75 @@ MCL_HD bool p_insert_seq(const PView& V, int* vhe, int v, PF2 t, const int* f, i
       h = go ^ 1;
       continue;
     }
-    const int zeros = (o1 == 0) + (o2 == 0) + (o3 == 0);
-    if (zeros >= 2) return false;  // t is a vertex
-    const Off Ov = K;              // v's copy in a's frame
-    if (zeros == 0) {
-      const int n = p_next(V, h), p = p_prev(V, h);
-      p_make_face(V, h, 2 * f[1], 2 * f[0] + 1, a, b, v, Ob, Ov);
-      p_make_face(V, n, 2 * f[2], 2 * f[1] + 1, b, c, v, off_sub(Oc, Ob), off_sub(Ov, Ob));
-      p_make_face(V, p, 2 * f[0], 2 * f[2] + 1, c, a, v, off_neg(Oc), off_sub(Ov, Oc));
-      vhe[v] = 2 * f[0] + 1;
-      link[0] = h;
-      link[1] = n;
-      link[2] = p;
-      *nlink = 3;
-      return true;
-    }
-    // on one edge: make it g (a -> b) with v on the segment a b
-    int g = h;
-    if (o2 == 0) g = p_next(V, h);
-    if (o3 == 0) g = p_prev(V, h);
-    const int ga = p_origin(V, g), gb = p_origin(V, g ^ 1), gc = p_apex(V, g), gd = p_apex(V, g ^ 1);
-    if ((unsigned)gd >= (unsigned)V.n) return false;
-    // offsets in ga's frame
-    const Off Gb = p_tof(V, g), Gc = p_xof(V, g), Gd = off_add(Gb, p_xof(V, g ^ 1));
-    Off Ka;
-    p_nearest_copy(t, off_translate(V.pos[ga], Off{0, 0}, V.L), V.L, Ka);
-    const int ng = p_next(V, g), pg = p_prev(V, g), g1 = g ^ 1, ng1 = p_next(V, g1), pg1 = p_prev(V, g1);
-    p_make_face(V, g, 2 * f[1] + 1, pg, ga, v, gc, Ka, Gc);
-    p_make_face(V, 2 * f[0], ng, 2 * f[1], v, gb, gc, off_sub(Gb, Ka), off_sub(Gc, Ka));
-    p_make_face(V, 2 * f[0] + 1, 2 * f[2] + 1, pg1, gb, v, gd, off_sub(Ka, Gb), off_sub(Gd, Gb));
-    p_make_face(V, g1, ng1, 2 * f[2], v, ga, gd, off_neg(Ka), off_sub(Gd, Ka));
-    vhe[v] = 2 * f[0];
-    if (vhe[gb] == g1) vhe[gb] = 2 * f[0] + 1;
-    link[0] = ng;
-    link[1] = pg;
-    link[2] = ng1;
-    link[3] = pg1;
-    *nlink = 4;
+    *face = h;
+    *vertex = (o1 == 0) + (o2 == 0) + (o3 == 0) >= 2;
     return true;
   }
   p_error(V, MCL_ERR_NO_CONVERGENCE, 17);
   return false;
+}
+
+// Splits the face of half-edge h, which holds t (inside or on one of its
+// sides, as p_locate_face found it), by vertex v at t with the three free
+// edges: 1 -> 3 inside, 2 -> 4 on a side; false when t is a corner.  The
+// half-edges of the new star's link go to link[0..3] (count in *nlink).
+MCL_HD bool p_split_at(const PView& V, int* vhe, int v, PF2 t, const int* f, int h, int* link, int* nlink) {
+  const int a = p_origin(V, h), b = p_origin(V, h ^ 1), c = p_apex(V, h);
+  const Off Ob = p_tof(V, h), Oc = p_xof(V, h);
+  const PF2 pa = V.pos[a], pb = off_translate(V.pos[b], Ob, V.L), pc = off_translate(V.pos[c], Oc, V.L);
+  Off K;
+  const PF2 pt = p_nearest_copy(t, pa, V.L, K);
+  const int o1 = p_orient_at(V, pa, pb, pt), o2 = p_orient_at(V, pb, pc, pt), o3 = p_orient_at(V, pc, pa, pt);
+  const int zeros = (o1 == 0) + (o2 == 0) + (o3 == 0);
+  if (zeros >= 2) return false;  // t is a vertex
+  const Off Ov = K;              // v's copy in a's frame
+  if (zeros == 0) {
+    const int n = p_next(V, h), p = p_prev(V, h);
+    p_make_face(V, h, 2 * f[1], 2 * f[0] + 1, a, b, v, Ob, Ov);
+    p_make_face(V, n, 2 * f[2], 2 * f[1] + 1, b, c, v, off_sub(Oc, Ob), off_sub(Ov, Ob));
+    p_make_face(V, p, 2 * f[0], 2 * f[2] + 1, c, a, v, off_neg(Oc), off_sub(Ov, Oc));
+    vhe[v] = 2 * f[0] + 1;
+    link[0] = h;
+    link[1] = n;
+    link[2] = p;
+    *nlink = 3;
+    return true;
+  }
+  // on one edge: make it g (a -> b) with v on the segment a b
+  int g = h;
+  if (o2 == 0) g = p_next(V, h);
+  if (o3 == 0) g = p_prev(V, h);
+  const int ga = p_origin(V, g), gb = p_origin(V, g ^ 1), gc = p_apex(V, g), gd = p_apex(V, g ^ 1);
+  if ((unsigned)gd >= (unsigned)V.n) return false;
+  // offsets in ga's frame
+  const Off Gb = p_tof(V, g), Gc = p_xof(V, g), Gd = off_add(Gb, p_xof(V, g ^ 1));
+  Off Ka;
+  p_nearest_copy(t, off_translate(V.pos[ga], Off{0, 0}, V.L), V.L, Ka);
+  const int ng = p_next(V, g), pg = p_prev(V, g), g1 = g ^ 1, ng1 = p_next(V, g1), pg1 = p_prev(V, g1);
+  p_make_face(V, g, 2 * f[1] + 1, pg, ga, v, gc, Ka, Gc);
+  p_make_face(V, 2 * f[0], ng, 2 * f[1], v, gb, gc, off_sub(Gb, Ka), off_sub(Gc, Ka));
+  p_make_face(V, 2 * f[0] + 1, 2 * f[2] + 1, pg1, gb, v, gd, off_sub(Ka, Gb), off_sub(Gd, Gb));
+  p_make_face(V, g1, ng1, 2 * f[2], v, ga, gd, off_neg(Ka), off_sub(Gd, Ka));
+  vhe[v] = 2 * f[0];
+  if (vhe[gb] == g1) vhe[gb] = 2 * f[0] + 1;
+  link[0] = ng;
+  link[1] = pg;
+  link[2] = ng1;
+  link[3] = pg1;
+  *nlink = 4;
+  return true;
+}
+
+// Inserts vertex v (not in the mesh) at canonical position t, using the
+// three free edges, starting the point location walk at half-edge `near`.
+// 1 -> 3 split inside a face, 2 -> 4 split on an edge; false when t is an
+// existing vertex or the walk does not end.  Returns the half-edges of the
+// new star's link in link[0..3] (count in *nlink) for the flips that follow.
+MCL_HD bool p_insert_seq(const PView& V, int* vhe, int v, PF2 t, const int* f, int near, int* link, int* nlink) {
+  int face = -1;
+  bool vertex = false;
+  if (!p_locate_face(V, t, near, &face, &vertex) || vertex) return false;
+  return p_split_at(V, vhe, v, t, f, face, link, nlink);
 }
 
 constexpr int kSeqStack = 512;
@@ -934,6 +960,191 @@ MCL_HD void p_body_reinsert(const PView& V, int* vhe, const int* list, int count
     }
     if (!p_lawson_seq(V, vhe, link, nlink)) return;
   }
+}
+
+// ---------------------------------------------------------------------------
+// Removal and reinsertion in parallel rounds (the GPU step's last phase; the
+// one-thread pass above is its serial counterpart).  The vertices still away
+// from their targets go through removal rounds (each claims every face of its
+// star; a winner, sharing no face with another, removes itself: spoke flips
+// down to degree 3, then a merge) and then insertion rounds (each locates its
+// target from a vertex that stays and claims the face, or the two faces of the
+// side, holding it; a winner splits them).  A winner rewrites only its own
+// faces and, field by field, its side of their edges, so winners of one round
+// never touch the same field; every edge a round rewrote is queued once on a
+// work-list (wl0, counted by *lq) from which flip rounds restore Delaunay.
+// Per vertex: pf[3 v .. 3 v + 2] its three free edges, pa[v] a vertex that
+// stays to start the walk from, ps[v] its state (kParPending ...).
+
+constexpr int kParRounds = 256;  // removal or insertion rounds at most
+enum : int { kParPending = 1, kParRemoved = 2, kParStays = 3, kParBack = 4, kParDone = 5 };
+
+// the smallest half-edge of h's face: its claim slot
+MCL_HD int p_face_min(const PView& V, int h) { return p_min(h, p_min(p_next(V, h), p_prev(V, h))); }
+// claim key of vertex v in the round with stamp s: the smaller id wins (the
+// order the one-thread pass takes them in)
+MCL_HD unsigned long long p_vkey(int v, unsigned s) { return ((unsigned long long)s << 32) | (unsigned)(~(unsigned)v); }
+
+// edge e onto the repair work-list, once for stamp s
+MCL_HD void p_lqueue(const PView& V, unsigned long long* lq, int e, unsigned s) {
+  if ((unsigned)e >= (unsigned)V.E) return;
+  if (p_exch(V.qstamp + e, s) == s) return;
+  V.wl0[p_inc(lq)] = e;
+}
+
+// v's star, by its outgoing half-edges from vhe[v]: f(h) for each; false (an
+// error flagged) when the star does not close
+template <typename F>
+MCL_HD bool p_each_spoke(const PView& V, const int* vhe, int v, F f) {
+  const unsigned H = 2u * (unsigned)V.E;
+  const int h0 = vhe[v];
+  if ((unsigned)h0 >= H || p_origin(V, h0) != v) {
+    p_error(V, MCL_ERR_DEGENERATE_INPUT, 23);
+    return false;
+  }
+  int h = h0, deg = 0;
+  do {
+    f(h);
+    h = p_rot(V, h);
+    ++deg;
+  } while (h != h0 && (unsigned)h < H && deg < kPeriodicMaxDeg);
+  if (h != h0) {
+    p_error(V, MCL_ERR_DEGENERATE_INPUT, 24);
+    return false;
+  }
+  return true;
+}
+
+// removal round, claims: every face of v's star
+MCL_HD void p_body_claim_star(const PView& V, const int* vhe, int v, unsigned s) {
+  const unsigned long long key = p_vkey(v, s);
+  p_each_spoke(V, vhe, v, [&](int h) { p_max(V.claim + p_face_min(V, h), key); });
+}
+
+// removal round, verification (nothing is written meanwhile): v holds every
+// claim of its star
+MCL_HD bool p_body_holds_star(const PView& V, const int* vhe, int v, unsigned s) {
+  const unsigned long long key = p_vkey(v, s);
+  bool all = true;
+  const bool ok = p_each_spoke(V, vhe, v, [&](int h) { all = all && V.claim[p_face_min(V, h)] == key; });
+  return ok && all;
+}
+
+// removal round, a winner: v leaves the mesh (its free edges to pf, a
+// neighbour that stays to pa, the hole's edges queued); a refused removal
+// leaves v where it is (state kParStays) and queues the hole's edges and v's
+// spokes, which its spoke flips may have left non-Delaunay
+MCL_HD void p_body_remove_par(const PView& V, int* vhe, int v, int* pf, int* pa, int* ps, unsigned long long* lq,
+                              unsigned s) {
+  int freed[3], near = -1, hole[2 * kSeqStar], nhole = 0;
+  // a neighbour that stays (not on the list), for the walk that reinserts v
+  int stay = -1, any = -1;
+  p_each_spoke(V, vhe, v, [&](int h) {
+    const int w = p_origin(V, h ^ 1);
+    if (any < 0) any = w;
+    if (stay < 0 && ps[w] == 0) stay = w;
+  });
+  if (!p_remove_seq(V, vhe, v, freed, &near, hole, &nhole)) {
+    ps[v] = kParStays;
+    if (V.cnt->error) return;
+    for (int k = 0; k < nhole; ++k) p_lqueue(V, lq, hole[k], s);
+    p_each_spoke(V, vhe, v, [&](int h) { p_lqueue(V, lq, h >> 1, s); });
+    return;
+  }
+  for (int k = 0; k < nhole; ++k)
+    if (hole[k] != freed[0] && hole[k] != freed[1] && hole[k] != freed[2]) p_lqueue(V, lq, hole[k], s);
+  pf[3 * v] = freed[0];
+  pf[3 * v + 1] = freed[1];
+  pf[3 * v + 2] = freed[2];
+  pa[v] = stay >= 0 ? stay : any;
+  ps[v] = kParRemoved;
+}
+
+// where v goes: its target, or (state kParBack: the target was taken) where it was
+MCL_HD PF2 p_goal(const PView& V, int v, const int* ps) { return ps[v] == kParBack ? V.pos[v] : V.target[v]; }
+
+// insertion round, location and claims (nothing is written but claims): the
+// face of v's goal from the walk start (the face found last round, or a
+// half-edge of v's neighbour that stays), into loc[v]; claims it, or the two
+// faces of the side holding the goal; a goal on a corner (taken) is marked
+// for the next round (-2 in loc)
+MCL_HD void p_body_locate_par(const PView& V, const int* vhe, int v, const int* pa, int* loc, const int* ps,
+                              unsigned s) {
+  const unsigned H = 2u * (unsigned)V.E;
+  int h = loc[v];
+  if ((unsigned)h >= H) {
+    const int a = pa[v];
+    h = (unsigned)a < (unsigned)V.n ? vhe[a] : -1;
+    for (int k = 1; (unsigned)h >= H && k <= V.n; ++k) h = vhe[(v + k) % V.n];  // any vertex in the mesh
+  }
+  int face = -1;
+  bool vertex = false;
+  if (!p_locate_face(V, p_goal(V, v, ps), h, &face, &vertex)) {
+    loc[v] = -1;
+    return;
+  }
+  if (vertex) {
+    loc[v] = -2;
+    return;
+  }
+  loc[v] = face;
+  const unsigned long long key = p_vkey(v, s);
+  p_max(V.claim + p_face_min(V, face), key);
+  // a goal on a side also claims the face across it (the orientations of the
+  // split decide which side; claiming across all three sides is enough and
+  // costs two more claims at most)
+  const PF2 t = p_goal(V, v, ps);
+  const int a = p_origin(V, face), b = p_origin(V, face ^ 1), c = p_apex(V, face);
+  const Off Ob = p_tof(V, face), Oc = p_xof(V, face);
+  const PF2 qa = V.pos[a], qb = off_translate(V.pos[b], Ob, V.L), qc = off_translate(V.pos[c], Oc, V.L);
+  Off K;
+  const PF2 pt = p_nearest_copy(t, qa, V.L, K);
+  const int sides[3] = {face, p_next(V, face), p_prev(V, face)};
+  const int o[3] = {p_orient_at(V, qa, qb, pt), p_orient_at(V, qb, qc, pt), p_orient_at(V, qc, qa, pt)};
+  for (int k = 0; k < 3; ++k)
+    if (o[k] == 0) p_max(V.claim + p_face_min(V, sides[k] ^ 1), key);
+}
+
+// insertion round, verification (nothing is written meanwhile): v holds the
+// claims of its face and of the face across a side holding its goal
+MCL_HD bool p_body_holds_face(const PView& V, int v, const int* loc, const int* ps, unsigned s) {
+  const int face = loc[v];
+  if (face < 0) return false;
+  const unsigned long long key = p_vkey(v, s);
+  if (V.claim[p_face_min(V, face)] != key) return false;
+  const PF2 t = p_goal(V, v, ps);
+  const int a = p_origin(V, face), b = p_origin(V, face ^ 1), c = p_apex(V, face);
+  const Off Ob = p_tof(V, face), Oc = p_xof(V, face);
+  const PF2 qa = V.pos[a], qb = off_translate(V.pos[b], Ob, V.L), qc = off_translate(V.pos[c], Oc, V.L);
+  Off K;
+  const PF2 pt = p_nearest_copy(t, qa, V.L, K);
+  const int sides[3] = {face, p_next(V, face), p_prev(V, face)};
+  const int o[3] = {p_orient_at(V, qa, qb, pt), p_orient_at(V, qb, qc, pt), p_orient_at(V, qc, qa, pt)};
+  for (int k = 0; k < 3; ++k)
+    if (o[k] == 0 && V.claim[p_face_min(V, sides[k] ^ 1)] != key) return false;
+  return true;
+}
+
+// insertion round, a winner: v splits its face (or the two faces of its side)
+// at its goal; the new star's link and spokes queued
+MCL_HD bool p_body_split_par(const PView& V, int* vhe, int v, const int* pf, const int* loc, int* ps,
+                             unsigned long long* lq, unsigned s) {
+  const int f[3] = {pf[3 * v], pf[3 * v + 1], pf[3 * v + 2]};
+  const bool back = ps[v] == kParBack;
+  const PF2 t = p_goal(V, v, ps);
+  int link[4], nlink = 0;
+  if (!p_split_at(V, vhe, v, t, f, loc[v], link, &nlink)) {
+    p_error(V, MCL_ERR_DEGENERATE_INPUT, 25);  // located inside this face, the split must succeed
+    return false;
+  }
+  if (!back) {
+    V.pos[v] = t;
+    p_add(&V.cnt->reinserted, 1);
+  }
+  ps[v] = kParDone;
+  for (int k = 0; k < nlink; ++k) p_lqueue(V, lq, link[k] >> 1, s);
+  for (int k = 0; k < 3; ++k) p_lqueue(V, lq, f[k], s);
+  return true;
 }
 
 // ---------------------------------------------------------------------------

@@ -87,10 +87,11 @@ int main(int argc, char** argv) {
   int rounds = 0, revert_passes = 0;
   unsigned stamp = 0;
   long long inverted = -1;
-  // the host loop of mcl_periodic_step, launch by launch
-  auto settle = [&]() {
+  // the phases of mcl_periodic_step's launch, one after another; starts from
+  // every edge (cur0 < 0) or from work-list cur0 (cnt.lcount[cur0] entries)
+  auto settle = [&](int cur0) {
     bool flipped = false;
-    int passes = 0, cur = -1;  // the work-list to classify (-1: every edge)
+    int passes = 0, cur = cur0;  // the work-list to classify (-1: every edge)
     for (int r = 0; r < 4096; ++r) {
       ++stamp;
       cnt.nondelaunay = 0;
@@ -127,7 +128,7 @@ int main(int argc, char** argv) {
   for (int v = 0; v < n; ++v) mcl::p_body_move(V, d.data(), v);
   if (!cnt.error)
     for (int e = 0; e < E; ++e) mcl::p_body_wrap(V, e);
-  if (!cnt.error) settle();
+  if (!cnt.error) settle(-1);
   long long behind_first = -1, behind = 0;
   for (int level = 1; !cnt.error; ++level) {
     const bool last = level >= kSubLevels;
@@ -138,14 +139,79 @@ int main(int argc, char** argv) {
     if (behind == 0 || level > kSubLevels) break;
     for (int v = 0; v < n; ++v) mcl::p_body_move(V, dsub.data(), v);
     for (int e = 0; e < E; ++e) mcl::p_body_wrap(V, e);
-    settle();
+    settle(-1);
   }
-  // the rest: removed and reinserted one by one
+  // the rest: removed and reinserted in the launch's claim-based rounds
+  // (each round's claims, then its verification, then its winners, as the
+  // launch's phases), then flip rounds from the edges those rewrote
   long long substep_arrivals = behind_first > behind ? behind_first - behind : 0;
   if (!cnt.error && behind > 0) {
     std::vector<int> vh(n, -1);
     for (int h = 0; h < 2 * E; ++h) mcl::p_body_vhe(V, vh.data(), h);
-    mcl::p_body_reinsert(V, vh.data(), nullptr, n, 1 << 16);
+    std::vector<int> list;
+    for (int v = 0; v < n; ++v)
+      if (pos[v].x != target[v].x || pos[v].y != target[v].y) list.push_back(v);
+    std::vector<int> par((size_t)8 * n, 0);
+    int* pf = par.data();
+    int* pa = pf + 3 * n;
+    int* loc = pf + 4 * n;
+    int* ps = pf + 5 * n;
+    constexpr int kWon = 16;
+    for (const int v : list) {
+      ps[v] = mcl::kParPending;
+      loc[v] = -1;
+    }
+    unsigned long long lq = 0;
+    const unsigned sq = ++stamp;
+    std::vector<int> la = list, lb;
+    for (int r = 0; r < mcl::kParRounds && !la.empty() && !cnt.error; ++r) {
+      const unsigned s = ++stamp;
+      for (const int v : la) mcl::p_body_claim_star(V, vh.data(), v, s);
+      for (const int v : la)
+        if (mcl::p_body_holds_star(V, vh.data(), v, s)) ps[v] = mcl::kParPending | kWon;
+      lb.clear();
+      for (const int v : la) {
+        if (ps[v] == (mcl::kParPending | kWon)) mcl::p_body_remove_par(V, vh.data(), v, pf, pa, ps, &lq, sq);
+        else lb.push_back(v);
+      }
+      la.swap(lb);
+    }
+    for (const int v : la) ps[v] = mcl::kParStays;
+    la.clear();
+    for (const int v : list)
+      if (ps[v] == mcl::kParRemoved) la.push_back(v);
+    for (int r = 0; !la.empty() && !cnt.error; ++r) {
+      if (r == mcl::kParRounds) {
+        cnt.error = MCL_ERR_NO_CONVERGENCE;
+        break;
+      }
+      const unsigned s = ++stamp;
+      for (const int v : la) mcl::p_body_locate_par(V, vh.data(), v, pa, loc, ps, s);
+      for (const int v : la)
+        if (mcl::p_body_holds_face(V, v, loc, ps, s)) ps[v] |= kWon;
+      lb.clear();
+      for (const int v : la) {
+        if (ps[v] & kWon) {
+          ps[v] &= ~kWon;
+          mcl::p_body_split_par(V, vh.data(), v, pf, loc, ps, &lq, sq);
+        } else if (loc[v] == -2) {
+          if (ps[v] == mcl::kParBack) {
+            mcl::p_error(V, MCL_ERR_DEGENERATE_INPUT, 20);
+          } else {
+            ps[v] = mcl::kParBack;
+            loc[v] = -1;
+            lb.push_back(v);
+          }
+        } else {
+          lb.push_back(v);
+        }
+      }
+      la.swap(lb);
+    }
+    if (!cnt.error) {
+      cnt.lcount[0] = lq;
+      settle(0);
+    }
     behind = 0;
     for (int v = 0; v < n; ++v) behind += pos[v].x != target[v].x || pos[v].y != target[v].y;
   }
