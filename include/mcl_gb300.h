@@ -460,11 +460,12 @@ int mcl_periodic_positions(mcl_periodic* m, mcl_float2** pos_dev);
  * the vertices still owing part of their displacement by half of it (the last
  * by all of it, landing exactly on the target), each with the same refusal
  * and flips; the vertices still away after that are removed and reinserted
- * at their targets one by one (one GPU thread; at most 65,536 a step), with
- * flips around each.  The whole step is one cooperative kernel launch; the
- * call returns after reading its result record (it synchronizes `stream`).  The result is the periodic Delaunay triangulation of
- * the moved points (a point whose target is taken by another stays where it
- * was).  stats (may be NULL): inverted_faces (turned by the move),
+ * at their targets in claim-based rounds (removal rounds, then insertion
+ * rounds; a point whose target is taken by an earlier one, by smallest id,
+ * goes back where it was), then flips from the edges those rewrote.  The
+ * whole step is one cooperative kernel launch; the call returns after reading
+ * its result record (it synchronizes `stream`).  The result is the periodic
+ * Delaunay triangulation of the moved points.  stats (may be NULL): inverted_faces (turned by the move),
  * substep_vertices (sent back, then brought to their target by sub-steps),
  * removed_vertices (removed and reinserted), reverted_vertices (not at their
  * target at the end), lawson_flips, lawson_rounds, the predicate counters,
