@@ -393,9 +393,9 @@ def run_ours(args, rank, world, dist):
     achieved = alg_bytes / (dev_s / K) / 1e9
     peak, peak_kind = peaks()
     # DRAM traffic of one k_step launch measured by ncu on this workload
-    # (dram__bytes_read.sum + dram__bytes_write.sum = 73.0 MB at 3,000,005
+    # (dram__bytes_read.sum + dram__bytes_write.sum = 73.4 MB at 3,000,005
     # edges), scaled by the edge count for other sizes
-    traffic = 73.01e6 * E / 3000005
+    traffic = 73.42e6 * E / 3000005
 
     # e2e: pinned host displacements through the pipelined C-ABI call (the
     # host-to-device copy of step k+1 overlaps step k); every step's counters
