@@ -1,9 +1,11 @@
-// The one-thread removal and reinsertion of the periodic step
-// (mcleap_gb300/csrc/periodic.cuh: p_body_reinsert) run on the CPU for chosen
-// vertices and targets, so that its rare branches (a target on an edge, a
-// target already taken) can be driven directly.
+// The removal and reinsertion of the periodic step run on the CPU for chosen
+// vertices and targets, so that the rare branches (a target on an edge, a
+// target already taken, a refused removal) can be driven directly: the
+// one-thread pass (mcleap_gb300/csrc/periodic.cuh: p_body_reinsert), or with
+// a third argument "rounds" the GPU launch's claim-based rounds
+// (periodic_rounds.h) followed by flip rounds from the edges they rewrote.
 //
-//   periodic_reinsert IN OUT
+//   periodic_reinsert IN OUT [rounds]
 //   IN : int32 n, int32 E, float L, int32 k, float pos[n][2], int32 ev[E][4],
 //        int32 en[E][4], uint32 eo[E], int32 vert[k], float target[k][2]
 //   OUT: int32 status, int32 reinserted, float pos[n][2], int32 ev[E][4],
@@ -13,6 +15,7 @@
 #include <vector>
 
 #include "periodic.cuh"
+#include "periodic_rounds.h"
 
 using mcl::PF2;
 using mcl::PI4;
@@ -23,7 +26,8 @@ template <typename T>
 static void wr(FILE* f, const T* p, size_t k) { fwrite(p, sizeof(T), k, f); }
 
 int main(int argc, char** argv) {
-  if (argc != 3) return 1;
+  if (argc != 3 && argc != 4) return 1;
+  const bool rounds = argc == 4;
   int n = 0, E = 0, k = 0;
   float L = 0;
   FILE* in = fopen(argv[1], "rb");
@@ -45,7 +49,35 @@ int main(int argc, char** argv) {
                eo.data(),   wv.data(),   wt.data(),   mark.data(),    pos_old.data(), target.data(), cand.data(),
                claim.data(), &cnt,       clist.data(), wl0.data(),    wl1.data(),    qstamp.data()};
   for (int h = 0; h < 2 * E; ++h) mcl::p_body_vhe(V, vhe.data(), h);
-  mcl::p_body_reinsert(V, vhe.data(), vert.data(), k, 1 << 16);
+  if (!rounds) {
+    mcl::p_body_reinsert(V, vhe.data(), vert.data(), k, 1 << 16);
+  } else {
+    unsigned stamp = 0;
+    unsigned long long lq = 0;
+    periodic_par_rounds(V, vhe.data(), vert, stamp, &lq);
+    // flip rounds from the rounds' work-list (wl0), as the launch's settle
+    // from a list: classify the list, flip the winners, classify their wings
+    int cur = 0;
+    unsigned long long len = lq;
+    for (int r = 0; r < 4096 && !cnt.error && len > 0; ++r) {
+      ++stamp;
+      cnt.nondelaunay = 0;
+      cnt.inverted = 0;
+      const int* wl = cur == 1 ? wl1.data() : wl0.data();
+      for (unsigned long long i = 0; i < len; ++i) mcl::p_body_classify(V, wl[i], stamp);
+      if (cnt.error) break;
+      if (cnt.inverted) {
+        cnt.error = MCL_ERR_DEGENERATE_INPUT;  // the rounds leave every face positive
+        break;
+      }
+      if (!cnt.nondelaunay) break;
+      const int next = cur == 0 ? 1 : 0;
+      cnt.lcount[next] = 0;
+      for (unsigned long long i = 0; i < cnt.nondelaunay; ++i) mcl::p_body_flip(V, clist[i], stamp, next);
+      cur = next;
+      len = cnt.lcount[next];
+    }
+  }
   FILE* out = fopen(argv[2], "wb");
   if (!out) return 4;
   const int32_t head[2] = {(int32_t)cnt.error, (int32_t)cnt.reinserted};

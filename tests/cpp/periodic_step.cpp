@@ -26,6 +26,7 @@
 #include <vector>
 
 #include "periodic.cuh"
+#include "periodic_rounds.h"
 
 using mcl::PF2;
 using mcl::PI4;
@@ -151,63 +152,8 @@ int main(int argc, char** argv) {
     std::vector<int> list;
     for (int v = 0; v < n; ++v)
       if (pos[v].x != target[v].x || pos[v].y != target[v].y) list.push_back(v);
-    std::vector<int> par((size_t)8 * n, 0);
-    int* pf = par.data();
-    int* pa = pf + 3 * n;
-    int* loc = pf + 4 * n;
-    int* ps = pf + 5 * n;
-    constexpr int kWon = 16;
-    for (const int v : list) {
-      ps[v] = mcl::kParPending;
-      loc[v] = -1;
-    }
     unsigned long long lq = 0;
-    const unsigned sq = ++stamp;
-    std::vector<int> la = list, lb;
-    for (int r = 0; r < mcl::kParRounds && !la.empty() && !cnt.error; ++r) {
-      const unsigned s = ++stamp;
-      for (const int v : la) mcl::p_body_claim_star(V, vh.data(), v, s);
-      for (const int v : la)
-        if (mcl::p_body_holds_star(V, vh.data(), v, s)) ps[v] = mcl::kParPending | kWon;
-      lb.clear();
-      for (const int v : la) {
-        if (ps[v] == (mcl::kParPending | kWon)) mcl::p_body_remove_par(V, vh.data(), v, pf, pa, ps, &lq, sq);
-        else lb.push_back(v);
-      }
-      la.swap(lb);
-    }
-    for (const int v : la) ps[v] = mcl::kParStays;
-    la.clear();
-    for (const int v : list)
-      if (ps[v] == mcl::kParRemoved) la.push_back(v);
-    for (int r = 0; !la.empty() && !cnt.error; ++r) {
-      if (r == mcl::kParRounds) {
-        cnt.error = MCL_ERR_NO_CONVERGENCE;
-        break;
-      }
-      const unsigned s = ++stamp;
-      for (const int v : la) mcl::p_body_locate_par(V, vh.data(), v, pa, loc, ps, s);
-      for (const int v : la)
-        if (mcl::p_body_holds_face(V, v, loc, ps, s)) ps[v] |= kWon;
-      lb.clear();
-      for (const int v : la) {
-        if (ps[v] & kWon) {
-          ps[v] &= ~kWon;
-          mcl::p_body_split_par(V, vh.data(), v, pf, loc, ps, &lq, sq);
-        } else if (loc[v] == -2) {
-          if (ps[v] == mcl::kParBack) {
-            mcl::p_error(V, MCL_ERR_DEGENERATE_INPUT, 20);
-          } else {
-            ps[v] = mcl::kParBack;
-            loc[v] = -1;
-            lb.push_back(v);
-          }
-        } else {
-          lb.push_back(v);
-        }
-      }
-      la.swap(lb);
-    }
+    periodic_par_rounds(V, vh.data(), list, stamp, &lq);
     if (!cnt.error) {
       cnt.lcount[0] = lq;
       settle(0);

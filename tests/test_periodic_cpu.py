@@ -408,7 +408,7 @@ def reinsert_harness(tmp_path_factory):
     return exe
 
 
-def run_reinsert(exe, tmp_path, pos, ev, en, eo, verts, targets):
+def run_reinsert(exe, tmp_path, pos, ev, en, eo, verts, targets, rounds=False):
     n, E, k = len(pos), len(ev), len(verts)
     src, dst = str(tmp_path / "rin.bin"), str(tmp_path / "rout.bin")
     with open(src, "wb") as f:
@@ -416,7 +416,7 @@ def run_reinsert(exe, tmp_path, pos, ev, en, eo, verts, targets):
         for a in (pos.astype(np.float32), ev.astype(np.int32), en.astype(np.int32), eo.astype(np.uint32),
                   np.asarray(verts, np.int32), np.asarray(targets, np.float32)):
             f.write(np.ascontiguousarray(a).tobytes())
-    subprocess.run([exe, src, dst], check=True)
+    subprocess.run([exe, src, dst] + (["rounds"] if rounds else []), check=True)
     raw = open(dst, "rb").read()
     status, reinserted = (int(x) for x in np.frombuffer(raw[:8], np.int32))
     o = 8
@@ -430,11 +430,14 @@ def run_reinsert(exe, tmp_path, pos, ev, en, eo, verts, targets):
     return status, reinserted, pos2, ev2, en2, eo2
 
 
-def test_reinsertion_inside_a_face_on_an_edge_and_onto_a_taken_spot(reinsert_harness, tmp_path):
-    """The one-thread removal and reinsertion: a target inside a face (1 -> 3
-    split), a target exactly on an edge (2 -> 4 split, three collinear points
-    afterwards) and a target that another point occupies (the vertex goes
-    back where it was); the mesh is the oracle's triangulation after each."""
+@pytest.mark.parametrize("rounds", [False, True], ids=["one-thread", "rounds"])
+def test_reinsertion_inside_a_face_on_an_edge_and_onto_a_taken_spot(reinsert_harness, tmp_path, rounds):
+    """Removal and reinsertion, by the one-thread pass and by the launch's
+    claim-based rounds (then flips from the edges they rewrote): a target
+    inside a face (1 -> 3 split), a target exactly on an edge (2 -> 4 split,
+    three collinear points afterwards) and a target that another point
+    occupies (the vertex goes back where it was); the mesh is the oracle's
+    triangulation afterwards."""
     n = 2000
     xy = torus_points(n, 81)
     h = L / np.sqrt(n)
@@ -451,7 +454,7 @@ def test_reinsertion_inside_a_face_on_an_edge_and_onto_a_taken_spot(reinsert_har
     t_face = np.float32([2.25 * L + 0.123, 2.75 * L - 0.456])
     targets = [mid, xy[5], t_face]
     st, re, pos, ev2, en2, eo2 = run_reinsert(reinsert_harness, tmp_path, xy, ev, en, eo,
-                                              [v_edge, v_taken, v_face], targets)
+                                              [v_edge, v_taken, v_face], targets, rounds)
     assert st == 0 and re == 2
     assert (pos[v_edge] == mid).all() and (pos[v_taken] == xy[v_taken]).all() and (pos[v_face] == t_face).all()
     assert torus_faces_consistent(ev2, en2, eo2)
@@ -463,10 +466,11 @@ def test_reinsertion_inside_a_face_on_an_edge_and_onto_a_taken_spot(reinsert_har
     assert ((got[:, 0] == min(1, v_edge)) & (got[:, 1] == max(1, v_edge))).any()
 
 
-def test_refused_removal_leaves_the_torus_delaunay(reinsert_harness, tmp_path):
+@pytest.mark.parametrize("rounds", [False, True], ids=["one-thread", "rounds"])
+def test_refused_removal_leaves_the_torus_delaunay(reinsert_harness, tmp_path, rounds):
     """Tiny tori, where a vertex's star can hold two copies of one neighbour:
-    the one-thread removal then refuses (the vertex stays where it was), some
-    of them after spoke flips.  Whatever happens, a call that returns OK leaves
+    the removal (one-thread pass or the launch's rounds) then refuses (the
+    vertex stays where it was), some of them after spoke flips.  Whatever happens, a call that returns OK leaves
     the oracle's triangulation of the final positions (a refusal is counted,
     never a silently non-Delaunay mesh); a failure is reported."""
     outcomes = {"reinserted": 0, "refused": 0, "error": 0}
@@ -480,7 +484,8 @@ def test_refused_removal_leaves_the_torus_delaunay(reinsert_harness, tmp_path):
             rng = np.random.default_rng(seed)
             for v in range(n):
                 t = (2 * L + rng.random(2) * L).astype(np.float32)
-                st, re, pos, ev2, en2, eo2 = run_reinsert(reinsert_harness, tmp_path, xy, ev, en, eo, [v], [t])
+                st, re, pos, ev2, en2, eo2 = run_reinsert(reinsert_harness, tmp_path, xy, ev, en, eo, [v], [t],
+                                                          rounds)
                 if st != 0:
                     outcomes["error"] += 1
                     continue
