@@ -3,15 +3,17 @@
 // target already taken, a refused removal) can be driven directly: the
 // one-thread pass (mcleap_gb300/csrc/periodic.cuh: p_body_reinsert), or with
 // a third argument "rounds" the GPU launch's claim-based rounds
-// (periodic_rounds.h) followed by flip rounds from the edges they rewrote.
+// (periodic_rounds.h) followed by flip rounds from the edges they rewrote
+// ("rounds:S": every phase in a pseudo-random order drawn from seed S).
 //
-//   periodic_reinsert IN OUT [rounds]
+//   periodic_reinsert IN OUT [rounds[:S]]
 //   IN : int32 n, int32 E, float L, int32 k, float pos[n][2], int32 ev[E][4],
 //        int32 en[E][4], uint32 eo[E], int32 vert[k], float target[k][2]
 //   OUT: int32 status, int32 reinserted, float pos[n][2], int32 ev[E][4],
 //        int32 en[E][4], uint32 eo[E]
 #include <cstdint>
 #include <cstdio>
+#include <cstdlib>
 #include <vector>
 
 #include "periodic.cuh"
@@ -28,6 +30,7 @@ static void wr(FILE* f, const T* p, size_t k) { fwrite(p, sizeof(T), k, f); }
 int main(int argc, char** argv) {
   if (argc != 3 && argc != 4) return 1;
   const bool rounds = argc == 4;
+  const unsigned shuffle = rounds && argv[3][6] == ':' ? (unsigned)atoi(argv[3] + 7) : 0u;
   int n = 0, E = 0, k = 0;
   float L = 0;
   FILE* in = fopen(argv[1], "rb");
@@ -54,7 +57,7 @@ int main(int argc, char** argv) {
   } else {
     unsigned stamp = 0;
     unsigned long long lq = 0;
-    periodic_par_rounds(V, vhe.data(), vert, stamp, &lq);
+    periodic_par_rounds(V, vhe.data(), vert, stamp, &lq, shuffle);
     // flip rounds from the rounds' work-list (wl0), as the launch's settle
     // from a list: classify the list, flip the winners, classify their wings
     int cur = 0;

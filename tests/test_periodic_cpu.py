@@ -416,7 +416,8 @@ def run_reinsert(exe, tmp_path, pos, ev, en, eo, verts, targets, rounds=False):
         for a in (pos.astype(np.float32), ev.astype(np.int32), en.astype(np.int32), eo.astype(np.uint32),
                   np.asarray(verts, np.int32), np.asarray(targets, np.float32)):
             f.write(np.ascontiguousarray(a).tobytes())
-    subprocess.run([exe, src, dst] + (["rounds"] if rounds else []), check=True)
+    mode = [] if not rounds else (["rounds"] if rounds is True else [f"rounds:{int(rounds)}"])
+    subprocess.run([exe, src, dst] + mode, check=True)
     raw = open(dst, "rb").read()
     status, reinserted = (int(x) for x in np.frombuffer(raw[:8], np.int32))
     o = 8
@@ -498,3 +499,26 @@ def test_refused_removal_leaves_the_torus_delaunay(reinsert_harness, tmp_path, r
                     assert (pos[v] == xy[v]).all()
                     outcomes["refused"] += 1
     assert outcomes["refused"] > 0 and outcomes["reinserted"] > 0, outcomes
+
+
+def test_many_reinsertions_in_rounds_do_not_depend_on_order(reinsert_harness, tmp_path):
+    """Two hundred vertices removed and reinserted far from where they were by
+    the launch's claim-based rounds (contested stars and faces, several
+    rounds), every phase taken in three different orders: the same positions
+    and the oracle's triangulation each time."""
+    n = 4000
+    xy = torus_points(n, 91)
+    ev, en, eo = P.periodic_mesh(xy, L)
+    rng = np.random.default_rng(92)
+    verts = np.sort(rng.choice(n, 200, replace=False))
+    targets = (2 * L + rng.random((len(verts), 2)) * L).astype(np.float32)
+    results = []
+    for seed in (1, 2, 3):
+        st, re, pos, ev2, en2, eo2 = run_reinsert(reinsert_harness, tmp_path, xy, ev, en, eo, verts, targets, seed)
+        assert st == 0 and re == len(verts), (st, re)
+        assert (pos[verts] == targets).all()
+        assert torus_faces_consistent(ev2, en2, eo2)
+        edges = P.mesh_edges(ev2, eo2)
+        assert np.array_equal(edges, P.periodic_edges(pos, L))
+        results.append((pos, edges))
+    assert all(np.array_equal(results[0][0], r[0]) and np.array_equal(results[0][1], r[1]) for r in results[1:])
